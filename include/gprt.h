@@ -1,0 +1,301 @@
+/*
+ * gprt.h - C ABI of the GB300-native rendering hot path of go-progressive-raytracer.
+ *
+ * The Go reference keeps its rendering path behind four seams (all paths are
+ * relative to the reference project root):
+ *   - scene.Scene + scene.SamplingConfig            pkg/scene/scene.go:11-30
+ *   - integrator.Integrator (PT and BDPT)           pkg/integrator/integrator.go:15-19,
+ *                                                   pkg/integrator/path_tracing.go:40,
+ *                                                   pkg/integrator/bdpt.go:64
+ *   - renderer.ProgressiveRaytracer                 pkg/renderer/progressive.go:62-223,286
+ *   - geometry.BVH.Hit (raw ray batches)            pkg/geometry/bvh.go:183-239
+ * This header is what a cgo binding of those seams calls.  Every entry point
+ * below cites the reference function it replaces.
+ *
+ * Conventions (mirroring the reference's Go conventions):
+ *   - Every function returns an int status: 0 = OK, negative = error
+ *     (GPRT_E_*).  No exception or abort crosses this boundary.  The message of
+ *     the last error of a context is returned by gprt_last_error().
+ *   - Host pointers passed in are borrowed for the duration of the call only
+ *     (cgo pointer rules: Go memory is never retained).  Scene descriptions are
+ *     copied.
+ *   - All device memory is owned by handles (context, scene, job).  A context
+ *     serialises the calls made on it and on its scenes and jobs with an
+ *     internal mutex, so handles may be used from several goroutines.
+ *   - Arithmetic on the device is FP32; descriptions are float64 like the
+ *     reference's core.Vec3 (pkg/core/vec3.go:9-11) and are rounded once.
+ */
+#ifndef GPRT_H
+#define GPRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPRT_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define GPRT_OK 0
+#define GPRT_E_INVALID (-1)      /* invalid argument or unsupported scene content */
+#define GPRT_E_OOM (-2)          /* device allocation failed */
+#define GPRT_E_DEVICE (-3)       /* CUDA error (launch, copy, sync) */
+#define GPRT_E_BOUND (-4)        /* a device-side bound (stack, queue, wait) was exceeded */
+#define GPRT_E_CANCELLED (-5)    /* job cancelled (context.Context cancellation analogue) */
+#define GPRT_E_ADMISSION (-6)    /* serving: request refused by the HBM budget */
+#define GPRT_E_NOT_FOUND (-7)    /* serving: unknown ticket */
+
+/* ---- scene description ----------------------------------------------------
+ * A flattened scene.Scene (pkg/scene/scene.go:11-19).  Shapes are listed in
+ * scene.Shapes order; lights in scene.Lights order.  An area light names the
+ * shape that holds its geometry (scene.AddQuadLight / AddSphereLight append
+ * both, pkg/scene/scene.go:102-115).
+ */
+
+enum gprt_material_kind {
+  GPRT_MAT_LAMBERTIAN = 0, /* pkg/material/lambertian.go (SolidColor albedo) */
+  GPRT_MAT_METAL = 1,      /* pkg/material/metal.go (fuzz clamped to [0,1]) */
+  GPRT_MAT_DIELECTRIC = 2, /* pkg/material/dielectric.go */
+  GPRT_MAT_EMISSIVE = 3,   /* pkg/material/emissive.go */
+  GPRT_MAT_LAYERED = 4     /* pkg/material/layered.go (outer, inner) */
+};
+
+typedef struct gprt_material_desc {
+  uint32_t kind;     /* gprt_material_kind */
+  uint32_t outer;    /* LAYERED: material index of the outer layer */
+  uint32_t inner;    /* LAYERED: material index of the inner layer */
+  uint32_t reserved;
+  double albedo[3];  /* LAMBERTIAN, METAL */
+  double fuzz;       /* METAL */
+  double ior;        /* DIELECTRIC */
+  double emission[3];/* EMISSIVE */
+} gprt_material_desc;
+
+enum gprt_shape_kind {
+  GPRT_SHAPE_SPHERE = 0,   /* p[0..2] center, p[3] radius (negative = inward normal) */
+  GPRT_SHAPE_QUAD = 1,     /* p[0..2] corner, p[3..5] u, p[6..8] v */
+  GPRT_SHAPE_BOX = 2,      /* p[0..2] center, p[3..5] half extents, p[6..8] rotation (rad, X->Y->Z) */
+  GPRT_SHAPE_MESH = 3,     /* mesh = index into gprt_scene_desc.meshes */
+  GPRT_SHAPE_TRIANGLE = 4  /* p[0..2] v0, p[3..5] v1, p[6..8] v2 */
+};
+
+typedef struct gprt_shape_desc {
+  uint32_t kind;     /* gprt_shape_kind */
+  uint32_t material; /* material index (ignored for MESH with per-triangle materials) */
+  uint32_t mesh;     /* MESH only */
+  uint32_t reserved;
+  double p[9];
+} gprt_shape_desc;
+
+/* geometry.NewTriangleMesh(vertices, faces, material, &TriangleMeshOptions{Materials})
+ * pkg/geometry/triangle_mesh.go:33-146.  Rotation/normals/UV options are
+ * applied by the caller (they only transform inputs). */
+typedef struct gprt_mesh_desc {
+  const double* vertices;      /* 3 * n_vertices */
+  const uint32_t* indices;     /* 3 * n_triangles */
+  const uint32_t* tri_materials; /* n_triangles material indices, or NULL */
+  uint32_t n_vertices;
+  uint32_t n_triangles;
+} gprt_mesh_desc;
+
+enum gprt_light_kind {
+  GPRT_LIGHT_QUAD = 0,              /* pkg/lights/quad_light.go; shape = a QUAD shape */
+  GPRT_LIGHT_SPHERE = 1,            /* pkg/lights/sphere_light.go; shape = a SPHERE shape */
+  GPRT_LIGHT_UNIFORM_INFINITE = 2,  /* pkg/lights/uniform_infinite_light.go; color_a = emission */
+  GPRT_LIGHT_GRADIENT_INFINITE = 3  /* pkg/lights/gradient_infinite_light.go; color_a = top, color_b = bottom */
+};
+
+typedef struct gprt_light_desc {
+  uint32_t kind;   /* gprt_light_kind */
+  uint32_t shape;  /* QUAD / SPHERE: index of the shape holding the geometry and emissive material */
+  double color_a[3];
+  double color_b[3];
+  double weight;   /* light-sampler weight; used when gprt_scene_desc.weighted_sampler != 0 */
+} gprt_light_desc;
+
+/* geometry.CameraConfig, pkg/geometry/camera.go:18-32 */
+typedef struct gprt_camera_desc {
+  double center[3];
+  double look_at[3];
+  double up[3];
+  double aspect_ratio;
+  double vfov_deg;
+  double aperture;
+  double focus_distance; /* <= 0: |center - look_at| */
+  uint32_t width;
+  uint32_t reserved;
+} gprt_camera_desc;
+
+/* scene.SamplingConfig, pkg/scene/scene.go:22-30 */
+typedef struct gprt_sampling_desc {
+  uint32_t width;
+  uint32_t height;
+  uint32_t samples_per_pixel;
+  uint32_t max_depth;
+  uint32_t rr_min_bounces;
+  uint32_t reserved;
+  double adaptive_min_samples; /* fraction of the pass target; 1.0 = fixed spp */
+  double adaptive_threshold;
+} gprt_sampling_desc;
+
+typedef struct gprt_scene_desc {
+  const gprt_material_desc* materials;
+  const gprt_shape_desc* shapes;
+  const gprt_mesh_desc* meshes;
+  const gprt_light_desc* lights;
+  uint32_t n_materials;
+  uint32_t n_shapes;
+  uint32_t n_meshes;
+  uint32_t n_lights;
+  uint32_t weighted_sampler; /* 0: lights.NewUniformLightSampler; 1: NewWeightedLightSampler(weights) */
+  uint32_t reserved;
+  gprt_camera_desc camera;
+  gprt_sampling_desc sampling;
+} gprt_scene_desc;
+
+/* ---- ray batches ----------------------------------------------------------
+ * Layout of a ray batch for gprt_intersect: 32 bytes per ray, two 16-byte
+ * vectors per ray.  tmin/tmax are the Hit(ray, tMin, tMax) interval of
+ * geometry.BVH.Hit. */
+typedef struct gprt_ray {
+  float ox, oy, oz, tmin;
+  float dx, dy, dz, tmax;
+} gprt_ray;
+
+/* Hit record: t, primitive id (GPRT_NO_HIT when missed), barycentric /
+ * parametric (u, v) as in SurfaceInteraction.UV for triangles and quads. */
+typedef struct gprt_hit {
+  float t;
+  uint32_t prim;
+  float u, v;
+} gprt_hit;
+
+#define GPRT_NO_HIT 0xFFFFFFFFu
+#define GPRT_CLOSEST 0u /* closest hit (BVH.Hit with the hit record used) */
+#define GPRT_ANY 1u     /* any hit in (tmin, tmax): the shadow-ray use of BVH.Hit */
+
+typedef struct gprt_scene_info {
+  double world_center[3]; /* BVH.Center, pkg/geometry/bvh.go:39-48 */
+  double world_radius;    /* BVH.Radius */
+  uint64_t n_primitives;
+  uint64_t n_triangles;
+  uint64_t n_quads;
+  uint64_t n_spheres;
+  uint64_t n_nodes;       /* 4-wide BVH nodes */
+  uint64_t device_bytes;  /* device memory held by the scene */
+  uint32_t image_width;
+  uint32_t image_height;
+  double build_ms;        /* host BVH build time */
+} gprt_scene_info;
+
+/* ---- progressive jobs ---------------------------------------------------- */
+enum gprt_integrator_kind {
+  GPRT_INTEGRATOR_PATH_TRACING = 0, /* integrator.NewPathTracingIntegrator */
+  GPRT_INTEGRATOR_BDPT = 1          /* integrator.NewBDPTIntegrator */
+};
+
+/* renderer.ProgressiveConfig (pkg/renderer/progressive.go:29-46) plus the
+ * integrator choice and the counter-based sampler seed. */
+typedef struct gprt_job_desc {
+  uint32_t integrator;           /* gprt_integrator_kind */
+  uint32_t tile_size;            /* 0 -> 64 */
+  uint32_t initial_samples;      /* 0 -> 1 */
+  uint32_t max_samples_per_pixel;/* 0 -> 50 */
+  uint32_t max_passes;           /* 0 -> 7 */
+  uint32_t chunk_paths;          /* wavefront size; 0 -> automatic */
+  uint32_t block_size;           /* threads per block; 0 -> automatic */
+  uint32_t reserved;
+  uint64_t seed;
+} gprt_job_desc;
+
+/* renderer.RenderStats, pkg/renderer/stats.go:10-17 */
+typedef struct gprt_render_stats {
+  uint64_t total_pixels;
+  uint64_t total_samples;
+  double average_samples;
+  uint32_t max_samples;
+  uint32_t min_samples;
+  uint32_t max_samples_used;
+  uint32_t pass_number;
+  double pass_ms;       /* device time of the pass */
+  uint64_t splats;      /* BDPT t=1 splats applied in the pass */
+} gprt_render_stats;
+
+typedef struct gprt_ctx gprt_ctx;
+typedef struct gprt_scene gprt_scene;
+typedef struct gprt_job gprt_job;
+
+/* ---- context ------------------------------------------------------------ */
+int gprt_version(void);
+/* Creates a context on CUDA device `device`. */
+int gprt_ctx_create(int device, gprt_ctx** out);
+int gprt_ctx_destroy(gprt_ctx* ctx);
+/* Message of the last failed call on this context ("" when none). */
+const char* gprt_last_error(const gprt_ctx* ctx);
+
+/* ---- scene ---------------------------------------------------------------
+ * Replaces scene.Scene.Preprocess (pkg/scene/scene.go:45-78): flattens the
+ * shapes into device primitive arrays, builds the device BVH (the reference
+ * builds geometry.NewBVH, pkg/geometry/bvh.go:26-109), computes the world
+ * center/radius used by the infinite lights (bvh.go:39-48,
+ * uniform_infinite_light.go:128-132) and the light sampler
+ * (weighted_light_sampler.go:57-78).  Unsupported content -> GPRT_E_INVALID. */
+int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** out);
+int gprt_scene_destroy(gprt_scene* scene);
+int gprt_scene_get_info(const gprt_scene* scene, gprt_scene_info* info);
+/* Maps primitive ids to (index in scene.Shapes, sub-index: box face 0..5 or
+ * mesh triangle index, 0 otherwise).  Arrays of n_primitives entries. */
+int gprt_scene_primitive_map(const gprt_scene* scene, uint32_t* shape_index, uint32_t* sub_index);
+
+/* ---- raw ray batches -----------------------------------------------------
+ * Replaces geometry.BVH.Hit / hitNode (pkg/geometry/bvh.go:183-239) for a
+ * batch.  `rays` and `hits` are DEVICE pointers; `stream` is a cudaStream_t
+ * (NULL = the context stream).  Asynchronous. */
+int gprt_intersect(gprt_scene* scene, const gprt_ray* rays, uint32_t n, uint32_t flags,
+                   gprt_hit* hits, void* stream);
+/* Same with HOST pointers; copies in, traces and copies out, synchronously. */
+int gprt_intersect_host(gprt_scene* scene, const gprt_ray* rays, uint32_t n, uint32_t flags,
+                        gprt_hit* hits);
+/* Algorithmic work of a host ray batch on this scene's BVH, counted by a CPU
+ * walk of the device layout: per-ray node visits (4-wide nodes), child-box
+ * tests and primitive tests, summed.  Instrumentation for roofline figures. */
+int gprt_traversal_counts(gprt_scene* scene, const gprt_ray* rays, uint32_t n, uint32_t flags,
+                          uint64_t* node_visits, uint64_t* box_tests, uint64_t* prim_tests);
+
+/* ---- progressive jobs ----------------------------------------------------
+ * Replaces renderer.NewProgressiveRaytracer + integrator constructors
+ * (pkg/renderer/progressive.go:62-95).  The job owns its film
+ * (PixelStats per pixel, pkg/renderer/stats.go:20-55) on the device. */
+int gprt_job_create(gprt_scene* scene, const gprt_job_desc* desc, gprt_job** out);
+int gprt_job_destroy(gprt_job* job);
+/* (*ProgressiveRaytracer).RenderPass (progressive.go:126-223): brings every
+ * pixel to the pass target of getSamplesForPass (progressive.go:98-123) with
+ * the adaptive stop of tile_renderer.go:51-101, then applies the pass's BDPT
+ * splats (progressive.go:371-391).  Synchronous. */
+int gprt_job_render_pass(gprt_job* job, uint32_t pass_number, gprt_render_stats* stats);
+/* Adds exactly `spp` samples to every pixel (no adaptive stop).  Asynchronous
+ * on the job stream; splats are applied. */
+int gprt_job_add_samples(gprt_job* job, uint32_t spp);
+int gprt_job_sync(gprt_job* job);
+/* Film read-back (host pointers): per-pixel ColorAccum (3 floats), luminance
+ * sum, luminance-squared sum and sample count; any pointer may be NULL. */
+int gprt_job_read_film(gprt_job* job, float* rgb_sum, float* lum_sum, float* lum2_sum,
+                       uint32_t* count);
+/* PixelStats.GetColor for every pixel: ColorAccum / SampleCount (3 floats/pixel). */
+int gprt_job_read_image(gprt_job* job, float* rgb_mean);
+/* assembleCurrentImage + vec3ToColor (progressive.go:395-495): RGBA8, gamma 2. */
+int gprt_job_read_rgba8(gprt_job* job, uint8_t* rgba);
+/* extractTileImage (progressive.go:225-255) for pixel bounds [x0,x1) x [y0,y1). */
+int gprt_job_read_tile(gprt_job* job, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                       uint8_t* rgba);
+/* Stats of the last pass (assembleCurrentImage statistics). */
+int gprt_job_get_stats(gprt_job* job, gprt_render_stats* stats);
+/* Kernel launches issued by this job so far (instrumentation). */
+int gprt_job_launch_count(const gprt_job* job, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPRT_H */
