@@ -1,0 +1,774 @@
+// capi.cu - the C ABI of include/gprt.h: context, scene and job handles and
+// the host orchestration of the kernels (chunked wavefront passes).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gprt.h"
+#include "kernels.h"
+#include "scene.h"
+
+using namespace gprt;
+
+struct gprt_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  std::string err;
+};
+
+struct gprt_scene {
+  gprt_ctx* ctx = nullptr;
+  HostScene host;
+  DevScene dev{};
+  std::vector<void*> buffers;
+  size_t bytes = 0;
+  int* d_err = nullptr;
+};
+
+struct gprt_job {
+  gprt_scene* scene = nullptr;
+  gprt_job_desc desc{};
+  DevFilm film{};
+  DevPaths paths{};
+  std::vector<void*> buffers;
+  cudaStream_t stream = nullptr;
+  uint32_t* d_pix_list = nullptr;
+  uint32_t* d_active = nullptr;
+  uint64_t launches = 0;
+  int64_t uniform_count = 0;  // every pixel holds this many samples (-1: differs)
+  uint64_t sample_index_base = 0;
+  gprt_render_stats last{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // instrumentation (GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL)
+  struct Timed {
+    int cls;  // 0 extend, 1 shade, 2 shadow, 3 other
+    cudaEvent_t a, b;
+  };
+  std::vector<Timed> timed;
+  size_t timed_used = 0;
+  unsigned long long* d_stats = nullptr;
+  gprt_job_counters acc{};
+};
+
+namespace {
+
+int fail(gprt_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_fail(gprt_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, GPRT_E_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(ctx, call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+template <class T>
+int dev_alloc(gprt_ctx* ctx, std::vector<void*>& bufs, T** out, size_t count, size_t* bytes = nullptr) {
+  *out = nullptr;
+  if (count == 0) return GPRT_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, GPRT_E_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  bufs.push_back(p);
+  *out = static_cast<T*>(p);
+  if (bytes) *bytes += count * sizeof(T);
+  return GPRT_OK;
+}
+
+template <class T>
+int upload(gprt_ctx* ctx, std::vector<void*>& bufs, const std::vector<T>& src, const T** out, size_t* bytes) {
+  T* d = nullptr;
+  int rc = dev_alloc(ctx, bufs, &d, src.size(), bytes);
+  if (rc) return rc;
+  if (!src.empty()) CK(ctx, cudaMemcpyAsync(d, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  *out = d;
+  return GPRT_OK;
+}
+
+void free_all(std::vector<void*>& bufs) {
+  for (void* p : bufs) cudaFree(p);
+  bufs.clear();
+}
+
+// getSamplesForPass (pkg/renderer/progressive.go:98-123)
+uint32_t samples_for_pass(const gprt_job_desc& d, uint32_t pass) {
+  if (d.max_passes == 1) return d.max_samples_per_pixel;
+  if (pass == 1) return d.initial_samples;
+  uint32_t rem = d.max_samples_per_pixel - d.initial_samples;
+  uint32_t per = rem / (d.max_passes - 1);
+  uint32_t t = d.initial_samples + (pass - 1) * per;
+  if (pass == d.max_passes) t = d.max_samples_per_pixel;
+  return t;
+}
+
+int ensure_paths(gprt_job* j) {
+  if (j->paths.capacity) return GPRT_OK;
+  gprt_ctx* ctx = j->scene->ctx;
+  uint32_t cap = j->desc.chunk_paths;
+  DevPaths& P = j->paths;
+  auto& b = j->buffers;
+  int rc = 0;
+  rc |= dev_alloc(ctx, b, &P.ray_o, cap);
+  rc |= dev_alloc(ctx, b, &P.ray_d, cap);
+  rc |= dev_alloc(ctx, b, &P.weight, cap);
+  rc |= dev_alloc(ctx, b, &P.thr, cap);
+  rc |= dev_alloc(ctx, b, &P.L, cap);
+  rc |= dev_alloc(ctx, b, &P.hit, cap);
+  rc |= dev_alloc(ctx, b, &P.pixel, cap);
+  rc |= dev_alloc(ctx, b, &P.sample, cap);
+  rc |= dev_alloc(ctx, b, &P.rng_pos, cap);
+  rc |= dev_alloc(ctx, b, &P.queue[0], cap);
+  rc |= dev_alloc(ctx, b, &P.queue[1], cap);
+  rc |= dev_alloc(ctx, b, &P.sh_o, cap);
+  rc |= dev_alloc(ctx, b, &P.sh_d, cap);
+  rc |= dev_alloc(ctx, b, &P.sh_c, cap);
+  rc |= dev_alloc(ctx, b, &P.counters, 8);
+  if (j->desc.flags & GPRT_JOB_COUNT_TRAVERSAL) rc |= dev_alloc(ctx, b, &j->d_stats, 8);
+  if (rc) return GPRT_E_OOM;
+  P.stats = j->d_stats;
+  CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), j->stream));
+  if (j->d_stats) CK(ctx, cudaMemsetAsync(j->d_stats, 0, 8 * sizeof(unsigned long long), j->stream));
+  P.capacity = cap;
+  return GPRT_OK;
+}
+
+// Runs one chunk: `layers` samples of `npix` pixels starting at pix0.
+// CUDA-event bracket of one launch on the job stream (when timing is on).
+struct TimedLaunch {
+  gprt_job* j;
+  size_t idx = (size_t)-1;
+  TimedLaunch(gprt_job* job, int cls) : j(job) {
+    if (!(j->desc.flags & GPRT_JOB_TIME_KERNELS)) return;
+    if (j->timed_used == j->timed.size()) {
+      gprt_job::Timed t{cls, nullptr, nullptr};
+      cudaEventCreate(&t.a);
+      cudaEventCreate(&t.b);
+      j->timed.push_back(t);
+    }
+    idx = j->timed_used++;
+    j->timed[idx].cls = cls;
+    cudaEventRecord(j->timed[idx].a, j->stream);
+  }
+  ~TimedLaunch() {
+    if (idx != (size_t)-1) cudaEventRecord(j->timed[idx].b, j->stream);
+  }
+};
+
+// Folds the recorded launch times and the device counters into j->acc.
+int collect_counters(gprt_job* j) {
+  gprt_ctx* ctx = j->scene->ctx;
+  CK(ctx, cudaStreamSynchronize(j->stream));
+  for (size_t i = 0; i < j->timed_used; i++) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, j->timed[i].a, j->timed[i].b);
+    switch (j->timed[i].cls) {
+      case 0: j->acc.extend_ms += ms; j->acc.extend_launches++; break;
+      case 1: j->acc.shade_ms += ms; j->acc.shade_launches++; break;
+      case 2: j->acc.shadow_ms += ms; j->acc.shadow_launches++; break;
+      default: j->acc.other_ms += ms; j->acc.other_launches++; break;
+    }
+  }
+  j->timed_used = 0;
+  if (j->d_stats) {
+    unsigned long long v[8];
+    CK(ctx, cudaMemcpy(v, j->d_stats, sizeof(v), cudaMemcpyDeviceToHost));
+    CK(ctx, cudaMemset(j->d_stats, 0, sizeof(v)));
+    j->acc.extend_rays += v[0];
+    j->acc.extend_nodes += v[1];
+    j->acc.extend_boxes += v[2];
+    j->acc.extend_prims += v[3];
+    j->acc.shadow_rays += v[4];
+    j->acc.shadow_nodes += v[5];
+    j->acc.shadow_boxes += v[6];
+    j->acc.shadow_prims += v[7];
+  }
+  return GPRT_OK;
+}
+
+void run_chunk(gprt_job* j, const ChunkDesc& ch) {
+  const DevScene& sc = j->scene->dev;
+  gprt_ctx* ctx = j->scene->ctx;
+  int block = (int)j->desc.block_size;
+  int grid = std::max(1, ctx->sm_count * (2048 / block));
+  uint32_t n = ch.npix * ch.layers;
+  int g = launch_grid(n, block, grid);
+  if (j->desc.integrator == GPRT_INTEGRATOR_BDPT) {
+    {
+      TimedLaunch t(j, 3);
+      launch_bdpt(sc, j->film, j->paths, ch, block, j->stream);
+    }
+    {
+      TimedLaunch t(j, 3);
+      launch_accumulate(j->film, j->paths, ch, 256, j->stream);
+    }
+    j->launches += 2;
+    return;
+  }
+  {
+    TimedLaunch t(j, 3);
+    launch_pt_raygen(sc, j->film, j->paths, ch, block, j->stream);
+  }
+  int cur = 0;
+  for (int b = 0; b < sc.max_depth; b++) {
+    {
+      TimedLaunch t(j, 0);
+      launch_pt_extend(sc, j->paths, cur, block, g, j->stream);
+    }
+    {
+      TimedLaunch t(j, 1);
+      launch_pt_shade(sc, j->paths, ch, cur, b, block, g, j->stream);
+    }
+    {
+      TimedLaunch t(j, 2);
+      launch_pt_shadow(sc, j->paths, block, g, j->stream);
+    }
+    cur ^= 1;
+  }
+  {
+    TimedLaunch t(j, 3);
+    launch_accumulate(j->film, j->paths, ch, 256, j->stream);
+  }
+  j->launches += 2 + 3 * (uint64_t)sc.max_depth;
+}
+
+// Adds `spp` samples to each of `npix` pixels (all pixels, or the list).
+int add_samples(gprt_job* j, uint32_t spp, uint32_t npix, const uint32_t* list) {
+  if (spp == 0 || npix == 0) return GPRT_OK;
+  int rc = ensure_paths(j);
+  if (rc) return rc;
+  uint32_t cap = j->paths.capacity;
+  ChunkDesc ch{};
+  ch.pix_list = list;
+  ch.seed = j->desc.seed;
+  ch.bounce_base = 0;
+  if (npix <= cap) {
+    uint32_t per = std::max(1u, cap / npix);
+    for (uint32_t done = 0; done < spp;) {
+      uint32_t layers = std::min(per, spp - done);
+      ch.pix0 = 0;
+      ch.npix = npix;
+      ch.layers = layers;
+      run_chunk(j, ch);
+      done += layers;
+    }
+  } else {
+    for (uint32_t s = 0; s < spp; s++)
+      for (uint32_t p0 = 0; p0 < npix; p0 += cap) {
+        ch.pix0 = p0;
+        ch.npix = std::min(cap, npix - p0);
+        ch.layers = 1;
+        run_chunk(j, ch);
+      }
+  }
+  if (j->desc.integrator == GPRT_INTEGRATOR_BDPT) {
+    launch_apply_splats(j->film, j->stream);
+    j->launches++;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(j->scene->ctx, e, "kernel launch");
+  return GPRT_OK;
+}
+
+int check_device_errors(gprt_job* j) {
+  gprt_ctx* ctx = j->scene->ctx;
+  uint32_t err = 0;
+  if (j->paths.counters) {
+    CK(ctx, cudaMemcpyAsync(&err, j->paths.counters + 3, 4, cudaMemcpyDeviceToHost, j->stream));
+  }
+  CK(ctx, cudaStreamSynchronize(j->stream));
+  if (err) {
+    return fail(ctx, GPRT_E_BOUND,
+                std::string("device bound exceeded:") + ((err & kErrStackOverflow) ? " traversal stack" : "") +
+                    ((err & kErrQueueOverflow) ? " queue" : ""));
+  }
+  return GPRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gprt_version(void) { return GPRT_ABI_VERSION; }
+
+int gprt_ctx_create(int device, gprt_ctx** out) {
+  if (!out) return GPRT_E_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return GPRT_E_DEVICE;
+  }
+  auto c = std::make_unique<gprt_ctx>();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) return GPRT_E_DEVICE;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return GPRT_E_DEVICE;
+  *out = c.release();
+  return GPRT_OK;
+}
+
+int gprt_ctx_destroy(gprt_ctx* ctx) {
+  if (!ctx) return GPRT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GPRT_OK;
+}
+
+const char* gprt_last_error(const gprt_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** out) {
+  if (!ctx || !out) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  auto s = std::make_unique<gprt_scene>();
+  s->ctx = ctx;
+  std::string err;
+  if (!build_scene(desc, s->host, err)) return fail(ctx, GPRT_E_INVALID, err);
+  HostScene& h = s->host;
+  DevScene& d = s->dev;
+  int rc = 0;
+  rc |= upload(ctx, s->buffers, h.nodes, &d.nodes, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tris, &d.tris, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
+  if (rc) {
+    free_all(s->buffers);
+    return rc;
+  }
+  if (dev_alloc(ctx, s->buffers, &s->d_err, 1)) {
+    free_all(s->buffers);
+    return GPRT_E_OOM;
+  }
+  cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
+  d.n_nodes = (int)(h.nodes.size() / 8);
+  d.n_lights = (int)h.lights.size();
+  d.quad_base = h.n_tris;
+  d.sphere_base = h.n_tris + h.n_quads;
+  d.n_prims = h.n_tris + h.n_quads + h.n_spheres;
+  d.has_infinite = h.has_infinite;
+  d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
+  d.world_radius = (float)h.world_radius;
+  d.cam = h.cam;
+  d.max_depth = (int)h.sampling.max_depth;
+  d.rr_min_bounces = (int)h.sampling.rr_min_bounces;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    free_all(s->buffers);
+    return cuda_fail(ctx, e, "scene upload");
+  }
+  *out = s.release();
+  return GPRT_OK;
+}
+
+int gprt_scene_destroy(gprt_scene* s) {
+  if (!s) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  free_all(s->buffers);
+  delete s;
+  return GPRT_OK;
+}
+
+int gprt_scene_get_info(const gprt_scene* s, gprt_scene_info* info) {
+  if (!s || !info) return GPRT_E_INVALID;
+  const HostScene& h = s->host;
+  std::memset(info, 0, sizeof(*info));
+  for (int k = 0; k < 3; k++) info->world_center[k] = h.world_center[k];
+  info->world_radius = h.world_radius;
+  info->n_triangles = h.n_tris;
+  info->n_quads = h.n_quads;
+  info->n_spheres = h.n_spheres;
+  info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres;
+  info->n_nodes = h.nodes.size() / 8;
+  info->device_bytes = s->bytes;
+  info->image_width = h.sampling.width;
+  info->image_height = h.sampling.height;
+  info->build_ms = h.build_ms;
+  return GPRT_OK;
+}
+
+int gprt_scene_validate(const gprt_scene_desc* desc, gprt_scene_info* info, char* errbuf, size_t err_len) {
+  HostScene h;
+  std::string err;
+  bool ok = build_scene(desc, h, err);
+  if (ok) err = validate_layout(h);
+  if (errbuf && err_len) {
+    std::strncpy(errbuf, err.c_str(), err_len - 1);
+    errbuf[err_len - 1] = 0;
+  }
+  if (!ok || !err.empty()) return GPRT_E_INVALID;
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    for (int k = 0; k < 3; k++) info->world_center[k] = h.world_center[k];
+    info->world_radius = h.world_radius;
+    info->n_triangles = h.n_tris;
+    info->n_quads = h.n_quads;
+    info->n_spheres = h.n_spheres;
+    info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres;
+    info->n_nodes = h.nodes.size() / 8;
+    info->image_width = h.sampling.width;
+    info->image_height = h.sampling.height;
+    info->build_ms = h.build_ms;
+  }
+  return GPRT_OK;
+}
+
+int gprt_scene_primitive_map(const gprt_scene* s, uint32_t* shape_index, uint32_t* sub_index) {
+  if (!s) return GPRT_E_INVALID;
+  if (shape_index) std::memcpy(shape_index, s->host.prim_shape.data(), s->host.prim_shape.size() * 4);
+  if (sub_index) std::memcpy(sub_index, s->host.prim_sub.data(), s->host.prim_sub.size() * 4);
+  return GPRT_OK;
+}
+
+int gprt_intersect(gprt_scene* s, const gprt_ray* rays, uint32_t n, uint32_t flags, gprt_hit* hits, void* stream) {
+  if (!s || (n && (!rays || !hits)) || flags > GPRT_ANY) return GPRT_E_INVALID;
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  launch_intersect(s->dev, rays, n, flags == GPRT_ANY, hits, s->d_err, st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "intersect launch");
+  return GPRT_OK;
+}
+
+int gprt_intersect_host(gprt_scene* s, const gprt_ray* rays, uint32_t n, uint32_t flags, gprt_hit* hits) {
+  if (!s || (n && (!rays || !hits)) || flags > GPRT_ANY) return GPRT_E_INVALID;
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (n == 0) return GPRT_OK;
+  std::vector<void*> tmp;
+  gprt_ray* dr = nullptr;
+  gprt_hit* dh = nullptr;
+  if (dev_alloc(ctx, tmp, &dr, n) || dev_alloc(ctx, tmp, &dh, n)) {
+    free_all(tmp);
+    return GPRT_E_OOM;
+  }
+  cudaError_t e = cudaMemcpyAsync(dr, rays, (size_t)n * sizeof(gprt_ray), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    launch_intersect(s->dev, dr, n, flags == GPRT_ANY, dh, s->d_err, ctx->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, (size_t)n * sizeof(gprt_hit), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  free_all(tmp);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "intersect_host");
+  int err = 0;
+  cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (err) return fail(ctx, GPRT_E_BOUND, "device bound exceeded: traversal stack");
+  return GPRT_OK;
+}
+
+int gprt_traversal_counts(gprt_scene* s, const gprt_ray* rays, uint32_t n, uint32_t flags, uint64_t* node_visits,
+                          uint64_t* box_tests, uint64_t* prim_tests) {
+  if (!s || (n && !rays)) return GPRT_E_INVALID;
+  uint64_t a, b, c;
+  count_traversal(s->host, rays, n, flags == GPRT_ANY, a, b, c);
+  if (node_visits) *node_visits = a;
+  if (box_tests) *box_tests = b;
+  if (prim_tests) *prim_tests = c;
+  return GPRT_OK;
+}
+
+int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
+  if (!s || !desc || !out) return GPRT_E_INVALID;
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  *out = nullptr;
+  if (desc->integrator > GPRT_INTEGRATOR_BDPT) return fail(ctx, GPRT_E_INVALID, "unknown integrator");
+  auto j = std::make_unique<gprt_job>();
+  j->scene = s;
+  j->desc = *desc;
+  gprt_job_desc& d = j->desc;
+  // DefaultProgressiveConfig (progressive.go:38-46)
+  if (d.tile_size == 0) d.tile_size = 64;
+  if (d.initial_samples == 0) d.initial_samples = 1;
+  if (d.max_samples_per_pixel == 0) d.max_samples_per_pixel = 50;
+  if (d.max_passes == 0) d.max_passes = 7;
+  if (d.block_size == 0) d.block_size = 128;
+  if (d.block_size % 32 || d.block_size > 1024) return fail(ctx, GPRT_E_INVALID, "block_size must be a multiple of 32, <= 1024");
+  uint32_t npix = s->host.sampling.width * s->host.sampling.height;
+  if (d.chunk_paths == 0) {
+    uint64_t want = (uint64_t)npix * std::max(1u, d.max_samples_per_pixel);
+    d.chunk_paths = (uint32_t)std::min<uint64_t>(want, d.integrator == GPRT_INTEGRATOR_BDPT ? (1u << 20) : (1u << 22));
+  }
+  if (d.max_samples_per_pixel < d.initial_samples) return fail(ctx, GPRT_E_INVALID, "max samples below initial samples");
+  if (d.integrator == GPRT_INTEGRATOR_BDPT && s->host.sampling.max_depth > 17)
+    return fail(ctx, GPRT_E_INVALID, "BDPT supports max_depth <= 17 (subpath vertices are kept per thread)");
+  DevFilm& f = j->film;
+  f.width = (int)s->host.sampling.width;
+  f.height = (int)s->host.sampling.height;
+  int rc = 0;
+  rc |= dev_alloc(ctx, j->buffers, &f.rgbl, npix);
+  rc |= dev_alloc(ctx, j->buffers, &f.lum2, npix);
+  rc |= dev_alloc(ctx, j->buffers, &f.count, npix);
+  rc |= dev_alloc(ctx, j->buffers, &f.splat, npix);
+  rc |= dev_alloc(ctx, j->buffers, &j->d_pix_list, npix);
+  rc |= dev_alloc(ctx, j->buffers, &j->d_active, 1);
+  if (rc) {
+    free_all(j->buffers);
+    return GPRT_E_OOM;
+  }
+  if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    free_all(j->buffers);
+    return fail(ctx, GPRT_E_DEVICE, "stream creation failed");
+  }
+  cudaEventCreate(&j->ev0);
+  cudaEventCreate(&j->ev1);
+  cudaMemsetAsync(f.rgbl, 0, (size_t)npix * sizeof(float4), j->stream);
+  cudaMemsetAsync(f.lum2, 0, (size_t)npix * sizeof(float), j->stream);
+  cudaMemsetAsync(f.count, 0, (size_t)npix * sizeof(uint32_t), j->stream);
+  cudaMemsetAsync(f.splat, 0, (size_t)npix * sizeof(float4), j->stream);
+  cudaError_t e = cudaStreamSynchronize(j->stream);
+  if (e != cudaSuccess) {
+    free_all(j->buffers);
+    return cuda_fail(ctx, e, "job init");
+  }
+  j->uniform_count = 0;
+  *out = j.release();
+  return GPRT_OK;
+}
+
+int gprt_job_destroy(gprt_job* j) {
+  if (!j) return GPRT_E_INVALID;
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(j->stream);
+  free_all(j->buffers);
+  cudaStreamDestroy(j->stream);
+  cudaEventDestroy(j->ev0);
+  cudaEventDestroy(j->ev1);
+  for (auto& t : j->timed) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  delete j;
+  return GPRT_OK;
+}
+
+int gprt_job_add_samples(gprt_job* j, uint32_t spp) {
+  if (!j) return GPRT_E_INVALID;
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  uint32_t npix = (uint32_t)j->film.width * j->film.height;
+  int rc = add_samples(j, spp, npix, nullptr);
+  if (rc) return rc;
+  if (j->uniform_count >= 0) j->uniform_count += spp;
+  return GPRT_OK;
+}
+
+int gprt_job_sync(gprt_job* j) {
+  if (!j) return GPRT_E_INVALID;
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  return check_device_errors(j);
+}
+
+int gprt_job_render_pass(gprt_job* j, uint32_t pass, gprt_render_stats* stats) {
+  if (!j || pass == 0) return GPRT_E_INVALID;
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const gprt_sampling_desc& sd = j->scene->host.sampling;
+  uint32_t target = samples_for_pass(j->desc, pass);
+  uint32_t npix = (uint32_t)j->film.width * j->film.height;
+  // shouldStopSampling minimum (tile_renderer.go:79)
+  uint32_t min_s = std::max(1u, (uint32_t)((double)target * sd.adaptive_min_samples));
+  cudaEventRecord(j->ev0, j->stream);
+  int rc = GPRT_OK;
+  uint64_t before_launches = j->launches;
+  if (j->uniform_count >= 0 && (uint64_t)j->uniform_count < min_s) {
+    // nobody can stop before min_s: one bulk wave
+    rc = add_samples(j, min_s - (uint32_t)j->uniform_count, npix, nullptr);
+    if (rc) return rc;
+    j->uniform_count = min_s;
+  }
+  if (min_s < target || j->uniform_count < 0 || (uint64_t)j->uniform_count < target) {
+    // adaptive rounds of one sample per still-active pixel
+    for (;;) {
+      CK(ctx, cudaMemsetAsync(j->d_active, 0, sizeof(uint32_t), j->stream));
+      launch_active_pixels(j->film, target, min_s, (float)sd.adaptive_threshold, j->d_pix_list, j->d_active,
+                           j->stream);
+      j->launches++;
+      uint32_t active = 0;
+      CK(ctx, cudaMemcpyAsync(&active, j->d_active, 4, cudaMemcpyDeviceToHost, j->stream));
+      CK(ctx, cudaStreamSynchronize(j->stream));
+      if (active == 0) break;
+      if (active != npix) j->uniform_count = -1;
+      rc = add_samples(j, 1, active, j->d_pix_list);
+      if (rc) return rc;
+      if (j->uniform_count >= 0) j->uniform_count++;
+    }
+  }
+  cudaEventRecord(j->ev1, j->stream);
+  rc = check_device_errors(j);
+  if (rc) return rc;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, j->ev0, j->ev1);
+  // assembleCurrentImage statistics (progressive.go:395-431)
+  gprt_render_stats st{};
+  st.total_pixels = npix;
+  st.max_samples = target;
+  st.pass_number = pass;
+  st.pass_ms = ms;
+  if (j->uniform_count >= 0) {
+    st.total_samples = (uint64_t)j->uniform_count * npix;
+    st.min_samples = std::min<uint32_t>(j->desc.max_samples_per_pixel, (uint32_t)j->uniform_count);
+    st.max_samples_used = (uint32_t)j->uniform_count;
+  } else {
+    std::vector<uint32_t> cnt(npix);
+    CK(ctx, cudaMemcpy(cnt.data(), j->film.count, (size_t)npix * 4, cudaMemcpyDeviceToHost));
+    st.min_samples = j->desc.max_samples_per_pixel;
+    for (uint32_t c : cnt) {
+      st.total_samples += c;
+      st.min_samples = std::min(st.min_samples, c);
+      st.max_samples_used = std::max(st.max_samples_used, c);
+    }
+  }
+  st.average_samples = (double)st.total_samples / (double)st.total_pixels;
+  (void)before_launches;
+  j->last = st;
+  if (stats) *stats = st;
+  return GPRT_OK;
+}
+
+int gprt_job_read_film(gprt_job* j, float* rgb_sum, float* lum_sum, float* lum2_sum, uint32_t* count) {
+  if (!j) return GPRT_E_INVALID;
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  uint32_t npix = (uint32_t)j->film.width * j->film.height;
+  CK(ctx, cudaStreamSynchronize(j->stream));
+  if (rgb_sum || lum_sum) {
+    std::vector<float4> v(npix);
+    CK(ctx, cudaMemcpy(v.data(), j->film.rgbl, (size_t)npix * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < npix; i++) {
+      if (rgb_sum) {
+        rgb_sum[3 * i] = v[i].x;
+        rgb_sum[3 * i + 1] = v[i].y;
+        rgb_sum[3 * i + 2] = v[i].z;
+      }
+      if (lum_sum) lum_sum[i] = v[i].w;
+    }
+  }
+  if (lum2_sum) CK(ctx, cudaMemcpy(lum2_sum, j->film.lum2, (size_t)npix * 4, cudaMemcpyDeviceToHost));
+  if (count) CK(ctx, cudaMemcpy(count, j->film.count, (size_t)npix * 4, cudaMemcpyDeviceToHost));
+  return GPRT_OK;
+}
+
+static int read_via_device(gprt_job* j, size_t bytes, int kind, void* out) {
+  gprt_ctx* ctx = j->scene->ctx;
+  std::vector<void*> tmp;
+  uint8_t* d = nullptr;
+  if (dev_alloc(ctx, tmp, &d, bytes)) return GPRT_E_OOM;
+  if (kind == 0) launch_resolve_rgba8(j->film, d, j->stream);
+  else launch_image_mean(j->film, reinterpret_cast<float*>(d), j->stream);
+  j->launches++;
+  cudaError_t e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, j->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->stream);
+  free_all(tmp);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "image read-back");
+  return GPRT_OK;
+}
+
+int gprt_job_read_image(gprt_job* j, float* rgb_mean) {
+  if (!j || !rgb_mean) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
+  cudaSetDevice(j->scene->ctx->device);
+  size_t npix = (size_t)j->film.width * j->film.height;
+  return read_via_device(j, npix * 3 * sizeof(float), 1, rgb_mean);
+}
+
+int gprt_job_read_rgba8(gprt_job* j, uint8_t* rgba) {
+  if (!j || !rgba) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
+  cudaSetDevice(j->scene->ctx->device);
+  size_t npix = (size_t)j->film.width * j->film.height;
+  return read_via_device(j, npix * 4, 0, rgba);
+}
+
+int gprt_job_read_tile(gprt_job* j, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint8_t* rgba) {
+  if (!j || !rgba || x1 <= x0 || y1 <= y0 || x1 > (uint32_t)j->film.width || y1 > (uint32_t)j->film.height)
+    return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
+  size_t npix = (size_t)j->film.width * j->film.height;
+  std::vector<uint8_t> full(npix * 4);
+  int rc = gprt_job_read_rgba8(j, full.data());
+  if (rc) return rc;
+  // extractTileImage leaves pixels with no samples at zero (progressive.go:242-250)
+  std::vector<uint32_t> cnt(npix);
+  if (cudaMemcpy(cnt.data(), j->film.count, npix * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(j->scene->ctx, GPRT_E_DEVICE, "tile read-back");
+  uint32_t tw = x1 - x0;
+  for (uint32_t y = y0; y < y1; y++)
+    for (uint32_t x = x0; x < x1; x++) {
+      size_t si = (size_t)y * j->film.width + x, di = (size_t)(y - y0) * tw + (x - x0);
+      for (int k = 0; k < 4; k++) rgba[4 * di + k] = cnt[si] ? full[4 * si + k] : 0;
+    }
+  return GPRT_OK;
+}
+
+int gprt_job_get_stats(gprt_job* j, gprt_render_stats* stats) {
+  if (!j || !stats) return GPRT_E_INVALID;
+  *stats = j->last;
+  return GPRT_OK;
+}
+
+int gprt_job_launch_count(const gprt_job* j, uint64_t* launches) {
+  if (!j || !launches) return GPRT_E_INVALID;
+  *launches = j->launches;
+  return GPRT_OK;
+}
+
+int gprt_job_get_counters(gprt_job* j, gprt_job_counters* out) {
+  if (!j || !out) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
+  cudaSetDevice(j->scene->ctx->device);
+  int rc = collect_counters(j);
+  if (rc) return rc;
+  *out = j->acc;
+  return GPRT_OK;
+}
+
+int gprt_job_reset_counters(gprt_job* j) {
+  if (!j) return GPRT_E_INVALID;
+  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
+  cudaSetDevice(j->scene->ctx->device);
+  int rc = collect_counters(j);
+  j->acc = gprt_job_counters{};
+  return rc;
+}
+
+int gprt_job_stream(gprt_job* j, void** stream) {
+  if (!j || !stream) return GPRT_E_INVALID;
+  *stream = j->stream;
+  return GPRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,757 @@
+// device.cuh - device-side core of the GB300 rendering path: FP32 vector
+// math, the counter-based sampler, primitive intersection, 4-wide BVH
+// traversal, materials, lights and the camera.  Each routine restates the
+// reference function cited beside it (paths relative to the reference
+// project root) in FP32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "layout.h"
+
+namespace gprt {
+
+// ----------------------------------------------------------------- float3
+__device__ __forceinline__ float3 f3(float a, float b, float c) { return make_float3(a, b, c); }
+__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3& operator+=(float3& a, float3 b) { a = a + b; return a; }
+__device__ __forceinline__ float3& operator*=(float3& a, float3 b) { a = a * b; return a; }
+__device__ __forceinline__ float3& operator*=(float3& a, float s) { a = a * s; return a; }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float length(float3 a) { return sqrtf(dot(a, a)); }
+// core.Vec3.Normalize (pkg/core/vec3.go:97-103): zero stays zero
+__device__ __forceinline__ float3 normalize(float3 a) {
+  float l = length(a);
+  return l == 0.f ? f3(0.f, 0.f, 0.f) : f3(a.x / l, a.y / l, a.z / l);
+}
+// core.Vec3.Luminance (pkg/core/vec3.go:134-136)
+__device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+__device__ __forceinline__ bool is_zero(float3 c) { return c.x == 0.f && c.y == 0.f && c.z == 0.f; }
+
+constexpr float kPi = 3.14159265358979323846f;
+#define kInfF (__int_as_float(0x7f800000))
+
+// ----------------------------------------------------------------- sampler
+// Counter-based sampler: every value is a pure function of (job seed, pixel,
+// sample index, dimension), so a sample renders identically alone, batched
+// with other jobs, or split across chunks.  The hash is the "pcg4d" mix of
+// Jarzynski & Olano, "Hash Functions for GPU Rendering", JCGT 9(3), 2020.
+// It replaces the per-tile math/rand stream of pkg/renderer/progressive.go:444.
+__device__ __forceinline__ uint4 pcg4d(uint4 v) {
+  v.x = v.x * 1664525u + 1013904223u;
+  v.y = v.y * 1664525u + 1013904223u;
+  v.z = v.z * 1664525u + 1013904223u;
+  v.w = v.w * 1664525u + 1013904223u;
+  v.x += v.y * v.w;
+  v.y += v.z * v.x;
+  v.z += v.x * v.y;
+  v.w += v.y * v.z;
+  v.x ^= v.x >> 16;
+  v.y ^= v.y >> 16;
+  v.z ^= v.z >> 16;
+  v.w ^= v.w >> 16;
+  v.x += v.y * v.w;
+  v.y += v.z * v.x;
+  v.z += v.x * v.y;
+  v.w += v.y * v.z;
+  return v;
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// The uniform numbers of one pixel sample, consumed sequentially in the
+// reference's draw order (RandomSampler, pkg/core/sampling.go:17-39): draw k
+// is word k % 4 of pcg4d(pixel ^ seed_lo, sample ^ seed_hi, k / 4, const).
+// `pos` (draws consumed) is all the state a wavefront path carries between
+// kernels.
+struct Rng {
+  uint32_t k0, k1, pos;
+  bool valid;
+  uint4 buf;
+  __device__ __forceinline__ void init(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t start = 0) {
+    k0 = pixel ^ (uint32_t)seed;
+    k1 = sample ^ (uint32_t)(seed >> 32);
+    pos = start;
+    valid = false;
+  }
+  __device__ __forceinline__ float next() {
+    uint32_t lane = pos & 3u;
+    if (lane == 0 || !valid) {
+      buf = pcg4d(make_uint4(k0, k1, pos >> 2, 0x9e3779b9u));
+      valid = true;
+    }
+    uint32_t r = lane == 0 ? buf.x : lane == 1 ? buf.y : lane == 2 ? buf.z : buf.w;
+    pos++;
+    return u01(r);
+  }
+  __device__ __forceinline__ float2 next2() {
+    float a = next();
+    float b = next();
+    return make_float2(a, b);
+  }
+};
+
+// ----------------------------------------------------------------- warps
+// SampleCosineHemisphere (pkg/core/sampling.go:42-67)
+__device__ __forceinline__ float3 sample_cosine_hemisphere(float3 n, float2 s) {
+  float sa, ca;
+  sincosf(2.0f * kPi * s.x, &sa, &ca);
+  float r = sqrtf(s.y);
+  float x = r * ca, y = r * sa, z = sqrtf(1.0f - s.y);
+  float3 nt = fabsf(n.x) > 0.1f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+  float3 t = normalize(cross(nt, n));
+  float3 b = cross(n, t);
+  return t * x + b * y + n * z;
+}
+// SampleOnUnitSphere (sampling.go:97-104)
+__device__ __forceinline__ float3 sample_on_unit_sphere(float2 s) {
+  float z = 1.0f - 2.0f * s.x;
+  float r = sqrtf(fmaxf(0.f, 1.0f - z * z));
+  float sp, cp;
+  sincosf(2.0f * kPi * s.y, &sp, &cp);
+  return f3(r * cp, r * sp, z);
+}
+// SamplePointInUnitDisk, concentric (sampling.go:108-126)
+__device__ __forceinline__ float2 sample_unit_disk(float2 s) {
+  float ux = 2.f * s.x - 1.f, uy = 2.f * s.y - 1.f;
+  if (ux == 0.f && uy == 0.f) return make_float2(0.f, 0.f);
+  float theta, r;
+  if (fabsf(ux) > fabsf(uy)) {
+    r = ux;
+    theta = kPi / 4.f * (uy / ux);
+  } else {
+    r = uy;
+    theta = kPi / 2.f - kPi / 4.f * (ux / uy);
+  }
+  float st, ct;
+  sincosf(theta, &st, &ct);
+  return make_float2(r * ct, r * st);
+}
+// SamplePointInUnitSphere (sampling.go:130-147); pow(x, 1/3) == cbrt(x)
+__device__ __forceinline__ float3 sample_in_unit_sphere(float3 s) {
+  float r = cbrtf(s.x);
+  float sp, cp;
+  sincosf(2.f * kPi * s.y, &sp, &cp);
+  float ct = 2.f * s.z - 1.f;
+  float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+  return f3(r * st * cp, r * st * sp, r * ct);
+}
+
+// ----------------------------------------------------------------- hit record
+struct Hit {
+  float t;
+  uint32_t prim;  // global primitive id or kNoHit
+  float u, v;
+};
+
+// ----------------------------------------------------------------- primitives
+// Triangle.Hit, Moller-Trumbore, epsilon 1e-8 (pkg/geometry/triangle.go:107-175)
+// Triangles are stored as (v0, e1 = v1 - v0, e2 = v2 - v0).
+__device__ __forceinline__ bool hit_triangle(float3 o, float3 d, float4 a, float4 b, float4 c, float tmin,
+                                             float tmax, float& t, float& uu, float& vv) {
+  float3 v0 = f3(a), e1 = f3(b), e2 = f3(c);
+  float3 h = cross(d, e2);
+  float det = dot(e1, h);
+  if (det > -1e-8f && det < 1e-8f) return false;
+  float f = 1.0f / det;
+  float3 s = o - v0;
+  float u = f * dot(s, h);
+  if (u < 0.f || u > 1.f) return false;
+  float3 q = cross(s, e1);
+  float v = f * dot(d, q);
+  if (v < 0.f || u + v > 1.f) return false;
+  float tt = f * dot(e2, q);
+  if (tt < tmin || tt > tmax) return false;
+  t = tt;
+  uu = u;
+  vv = v;
+  return true;
+}
+
+// Quad.Hit (pkg/geometry/quad.go:133-180).  Stored as 5 float4:
+// (corner, D) (u, mat) (v, id) (normal, -) (W, -).
+__device__ __forceinline__ bool hit_quad(float3 o, float3 d, const float4* q, float tmin, float tmax, float& t,
+                                         float& alpha, float& beta) {
+  float4 c = q[0];
+  float3 n = f3(q[3]);
+  float den = dot(d, n);
+  if (fabsf(den) < 1e-8f) return false;
+  float tt = (c.w - dot(o, n)) / den;
+  if (tt < tmin || tt > tmax) return false;
+  float3 p = o + d * tt;
+  float3 hv = p - f3(c);
+  float3 U = f3(q[1]), V = f3(q[2]), W = f3(q[4]);
+  float a = dot(W, cross(hv, V));
+  float b = dot(W, cross(U, hv));
+  if (a < 0.f || a > 1.f || b < 0.f || b > 1.f) return false;
+  t = tt;
+  alpha = a;
+  beta = b;
+  return true;
+}
+
+// Sphere.Hit (pkg/geometry/sphere.go:27-81): nearer root first, then the
+// farther.  The discriminant uses the formulation of Haines, Guenther &
+// Akenine-Moller, "Precision Improvements for Ray/Sphere Intersection"
+// (Ray Tracing Gems, 2019, ch. 7) to keep FP32 usable for radius-1000
+// spheres; the roots are the same quantities as (-halfB -/+ sqrt(D)) / a.
+__device__ __forceinline__ bool hit_sphere(float3 o, float3 d, float4 s, float tmin, float tmax, float& t) {
+  float3 f = o - f3(s);
+  float a = dot(d, d);
+  float halfB = dot(f, d);
+  float3 l = f - d * (halfB / a);
+  float r2 = s.w * s.w;
+  float disc = a * (r2 - dot(l, l));
+  if (disc < 0.f) return false;
+  float sq = sqrtf(disc);
+  float qq = -halfB - copysignf(sq, halfB);
+  float c = dot(f, f) - r2;
+  float t0, t1;
+  if (qq == 0.f) {
+    t0 = t1 = -halfB / a;
+  } else {
+    float ra = c / qq, rb = qq / a;
+    t0 = fminf(ra, rb);
+    t1 = fmaxf(ra, rb);
+  }
+  float root = t0;
+  if (root < tmin || root > tmax) {
+    root = t1;
+    if (root < tmin || root > tmax) return false;
+  }
+  t = root;
+  return true;
+}
+
+// ----------------------------------------------------------------- BVH traversal
+// Replaces geometry.BVH.Hit / hitNode (pkg/geometry/bvh.go:183-239).  The
+// tree is this library's own 4-wide SAH BVH (layout.h) instead of the
+// reference's binary midpoint BVH; the closest hit is the same, except that
+// among candidates at exactly equal t the reference keeps the later one in
+// its depth-first order while this traversal keeps the first one it meets.
+struct TraceStats {
+  uint32_t nodes, boxes, prims;
+};
+
+// `skip` is the primitive the ray leaves from: a ray cannot re-enter the
+// plane of the triangle or quad it starts on, and for the sphere it starts on
+// hits closer than 2e-4 x radius are rounding noise of the FP32 origin.
+template <bool kAnyHit, bool kCount>
+__device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
+                                      Hit& hit, int* err, TraceStats* st = nullptr) {
+  float3 inv;
+  inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+  inv.y = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+  inv.z = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
+  float3 ood = o * inv;
+  const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
+  int stack[kTraceStack];
+  int sp = 0;
+  int node = sc.n_nodes > 0 ? 0 : -1;
+  float best = tmax;
+  bool found = false;
+  hit.prim = kNoHit;
+  while (node >= 0) {
+    const float4* N = sc.nodes + (size_t)node * 8;
+    float4 lx = __ldg(N + 0), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3);
+    float4 lz = __ldg(N + 4), hz = __ldg(N + 5);
+    int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+    int4 mt = __ldg(reinterpret_cast<const int4*>(N + 7));
+    if (kCount) st->nodes++;
+    float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+    float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+    float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+    int cha[4] = {ch.x, ch.y, ch.z, ch.w}, mta[4] = {mt.x, mt.y, mt.z, mt.w};
+    // near-first order of the internal children hit
+    int nint = 0;
+    int ich[4];
+    float itn[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (cha[i] == kEmptyChild) continue;
+      if (kCount) st->boxes++;
+      float x0 = fmaf(nx ? hxa[i] : lxa[i], inv.x, -ood.x), x1 = fmaf(nx ? lxa[i] : hxa[i], inv.x, -ood.x);
+      float y0 = fmaf(ny ? hya[i] : lya[i], inv.y, -ood.y), y1 = fmaf(ny ? lya[i] : hya[i], inv.y, -ood.y);
+      float z0 = fmaf(nz ? hza[i] : lza[i], inv.z, -ood.z), z1 = fmaf(nz ? lza[i] : hza[i], inv.z, -ood.z);
+      float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, tmin));
+      float tf = fminf(fminf(x1, y1), fminf(z1, best));
+      if (tn > tf) continue;
+      if (mta[i] == 0) {
+        // insertion into the near-first list
+        int k = nint++;
+        while (k > 0 && itn[k - 1] > tn) {
+          itn[k] = itn[k - 1];
+          ich[k] = ich[k - 1];
+          k--;
+        }
+        itn[k] = tn;
+        ich[k] = cha[i];
+        continue;
+      }
+      // leaf: intersect its primitives now
+      int cnt = mta[i] & kLeafCountMask;
+      int type = (mta[i] >> kLeafTypeShift) & 3;
+      int first = cha[i];
+      for (int k = 0; k < cnt; k++) {
+        int p = first + k;
+        uint32_t gid = (type == kPrimTriangle ? 0u : type == kPrimQuad ? sc.quad_base : sc.sphere_base) + (uint32_t)p;
+        float t, u = 0.f, v = 0.f;
+        bool h;
+        if (kCount) st->prims++;
+        if (type == kPrimTriangle) {
+          if (gid == skip) continue;
+          const float4* T = sc.tris + (size_t)p * 3;
+          h = hit_triangle(o, d, __ldg(T), __ldg(T + 1), __ldg(T + 2), tmin, best, t, u, v);
+        } else if (type == kPrimQuad) {
+          if (gid == skip) continue;
+          const float4* Q = sc.quads + (size_t)p * 5;
+          float4 qq[5] = {__ldg(Q), __ldg(Q + 1), __ldg(Q + 2), __ldg(Q + 3), __ldg(Q + 4)};
+          h = hit_quad(o, d, qq, tmin, best, t, u, v);
+        } else {
+          float4 S = __ldg(sc.spheres + (size_t)p * 2);
+          float lo = gid == skip ? fmaxf(tmin, 2e-4f * fabsf(S.w)) : tmin;
+          h = hit_sphere(o, d, S, lo, best, t);
+        }
+        if (h) {
+          found = true;
+          best = t;
+          hit.t = t;
+          hit.u = u;
+          hit.v = v;
+          hit.prim = gid;
+          if (kAnyHit) return true;
+        }
+      }
+    }
+    // children that survived the (possibly shrunk) best distance
+    int keep = 0;
+    for (int k = 0; k < nint; k++)
+      if (itn[k] <= best) {
+        itn[keep] = itn[k];
+        ich[keep] = ich[k];
+        keep++;
+      }
+    if (keep > 0) {
+      for (int k = keep - 1; k >= 1; k--) {
+        if (sp < kTraceStack) {
+          stack[sp++] = ich[k];
+        } else {
+          atomicOr(err, kErrStackOverflow);
+        }
+      }
+      node = ich[0];
+    } else {
+      node = sp > 0 ? stack[--sp] : -1;
+    }
+  }
+  return found;
+}
+
+// ----------------------------------------------------------------- surface data
+// Resolves a hit into the SurfaceInteraction of the reference: point,
+// front-face shading normal (SetFaceNormal, pkg/material/interfaces.go:58-65)
+// and material.
+struct Surface {
+  float3 p, n;
+  bool front;
+  int mat;
+};
+
+__device__ __forceinline__ void surface_at(const DevScene& sc, float3 o, float3 d, const Hit& h, Surface& s) {
+  s.p = o + d * h.t;  // Ray.At (pkg/core/vec3.go:216-218)
+  float3 outward;
+  uint32_t p = h.prim;
+  if (p < sc.quad_base) {
+    const float4* T = sc.tris + (size_t)p * 3;
+    float4 a = __ldg(T);
+    float4 nn = __ldg(sc.tri_normals + p);
+    outward = f3(nn);  // precomputed normalize(e1 x e2) (triangle.go:92-99)
+    s.mat = __float_as_int(a.w);
+  } else if (p < sc.sphere_base) {
+    const float4* Q = sc.quads + (size_t)(p - sc.quad_base) * 5;
+    outward = f3(__ldg(Q + 3));
+    s.mat = __float_as_int(__ldg(Q + 1).w);
+  } else {
+    const float4* S = sc.spheres + (size_t)(p - sc.sphere_base) * 2;
+    float4 c = __ldg(S);
+    outward = (s.p - f3(c)) * (1.0f / c.w);  // (p - c) / r (sphere.go:62)
+    s.mat = __float_as_int(__ldg(S + 1).x);
+  }
+  s.front = dot(d, outward) < 0.f;
+  s.n = s.front ? outward : -outward;
+}
+
+// ----------------------------------------------------------------- materials
+__device__ __forceinline__ DevMaterial load_material(const DevScene& sc, int m) { return sc.materials[m]; }
+
+__device__ __forceinline__ float3 reflect(float3 v, float3 n) { return v - n * (2.f * dot(v, n)); }
+// refractVector (pkg/material/dielectric.go:158-163)
+__device__ __forceinline__ float3 refract(float3 uv, float3 n, float eta) {
+  float ct = fminf(-dot(uv, n), 1.0f);
+  float3 perp = (uv + n * ct) * eta;
+  float3 par = n * (-sqrtf(fabsf(1.0f - dot(perp, perp))));
+  return perp + par;
+}
+// Reflectance, Schlick (dielectric.go:166-172); pow(x,5) as a product
+__device__ __forceinline__ float schlick(float c, float ratio) {
+  float r0 = (1.f - ratio) / (1.f + ratio);
+  r0 = r0 * r0;
+  float x = 1.f - c;
+  float x2 = x * x;
+  return r0 + (1.f - r0) * (x2 * x2 * x);
+}
+
+struct Scatter {
+  float3 dir;  // scattered direction (not normalised for metal, like the reference)
+  float3 att;
+  float pdf;   // <= 0: specular (ScatterResult.IsSpecular, interfaces.go:42-45)
+};
+
+// Material.Scatter for Lambertian / Metal / Dielectric / Emissive / Layered
+// (lambertian.go:25-49, metal.go:38-62, dielectric.go:20-59,
+// emissive.go:17-21, layered.go:24-79).  Returns didScatter.
+__device__ __forceinline__ bool scatter_basic(const DevMaterial& m, float3 din, const Surface& s, Rng& rng,
+                                              Scatter& out) {
+  switch (m.kind) {
+    case kMatLambertian: {
+      float2 u = rng.next2();
+      float3 dir = sample_cosine_hemisphere(s.n, u);
+      float c = fmaxf(0.f, dot(normalize(dir), s.n));
+      out.dir = dir;
+      out.att = m.albedo * (1.0f / kPi);
+      out.pdf = c / kPi;
+      return true;
+    }
+    case kMatMetal: {
+      float3 r = reflect(normalize(din), s.n);
+      if (m.fuzz > 0.f) {
+        float a = rng.next(), b = rng.next(), c = rng.next();
+        r = r + sample_in_unit_sphere(f3(a, b, c)) * m.fuzz;
+      }
+      out.dir = r;
+      out.att = m.albedo;
+      out.pdf = 0.f;
+      return dot(r, s.n) > 0.f;
+    }
+    case kMatDielectric: {
+      float ratio = s.front ? 1.0f / m.ior : m.ior;
+      float3 ud = normalize(din);
+      float ct = fminf(-dot(ud, s.n), 1.0f);
+      float st = sqrtf(1.0f - ct * ct);
+      bool cannot = ratio * st > 1.0f;
+      // no sample is drawn under total internal reflection (Go's || short-circuit)
+      if (cannot || schlick(ct, ratio) > rng.next())
+        out.dir = reflect(ud, s.n);
+      else
+        out.dir = refract(ud, s.n, ratio);
+      out.att = f3(1.f, 1.f, 1.f);
+      out.pdf = 0.f;
+      return true;
+    }
+    default:
+      return false;  // Emissive absorbs
+  }
+}
+
+__device__ __forceinline__ bool scatter(const DevScene& sc, const DevMaterial& m, float3 din, const Surface& s,
+                                        Rng& rng, Scatter& out) {
+  if (m.kind != kMatLayered) return scatter_basic(m, din, s, rng, out);
+  DevMaterial mo = load_material(sc, m.outer);
+  Scatter o;
+  if (!scatter_basic(mo, din, s, rng, o)) return false;
+  float3 sd = normalize(o.dir);
+  if (!(dot(sd, s.n) < 0.f)) {
+    out = o;
+    return true;
+  }
+  DevMaterial mi = load_material(sc, m.inner);
+  Scatter in;
+  if (!scatter_basic(mi, sd, s, rng, in)) {
+    out = o;
+    return true;
+  }
+  out.dir = in.dir;
+  out.att = o.att * in.att;
+  out.pdf = in.pdf;
+  return true;
+}
+
+// EvaluateBRDF (lambertian.go:52-62, metal.go:65-77, dielectric.go:62-142,
+// emissive.go:35-38, layered.go:81-95)
+__device__ __forceinline__ float3 brdf_basic(const DevMaterial& m, float3 in, float3 out, const Surface& s,
+                                             bool radiance) {
+  switch (m.kind) {
+    case kMatLambertian:
+      if (dot(out, s.n) <= 0.f) return f3(0.f, 0.f, 0.f);
+      return m.albedo * (1.0f / kPi);
+    case kMatMetal: {
+      float3 r = reflect(-in, s.n);
+      if (length(out - r) < 0.001f) return m.albedo;
+      return f3(0.f, 0.f, 0.f);
+    }
+    case kMatDielectric: {
+      float3 wi = normalize(in), wo = normalize(out), n = normalize(s.n);
+      float wiN = dot(wi, n), woN = dot(wo, n);
+      bool same = (wiN > 0.f) == (woN > 0.f);
+      float ratio = s.front ? 1.0f / m.ior : m.ior;
+      if (!same) {
+        float3 r = reflect(wi, n);
+        if (length(wo - r) < 0.001f) {
+          float f = schlick(fabsf(wiN), ratio);
+          return f3(f, f, f);
+        }
+      } else {
+        float3 rf = refract(wi, n, ratio);
+        if (length(wo - rf) < 0.001f) {
+          float tr = 1.f - schlick(fabsf(wiN), ratio);
+          if (radiance) {
+            float etap = s.front ? m.ior : 1.0f / m.ior;
+            tr /= etap * etap;
+          }
+          return f3(tr, tr, tr);
+        }
+      }
+      return f3(0.f, 0.f, 0.f);
+    }
+    default:
+      return f3(0.f, 0.f, 0.f);
+  }
+}
+
+// isReflectionPath (layered.go:110-119)
+__device__ __forceinline__ bool is_reflection_path(float3 in, float3 out, float3 n) {
+  float3 inc = -in;
+  float3 r = inc - n * (2.f * dot(inc, n));
+  return length(out - r) < 0.1f;
+}
+
+__device__ __forceinline__ float3 brdf(const DevScene& sc, const DevMaterial& m, float3 in, float3 out,
+                                       const Surface& s, bool radiance) {
+  if (m.kind != kMatLayered) return brdf_basic(m, in, out, s, radiance);
+  int sub = is_reflection_path(in, out, s.n) ? m.outer : m.inner;
+  return brdf_basic(load_material(sc, sub), in, out, s, radiance);
+}
+
+// Material.PDF (lambertian.go:65-72, metal.go:80-84, dielectric.go:145-149,
+// emissive.go:41-44, layered.go:98-107).  Returns pdf; sets delta.
+__device__ __forceinline__ float pdf_basic(const DevMaterial& m, float3 out, float3 n, bool& delta) {
+  switch (m.kind) {
+    case kMatLambertian: {
+      delta = false;
+      float c = dot(out, n);
+      return c <= 0.f ? 0.f : c / kPi;
+    }
+    case kMatMetal:
+    case kMatDielectric:
+      delta = true;
+      return 0.f;
+    default:
+      delta = false;
+      return 0.f;
+  }
+}
+__device__ __forceinline__ float mat_pdf(const DevScene& sc, const DevMaterial& m, float3 in, float3 out, float3 n,
+                                         bool& delta) {
+  if (m.kind != kMatLayered) return pdf_basic(m, out, n, delta);
+  int sub = is_reflection_path(in, out, n) ? m.outer : m.inner;
+  bool d;
+  float p = pdf_basic(load_material(sc, sub), out, n, d);
+  delta = false;
+  return p;
+}
+
+// Emissive.Emit with a hit record (emissive.go:24-32): front face only
+__device__ __forceinline__ float3 emitted(const DevMaterial& m, bool front) {
+  if (m.kind != kMatEmissive || !front) return f3(0.f, 0.f, 0.f);
+  return m.emission;
+}
+
+// ----------------------------------------------------------------- lights
+struct LightSample {
+  float3 point, normal, dir;
+  float dist;
+  float3 emission;
+  float pdf;
+};
+
+__device__ __forceinline__ float3 gradient_emission(const DevLight& L, float3 dnorm) {
+  float t = 0.5f * (dnorm.y + 1.0f);
+  return L.b * (1.0f - t) + L.a * t;
+}
+
+// Light.Sample (quad_light.go:36-86, sphere_light.go:29-141,
+// uniform_infinite_light.go:66-80, gradient_infinite_light.go:77-91)
+__device__ __forceinline__ LightSample light_sample(const DevScene& sc, const DevLight& L, float3 p, float3 n,
+                                                    float2 u) {
+  LightSample ls;
+  if (L.kind == kLightQuad) {
+    const float4* Q = sc.quads + (size_t)L.prim * 5;
+    float3 c = f3(__ldg(Q)), U = f3(__ldg(Q + 1)), V = f3(__ldg(Q + 2)), N = f3(__ldg(Q + 3));
+    float3 sp = c + U * u.x + V * u.y;
+    float3 to = sp - p;
+    float dist = length(to);
+    float3 dir = to * (1.0f / dist);
+    float ct = fabsf(dot(N, -dir));
+    ls.point = sp;
+    ls.normal = N;
+    ls.dir = dir;
+    ls.dist = dist;
+    if (ct < 1e-8f) {
+      ls.emission = f3(0.f, 0.f, 0.f);
+      ls.pdf = 0.f;
+      return ls;
+    }
+    ls.pdf = (1.0f / L.area) * dist * dist / ct;
+    ls.emission = dot(dir, N) < 0.f ? L.a : f3(0.f, 0.f, 0.f);
+    return ls;
+  }
+  if (L.kind == kLightSphere) {
+    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float3 c = f3(S);
+    float r = S.w;
+    float3 tc = c - p;
+    float dc = length(tc);
+    bool uniform = dc <= r;
+    if (!uniform) {
+      // sampleVisible (sphere_light.go:81-141)
+      float3 w = normalize(tc);
+      float3 uu = fabsf(w.x) > 0.1f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+      uu = normalize(cross(uu, w));
+      float3 vv = cross(w, uu);
+      float sinMax = r / dc;
+      float cosMax = sqrtf(fmaxf(0.f, 1.f - sinMax * sinMax));
+      float ct = 1.f - u.x * (1.f - cosMax);
+      float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+      float sp2, cp2;
+      sincosf(2.f * kPi * u.y, &sp2, &cp2);
+      float3 dir = uu * (st * cp2) + vv * (st * sp2) + w * ct;
+      float t;
+      if (hit_sphere(p, dir, S, 0.001f, kInfF, t)) {
+        float3 hp = p + dir * t;
+        float3 on = (hp - c) * (1.0f / r);
+        ls.point = hp;
+        ls.normal = dot(dir, on) < 0.f ? on : -on;
+        ls.dir = dir;
+        ls.dist = t;
+        ls.emission = L.a;
+        ls.pdf = 1.0f / (2.f * kPi * (1.f - cosMax));
+        return ls;
+      }
+      uniform = true;  // the reference falls back to uniform sampling
+    }
+    // sampleUniform (sphere_light.go:44-78)
+    float z = 1.f - 2.f * u.x;
+    float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float sp3, cp3;
+    sincosf(2.f * kPi * u.y, &sp3, &cp3);
+    float3 ld = f3(rr * cp3, rr * sp3, z);
+    float3 sp = c + ld * r;
+    float3 dd = sp - p;
+    ls.point = sp;
+    ls.normal = ld;
+    ls.dir = normalize(dd);
+    ls.dist = length(dd);
+    ls.emission = L.a;
+    ls.pdf = 1.0f / (4.f * kPi * r * r);
+    return ls;
+  }
+  // infinite lights: cosine-weighted hemisphere about the shading normal
+  float3 dir = sample_cosine_hemisphere(n, u);
+  ls.point = p + dir * 1e10f;
+  ls.normal = -dir;
+  ls.dir = dir;
+  ls.dist = kInfF;
+  ls.emission = L.kind == kLightUniformInfinite ? L.a : gradient_emission(L, dir);
+  ls.pdf = dot(dir, n) / kPi;
+  return ls;
+}
+
+// Light.PDF (quad_light.go:90-109, sphere_light.go:144-166,
+// uniform_infinite_light.go:83-91, gradient_infinite_light.go:94-102)
+__device__ __forceinline__ float light_pdf(const DevScene& sc, const DevLight& L, float3 p, float3 n, float3 dir) {
+  if (L.kind == kLightQuad) {
+    const float4* Q = sc.quads + (size_t)L.prim * 5;
+    float4 qq[5] = {__ldg(Q), __ldg(Q + 1), __ldg(Q + 2), __ldg(Q + 3), __ldg(Q + 4)};
+    float t, a, b;
+    if (!hit_quad(p, dir, qq, 0.001f, kInfF, t, a, b)) return 0.f;
+    float ct = fabsf(dot(f3(qq[3]), -dir));
+    if (ct < 1e-8f) return 0.f;
+    return (1.0f / L.area) * t * t / ct;
+  }
+  if (L.kind == kLightSphere) {
+    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float t;
+    if (!hit_sphere(p, dir, S, 0.001f, kInfF, t)) return 0.f;
+    float dc = length(f3(S) - p);
+    if (dc <= S.w) return 1.0f / (4.f * kPi * S.w * S.w);
+    float sinMax = S.w / dc;
+    float cosMax = sqrtf(fmaxf(0.f, 1.f - sinMax * sinMax));
+    return 1.0f / (2.f * kPi * (1.f - cosMax));
+  }
+  float c = dot(dir, n);
+  return c <= 0.f ? 0.f : c / kPi;
+}
+
+// CalculateLightPDF (pkg/lights/light_sampling.go:11-26): sum over ALL lights
+__device__ __forceinline__ float total_light_pdf(const DevScene& sc, float3 p, float3 n, float3 dir) {
+  float total = 0.f;
+  for (int i = 0; i < sc.n_lights; i++) {
+    DevLight L = sc.lights[i];
+    total += light_pdf(sc, L, p, n, dir) * L.prob;
+  }
+  return total;
+}
+
+// WeightedLightSampler.SampleLight (weighted_light_sampler.go:82-100)
+__device__ __forceinline__ int pick_light(const DevScene& sc, float u) {
+  float cum = 0.f;
+  for (int i = 0; i < sc.n_lights; i++) {
+    cum += sc.lights[i].prob;
+    if (u <= cum) return i;
+  }
+  return sc.n_lights - 1;
+}
+
+// Sum of Light.Emit over the infinite lights for a missed ray
+// (path_tracing.go:51-59, bdpt.go:214-229)
+__device__ __forceinline__ float3 background(const DevScene& sc, float3 d) {
+  float3 e = f3(0.f, 0.f, 0.f);
+  if (!sc.has_infinite) return e;
+  float3 dn = normalize(d);
+  for (int i = 0; i < sc.n_lights; i++) {
+    DevLight L = sc.lights[i];
+    if (L.kind == kLightUniformInfinite) e += L.a;
+    else if (L.kind == kLightGradientInfinite) e += gradient_emission(L, dn);
+  }
+  return e;
+}
+
+// powerHeuristic (path_tracing.go:225-235)
+__device__ __forceinline__ float power_heuristic(float f, float g) {
+  if (f == 0.f) return 0.f;
+  return (f * f) / (f * f + g * g);
+}
+
+// ----------------------------------------------------------------- camera
+// Camera.GetRay (pkg/geometry/camera.go:173-190)
+__device__ __forceinline__ void camera_ray(const DevCamera& c, int i, int j, float2 lens, float2 jit, float3& o,
+                                           float3& d) {
+  float3 ps = c.pixel00 + c.du * ((float)i + (jit.x - 0.5f)) + c.dv * ((float)j + (jit.y - 0.5f));
+  o = c.center;
+  if (c.has_lens) {
+    float2 p = sample_unit_disk(lens);
+    o = c.center + c.disk_u * p.x + c.disk_v * p.y;
+  }
+  d = normalize(ps - o);
+}
+
+}  // namespace gprt

@@ -1,0 +1,317 @@
+// kernels_pt.cu - raw ray batches and the wavefront path tracer.
+//
+// The reference's PathTracingIntegrator.rayColorRecursive
+// (pkg/integrator/path_tracing.go:35-104) recurses once per bounce and
+// returns emitted + direct + indirect radiance, every level scaled by its
+// Russian-roulette compensation, and the indirect term scaled by the BSDF
+// MIS weight.  Unrolled, the radiance of a sample is a sum over bounces of
+//     W_k * (Le_k + Ld_k)
+// where W_k is the product of the per-level factors of the levels above:
+// rr compensation, and attenuation (specular) or attenuation*cos*w_bsdf/pdf
+// (diffuse).  The wavefront keeps W_k, the Russian-roulette throughput and
+// the gathered radiance per path and advances all paths one bounce per
+// kernel sequence:  extend (closest hit) -> shade -> shadow (any hit).
+#include "device.cuh"
+#include "kernels.h"
+
+namespace gprt {
+
+int launch_grid(uint32_t n, int block, int max_blocks) {
+  uint32_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (max_blocks > 0 && g > (uint32_t)max_blocks) g = (uint32_t)max_blocks;
+  return (int)g;
+}
+
+// ----------------------------------------------------------------- raw batches
+template <bool kAny>
+__global__ void __launch_bounds__(256) k_intersect(DevScene sc, const gprt_ray* __restrict__ rays, uint32_t n,
+                                                   gprt_hit* __restrict__ hits, int* err) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4* r = reinterpret_cast<const float4*>(rays + i);
+    float4 a = __ldg(r), b = __ldg(r + 1);
+    Hit h;
+    bool any = trace<kAny, false>(sc, f3(a), f3(b), a.w, b.w, kNoHit, h, err);
+    float4 out = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), any ? h.u : 0.f,
+                             any ? h.v : 0.f);
+    reinterpret_cast<float4*>(hits)[i] = out;
+  }
+}
+
+void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool any_hit, gprt_hit* hits, int* err,
+                      cudaStream_t st) {
+  if (n == 0) return;
+  int grid = launch_grid(n, 256, 0);
+  if (any_hit) k_intersect<true><<<grid, 256, 0, st>>>(sc, rays, n, hits, err);
+  else k_intersect<false><<<grid, 256, 0, st>>>(sc, rays, n, hits, err);
+}
+
+// ----------------------------------------------------------------- queues
+// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+  unsigned mask = __ballot_sync(__activemask(), want);
+  if (!want) return 0;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// ----------------------------------------------------------------- raygen
+// TileRenderer sample loop + Camera.GetRay (tile_renderer.go:55-59,
+// camera.go:173-190): path p of the chunk is sample `layer` of pixel i.
+__global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch) {
+  uint32_t n = ch.npix * ch.layers;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    uint32_t layer = p / ch.npix, i = p - layer * ch.npix;
+    uint32_t pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
+    uint32_t sample = film.count[pix] + layer;
+    int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
+    Rng rng;
+    rng.init(ch.seed, pix, sample);
+    // Camera.GetRay(i, j, sampler.Get2D(), sampler.Get2D()) (tile_renderer.go:56)
+    float2 lens = rng.next2();
+    float2 jit = rng.next2();
+    float3 o, d;
+    camera_ray(sc.cam, x, y, lens, jit, o, d);
+    P.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
+    P.ray_d[p] = make_float4(d.x, d.y, d.z, 0.f);
+    P.weight[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.pixel[p] = pix;
+    P.sample[p] = sample;
+    P.rng_pos[p] = rng.pos;
+    P.queue[0][p] = p;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.counters[0] = n;
+}
+
+void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
+                      cudaStream_t st) {
+  uint32_t n = ch.npix * ch.layers;
+  k_pt_raygen<<<launch_grid(n, block, 0), block, 0, st>>>(sc, film, P, ch);
+}
+
+// ----------------------------------------------------------------- extend
+// scene.BVH.Hit(ray, 0.001, +Inf) for every live path (path_tracing.go:67)
+// Adds one thread's traversal work to the job's counters (one atomic per warp).
+__device__ __forceinline__ void add_counts(unsigned long long* dst, uint32_t rays, const TraceStats& s) {
+  unsigned long long v[4] = {rays, s.nodes, s.boxes, s.prims};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    unsigned long long x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(dst + k, x);
+  }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_pt_extend(DevScene sc, DevPaths P, int cur) {
+  uint32_t n = P.counters[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[cur ^ 1] = 0;  // next queue and shadow queue start empty
+    P.counters[2] = 0;
+  }
+  const uint32_t* q = P.queue[cur];
+  TraceStats ts{0, 0, 0};
+  uint32_t rays = 0;
+  uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t end = kCount ? ((n + 31) & ~31u) : n;  // whole warps stay in the loop for the reduction
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += stride) {
+    if (i < n) {
+      uint32_t p = q[i];
+      float4 o = P.ray_o[p], d = P.ray_d[p];
+      Hit h;
+      bool any = trace<false, kCount>(sc, f3(o), f3(d), 0.001f, kInfF, __float_as_uint(o.w), h,
+                                      reinterpret_cast<int*>(P.counters + 3), &ts);
+      P.hit[p] = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), h.u, h.v);
+      rays++;
+    }
+  }
+  if (kCount) add_counts(P.stats, rays, ts);
+}
+
+void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
+  if (P.stats) k_pt_extend<true><<<grid, block, 0, st>>>(sc, P, cur);
+  else k_pt_extend<false><<<grid, block, 0, st>>>(sc, P, cur);
+}
+
+// ----------------------------------------------------------------- shade
+// One level of rayColorRecursive (path_tracing.go:35-104) with
+// CalculateDirectLighting (:116-157), CalculateIndirectLighting (:160-189)
+// and ApplyRussianRoulette (:193-220).  The Russian-roulette draw happens
+// first at every level, as in the reference.
+__global__ void __launch_bounds__(256) k_pt_shade(DevScene sc, DevPaths P, ChunkDesc ch, int cur, int bounce) {
+  uint32_t n = P.counters[cur];
+  const uint32_t* q = P.queue[cur];
+  uint32_t* qn = P.queue[cur ^ 1];
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    bool live = i < n;
+    bool cont = false, shadow = false;
+    uint32_t p = 0;
+    float3 sh_o, sh_d, sh_c;
+    float sh_t = 0.f;
+    uint32_t sh_skip = kNoHit;
+    if (live) {
+      p = q[i];
+      float4 o4 = P.ray_o[p], d4 = P.ray_d[p], h4 = P.hit[p];
+      float3 d = f3(d4);
+      float3 W = f3(P.weight[p]), thr = f3(P.thr[p]), L = f3(P.L[p]);
+      Rng rng;
+      rng.init(ch.seed, P.pixel[p], P.sample[p], P.rng_pos[p]);
+      // ApplyRussianRoulette: currentBounce = MaxDepth - depth = bounce
+      float u = rng.next();
+      bool dead = false;
+      if (bounce >= sc.rr_min_bounces) {
+        float surv = fminf(0.95f, fmaxf(0.5f, luminance(thr)));
+        if (u > surv) dead = true;
+        else W *= 1.0f / surv;
+      }
+      if (!dead) {
+        uint32_t prim = __float_as_uint(h4.y);
+        if (prim == kNoHit) {
+          L += W * background(sc, d);  // infinite-light emission of a missed ray
+        } else {
+          Hit h{h4.x, prim, h4.z, h4.w};
+          Surface s;
+          surface_at(sc, f3(o4), d, h, s);
+          DevMaterial m = load_material(sc, s.mat);
+          L += W * emitted(m, s.front);  // getEmittedLight (:108-113)
+          Scatter sc_;
+          if (scatter(sc, m, d, s, rng, sc_)) {
+            if (sc_.pdf <= 0.f) {
+              // calculateSpecularColor (:88-97)
+              W *= sc_.att;
+              thr *= sc_.att;
+              cont = true;
+            } else {
+              // CalculateDirectLighting: light choice + light sample
+              if (sc.n_lights > 0) {
+                int li = pick_light(sc, rng.next());
+                DevLight Lt = sc.lights[li];
+                LightSample ls = light_sample(sc, Lt, s.p, s.n, rng.next2());
+                ls.pdf *= Lt.prob;
+                if (luminance(ls.emission) > 0.f && ls.pdf > 0.f) {
+                  float cosine = dot(ls.dir, s.n);
+                  bool delta;
+                  float mp = mat_pdf(sc, m, d, ls.dir, s.n, delta);
+                  if (cosine > 0.f && !delta) {
+                    float w = power_heuristic(ls.pdf, mp);
+                    float3 f = brdf(sc, m, d, ls.dir, s, true);
+                    float3 c = W * (f * ls.emission) * (cosine * w / ls.pdf);
+                    if (!is_zero(c)) {
+                      shadow = true;
+                      sh_o = s.p;
+                      sh_d = ls.dir;
+                      sh_t = ls.dist - 0.001f;
+                      sh_c = c;
+                      sh_skip = prim;
+                    }
+                  }
+                }
+              }
+              // CalculateIndirectLighting
+              float3 sd = normalize(sc_.dir);
+              float cosine = dot(sd, s.n);
+              if (cosine > 0.f) {
+                float lp = total_light_pdf(sc, s.p, s.n, sd);
+                float w = power_heuristic(sc_.pdf, lp);
+                W *= sc_.att * (cosine * w / sc_.pdf);
+                thr *= sc_.att * (cosine / sc_.pdf);
+                cont = true;
+              }
+            }
+            if (cont) {
+              P.ray_o[p] = make_float4(s.p.x, s.p.y, s.p.z, __uint_as_float(prim));
+              P.ray_d[p] = make_float4(sc_.dir.x, sc_.dir.y, sc_.dir.z, 0.f);
+            }
+          }
+        }
+      }
+      cont = cont && (bounce + 1 < sc.max_depth);
+      P.L[p] = make_float4(L.x, L.y, L.z, 0.f);
+      P.rng_pos[p] = rng.pos;
+      if (cont) {
+        P.weight[p] = make_float4(W.x, W.y, W.z, 0.f);
+        P.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
+      }
+    }
+    uint32_t slot = warp_append(&P.counters[cur ^ 1], cont);
+    if (cont) qn[slot] = p;
+    uint32_t ss = warp_append(&P.counters[2], shadow);
+    if (shadow) {
+      P.sh_o[ss] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_t);
+      P.sh_d[ss] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(sh_skip));
+      P.sh_c[ss] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(p));
+    }
+  }
+}
+
+void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
+                     int grid, cudaStream_t st) {
+  k_pt_shade<<<grid, block, 0, st>>>(sc, P, ch, cur, bounce);
+}
+
+// ----------------------------------------------------------------- shadow
+// scene.BVH.Hit(shadowRay, 0.001, distance - 0.001) used as a boolean
+// (path_tracing.go:143-148): the contribution is kept when nothing is hit.
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_pt_shadow(DevScene sc, DevPaths P) {
+  uint32_t n = P.counters[2];
+  TraceStats ts{0, 0, 0};
+  uint32_t rays = 0;
+  uint32_t end = kCount ? ((n + 31) & ~31u) : n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+    if (i < n) {
+      float4 o = P.sh_o[i], d = P.sh_d[i];
+      Hit h;
+      bool blocked = trace<true, kCount>(sc, f3(o), f3(d), 0.001f, o.w, __float_as_uint(d.w), h,
+                                         reinterpret_cast<int*>(P.counters + 3), &ts);
+      rays++;
+      if (!blocked) {
+        float4 c = P.sh_c[i];
+        uint32_t p = __float_as_uint(c.w);
+        float4 L = P.L[p];
+        P.L[p] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
+      }
+    }
+  }
+  if (kCount) add_counts(P.stats + 4, rays, ts);
+}
+
+void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int block, int grid, cudaStream_t st) {
+  if (P.stats) k_pt_shadow<true><<<grid, block, 0, st>>>(sc, P);
+  else k_pt_shadow<false><<<grid, block, 0, st>>>(sc, P);
+}
+
+// ----------------------------------------------------------------- accumulate
+// PixelStats.AddSample (pkg/renderer/stats.go:41-47), in sample order per pixel
+__global__ void k_accumulate(DevFilm film, DevPaths P, ChunkDesc ch) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ch.npix; i += gridDim.x * blockDim.x) {
+    uint32_t pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
+    float4 acc = film.rgbl[pix];
+    float l2 = film.lum2[pix];
+    for (uint32_t layer = 0; layer < ch.layers; layer++) {
+      float4 c = P.L[layer * ch.npix + i];
+      float lum = luminance(f3(c));
+      acc.x += c.x;
+      acc.y += c.y;
+      acc.z += c.z;
+      acc.w += lum;
+      l2 += lum * lum;
+    }
+    film.rgbl[pix] = acc;
+    film.lum2[pix] = l2;
+    film.count[pix] += ch.layers;
+  }
+}
+
+void launch_accumulate(const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block, cudaStream_t st) {
+  k_accumulate<<<launch_grid(ch.npix, block, 0), block, 0, st>>>(film, P, ch);
+}
+
+}  // namespace gprt

@@ -1,0 +1,82 @@
+// layout.h - device data layout of a flattened scene, shared by the host
+// builder (scene.cpp) and the kernels (device.cuh).
+//
+// HBM layout (all arrays 16-byte aligned, read with 16-byte vector loads):
+//   nodes      8 x float4 (128 B) per 4-wide BVH node:
+//                lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] meta[4]
+//              child = node index (meta == 0), first primitive of a leaf
+//              (meta = count | type << 8), or kEmptyChild.
+//   tris       3 x float4 (48 B): (v0, material) (e1 = v1 - v0, -) (e2 = v2 - v0, -)
+//   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64
+//   quads      5 x float4 (80 B): (corner, D) (u, material) (v, -) (normal, -) (W, -)
+//   spheres    2 x float4 (32 B): (center, radius) (material, -, -, -)
+// Primitive ids: triangles [0, quad_base), quads [quad_base, sphere_base),
+// spheres [sphere_base, n_prims); each type array is in BVH leaf order.
+#pragma once
+
+#include <cstdint>
+#include <vector_types.h>
+#include <vector_functions.h>
+
+namespace gprt {
+
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+constexpr int kEmptyChild = -1;
+constexpr int kLeafCountMask = 0xFF;
+constexpr int kLeafTypeShift = 8;
+constexpr int kPrimTriangle = 0, kPrimQuad = 1, kPrimSphere = 2;
+constexpr int kTraceStack = 64;
+
+// device error bits (status word read by the host after each pass)
+constexpr int kErrStackOverflow = 1;
+constexpr int kErrQueueOverflow = 2;
+
+enum : int { kMatLambertian = 0, kMatMetal = 1, kMatDielectric = 2, kMatEmissive = 3, kMatLayered = 4 };
+enum : int { kLightQuad = 0, kLightSphere = 1, kLightUniformInfinite = 2, kLightGradientInfinite = 3 };
+
+struct DevMaterial {
+  int kind, outer, inner, pad;
+  float3 albedo;
+  float fuzz;
+  float3 emission;
+  float ior;
+};
+
+struct DevLight {
+  int kind;
+  int prim;   // index in the quad or sphere array (area lights)
+  float prob; // light-sampler selection probability
+  float area; // quad area |u x v| (quad_light.go:19-27)
+  float3 a;   // emission (area, uniform) or top colour (gradient)
+  float3 b;   // bottom colour (gradient)
+};
+
+// Camera (pkg/geometry/camera.go:35-67), derived in float64 on the host
+struct DevCamera {
+  float3 center, pixel00, du, dv, disk_u, disk_v;
+  float3 u, v, w, forward;
+  float focus_distance, lens_radius, lens_area, image_plane_area;
+  float viewport_width, viewport_height, cos_total_width;
+  int width, height, has_lens;
+};
+
+struct DevScene {
+  const float4* nodes;
+  const float4* tris;
+  const float4* tri_normals;
+  const float4* quads;
+  const float4* spheres;
+  const DevMaterial* materials;
+  const DevLight* lights;
+  int n_nodes;
+  int n_lights;
+  uint32_t quad_base, sphere_base, n_prims;
+  int has_infinite;
+  float3 world_center;
+  float world_radius;
+  DevCamera cam;
+  int max_depth;
+  int rr_min_bounces;
+};
+
+}  // namespace gprt

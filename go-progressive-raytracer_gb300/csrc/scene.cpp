@@ -1,0 +1,922 @@
+// scene.cpp - flattens a scene description into the device layout of
+// layout.h and builds the 4-wide BVH.
+//
+// The reference builds a binary BVH with a midpoint split and leaves of up to
+// 8 shapes (pkg/geometry/bvh.go:26-160), nested per triangle mesh
+// (pkg/geometry/triangle_mesh.go:123).  This builder flattens every shape to
+// primitives (box -> 6 quads as in pkg/geometry/box.go:41-122, mesh ->
+// triangles) and builds ONE tree with a binned surface-area heuristic, then
+// collapses it to 4-wide nodes for 128-byte node fetches.  Leaves hold one
+// primitive type, so each leaf is a contiguous run of one type array.
+// The world center/radius the infinite lights need (pkg/geometry/bvh.go:39-48)
+// are computed exactly as the reference does, in float64, from the
+// reference's own shape bounding boxes.
+#include "scene.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <memory>
+
+namespace gprt {
+namespace {
+
+struct D3 {
+  double x = 0, y = 0, z = 0;
+  D3() = default;
+  D3(double a, double b, double c) : x(a), y(b), z(c) {}
+  explicit D3(const double* p) : x(p[0]), y(p[1]), z(p[2]) {}
+  D3 operator+(const D3& o) const { return {x + o.x, y + o.y, z + o.z}; }
+  D3 operator-(const D3& o) const { return {x - o.x, y - o.y, z - o.z}; }
+  D3 operator*(double s) const { return {x * s, y * s, z * s}; }
+  double dot(const D3& o) const { return x * o.x + y * o.y + z * o.z; }
+  D3 cross(const D3& o) const { return {y * o.z - z * o.y, z * o.x - x * o.z, x * o.y - y * o.x}; }
+  double len() const { return std::sqrt(dot(*this)); }
+  D3 norm() const {
+    double l = len();
+    return l == 0 ? D3() : D3(x / l, y / l, z / l);
+  }
+  double at(int a) const { return a == 0 ? x : a == 1 ? y : z; }
+  // Vec3.Rotate X -> Y -> Z (pkg/core/vec3.go:162-198)
+  D3 rotate(const D3& r) const {
+    if (r.x == 0 && r.y == 0 && r.z == 0) return *this;
+    D3 v = *this;
+    if (r.x != 0) {
+      double c = std::cos(r.x), s = std::sin(r.x);
+      v = D3(v.x, v.y * c - v.z * s, v.y * s + v.z * c);
+    }
+    if (r.y != 0) {
+      double c = std::cos(r.y), s = std::sin(r.y);
+      v = D3(v.x * c + v.z * s, v.y, -v.x * s + v.z * c);
+    }
+    if (r.z != 0) {
+      double c = std::cos(r.z), s = std::sin(r.z);
+      v = D3(v.x * c - v.y * s, v.x * s + v.y * c, v.z);
+    }
+    return v;
+  }
+};
+
+struct DBox {  // reference AABB semantics (pkg/geometry/aabb.go)
+  D3 mn, mx;
+  DBox unite(const DBox& o) const {
+    return {{std::min(mn.x, o.mn.x), std::min(mn.y, o.mn.y), std::min(mn.z, o.mn.z)},
+            {std::max(mx.x, o.mx.x), std::max(mx.y, o.mx.y), std::max(mx.z, o.mx.z)}};
+  }
+};
+DBox box_of(const D3* p, int n) {
+  DBox b{p[0], p[0]};
+  for (int i = 1; i < n; i++) b = b.unite(DBox{p[i], p[i]});
+  return b;
+}
+// Quad.BoundingBox with the thin box for axis-aligned quads (quad.go:183-210)
+DBox quad_ref_box(const D3& c, const D3& u, const D3& v) {
+  D3 n = u.cross(v).norm();
+  D3 cs[4] = {c, c + u, c + v, c + u + v};
+  const double th = 0.9999, tol = 0.0001, eps = 0.001;
+  int al = 0;
+  if (std::fabs(n.x) > th && std::fabs(n.y) < tol && std::fabs(n.z) < tol) al = 1;
+  else if (std::fabs(n.y) > th && std::fabs(n.x) < tol && std::fabs(n.z) < tol) al = 2;
+  else if (std::fabs(n.z) > th && std::fabs(n.x) < tol && std::fabs(n.y) < tol) al = 3;
+  DBox b = box_of(cs, 4);
+  if (al == 1) { b.mn.x = cs[0].x - eps; b.mx.x = cs[0].x + eps; }
+  if (al == 2) { b.mn.y = cs[0].y - eps; b.mx.y = cs[0].y + eps; }
+  if (al == 3) { b.mn.z = cs[0].z - eps; b.mx.z = cs[0].z + eps; }
+  return b;
+}
+
+// generateFaces (pkg/geometry/box.go:41-122): corner, u, v of the 6 faces
+void box_faces(const D3& center, const D3& size, const D3& rot, D3 corner[6], D3 u[6], D3 v[6], DBox& bbox) {
+  D3 cs[8] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1}};
+  for (auto& p : cs) p = D3(p.x * size.x, p.y * size.y, p.z * size.z).rotate(rot) + center;
+  const int f[6][3] = {{4, 5, 7}, {1, 0, 2}, {5, 1, 6}, {0, 4, 3}, {3, 7, 2}, {4, 0, 5}};
+  for (int i = 0; i < 6; i++) {
+    corner[i] = cs[f[i][0]];
+    u[i] = cs[f[i][1]] - cs[f[i][0]];
+    v[i] = cs[f[i][2]] - cs[f[i][0]];
+  }
+  bbox = box_of(cs, 8);
+}
+
+float4 mk4(const D3& a, float w) { return make_float4((float)a.x, (float)a.y, (float)a.z, w); }
+float i2f(uint32_t i) {
+  float f;
+  std::memcpy(&f, &i, 4);
+  return f;
+}
+
+// ---------------------------------------------------------------- primitives
+struct Prim {
+  int type;
+  uint32_t shape, sub, material;
+  D3 a, b, c;  // tri: v0,v1,v2 ; quad: corner,u,v ; sphere: center,(r,_,_)
+};
+
+struct Ref {
+  float lo[3], hi[3], ct[3];
+  uint32_t prim;
+};
+
+// ---------------------------------------------------------------- SAH BVH2
+struct BNode {
+  float lo[3], hi[3];
+  std::unique_ptr<BNode> l, r;
+  uint32_t begin = 0, count = 0;
+  int type = 0;
+  bool leaf = false;
+  double area() const {
+    double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    if (dx < 0 || dy < 0 || dz < 0) return 0;
+    return 2 * (dx * dy + dy * dz + dz * dx);
+  }
+};
+
+struct Builder {
+  std::vector<Ref>& refs;
+  const std::vector<Prim>& prims;
+  explicit Builder(std::vector<Ref>& r, const std::vector<Prim>& p) : refs(r), prims(p) {}
+
+  static int max_leaf(int type) { return type == kPrimQuad ? 2 : 4; }
+
+  std::unique_ptr<BNode> build(uint32_t b, uint32_t e, int depth) {
+    auto n = std::make_unique<BNode>();
+    for (int k = 0; k < 3; k++) {
+      n->lo[k] = INFINITY;
+      n->hi[k] = -INFINITY;
+    }
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = b; i < e; i++) {
+      const Ref& r = refs[i];
+      for (int k = 0; k < 3; k++) {
+        n->lo[k] = std::min(n->lo[k], r.lo[k]);
+        n->hi[k] = std::max(n->hi[k], r.hi[k]);
+        clo[k] = std::min(clo[k], r.ct[k]);
+        chi[k] = std::max(chi[k], r.ct[k]);
+      }
+    }
+    uint32_t cnt = e - b;
+    int type = prims[refs[b].prim].type;
+    n->type = type;
+    auto make_leaf = [&]() {
+      n->leaf = true;
+      n->begin = b;
+      n->count = cnt;
+      return std::move(n);
+    };
+    if (cnt <= 1) return make_leaf();
+    // binned SAH over the three axes (16 bins)
+    const int B = 16;
+    double best_cost = INFINITY;
+    int best_axis = -1, best_bin = -1;
+    double parent = n->area();
+    for (int ax = 0; ax < 3; ax++) {
+      float ext = chi[ax] - clo[ax];
+      if (!(ext > 0)) continue;
+      float lo[B][3], hi[B][3];
+      uint32_t nb[B] = {0};
+      for (int k = 0; k < B; k++)
+        for (int j = 0; j < 3; j++) {
+          lo[k][j] = INFINITY;
+          hi[k][j] = -INFINITY;
+        }
+      float scale = B / ext;
+      for (uint32_t i = b; i < e; i++) {
+        const Ref& r = refs[i];
+        int k = std::min(B - 1, (int)((r.ct[ax] - clo[ax]) * scale));
+        nb[k]++;
+        for (int j = 0; j < 3; j++) {
+          lo[k][j] = std::min(lo[k][j], r.lo[j]);
+          hi[k][j] = std::max(hi[k][j], r.hi[j]);
+        }
+      }
+      double rarea[B];
+      uint32_t rcount[B];
+      float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
+      uint32_t rc = 0;
+      for (int k = B - 1; k > 0; k--) {
+        rc += nb[k];
+        for (int j = 0; j < 3; j++) {
+          rl[j] = std::min(rl[j], lo[k][j]);
+          rh[j] = std::max(rh[j], hi[k][j]);
+        }
+        double dx = rh[0] - rl[0], dy = rh[1] - rl[1], dz = rh[2] - rl[2];
+        rarea[k] = rc ? 2 * (dx * dy + dy * dz + dz * dx) : 0;
+        rcount[k] = rc;
+      }
+      float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
+      uint32_t lc = 0;
+      for (int k = 0; k < B - 1; k++) {
+        lc += nb[k];
+        for (int j = 0; j < 3; j++) {
+          ll[j] = std::min(ll[j], lo[k][j]);
+          lh[j] = std::max(lh[j], hi[k][j]);
+        }
+        if (lc == 0 || rcount[k + 1] == 0) continue;
+        double dx = lh[0] - ll[0], dy = lh[1] - ll[1], dz = lh[2] - ll[2];
+        double la = 2 * (dx * dy + dy * dz + dz * dx);
+        double cost = la * lc + rarea[k + 1] * rcount[k + 1];
+        if (cost < best_cost) {
+          best_cost = cost;
+          best_axis = ax;
+          best_bin = k;
+        }
+      }
+    }
+    uint32_t mid;
+    if (best_axis < 0) {
+      // all centroids coincide: split by index
+      if (cnt <= (uint32_t)max_leaf(type)) return make_leaf();
+      mid = b + cnt / 2;
+    } else {
+      double split_cost = 1.0 + best_cost / std::max(parent, 1e-30);
+      if (cnt <= (uint32_t)max_leaf(type) && (double)cnt <= split_cost) return make_leaf();
+      float ext = chi[best_axis] - clo[best_axis];
+      float scale = B / ext;
+      auto it = std::partition(refs.begin() + b, refs.begin() + e, [&](const Ref& r) {
+        int k = std::min(B - 1, (int)((r.ct[best_axis] - clo[best_axis]) * scale));
+        return k <= best_bin;
+      });
+      mid = (uint32_t)(it - refs.begin());
+      if (mid == b || mid == e) mid = b + cnt / 2;
+    }
+    if (cnt > 200000 && depth < 10) {
+      auto fl = std::async(std::launch::async, [&, b, mid, depth]() { return build(b, mid, depth + 1); });
+      n->r = build(mid, e, depth + 1);
+      n->l = fl.get();
+    } else {
+      n->l = build(b, mid, depth + 1);
+      n->r = build(mid, e, depth + 1);
+    }
+    return n;
+  }
+};
+
+std::unique_ptr<BNode> join(std::unique_ptr<BNode> a, std::unique_ptr<BNode> b) {
+  if (!a) return b;
+  if (!b) return a;
+  auto n = std::make_unique<BNode>();
+  for (int k = 0; k < 3; k++) {
+    n->lo[k] = std::min(a->lo[k], b->lo[k]);
+    n->hi[k] = std::max(a->hi[k], b->hi[k]);
+  }
+  n->l = std::move(a);
+  n->r = std::move(b);
+  return n;
+}
+
+// ---------------------------------------------------------------- BVH4 emission
+struct Emitter {
+  HostScene& out;
+  const std::vector<Ref>& refs;
+  const std::vector<Prim>& prims;
+  std::vector<uint32_t>& final_index;  // prim -> index in its type array
+  int max_depth = 0;
+
+  void emit_prims(const BNode* leaf, int& first) {
+    for (uint32_t i = 0; i < leaf->count; i++) {
+      uint32_t pid = refs[leaf->begin + i].prim;
+      const Prim& p = prims[pid];
+      if (p.type == kPrimTriangle) {
+        uint32_t idx = (uint32_t)(out.tris.size() / 3);
+        if (i == 0) first = (int)idx;
+        final_index[pid] = idx;
+        D3 e1 = p.b - p.a, e2 = p.c - p.a;
+        out.tris.push_back(mk4(p.a, i2f(p.material)));
+        out.tris.push_back(mk4(e1, 0.f));
+        out.tris.push_back(mk4(e2, 0.f));
+        out.tri_normals.push_back(mk4(e1.cross(e2).norm(), 0.f));  // computeNormal (triangle.go:92-99)
+      } else if (p.type == kPrimQuad) {
+        uint32_t idx = (uint32_t)(out.quads.size() / 5);
+        if (i == 0) first = (int)idx;
+        final_index[pid] = idx;
+        // NewQuad (quad.go:109-130)
+        D3 n = p.b.cross(p.c).norm();
+        double d = n.dot(p.a);
+        D3 w = n * (1.0 / n.dot(p.b.cross(p.c)));
+        out.quads.push_back(mk4(p.a, (float)d));
+        out.quads.push_back(mk4(p.b, i2f(p.material)));
+        out.quads.push_back(mk4(p.c, 0.f));
+        out.quads.push_back(mk4(n, 0.f));
+        out.quads.push_back(mk4(w, 0.f));
+      } else {
+        uint32_t idx = (uint32_t)(out.spheres.size() / 2);
+        if (i == 0) first = (int)idx;
+        final_index[pid] = idx;
+        out.spheres.push_back(mk4(p.a, (float)p.b.x));
+        out.spheres.push_back(make_float4(i2f(p.material), 0.f, 0.f, 0.f));
+      }
+    }
+  }
+
+  int emit(const BNode* n, int depth) {
+    max_depth = std::max(max_depth, depth);
+    int idx = (int)(out.nodes.size() / 8);
+    out.nodes.resize(out.nodes.size() + 8);
+    // gather up to 4 children, opening the largest internal child first
+    std::vector<const BNode*> slots;
+    if (n->leaf) {
+      slots.push_back(n);
+    } else {
+      slots.push_back(n->l.get());
+      slots.push_back(n->r.get());
+      while (slots.size() < 4) {
+        int pick = -1;
+        double best = -1;
+        for (size_t i = 0; i < slots.size(); i++)
+          if (!slots[i]->leaf && slots[i]->area() > best) {
+            best = slots[i]->area();
+            pick = (int)i;
+          }
+        if (pick < 0) break;
+        const BNode* o = slots[pick];
+        slots[pick] = o->l.get();
+        slots.push_back(o->r.get());
+      }
+    }
+    float lo[3][4], hi[3][4];
+    int child[4], meta[4];
+    for (int i = 0; i < 4; i++) {
+      for (int k = 0; k < 3; k++) {
+        lo[k][i] = 1e30f;  // empty slot: inverted box, also flagged kEmptyChild
+        hi[k][i] = -1e30f;
+      }
+      child[i] = kEmptyChild;
+      meta[i] = 0;
+    }
+    for (size_t i = 0; i < slots.size(); i++) {
+      const BNode* s = slots[i];
+      for (int k = 0; k < 3; k++) {
+        lo[k][i] = s->lo[k];
+        hi[k][i] = s->hi[k];
+      }
+      if (s->leaf) {
+        int first = 0;
+        emit_prims(s, first);
+        child[i] = first;
+        meta[i] = (int)s->count | (s->type << kLeafTypeShift);
+      } else {
+        child[i] = emit(s, depth + 1);
+        meta[i] = 0;
+      }
+    }
+    float4* N = &out.nodes[(size_t)idx * 8];
+    N[0] = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+    N[1] = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+    N[2] = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+    N[3] = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+    N[4] = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+    N[5] = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+    N[6] = make_float4(i2f((uint32_t)child[0]), i2f((uint32_t)child[1]), i2f((uint32_t)child[2]), i2f((uint32_t)child[3]));
+    N[7] = make_float4(i2f((uint32_t)meta[0]), i2f((uint32_t)meta[1]), i2f((uint32_t)meta[2]), i2f((uint32_t)meta[3]));
+    return idx;
+  }
+};
+
+// conservative float box of a primitive: rounded outward by a few ulps
+void pad_box(float lo[3], float hi[3], float extent) {
+  for (int k = 0; k < 3; k++) {
+    float pl = 4e-7f * std::fabs(lo[k]) + 1e-7f * extent;
+    float ph = 4e-7f * std::fabs(hi[k]) + 1e-7f * extent;
+    lo[k] -= pl;
+    hi[k] += ph;
+  }
+}
+
+}  // namespace
+
+bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (!d) {
+    err = "null scene description";
+    return false;
+  }
+  if (d->n_shapes && !d->shapes) {
+    err = "shapes pointer is null";
+    return false;
+  }
+  if (d->n_materials && !d->materials) {
+    err = "materials pointer is null";
+    return false;
+  }
+  // materials (NewMetal clamps fuzz, metal.go:18-30)
+  out.materials.resize(d->n_materials);
+  for (uint32_t i = 0; i < d->n_materials; i++) {
+    const gprt_material_desc& m = d->materials[i];
+    DevMaterial dm{};
+    dm.kind = (int)m.kind;
+    if (m.kind > GPRT_MAT_LAYERED) {
+      err = "unknown material kind";
+      return false;
+    }
+    dm.albedo = make_float3((float)m.albedo[0], (float)m.albedo[1], (float)m.albedo[2]);
+    dm.fuzz = (float)std::min(1.0, std::max(0.0, m.fuzz));
+    dm.ior = (float)m.ior;
+    dm.emission = make_float3((float)m.emission[0], (float)m.emission[1], (float)m.emission[2]);
+    if (m.kind == GPRT_MAT_LAYERED) {
+      if (m.outer >= d->n_materials || m.inner >= d->n_materials ||
+          d->materials[m.outer].kind == GPRT_MAT_LAYERED || d->materials[m.inner].kind == GPRT_MAT_LAYERED) {
+        err = "layered material must reference two non-layered materials";
+        return false;
+      }
+      dm.outer = (int)m.outer;
+      dm.inner = (int)m.inner;
+    }
+    out.materials[i] = dm;
+  }
+  auto check_mat = [&](uint32_t m) {
+    if (m >= d->n_materials) {
+      err = "material index out of range";
+      return false;
+    }
+    return true;
+  };
+  // primitives and the reference's world box
+  std::vector<Prim> prims;
+  std::vector<int> shape_quad_prim(d->n_shapes, -1), shape_sphere_prim(d->n_shapes, -1);
+  DBox world{};
+  bool have_world = false;
+  auto add_world = [&](const DBox& b) {
+    world = have_world ? world.unite(b) : b;
+    have_world = true;
+  };
+  for (uint32_t i = 0; i < d->n_shapes; i++) {
+    const gprt_shape_desc& s = d->shapes[i];
+    const double* p = s.p;
+    switch (s.kind) {
+      case GPRT_SHAPE_SPHERE: {
+        if (!check_mat(s.material)) return false;
+        D3 c(p);
+        double r = p[3];
+        shape_sphere_prim[i] = (int)prims.size();
+        prims.push_back({kPrimSphere, i, 0, s.material, c, D3(r, 0, 0), D3()});
+        add_world(DBox{c - D3(r, r, r), c + D3(r, r, r)});  // Sphere.BoundingBox (sphere.go:84-90)
+        break;
+      }
+      case GPRT_SHAPE_QUAD: {
+        if (!check_mat(s.material)) return false;
+        D3 c(p), u(p + 3), v(p + 6);
+        if (u.cross(v).len() == 0) {
+          err = "degenerate quad";
+          return false;
+        }
+        shape_quad_prim[i] = (int)prims.size();
+        prims.push_back({kPrimQuad, i, 0, s.material, c, u, v});
+        add_world(quad_ref_box(c, u, v));
+        break;
+      }
+      case GPRT_SHAPE_BOX: {
+        if (!check_mat(s.material)) return false;
+        D3 corner[6], u[6], v[6];
+        DBox bb;
+        box_faces(D3(p), D3(p + 3), D3(p + 6), corner, u, v, bb);
+        for (int f = 0; f < 6; f++) prims.push_back({kPrimQuad, i, (uint32_t)f, s.material, corner[f], u[f], v[f]});
+        add_world(bb);
+        break;
+      }
+      case GPRT_SHAPE_TRIANGLE: {
+        if (!check_mat(s.material)) return false;
+        D3 a(p), b(p + 3), c(p + 6);
+        prims.push_back({kPrimTriangle, i, 0, s.material, a, b, c});
+        D3 v3[3] = {a, b, c};
+        add_world(box_of(v3, 3));
+        break;
+      }
+      case GPRT_SHAPE_MESH: {
+        if (s.mesh >= d->n_meshes || !d->meshes) {
+          err = "mesh index out of range";
+          return false;
+        }
+        const gprt_mesh_desc& m = d->meshes[s.mesh];
+        if (m.n_triangles == 0) {
+          err = "empty triangle mesh";
+          return false;
+        }
+        if (!m.vertices || !m.indices) {
+          err = "mesh arrays are null";
+          return false;
+        }
+        DBox mb{};
+        for (uint32_t t = 0; t < m.n_triangles; t++) {
+          uint32_t ia = m.indices[3 * t], ib = m.indices[3 * t + 1], ic = m.indices[3 * t + 2];
+          if (ia >= m.n_vertices || ib >= m.n_vertices || ic >= m.n_vertices) {
+            err = "Face index out of bounds";  // NewTriangleMesh panics (triangle_mesh.go:73-76)
+            return false;
+          }
+          uint32_t mat = m.tri_materials ? m.tri_materials[t] : s.material;
+          if (!check_mat(mat)) return false;
+          D3 a(m.vertices + 3 * ia), b(m.vertices + 3 * ib), c(m.vertices + 3 * ic);
+          prims.push_back({kPrimTriangle, i, t, mat, a, b, c});
+          D3 v3[3] = {a, b, c};
+          DBox tb = box_of(v3, 3);
+          mb = t == 0 ? tb : mb.unite(tb);
+        }
+        add_world(mb);
+        break;
+      }
+      default:
+        err = "unknown shape kind";
+        return false;
+    }
+  }
+  if (have_world) {  // NewBVH (bvh.go:39-48)
+    D3 c = (world.mn + world.mx) * 0.5;
+    out.world_center[0] = c.x;
+    out.world_center[1] = c.y;
+    out.world_center[2] = c.z;
+    out.world_radius = (world.mx - c).len();
+  }
+  // scene extent for box padding
+  double ext = 0;
+  if (have_world) ext = std::max({std::fabs(world.mx.x - world.mn.x), std::fabs(world.mx.y - world.mn.y),
+                                  std::fabs(world.mx.z - world.mn.z)});
+  float fext = (float)std::min(ext, 1e30);
+  // references per type
+  std::vector<Ref> refs[3];
+  for (uint32_t k = 0; k < prims.size(); k++) {
+    const Prim& p = prims[k];
+    Ref r;
+    r.prim = k;
+    D3 pts[4];
+    int np;
+    if (p.type == kPrimTriangle) {
+      pts[0] = p.a, pts[1] = p.b, pts[2] = p.c;
+      np = 3;
+    } else if (p.type == kPrimQuad) {
+      pts[0] = p.a, pts[1] = p.a + p.b, pts[2] = p.a + p.c, pts[3] = p.a + p.b + p.c;
+      np = 4;
+    } else {
+      double ar = std::fabs(p.b.x);
+      pts[0] = p.a - D3(ar, ar, ar);
+      pts[1] = p.a + D3(ar, ar, ar);
+      np = 2;
+    }
+    DBox b = box_of(pts, np);
+    r.lo[0] = (float)b.mn.x, r.lo[1] = (float)b.mn.y, r.lo[2] = (float)b.mn.z;
+    r.hi[0] = (float)b.mx.x, r.hi[1] = (float)b.mx.y, r.hi[2] = (float)b.mx.z;
+    pad_box(r.lo, r.hi, fext);
+    for (int j = 0; j < 3; j++) r.ct[j] = 0.5f * (r.lo[j] + r.hi[j]);
+    refs[p.type].push_back(r);
+  }
+  out.n_tris = (uint32_t)refs[kPrimTriangle].size();
+  out.n_quads = (uint32_t)refs[kPrimQuad].size();
+  out.n_spheres = (uint32_t)refs[kPrimSphere].size();
+  std::vector<Ref> all;
+  all.reserve(prims.size());
+  uint32_t off[3];
+  for (int t = 0; t < 3; t++) {
+    off[t] = (uint32_t)all.size();
+    all.insert(all.end(), refs[t].begin(), refs[t].end());
+  }
+  Builder bld(all, prims);
+  std::unique_ptr<BNode> roots[3];
+  for (int t = 0; t < 3; t++)
+    if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
+  std::unique_ptr<BNode> root = join(std::move(roots[0]), join(std::move(roots[1]), std::move(roots[2])));
+  std::vector<uint32_t> final_index(prims.size(), 0);
+  if (root) {
+    Emitter em{out, all, prims, final_index};
+    em.emit(root.get(), 0);
+    out.bvh_depth = em.max_depth;
+  }
+  // primitive id maps
+  out.prim_shape.assign(prims.size(), 0);
+  out.prim_sub.assign(prims.size(), 0);
+  uint32_t base[3] = {0, out.n_tris, out.n_tris + out.n_quads};
+  for (uint32_t k = 0; k < prims.size(); k++) {
+    uint32_t gid = base[prims[k].type] + final_index[k];
+    out.prim_shape[gid] = prims[k].shape;
+    out.prim_sub[gid] = prims[k].sub;
+  }
+  // lights (pkg/scene/scene.go:102-141) and the light sampler
+  // (weighted_light_sampler.go:22-78)
+  double wsum = 0;
+  for (uint32_t i = 0; i < d->n_lights; i++) {
+    if (d->weighted_sampler && d->lights[i].weight < 0) {
+      err = "weights must be non-negative";
+      return false;
+    }
+    wsum += d->lights[i].weight;
+  }
+  out.has_infinite = 0;
+  for (uint32_t i = 0; i < d->n_lights; i++) {
+    const gprt_light_desc& l = d->lights[i];
+    DevLight L{};
+    L.kind = (int)l.kind;
+    L.prob = (float)(d->weighted_sampler ? (wsum == 0 ? 1.0 / d->n_lights : l.weight / wsum) : 1.0 / d->n_lights);
+    auto emission_of = [&](uint32_t mat) {
+      const gprt_material_desc& m = d->materials[mat];
+      return m.kind == GPRT_MAT_EMISSIVE ? make_float3((float)m.emission[0], (float)m.emission[1], (float)m.emission[2])
+                                         : make_float3(0.f, 0.f, 0.f);
+    };
+    switch (l.kind) {
+      case GPRT_LIGHT_QUAD: {
+        if (l.shape >= d->n_shapes || shape_quad_prim[l.shape] < 0) {
+          err = "quad light must reference a quad shape";
+          return false;
+        }
+        int pid = shape_quad_prim[l.shape];
+        L.prim = (int)final_index[pid];
+        L.area = (float)prims[pid].b.cross(prims[pid].c).len();
+        L.a = emission_of(prims[pid].material);
+        break;
+      }
+      case GPRT_LIGHT_SPHERE: {
+        if (l.shape >= d->n_shapes || shape_sphere_prim[l.shape] < 0) {
+          err = "sphere light must reference a sphere shape";
+          return false;
+        }
+        int pid = shape_sphere_prim[l.shape];
+        L.prim = (int)final_index[pid];
+        L.a = emission_of(prims[pid].material);
+        break;
+      }
+      case GPRT_LIGHT_UNIFORM_INFINITE:
+        L.a = make_float3((float)l.color_a[0], (float)l.color_a[1], (float)l.color_a[2]);
+        out.has_infinite = 1;
+        break;
+      case GPRT_LIGHT_GRADIENT_INFINITE:
+        L.a = make_float3((float)l.color_a[0], (float)l.color_a[1], (float)l.color_a[2]);
+        L.b = make_float3((float)l.color_b[0], (float)l.color_b[1], (float)l.color_b[2]);
+        out.has_infinite = 1;
+        break;
+      default:
+        err = "unknown light kind";
+        return false;
+    }
+    out.lights.push_back(L);
+  }
+  // camera (NewCamera, pkg/geometry/camera.go:70-170) in float64
+  const gprt_camera_desc& c = d->camera;
+  if (c.width == 0 || !(c.aspect_ratio > 0)) {
+    err = "camera width and aspect ratio must be positive";
+    return false;
+  }
+  D3 center(c.center), look(c.look_at), up(c.up);
+  D3 w = (center - look).norm();
+  D3 u = w.cross(up).norm();
+  D3 v = w.cross(u);
+  double fd = c.focus_distance > 0 ? c.focus_distance : (center - look).len();
+  double lens_radius = c.aperture / 2;
+  double lens_area = c.aperture == 0 ? 1.0 : M_PI * lens_radius * lens_radius;
+  int width = (int)c.width;
+  int height = (int)((double)width / c.aspect_ratio);
+  double theta = c.vfov_deg * M_PI / 180.0;
+  double h = std::tan(theta / 2.0);
+  double vh = 2.0 * h * fd, vw = vh * c.aspect_ratio;
+  double vh1 = 2.0 * h, vw1 = vh1 * c.aspect_ratio;
+  D3 vu = u * vw, vv = v * vh;
+  D3 du = vu * (1.0 / width), dv = vv * (1.0 / height);
+  D3 ul = center - w * fd - vu * 0.5 - vv * 0.5;
+  D3 p00 = ul + (du + dv) * 0.5;
+  D3 corner = D3(-vw / 2, -vh / 2, -fd).norm();
+  auto f3d = [](const D3& a) { return make_float3((float)a.x, (float)a.y, (float)a.z); };
+  DevCamera& cam = out.cam;
+  cam.center = f3d(center);
+  cam.pixel00 = f3d(p00);
+  cam.du = f3d(du);
+  cam.dv = f3d(dv);
+  cam.disk_u = f3d(u * (c.aperture / 2));
+  cam.disk_v = f3d(v * (c.aperture / 2));
+  cam.u = f3d(u);
+  cam.v = f3d(v);
+  cam.w = f3d(w);
+  cam.forward = f3d((look - center).norm());
+  cam.focus_distance = (float)fd;
+  cam.lens_radius = (float)lens_radius;
+  cam.lens_area = (float)lens_area;
+  cam.image_plane_area = (float)(vw1 * vh1);
+  cam.viewport_width = (float)vw;
+  cam.viewport_height = (float)vh;
+  cam.cos_total_width = (float)corner.dot(D3(0, 0, -1));
+  cam.width = width;
+  cam.height = height;
+  cam.has_lens = (u * (c.aperture / 2)).len() > 0 ? 1 : 0;
+  out.sampling = d->sampling;
+  if (out.sampling.width == 0) out.sampling.width = (uint32_t)width;
+  if (out.sampling.height == 0) out.sampling.height = (uint32_t)height;
+  if (out.sampling.width != (uint32_t)width || out.sampling.height != (uint32_t)height) {
+    err = "sampling width/height must match the camera image size";
+    return false;
+  }
+  if (height <= 0) {
+    err = "image height must be positive";
+    return false;
+  }
+  if (out.sampling.max_depth > 64) {
+    err = "max_depth above 64 is not supported";
+    return false;
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  out.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  return true;
+}
+
+// ---------------------------------------------------------------- invariants
+std::string validate_layout(const HostScene& s) {
+  size_t nn = s.nodes.size() / 8;
+  std::vector<uint8_t> seen[3];
+  seen[kPrimTriangle].assign(s.n_tris, 0);
+  seen[kPrimQuad].assign(s.n_quads, 0);
+  seen[kPrimSphere].assign(s.n_spheres, 0);
+  std::vector<uint8_t> node_seen(nn, 0);
+  auto rd = [](const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; };
+  auto ri = [&](const float4& v, int i) {
+    float f = rd(v, i);
+    int x;
+    std::memcpy(&x, &f, 4);
+    return x;
+  };
+  if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres) ? "primitives without a BVH" : "";
+  std::vector<int> todo = {0};
+  node_seen[0] = 1;
+  while (!todo.empty()) {
+    int n = todo.back();
+    todo.pop_back();
+    const float4* N = &s.nodes[(size_t)n * 8];
+    for (int i = 0; i < 4; i++) {
+      int ch = ri(N[6], i), mt = ri(N[7], i);
+      if (ch == kEmptyChild) continue;
+      float lo[3] = {rd(N[0], i), rd(N[2], i), rd(N[4], i)}, hi[3] = {rd(N[1], i), rd(N[3], i), rd(N[5], i)};
+      auto inside = [&](float x, int k) { return x >= lo[k] && x <= hi[k]; };
+      if (mt == 0) {
+        if (ch <= 0 || (size_t)ch >= nn || node_seen[ch]) return "bad child node index";
+        node_seen[ch] = 1;
+        const float4* C = &s.nodes[(size_t)ch * 8];
+        for (int j = 0; j < 4; j++) {
+          if (ri(C[6], j) == kEmptyChild) continue;
+          if (!(rd(C[0], j) >= lo[0] && rd(C[1], j) <= hi[0] && rd(C[2], j) >= lo[1] && rd(C[3], j) <= hi[1] &&
+                rd(C[4], j) >= lo[2] && rd(C[5], j) <= hi[2]))
+            return "child box not inside its parent slot";
+        }
+        todo.push_back(ch);
+        continue;
+      }
+      int cnt = mt & kLeafCountMask, type = (mt >> kLeafTypeShift) & 3;
+      if (type > kPrimSphere || cnt <= 0) return "bad leaf meta";
+      if (ch < 0 || (size_t)ch + cnt > seen[type].size()) return "leaf range out of bounds";
+      for (int k = 0; k < cnt; k++) {
+        int p = ch + k;
+        if (seen[type][p]++) return "primitive referenced twice";
+        if (type == kPrimTriangle) {
+          const float4* T = &s.tris[(size_t)p * 3];
+          float v[3][3] = {{T[0].x, T[0].y, T[0].z}, {T[0].x + T[1].x, T[0].y + T[1].y, T[0].z + T[1].z},
+                           {T[0].x + T[2].x, T[0].y + T[2].y, T[0].z + T[2].z}};
+          for (auto& q : v)
+            for (int a = 0; a < 3; a++)
+              if (!inside(q[a], a)) return "triangle outside its leaf box";
+        } else if (type == kPrimSphere) {
+          const float4& S = s.spheres[(size_t)p * 2];
+          float r = std::fabs(S.w), c[3] = {S.x, S.y, S.z};
+          for (int a = 0; a < 3; a++)
+            if (!inside(c[a] - r, a) || !inside(c[a] + r, a)) return "sphere outside its leaf box";
+        } else {
+          const float4* Q = &s.quads[(size_t)p * 5];
+          float c[3] = {Q[0].x, Q[0].y, Q[0].z}, u[3] = {Q[1].x, Q[1].y, Q[1].z}, v[3] = {Q[2].x, Q[2].y, Q[2].z};
+          for (int a = 0; a < 3; a++) {
+            float xs[4] = {c[a], c[a] + u[a], c[a] + v[a], c[a] + u[a] + v[a]};
+            for (float x : xs)
+              if (!inside(x, a)) return "quad outside its leaf box";
+          }
+        }
+      }
+    }
+  }
+  for (int t = 0; t < 3; t++)
+    for (uint8_t x : seen[t])
+      if (!x) return "primitive missing from the BVH";
+  for (size_t i = 0; i < nn; i++)
+    if (!node_seen[i]) return "unreachable node";
+  return "";
+}
+
+// ---------------------------------------------------------------- CPU walk
+void count_traversal(const HostScene& s, const gprt_ray* rays, uint32_t n, bool any_hit, uint64_t& nodes,
+                     uint64_t& boxes, uint64_t& prims) {
+  nodes = boxes = prims = 0;
+  if (s.nodes.empty()) return;
+  auto rd = [](const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; };
+  auto ri = [&](const float4& v, int i) {
+    float f = rd(v, i);
+    int x;
+    std::memcpy(&x, &f, 4);
+    return x;
+  };
+  for (uint32_t r = 0; r < n; r++) {
+    const gprt_ray& ray = rays[r];
+    float o[3] = {ray.ox, ray.oy, ray.oz}, d[3] = {ray.dx, ray.dy, ray.dz};
+    float inv[3], ood[3];
+    for (int k = 0; k < 3; k++) {
+      float dd = std::fabs(d[k]) > 1e-20f ? d[k] : std::copysign(1e-20f, d[k]);
+      inv[k] = 1.0f / dd;
+      ood[k] = o[k] * inv[k];
+    }
+    std::vector<int> stack;
+    int node = 0;
+    float best = ray.tmax;
+    bool done = false;
+    while (node >= 0 && !done) {
+      const float4* N = &s.nodes[(size_t)node * 8];
+      nodes++;
+      int ich[4];
+      float itn[4];
+      int nint = 0;
+      for (int i = 0; i < 4 && !done; i++) {
+        int ch = ri(N[6], i), mt = ri(N[7], i);
+        if (ch == kEmptyChild) continue;
+        boxes++;
+        float t0[3], t1[3];
+        for (int k = 0; k < 3; k++) {
+          float lo = rd(N[2 * k], i), hi = rd(N[2 * k + 1], i);
+          bool neg = inv[k] < 0;
+          t0[k] = std::fma(neg ? hi : lo, inv[k], -ood[k]);
+          t1[k] = std::fma(neg ? lo : hi, inv[k], -ood[k]);
+        }
+        float tn = std::max(std::max(t0[0], t0[1]), std::max(t0[2], ray.tmin));
+        float tf = std::min(std::min(t1[0], t1[1]), std::min(t1[2], best));
+        if (tn > tf) continue;
+        if (mt == 0) {
+          int k = nint++;
+          while (k > 0 && itn[k - 1] > tn) {
+            itn[k] = itn[k - 1];
+            ich[k] = ich[k - 1];
+            k--;
+          }
+          itn[k] = tn;
+          ich[k] = ch;
+          continue;
+        }
+        int cnt = mt & kLeafCountMask, type = (mt >> kLeafTypeShift) & 3;
+        for (int k = 0; k < cnt; k++) {
+          prims++;
+          int p = ch + k;
+          // exact distance of the candidate in float64 (counts only)
+          double t = -1;
+          if (type == kPrimTriangle) {
+            const float4* T = &s.tris[(size_t)p * 3];
+            double e1[3] = {T[1].x, T[1].y, T[1].z}, e2[3] = {T[2].x, T[2].y, T[2].z};
+            double sv[3] = {o[0] - T[0].x, o[1] - T[0].y, o[2] - T[0].z};
+            double h[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+            double a = e1[0] * h[0] + e1[1] * h[1] + e1[2] * h[2];
+            if (std::fabs(a) < 1e-8) continue;
+            double f = 1.0 / a, u = f * (sv[0] * h[0] + sv[1] * h[1] + sv[2] * h[2]);
+            if (u < 0 || u > 1) continue;
+            double q[3] = {sv[1] * e1[2] - sv[2] * e1[1], sv[2] * e1[0] - sv[0] * e1[2], sv[0] * e1[1] - sv[1] * e1[0]};
+            double vv = f * (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]);
+            if (vv < 0 || u + vv > 1) continue;
+            t = f * (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]);
+          } else if (type == kPrimQuad) {
+            const float4* Q = &s.quads[(size_t)p * 5];
+            double nn[3] = {Q[3].x, Q[3].y, Q[3].z};
+            double den = d[0] * nn[0] + d[1] * nn[1] + d[2] * nn[2];
+            if (std::fabs(den) < 1e-8) continue;
+            t = (Q[0].w - (o[0] * nn[0] + o[1] * nn[1] + o[2] * nn[2])) / den;
+            double hp[3] = {o[0] + d[0] * t - Q[0].x, o[1] + d[1] * t - Q[0].y, o[2] + d[2] * t - Q[0].z};
+            double U[3] = {Q[1].x, Q[1].y, Q[1].z}, V[3] = {Q[2].x, Q[2].y, Q[2].z}, W[3] = {Q[4].x, Q[4].y, Q[4].z};
+            double hv[3] = {hp[1] * V[2] - hp[2] * V[1], hp[2] * V[0] - hp[0] * V[2], hp[0] * V[1] - hp[1] * V[0]};
+            double uh[3] = {U[1] * hp[2] - U[2] * hp[1], U[2] * hp[0] - U[0] * hp[2], U[0] * hp[1] - U[1] * hp[0]};
+            double al = W[0] * hv[0] + W[1] * hv[1] + W[2] * hv[2], be = W[0] * uh[0] + W[1] * uh[1] + W[2] * uh[2];
+            if (al < 0 || al > 1 || be < 0 || be > 1) continue;
+          } else {
+            const float4& S = s.spheres[(size_t)p * 2];
+            double f[3] = {o[0] - S.x, o[1] - S.y, o[2] - S.z};
+            double a = (double)d[0] * d[0] + (double)d[1] * d[1] + (double)d[2] * d[2];
+            double hb = f[0] * d[0] + f[1] * d[1] + f[2] * d[2];
+            double c = f[0] * f[0] + f[1] * f[1] + f[2] * f[2] - (double)S.w * S.w;
+            double disc = hb * hb - a * c;
+            if (disc < 0) continue;
+            t = (-hb - std::sqrt(disc)) / a;
+            if (t < ray.tmin || t > best) t = (-hb + std::sqrt(disc)) / a;
+          }
+          if (t >= ray.tmin && t <= best) {
+            best = (float)t;
+            if (any_hit) {
+              done = true;
+              break;
+            }
+          }
+        }
+      }
+      if (done) break;
+      int keep = 0;
+      for (int k = 0; k < nint; k++)
+        if (itn[k] <= best) {
+          itn[keep] = itn[k];
+          ich[keep] = ich[k];
+          keep++;
+        }
+      if (keep > 0) {
+        for (int k = keep - 1; k >= 1; k--) stack.push_back(ich[k]);
+        node = ich[0];
+      } else if (!stack.empty()) {
+        node = stack.back();
+        stack.pop_back();
+      } else {
+        node = -1;
+      }
+    }
+  }
+}
+
+}  // namespace gprt

@@ -1,0 +1,12 @@
+"""GB300-native rendering hot path of go-progressive-raytracer.
+
+Host-side mirror of the reference's Go API (scene, integrators, progressive
+renderer) over the C ABI of include/gprt.h, implemented by the CUDA library
+built from ../csrc.
+"""
+from . import _capi as capi  # noqa: F401
+from .renderer import (BDPTIntegrator, Context, GpuScene, PassResult, PathTracingIntegrator,  # noqa: F401
+                       ProgressiveConfig, ProgressiveRaytracer, RenderStats, TileCompletionResult)
+from .scene import (Box, CameraConfig, Dielectric, Emissive, Lambertian, Layered, MaterialTable, Mesh,  # noqa: F401
+                    Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, Triangle, TriangleMesh)
+from . import scenes  # noqa: F401

@@ -206,9 +206,24 @@ typedef struct gprt_job_desc {
   uint32_t max_passes;           /* 0 -> 7 */
   uint32_t chunk_paths;          /* wavefront size; 0 -> automatic */
   uint32_t block_size;           /* threads per block; 0 -> automatic */
-  uint32_t reserved;
+  uint32_t flags;                /* GPRT_JOB_* instrumentation flags */
   uint64_t seed;
 } gprt_job_desc;
+
+#define GPRT_JOB_TIME_KERNELS 1u     /* CUDA-event timing of every kernel launch, per kernel class */
+#define GPRT_JOB_COUNT_TRAVERSAL 2u  /* count BVH node / box / primitive tests (slower kernels) */
+
+/* Instrumentation of a job (GPRT_JOB_* flags), summed since the last reset.
+ * "extend" is the closest-hit traversal of the live paths (one launch per
+ * bounce), "shadow" the any-hit traversal of the shadow rays, "shade" the
+ * material / light sampling kernel. */
+typedef struct gprt_job_counters {
+  uint64_t extend_launches, shade_launches, shadow_launches, other_launches;
+  double extend_ms, shade_ms, shadow_ms, other_ms;
+  uint64_t extend_rays, shadow_rays;
+  uint64_t extend_nodes, extend_boxes, extend_prims;
+  uint64_t shadow_nodes, shadow_boxes, shadow_prims;
+} gprt_job_counters;
 
 /* renderer.RenderStats, pkg/renderer/stats.go:10-17 */
 typedef struct gprt_render_stats {
@@ -248,6 +263,13 @@ int gprt_scene_get_info(const gprt_scene* scene, gprt_scene_info* info);
 /* Maps primitive ids to (index in scene.Shapes, sub-index: box face 0..5 or
  * mesh triangle index, 0 otherwise).  Arrays of n_primitives entries. */
 int gprt_scene_primitive_map(const gprt_scene* scene, uint32_t* shape_index, uint32_t* sub_index);
+
+/* Host-only check of a description: flattens it and builds the BVH on the
+ * host, verifies the layout invariants (every primitive in exactly one leaf,
+ * every box containing what it bounds) and fills `info` (n_nodes, counts,
+ * world center/radius).  Needs no GPU.  Returns GPRT_E_INVALID with a message
+ * in `err` (size err_len) on failure. */
+int gprt_scene_validate(const gprt_scene_desc* desc, gprt_scene_info* info, char* err, size_t err_len);
 
 /* ---- raw ray batches -----------------------------------------------------
  * Replaces geometry.BVH.Hit / hitNode (pkg/geometry/bvh.go:183-239) for a
@@ -294,6 +316,11 @@ int gprt_job_read_tile(gprt_job* job, uint32_t x0, uint32_t y0, uint32_t x1, uin
 int gprt_job_get_stats(gprt_job* job, gprt_render_stats* stats);
 /* Kernel launches issued by this job so far (instrumentation). */
 int gprt_job_launch_count(const gprt_job* job, uint64_t* launches);
+/* Synchronises the job and returns / clears its instrumentation. */
+int gprt_job_get_counters(gprt_job* job, gprt_job_counters* out);
+int gprt_job_reset_counters(gprt_job* job);
+/* The cudaStream_t every kernel of the job is launched on. */
+int gprt_job_stream(gprt_job* job, void** stream);
 
 #ifdef __cplusplus
 }

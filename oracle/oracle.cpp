@@ -163,6 +163,7 @@ struct Renderer {
   int tileSize, initialSamples, maxSamples, maxPasses, threads;
   uint64_t seed;
   int width, height;
+  bool counterStream = false;  // draw from the GPU's per-sample counter stream
   std::vector<PixelStats> stats;
   struct Tile {
     int id, x0, y0, x1, y1;
@@ -216,12 +217,13 @@ struct Renderer {
   void renderTile(Tile& t, int target, std::vector<std::pair<int, Vec3>>& splats) {
     PathTracingIntegrator pt(scene->sampling);
     BDPTIntegrator bd(scene->sampling);
-    Sampler& s = *t.sampler;
     std::vector<SplatRay> sr;
     for (int j = t.y0; j < t.y1; j++)
       for (int i = t.x0; i < t.x1; i++) {
         PixelStats& ps = stats[(size_t)j * width + i];
         while (ps.count < target && !shouldStop(ps, target)) {
+          CounterSampler cs(seed, (uint32_t)(j * width + i), (uint32_t)ps.count);
+          Sampler& s = counterStream ? static_cast<Sampler&>(cs) : static_cast<Sampler&>(*t.sampler);
           Vec2 a = s.get2D();
           Vec2 b = s.get2D();
           Ray ray = scene->camera->getRay(i, j, a, b);
@@ -361,10 +363,15 @@ int oracle_intersect(void* sp, const gprt_ray* rays, uint32_t n, double* t, int3
   return 0;
 }
 
+// counter_stream != 0: every pixel sample draws from CounterSampler(seed,
+// pixel, sample index), the GPU library's stream; otherwise a PCG32 stream
+// per 64x64 tile.
 void* oracle_renderer_create(void* sp, int integrator, int tile, int initial, int maxSpp, int passes,
-                             uint64_t seed, int threads) {
-  return new Renderer(static_cast<Scene*>(sp), integrator, tile > 0 ? tile : 64,
-                      initial > 0 ? initial : 1, maxSpp, passes > 0 ? passes : 1, seed, threads);
+                             uint64_t seed, int threads, int counter_stream) {
+  Renderer* r = new Renderer(static_cast<Scene*>(sp), integrator, tile > 0 ? tile : 64,
+                             initial > 0 ? initial : 1, maxSpp, passes > 0 ? passes : 1, seed, threads);
+  r->counterStream = counter_stream != 0;
+  return r;
 }
 void oracle_renderer_destroy(void* r) { delete static_cast<Renderer*>(r); }
 

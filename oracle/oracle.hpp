@@ -158,6 +158,53 @@ struct PcgSampler : Sampler {
   }
 };
 
+// The GPU library's counter-based stream for one pixel sample: draw k is
+// word k % 4 of pcg4d(pixel ^ seed_lo, sample ^ seed_hi, k / 4, 0x9e3779b9)
+// (Jarzynski & Olano, "Hash Functions for GPU Rendering", JCGT 9(3), 2020),
+// mapped to [0,1) as (word >> 8) * 2^-24.  Consumed in the reference's order,
+// it gives the oracle the same inputs as the GPU for per-sample comparisons.
+struct CounterSampler : Sampler {
+  uint32_t k0, k1, pos = 0;
+  uint32_t buf[4] = {0, 0, 0, 0};
+  CounterSampler(uint64_t seed, uint32_t pixel, uint32_t sample)
+      : k0(pixel ^ (uint32_t)seed), k1(sample ^ (uint32_t)(seed >> 32)) {}
+  static void pcg4d(uint32_t v[4]) {
+    for (int i = 0; i < 4; i++) v[i] = v[i] * 1664525u + 1013904223u;
+    v[0] += v[1] * v[3];
+    v[1] += v[2] * v[0];
+    v[2] += v[0] * v[1];
+    v[3] += v[1] * v[2];
+    for (int i = 0; i < 4; i++) v[i] ^= v[i] >> 16;
+    v[0] += v[1] * v[3];
+    v[1] += v[2] * v[0];
+    v[2] += v[0] * v[1];
+    v[3] += v[1] * v[2];
+  }
+  double get1D() override {
+    uint32_t lane = pos & 3u;
+    if (lane == 0) {
+      buf[0] = k0;
+      buf[1] = k1;
+      buf[2] = pos >> 2;
+      buf[3] = 0x9e3779b9u;
+      pcg4d(buf);
+    }
+    pos++;
+    return (double)(buf[lane] >> 8) * (1.0 / 16777216.0);
+  }
+  Vec2 get2D() override {
+    double a = get1D();
+    double b = get1D();
+    return {a, b};
+  }
+  Vec3 get3D() override {
+    double a = get1D();
+    double b = get1D();
+    double c = get1D();
+    return {a, b, c};
+  }
+};
+
 // TestSampler (pkg/integrator/bdpt_test.go:17-74): predetermined values.
 struct ListSampler : Sampler {
   std::vector<double> v1;
