@@ -5,6 +5,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -14,12 +15,15 @@
 
 using namespace gprt;
 
+// Ownership: a context owns its scenes and a scene owns its jobs, so
+// destroying a parent releases whatever children the caller did not.
 struct gprt_ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
   std::recursive_mutex mu;
   std::string err;
+  std::set<gprt_scene*> scenes;
 };
 
 struct gprt_scene {
@@ -29,6 +33,7 @@ struct gprt_scene {
   std::vector<void*> buffers;
   size_t bytes = 0;
   int* d_err = nullptr;
+  std::set<gprt_job*> jobs;
 };
 
 struct gprt_job {
@@ -323,9 +328,13 @@ int gprt_ctx_create(int device, gprt_ctx** out) {
 
 int gprt_ctx_destroy(gprt_ctx* ctx) {
   if (!ctx) return GPRT_E_INVALID;
-  cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  cudaStreamDestroy(ctx->stream);
+  {
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    while (!ctx->scenes.empty()) gprt_scene_destroy(*ctx->scenes.begin());
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
   delete ctx;
   return GPRT_OK;
 }
@@ -376,16 +385,20 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
     free_all(s->buffers);
     return cuda_fail(ctx, e, "scene upload");
   }
+  ctx->scenes.insert(s.get());
   *out = s.release();
   return GPRT_OK;
 }
 
 int gprt_scene_destroy(gprt_scene* s) {
   if (!s) return GPRT_E_INVALID;
-  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
-  cudaSetDevice(s->ctx->device);
-  cudaStreamSynchronize(s->ctx->stream);
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  while (!s->jobs.empty()) gprt_job_destroy(*s->jobs.begin());
+  cudaStreamSynchronize(ctx->stream);
   free_all(s->buffers);
+  ctx->scenes.erase(s);
   delete s;
   return GPRT_OK;
 }
@@ -548,6 +561,7 @@ int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
     return cuda_fail(ctx, e, "job init");
   }
   j->uniform_count = 0;
+  s->jobs.insert(j.get());
   *out = j.release();
   return GPRT_OK;
 }
@@ -566,6 +580,7 @@ int gprt_job_destroy(gprt_job* j) {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
   }
+  j->scene->jobs.erase(j);
   delete j;
   return GPRT_OK;
 }

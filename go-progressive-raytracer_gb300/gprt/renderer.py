@@ -82,9 +82,10 @@ class GpuScene:
         return a.value, b.value, c.value
 
     def close(self):
-        if self.h:
+        # a destroyed context has already released its scenes
+        if self.h and self.ctx.h:
             self.ctx.lib.gprt_scene_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -252,9 +253,10 @@ class ProgressiveRaytracer:
         return s.value or 0
 
     def close(self):
-        if self.h:
+        # a destroyed scene or context has already released its jobs
+        if self.h and self.scene.h and self.ctx.h:
             self.ctx.lib.gprt_job_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -2,7 +2,7 @@
 
 Each fixture is the oracle's (float64 restatement of the reference) render of
 a small scene at 4096 samples per pixel with its own per-tile PCG streams,
-plus two independent 64-spp oracle renders for the noise floor of the
+plus four independent 64-spp oracle renders for the noise floor of the
 parity rule.  Run from the repository root:
 
     python tests/golden/make_golden.py            # all fixtures
@@ -52,10 +52,9 @@ def make(name, threads=None):
     threads = threads or os.cpu_count()
     t0 = time.time()
     ref = client.render(flat, integ, spp=spp, seed=4242, threads=threads)
-    a = client.render(flat, integ, spp=64, seed=101, threads=threads)
-    b = client.render(flat, integ, spp=64, seed=102, threads=threads)
-    np.savez_compressed(os.path.join(HERE, name + ".npz"), ref=ref.astype(np.float32), noise_a=a.astype(np.float32),
-                        noise_b=b.astype(np.float32), spp=spp, integrator=integ)
+    noise = np.stack([client.render(flat, integ, spp=64, seed=101 + k, threads=threads) for k in range(4)])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), ref=ref.astype(np.float32), noise=noise.astype(np.float32),
+                        spp=spp, integrator=integ)
     print("%s: %.1fs, mean %s" % (name, time.time() - t0, ref.mean(axis=(0, 1))))
 
 

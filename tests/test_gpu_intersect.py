@@ -2,8 +2,11 @@
 seeded ray batches.
 
 Rule: the hit primitive (index in scene.Shapes, box face / mesh triangle)
-matches exactly, except near-ties where the two distances agree within 1e-5
-relative; hit distances agree within 1e-5 relative.  FP32 rays grazing a
+matches exactly, except near-ties where the two distances agree within the
+distance tolerance; hit distances agree within 1e-5 relative.  An FP32 ray
+origin carries an absolute error of ~6e-8 x |origin|, so the relative error
+is taken against max(t, |origin| / |direction|): for hits far from the
+origin this is the plain 1e-5 relative rule.  FP32 rays grazing a
 silhouette may legitimately hit in one precision and miss in the other; at
 most 1e-4 of the rays may disagree that way.
 """
@@ -51,7 +54,9 @@ def _compare(ctx, oracle, scene, rays, any_hit=False):
     both = g_hit & o_hit
     pid = hits["prim"][both]
     same = (shape_map[pid] == shape_o[both]) & (sub_map[pid] == sub_o[both])
-    rel = np.abs(hits["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), 1e-30)
+    o_len = np.linalg.norm(rays[both, 0:3].astype(np.float64), axis=1) / np.linalg.norm(
+        rays[both, 4:7].astype(np.float64), axis=1)
+    rel = np.abs(hits["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), np.maximum(o_len, 1e-30))
     near_tie = rel <= REL
     bad_prim = ~same & ~near_tie
     return dict(n=len(rays), hit_disagree=int((g_hit != o_hit).sum()), bad_prim=int(bad_prim.sum()),
@@ -76,6 +81,7 @@ def test_closest_hit_parity(ctx, oracle, name):
     rays = np.concatenate([_camera_rays(scene, 20000, 1), _rays_in_bounds(o.world_center, min(o.world_radius, 600.0),
                                                                           20000, 2)])
     r = _compare(ctx, oracle, scene, rays)
+    print(name, r)
     assert r["hits"] > 1000
     assert r["hit_disagree"] <= max(2, 1e-4 * r["n"]), r
     assert r["bad_prim"] <= max(2, 1e-4 * r["n"]), r
@@ -91,6 +97,7 @@ def test_icosphere_raw_batch_parity(ctx, oracle):
     mesh = scene.shapes[0].mesh
     rays = scenes.ray_batch(mesh.vertices, mesh.faces, 1 << 16, seed=13, width=256)
     r = _compare(ctx, oracle, scene, rays)
+    print("icosphere7 raw batch", r)
     assert r["hits"] > 30000
     assert r["hit_disagree"] <= max(3, 1e-4 * r["n"]), r
     assert r["bad_prim"] <= max(3, 1e-4 * r["n"]), r
@@ -130,7 +137,7 @@ def test_edge_cases(ctx, oracle):
             assert h["prim"][i] == gprt.capi.NO_HIT
         else:
             assert shape_map[h["prim"][i]] == shape_o[i]
-            assert abs(h["t"][i] - t_o[i]) <= 1e-5 * abs(t_o[i])
+            assert abs(h["t"][i] - t_o[i]) <= 1e-5 * max(abs(t_o[i]), float(np.linalg.norm(rays[i, :3])))
 
 
 def test_device_pointer_entry_point(ctx):

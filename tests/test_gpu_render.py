@@ -8,8 +8,11 @@ Two comparisons:
   draw).  Tolerance: median relative pixel error <= 1e-4, and at most 2 % of
   pixels off by more than 1e-2 relative (+1e-4 absolute).
 * statistics: against the committed 4096-spp oracle reference
-  (tests/golden), relative RMSE(gpu_N) <= 1.10 x RMSE(oracle_N) and the mean
-  luminance bias is below 3 standard errors.
+  (tests/golden), relative RMSE(gpu_N) <= 1.10 x RMSE(oracle_N), both
+  averaged over 4 seeds and taken on the displayed range (radiance clamped
+  to [0, 1], as the RGBA8 output is; unclamped caustic fireflies make single
+  RMSE estimates swing by +-25 %), and the unclamped mean luminance bias is
+  below 3 standard errors.
 """
 import os
 
@@ -100,6 +103,7 @@ def test_bdpt_same_inputs_parity(ctx, oracle, name):
 
 
 def _rel_rmse(img, ref):
+    img, ref = np.clip(img, 0.0, 1.0), np.clip(ref, 0.0, 1.0)
     return float(np.sqrt(np.mean((img - ref) ** 2)) / np.mean(ref))
 
 
@@ -114,20 +118,18 @@ def test_statistical_parity_against_converged_reference(ctx, name):
                "cornell_boxes_bdpt": lambda: scenes.cornell_boxes_bdpt(width=40, max_depth=8),
                "spheres_pt": lambda: scenes.default_style_scene(17, 48, 48)}[name]
     integ = gprt.BDPTIntegrator() if int(g["integrator"]) == 1 else None
-    floor = 0.5 * (_rel_rmse(g["noise_a"], ref) + _rel_rmse(g["noise_b"], ref))
-    errs, means = [], []
-    for seed in (1, 2):
-        img, _, _ = gpu_render(ctx, factory(), 64, seed=seed, integrator=integ)
-        errs.append(_rel_rmse(img.astype(np.float64), ref))
-        means.append(img.mean())
+    noise = g["noise"].astype(np.float64)
+    floor = float(np.mean([_rel_rmse(x, ref) for x in noise]))
+    imgs = [gpu_render(ctx, factory(), 64, seed=seed, integrator=integ)[0].astype(np.float64) for seed in (1, 2, 3, 4)]
+    errs = [_rel_rmse(x, ref) for x in imgs]
     print(name, "gpu rel rmse", errs, "oracle noise floor", floor)
-    assert max(errs) <= 1.10 * floor, (errs, floor)
-    # mean bias: |mean(gpu) - mean(ref)| < 3 standard errors of the 64-spp mean
+    assert np.mean(errs) <= 1.10 * floor, (errs, floor)
+    # mean bias: |mean(gpu) - mean(ref)| < 3 standard errors of the 4 x 64-spp mean
     lum = lambda im: 0.2126 * im[..., 0] + 0.7152 * im[..., 1] + 0.0722 * im[..., 2]
-    se = np.std(lum(g["noise_a"]) - lum(ref)) / np.sqrt(ref.shape[0] * ref.shape[1])
-    for seed in (1, 2):
-        img, _, _ = gpu_render(ctx, factory(), 64, seed=seed, integrator=integ)
-        assert abs(lum(img).mean() - lum(ref).mean()) < 3 * se + 1e-6
+    se = np.std([lum(x).mean() for x in noise], ddof=1) / 2.0
+    bias = np.mean([lum(x).mean() for x in imgs]) - lum(ref).mean()
+    print(name, "bias", bias, "se", se)
+    assert abs(bias) < 3 * se + 1e-6, (bias, se)
 
 
 def test_pt_deterministic_and_chunk_invariant(ctx):
