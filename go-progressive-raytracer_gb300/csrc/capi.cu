@@ -787,3 +787,135 @@ int gprt_job_stream(gprt_job* j, void** stream) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free rendering (gprt_render_noalloc).
+//
+// For callers that cannot allocate device memory while rendering: code that
+// records a CUDA graph (allocation is not capturable), render loops that fix
+// their device-memory budget at start-up, and hosts that share the GPU with an
+// allocator they do not control.  The wavefront path state of one call lives
+// in the file-scope device array below, sized for GPRT_NOALLOC_MAX_PATHS
+// pixel samples; every GPU that loads the library holds it until exit.
+// In host code the name `g_noalloc_scratch` is a host-side stand-in, not a
+// device address: the address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) and passed to the kernels.
+// Calls share the array and keep the previous call's contents, so every
+// counter is cleared at the start of a call; calls that overlap on the GPU
+// race.
+// ============================================================================
+namespace {
+
+constexpr size_t kNoAllocPaths = GPRT_NOALLOC_MAX_PATHS;
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+// per-path arrays: 9 float4 (ray o/d, weight, thr, L, hit, shadow o/d/c) and
+// 5 uint32 (pixel, sample, rng position, two queues), plus 8 counters
+constexpr size_t kNoAllocF4 = align256(kNoAllocPaths * sizeof(float4));
+constexpr size_t kNoAllocU32 = align256(kNoAllocPaths * sizeof(uint32_t));
+constexpr size_t kNoAllocBytes = 256 + 9 * kNoAllocF4 + 5 * kNoAllocU32;
+
+__device__ __align__(256) static unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device).
+int noalloc_scratch(gprt_ctx* ctx, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+    return fail(ctx, GPRT_E_INVALID, "device ordinal out of range for the allocation-free entry point");
+  if (!g_noalloc_addr[ctx->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[ctx->device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_addr[ctx->device];
+  return GPRT_OK;
+}
+
+// Mean of the `layers` samples of every pixel: the sums of PixelStats.AddSample
+// in sample order, then GetColor (pkg/renderer/stats.go:41-55).
+__global__ void k_noalloc_mean(DevPaths P, uint32_t npix, uint32_t layers, float* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint32_t l = 0; l < layers; l++) {
+      float4 c = P.L[l * npix + i];
+      acc.x += c.x;
+      acc.y += c.y;
+      acc.z += c.z;
+    }
+    float inv = 1.0f / (float)layers;
+    out[3 * i] = acc.x * inv;
+    out[3 * i + 1] = acc.y * inv;
+    out[3 * i + 2] = acc.z * inv;
+  }
+}
+
+// The film counts a fresh job starts from: all zero, read by raygen as the
+// first sample index of every pixel.
+__global__ void k_noalloc_zero(uint32_t* p, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+}
+
+}  // namespace
+
+extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, float* rgb_out, void* stream) {
+  if (!s || !rgb_out || spp == 0) return GPRT_E_INVALID;
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  uint64_t npix = (uint64_t)s->host.sampling.width * s->host.sampling.height;
+  if (npix * spp > kNoAllocPaths)
+    return fail(ctx, GPRT_E_INVALID,
+                "width * height * spp = " + std::to_string(npix * spp) + " exceeds the " +
+                    std::to_string(kNoAllocPaths) +
+                    " pixel samples of the allocation-free entry point; use gprt_job_* or a smaller request");
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch(ctx, &base);
+  if (rc) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  DevPaths P{};
+  P.counters = reinterpret_cast<uint32_t*>(base);
+  unsigned char* f4 = base + 256;
+  float4** f4s[9] = {&P.ray_o, &P.ray_d, &P.weight, &P.thr, &P.L, &P.hit, &P.sh_o, &P.sh_d, &P.sh_c};
+  for (int k = 0; k < 9; k++) *f4s[k] = reinterpret_cast<float4*>(f4 + k * kNoAllocF4);
+  unsigned char* u = f4 + 9 * kNoAllocF4;
+  uint32_t** u32s[5] = {&P.pixel, &P.sample, &P.rng_pos, &P.queue[0], &P.queue[1]};
+  for (int k = 0; k < 5; k++) *u32s[k] = reinterpret_cast<uint32_t*>(u + k * kNoAllocU32);
+  P.stats = nullptr;
+  P.capacity = (uint32_t)kNoAllocPaths;
+  // queue counters and the error word start at zero
+  CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), st));
+  // a film view whose sample counts are zero: the queue[1] array holds them
+  // until the first bounce (raygen reads them before any path is queued there)
+  DevFilm film{};
+  film.width = (int)s->host.sampling.width;
+  film.height = (int)s->host.sampling.height;
+  film.count = P.queue[1];
+  k_noalloc_zero<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(film.count, (uint32_t)npix);
+  ChunkDesc ch{};
+  ch.pix0 = 0;
+  ch.npix = (uint32_t)npix;
+  ch.layers = spp;
+  ch.pix_list = nullptr;
+  ch.seed = seed;
+  ch.bounce_base = 0;
+  const DevScene& sc = s->dev;
+  const int block = 128;
+  int grid = launch_grid((uint32_t)(npix * spp), block, std::max(1, ctx->sm_count * (2048 / block)));
+  launch_pt_raygen(sc, film, P, ch, block, st);
+  int cur = 0;
+  for (int b = 0; b < sc.max_depth; b++) {
+    launch_pt_extend(sc, P, cur, block, grid, st);
+    launch_pt_shade(sc, P, ch, cur, b, block, grid, st);
+    launch_pt_shadow(sc, P, block, grid, st);
+    cur ^= 1;
+  }
+  k_noalloc_mean<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(P, (uint32_t)npix, spp, rgb_out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "allocation-free render launch");
+  return GPRT_OK;
+}

@@ -25,6 +25,7 @@ LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE = rang
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
 CLOSEST, ANY = 0, 1
 NO_HIT = 0xFFFFFFFF
+NOALLOC_MAX_PATHS = 131072  # GPRT_NOALLOC_MAX_PATHS
 
 
 class MaterialDesc(C.Structure):
@@ -142,6 +143,7 @@ SIGNATURES = {
     "gprt_job_get_counters": (C.c_int, [P, C.POINTER(JobCounters)]),
     "gprt_job_reset_counters": (C.c_int, [P]),
     "gprt_job_stream": (C.c_int, [P, PP]),
+    "gprt_render_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint64, P, P]),
 }
 
 _lib = None

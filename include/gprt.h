@@ -322,6 +322,27 @@ int gprt_job_reset_counters(gprt_job* job);
 /* The cudaStream_t every kernel of the job is launched on. */
 int gprt_job_stream(gprt_job* job, void** stream);
 
+/* ---- allocation-free rendering ---------------------------------------------
+ * No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory at render time -- code recording a CUDA graph
+ * (stream capture), render loops whose device-memory budget is fixed at
+ * start-up, and hosts that share the GPU with an allocator they do not own.
+ * It path-traces `spp` samples per pixel of `scene` (samples 0..spp-1 of the
+ * counter-based sampler keyed by `seed`, the same samples a fresh job with
+ * that seed takes) and writes the per-pixel mean radiance, 3 floats per pixel
+ * (PixelStats.GetColor), into the caller's DEVICE buffer `rgb_out`.  The
+ * path state lives in one statically sized device array inside the library
+ * (GPRT_NOALLOC_MAX_PATHS paths, about 22 MB, held by every GPU that loads
+ * the library until the process exits); requests with
+ * width * height * spp > GPRT_NOALLOC_MAX_PATHS return GPRT_E_INVALID.  It
+ * calls no cudaMalloc or cudaFree.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  Asynchronous on
+ * `stream` (NULL = the context stream). */
+#define GPRT_NOALLOC_MAX_PATHS 131072u
+int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* rgb_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
