@@ -214,8 +214,12 @@ def run_gprt(args):
     cnt = cj.counters()
     cj.close()
 
+    # autotuned wavefront size / traversal variants / block size (not timed)
+    tuned, tune = gprt.renderer.autotune(g, spp=SPP, config=gprt.ProgressiveConfig(max_samples_per_pixel=SPP))
     job = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1,
-                                                              flags=capi.JOB_TIME_KERNELS))
+                                                              flags=capi.JOB_TIME_KERNELS | tuned.flags,
+                                                              block_size=tuned.block_size,
+                                                              chunk_paths=tuned.chunk_paths))
     stream = torch.cuda.ExternalStream(job.stream())
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
@@ -311,7 +315,12 @@ def run_gprt(args):
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere, no dataset)",
                 "config": {"workload": WORKLOAD, "samples_per_step": samples_per_step, "triangles": 1310720,
                            "l2": "flushed (512 MB write before every timed step)",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size,
+                                         "simple_extend": bool(tuned.flags & capi.JOB_SIMPLE_EXTEND),
+                                         "simple_shadow": bool(tuned.flags & capi.JOB_SIMPLE_SHADOW),
+                                         "candidates": tune["candidates"], "tuning_pass_ms": tune["best_ms"],
+                                         "default_pass_ms": tune["default_ms"]}},
                 "mrays_per_s": rays_total * world / (ms / 1e3) / 1e6,
                 "roofline": roof, "kernel_ms": kernel_share, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(timed_launches), "clocks": clk,

@@ -145,6 +145,7 @@ int ensure_paths(gprt_job* j) {
   if (j->desc.flags & GPRT_JOB_COUNT_TRAVERSAL) rc |= dev_alloc(ctx, b, &j->d_stats, 8);
   if (rc) return GPRT_E_OOM;
   P.stats = j->d_stats;
+  P.variant = j->desc.flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
   CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), j->stream));
   if (j->d_stats) CK(ctx, cudaMemsetAsync(j->d_stats, 0, 8 * sizeof(unsigned long long), j->stream));
   P.capacity = cap;
@@ -526,7 +527,9 @@ int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
   uint32_t npix = s->host.sampling.width * s->host.sampling.height;
   if (d.chunk_paths == 0) {
     uint64_t want = (uint64_t)npix * std::max(1u, d.max_samples_per_pixel);
-    d.chunk_paths = (uint32_t)std::min<uint64_t>(want, d.integrator == GPRT_INTEGRATOR_BDPT ? (1u << 20) : (1u << 22));
+    // path tracing: up to 2^24 paths per wavefront (about 3 GB of path state);
+    // BDPT keeps its subpaths per thread, 2^20 samples per launch
+    d.chunk_paths = (uint32_t)std::min<uint64_t>(want, d.integrator == GPRT_INTEGRATOR_BDPT ? (1u << 20) : (1u << 24));
   }
   if (d.max_samples_per_pixel < d.initial_samples) return fail(ctx, GPRT_E_INVALID, "max samples below initial samples");
   if (d.integrator == GPRT_INTEGRATOR_BDPT && s->host.sampling.max_depth > 17)
@@ -917,5 +920,90 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
   k_noalloc_mean<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(P, (uint32_t)npix, spp, rgb_out);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "allocation-free render launch");
+  return GPRT_OK;
+}
+
+// ============================================================================
+// Autotuner (gprt_autotune): coordinate descent over the wavefront size, the
+// traversal variants and the block size, timing real tuning passes.
+// ============================================================================
+namespace {
+
+// Device time of `spp` samples per pixel with `d` (after one warm-up pass),
+// or a negative value when the configuration cannot run (e.g. out of memory).
+double time_config(gprt_scene* s, const gprt_job_desc& d, uint32_t spp) {
+  gprt_job* j = nullptr;
+  if (gprt_job_create(s, &d, &j) != GPRT_OK) return -1.0;
+  double ms = -1.0;
+  if (gprt_job_add_samples(j, spp) == GPRT_OK && gprt_job_sync(j) == GPRT_OK) {
+    cudaEventRecord(j->ev0, j->stream);
+    if (gprt_job_add_samples(j, spp) == GPRT_OK) {
+      cudaEventRecord(j->ev1, j->stream);
+      if (gprt_job_sync(j) == GPRT_OK) {
+        float f = 0;
+        cudaEventElapsedTime(&f, j->ev0, j->ev1);
+        ms = f;
+      }
+    }
+  }
+  gprt_job_destroy(j);
+  return ms;
+}
+
+}  // namespace
+
+extern "C" int gprt_autotune(gprt_scene* s, const gprt_job_desc* base, uint32_t spp, gprt_tune_result* out) {
+  if (!s || !base || !out || spp == 0) return GPRT_E_INVALID;
+  gprt_ctx* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  std::memset(out, 0, sizeof(*out));
+  gprt_job_desc d = *base;
+  d.flags &= ~(GPRT_JOB_TIME_KERNELS | GPRT_JOB_COUNT_TRAVERSAL | GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  d.max_samples_per_pixel = std::max(d.max_samples_per_pixel, 2 * spp);
+  uint64_t npix = (uint64_t)s->host.sampling.width * s->host.sampling.height;
+  uint64_t work = npix * spp;
+  if (d.block_size == 0) d.block_size = 128;
+  if (d.chunk_paths == 0) d.chunk_paths = (uint32_t)std::min<uint64_t>(work, 1u << 24);
+  double best = time_config(s, d, spp);
+  if (best < 0) return fail(ctx, GPRT_E_DEVICE, "autotune: the default configuration failed");
+  out->default_ms = best;
+  out->candidates = 1;
+  auto consider = [&](gprt_job_desc c) {
+    double t = time_config(s, c, spp);
+    out->candidates++;
+    if (t >= 0 && t < best) {
+      best = t;
+      d = c;
+    }
+  };
+  if (d.integrator == GPRT_INTEGRATOR_PATH_TRACING) {
+    // wavefront size: whole pass, a quarter, a sixteenth (at least 64 Ki paths)
+    uint32_t base_chunk = d.chunk_paths;
+    for (uint32_t div : {4u, 16u}) {
+      uint32_t c = base_chunk / div;
+      if (c < (1u << 16)) continue;
+      gprt_job_desc cand = d;
+      cand.chunk_paths = c;
+      consider(cand);
+    }
+    // traversal variants
+    uint32_t fl0 = d.flags;
+    for (uint32_t v : {GPRT_JOB_SIMPLE_EXTEND, GPRT_JOB_SIMPLE_SHADOW, GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW}) {
+      gprt_job_desc cand = d;
+      cand.flags = fl0 | v;
+      consider(cand);
+    }
+  }
+  // block size of the non-persistent kernels
+  for (uint32_t b : {64u, 256u}) {
+    gprt_job_desc cand = d;
+    cand.block_size = b;
+    consider(cand);
+  }
+  out->flags = d.flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  out->block_size = d.block_size;
+  out->chunk_paths = d.chunk_paths;
+  out->best_ms = best;
   return GPRT_OK;
 }

@@ -242,118 +242,211 @@ struct TraceStats {
   uint32_t nodes, boxes, prims;
 };
 
-// `skip` is the primitive the ray leaves from: a ray cannot re-enter the
-// plane of the triangle or quad it starts on, and for the sphere it starts on
-// hits closer than 2e-4 x radius are rounding noise of the FP32 origin.
+// State of one ray's traversal; `skip` is the primitive the ray leaves from:
+// a ray cannot re-enter the plane of the triangle or quad it starts on, and
+// for the sphere it starts on hits closer than 2e-4 x radius are rounding
+// noise of the FP32 origin.
+struct Trav {
+  float3 o, d, inv, ood;
+  float tmin, best;
+  uint32_t skip;
+  int node, sp;
+  Hit hit;
+};
+
+__device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
+                                          int n_nodes) {
+  s.o = o;
+  s.d = d;
+  s.inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+  s.inv.y = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+  s.inv.z = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
+  s.ood = o * s.inv;
+  s.tmin = tmin;
+  s.best = tmax;
+  s.skip = skip;
+  s.node = n_nodes > 0 ? 0 : -1;
+  s.sp = 0;
+  s.hit.prim = kNoHit;
+  s.hit.t = -1.f;
+  s.hit.u = s.hit.v = 0.f;
+}
+
+// Visits node s.node: tests its children near-first, intersects the leaves
+// it hits, pushes the farther internal children and moves s.node to the
+// nearest one or to the top of the stack (-1 when the ray is finished).
+// Returns true when an any-hit query found a hit.
+template <bool kAnyHit, bool kCount>
+__device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* stack, int* err, TraceStats* st) {
+  const float4* N = sc.nodes + (size_t)s.node * 8;
+  if (kCount) st->nodes++;
+  int nint = 0;
+  int ich[4];
+  float itn[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    float4 a = __ldg(N + 2 * i);
+    int ref = __float_as_int(a.w);
+    if (ref == kEmptyChild) break;
+    float4 b = __ldg(N + 2 * i + 1);
+    int meta = __float_as_int(b.w);
+    if (kCount) st->boxes++;
+    float x0 = fmaf(s.inv.x < 0.f ? b.x : a.x, s.inv.x, -s.ood.x);
+    float x1 = fmaf(s.inv.x < 0.f ? a.x : b.x, s.inv.x, -s.ood.x);
+    float y0 = fmaf(s.inv.y < 0.f ? b.y : a.y, s.inv.y, -s.ood.y);
+    float y1 = fmaf(s.inv.y < 0.f ? a.y : b.y, s.inv.y, -s.ood.y);
+    float z0 = fmaf(s.inv.z < 0.f ? b.z : a.z, s.inv.z, -s.ood.z);
+    float z1 = fmaf(s.inv.z < 0.f ? a.z : b.z, s.inv.z, -s.ood.z);
+    float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
+    float tf = fminf(fminf(x1, y1), fminf(z1, s.best));
+    if (tn > tf) continue;
+    if (meta == 0) {
+      int k = nint++;
+      while (k > 0 && itn[k - 1] > tn) {
+        itn[k] = itn[k - 1];
+        ich[k] = ich[k - 1];
+        k--;
+      }
+      itn[k] = tn;
+      ich[k] = ref;
+      continue;
+    }
+    int cnt = meta & kLeafCountMask;
+    int type = (meta >> kLeafTypeShift) & 3;
+    for (int k = 0; k < cnt; k++) {
+      int p = ref + k;
+      uint32_t gid = (type == kPrimTriangle ? 0u : type == kPrimQuad ? sc.quad_base : sc.sphere_base) + (uint32_t)p;
+      float t, u = 0.f, v = 0.f;
+      bool h;
+      if (kCount) st->prims++;
+      if (type == kPrimTriangle) {
+        if (gid == s.skip) continue;
+        const float4* T = sc.tris + (size_t)p * 3;
+        h = hit_triangle(s.o, s.d, __ldg(T), __ldg(T + 1), __ldg(T + 2), s.tmin, s.best, t, u, v);
+      } else if (type == kPrimQuad) {
+        if (gid == s.skip) continue;
+        const float4* Q = sc.quads + (size_t)p * 5;
+        float4 qq[5] = {__ldg(Q), __ldg(Q + 1), __ldg(Q + 2), __ldg(Q + 3), __ldg(Q + 4)};
+        h = hit_quad(s.o, s.d, qq, s.tmin, s.best, t, u, v);
+      } else {
+        float4 S = __ldg(sc.spheres + (size_t)p * 2);
+        float lo = gid == s.skip ? fmaxf(s.tmin, 2e-4f * fabsf(S.w)) : s.tmin;
+        h = hit_sphere(s.o, s.d, S, lo, s.best, t);
+      }
+      if (h) {
+        s.best = t;
+        s.hit.t = t;
+        s.hit.u = u;
+        s.hit.v = v;
+        s.hit.prim = gid;
+        if (kAnyHit) {
+          s.node = -1;
+          return true;
+        }
+      }
+    }
+  }
+  // internal children still nearer than the (possibly shrunk) best distance
+  int keep = 0;
+  for (int k = 0; k < nint; k++)
+    if (itn[k] <= s.best) {
+      itn[keep] = itn[k];
+      ich[keep] = ich[k];
+      keep++;
+    }
+  if (keep > 0) {
+    for (int k = keep - 1; k >= 1; k--) {
+      if (s.sp < kTraceStack) stack[s.sp++] = ich[k];
+      else atomicOr(err, kErrStackOverflow);
+    }
+    s.node = ich[0];
+  } else {
+    s.node = s.sp > 0 ? stack[--s.sp] : -1;
+  }
+  return false;
+}
+
+// Whole traversal of one ray (used inside the BDPT and shading kernels).
 template <bool kAnyHit, bool kCount>
 __device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
                                       Hit& hit, int* err, TraceStats* st = nullptr) {
-  float3 inv;
-  inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
-  inv.y = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
-  inv.z = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
-  float3 ood = o * inv;
-  const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
+  Trav s;
+  trav_init(s, o, d, tmin, tmax, skip, sc.n_nodes);
   int stack[kTraceStack];
-  int sp = 0;
-  int node = sc.n_nodes > 0 ? 0 : -1;
-  float best = tmax;
-  bool found = false;
-  hit.prim = kNoHit;
-  while (node >= 0) {
-    const float4* N = sc.nodes + (size_t)node * 8;
-    float4 lx = __ldg(N + 0), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3);
-    float4 lz = __ldg(N + 4), hz = __ldg(N + 5);
-    int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
-    int4 mt = __ldg(reinterpret_cast<const int4*>(N + 7));
-    if (kCount) st->nodes++;
-    float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-    float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-    float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-    int cha[4] = {ch.x, ch.y, ch.z, ch.w}, mta[4] = {mt.x, mt.y, mt.z, mt.w};
-    // near-first order of the internal children hit
-    int nint = 0;
-    int ich[4];
-    float itn[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      if (cha[i] == kEmptyChild) continue;
-      if (kCount) st->boxes++;
-      float x0 = fmaf(nx ? hxa[i] : lxa[i], inv.x, -ood.x), x1 = fmaf(nx ? lxa[i] : hxa[i], inv.x, -ood.x);
-      float y0 = fmaf(ny ? hya[i] : lya[i], inv.y, -ood.y), y1 = fmaf(ny ? lya[i] : hya[i], inv.y, -ood.y);
-      float z0 = fmaf(nz ? hza[i] : lza[i], inv.z, -ood.z), z1 = fmaf(nz ? lza[i] : hza[i], inv.z, -ood.z);
-      float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, tmin));
-      float tf = fminf(fminf(x1, y1), fminf(z1, best));
-      if (tn > tf) continue;
-      if (mta[i] == 0) {
-        // insertion into the near-first list
-        int k = nint++;
-        while (k > 0 && itn[k - 1] > tn) {
-          itn[k] = itn[k - 1];
-          ich[k] = ich[k - 1];
-          k--;
-        }
-        itn[k] = tn;
-        ich[k] = cha[i];
-        continue;
+  while (s.node >= 0) {
+    if (trav_visit<kAnyHit, kCount>(sc, s, stack, err, st)) break;
+  }
+  hit = s.hit;
+  return s.hit.prim != kNoHit;
+}
+
+// Persistent traversal of a batch of rays: every warp loops until its work
+// is exhausted, one node visit per iteration, and lanes whose ray finished
+// take new rays once at least 8 lanes are idle, so warps stay full instead
+// of waiting for their slowest ray.  A warp draws rays from a chunk: with
+// `work` != null, chunks of 64 rays come from that counter (zeroed by the
+// previous kernel on the same stream); otherwise each warp owns a static
+// contiguous range of the batch.  Source provides count(),
+// load(i, o, d, tmin, tmax, skip) and store(i, hit).
+constexpr uint32_t kFetchChunk = 64;
+
+template <bool kAnyHit, bool kCount, class Source>
+__device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src, uint32_t* work, int* err,
+                                                 TraceStats* st, uint32_t* traced) {
+  const uint32_t n = src.count();
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t cur, end;  // the warp's current chunk [cur, end), warp-uniform
+  if (work) {
+    cur = end = 0;
+  } else {
+    uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    cur = (uint32_t)(n * w / nw);
+    end = (uint32_t)(n * (w + 1) / nw);
+  }
+  bool more = true;  // the warp may still draw rays
+  Trav s;
+  int stack[kTraceStack];
+  int ray = -1;
+  for (;;) {
+    bool idle = ray < 0;
+    unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
+    if (more && idle_mask && (__popc(idle_mask) >= 8 || idle_mask == 0xffffffffu)) {
+      if (cur == end && work) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, kFetchChunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        cur = min(base, n);
+        end = min(base + kFetchChunk, n);
       }
-      // leaf: intersect its primitives now
-      int cnt = mta[i] & kLeafCountMask;
-      int type = (mta[i] >> kLeafTypeShift) & 3;
-      int first = cha[i];
-      for (int k = 0; k < cnt; k++) {
-        int p = first + k;
-        uint32_t gid = (type == kPrimTriangle ? 0u : type == kPrimQuad ? sc.quad_base : sc.sphere_base) + (uint32_t)p;
-        float t, u = 0.f, v = 0.f;
-        bool h;
-        if (kCount) st->prims++;
-        if (type == kPrimTriangle) {
-          if (gid == skip) continue;
-          const float4* T = sc.tris + (size_t)p * 3;
-          h = hit_triangle(o, d, __ldg(T), __ldg(T + 1), __ldg(T + 2), tmin, best, t, u, v);
-        } else if (type == kPrimQuad) {
-          if (gid == skip) continue;
-          const float4* Q = sc.quads + (size_t)p * 5;
-          float4 qq[5] = {__ldg(Q), __ldg(Q + 1), __ldg(Q + 2), __ldg(Q + 3), __ldg(Q + 4)};
-          h = hit_quad(o, d, qq, tmin, best, t, u, v);
-        } else {
-          float4 S = __ldg(sc.spheres + (size_t)p * 2);
-          float lo = gid == skip ? fmaxf(tmin, 2e-4f * fabsf(S.w)) : tmin;
-          h = hit_sphere(o, d, S, lo, best, t);
+      if (cur == end) {
+        more = false;
+      } else {
+        uint32_t take = min((uint32_t)__popc(idle_mask), end - cur);
+        uint32_t rank = (uint32_t)__popc(idle_mask & lt);
+        if (idle && rank < take) {
+          float3 o, d;
+          float tmin, tmax;
+          uint32_t skip;
+          uint32_t mine = cur + rank;
+          src.load(mine, o, d, tmin, tmax, skip);
+          trav_init(s, o, d, tmin, tmax, skip, sc.n_nodes);
+          ray = (int)mine;
+          if (kCount) (*traced)++;
         }
-        if (h) {
-          found = true;
-          best = t;
-          hit.t = t;
-          hit.u = u;
-          hit.v = v;
-          hit.prim = gid;
-          if (kAnyHit) return true;
-        }
+        cur += take;
       }
     }
-    // children that survived the (possibly shrunk) best distance
-    int keep = 0;
-    for (int k = 0; k < nint; k++)
-      if (itn[k] <= best) {
-        itn[keep] = itn[k];
-        ich[keep] = ich[k];
-        keep++;
+    if (__ballot_sync(0xffffffffu, ray >= 0) == 0 && !more) break;
+    if (ray >= 0) {
+      if (s.node >= 0) trav_visit<kAnyHit, kCount>(sc, s, stack, err, st);
+      if (s.node < 0) {
+        src.store((uint32_t)ray, s.hit);
+        ray = -1;
       }
-    if (keep > 0) {
-      for (int k = keep - 1; k >= 1; k--) {
-        if (sp < kTraceStack) {
-          stack[sp++] = ich[k];
-        } else {
-          atomicOr(err, kErrStackOverflow);
-        }
-      }
-      node = ich[0];
-    } else {
-      node = sp > 0 ? stack[--sp] : -1;
     }
   }
-  return found;
 }
 
 // ----------------------------------------------------------------- surface data

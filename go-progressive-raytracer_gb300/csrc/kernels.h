@@ -35,6 +35,7 @@ struct DevPaths {
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
+  uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW
 };
 
 // Pixels a chunk covers: `layers` consecutive samples of `npix` pixels,

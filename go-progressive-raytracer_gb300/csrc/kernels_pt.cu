@@ -11,6 +11,8 @@
 // (diffuse).  The wavefront keeps W_k, the Russian-roulette throughput and
 // the gathered radiance per path and advances all paths one bounce per
 // kernel sequence:  extend (closest hit) -> shade -> shadow (any hit).
+#include <algorithm>
+
 #include "device.cuh"
 #include "kernels.h"
 
@@ -24,26 +26,45 @@ int launch_grid(uint32_t n, int block, int max_blocks) {
 }
 
 // ----------------------------------------------------------------- raw batches
-template <bool kAny>
-__global__ void __launch_bounds__(256) k_intersect(DevScene sc, const gprt_ray* __restrict__ rays, uint32_t n,
-                                                   gprt_hit* __restrict__ hits, int* err) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+struct BatchSource {
+  const gprt_ray* rays;
+  gprt_hit* hits;
+  uint32_t n;
+  __device__ uint32_t count() const { return n; }
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
     const float4* r = reinterpret_cast<const float4*>(rays + i);
     float4 a = __ldg(r), b = __ldg(r + 1);
-    Hit h;
-    bool any = trace<kAny, false>(sc, f3(a), f3(b), a.w, b.w, kNoHit, h, err);
-    float4 out = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), any ? h.u : 0.f,
-                             any ? h.v : 0.f);
-    reinterpret_cast<float4*>(hits)[i] = out;
+    o = f3(a);
+    d = f3(b);
+    tmin = a.w;
+    tmax = b.w;
+    skip = kNoHit;
   }
+  __device__ void store(uint32_t i, const Hit& h) const {
+    bool any = h.prim != kNoHit;
+    reinterpret_cast<float4*>(hits)[i] =
+        make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), any ? h.u : 0.f, any ? h.v : 0.f);
+  }
+};
+
+// Batches use static per-warp ranges: calls on different streams share no counter.
+template <bool kAny>
+__global__ void __launch_bounds__(128, 8) k_intersect(DevScene sc, BatchSource src, int* err) {
+  trace_persistent<kAny, false>(sc, src, nullptr, err, nullptr, nullptr);
 }
+
+int persistent_grid(int sm_count, int block) { return std::max(1, sm_count * (1024 / block)); }
 
 void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool any_hit, gprt_hit* hits, int* err,
                       cudaStream_t st) {
   if (n == 0) return;
-  int grid = launch_grid(n, 256, 0);
-  if (any_hit) k_intersect<true><<<grid, 256, 0, st>>>(sc, rays, n, hits, err);
-  else k_intersect<false><<<grid, 256, 0, st>>>(sc, rays, n, hits, err);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = launch_grid((n + 31) / 32 * 32, 128, persistent_grid(sms, 128));
+  BatchSource src{rays, hits, n};
+  if (any_hit) k_intersect<true><<<grid, 128, 0, st>>>(sc, src, err);
+  else k_intersect<false><<<grid, 128, 0, st>>>(sc, src, err);
 }
 
 // ----------------------------------------------------------------- queues
@@ -86,7 +107,11 @@ __global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch)
     P.rng_pos[p] = rng.pos;
     P.queue[0][p] = p;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) P.counters[0] = n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[0] = n;
+    P.counters[4] = 0;  // ray-fetch counters of the first extend and shadow launches
+    P.counters[5] = 0;
+  }
 }
 
 void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
@@ -97,6 +122,7 @@ void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P
 
 // ----------------------------------------------------------------- extend
 // scene.BVH.Hit(ray, 0.001, +Inf) for every live path (path_tracing.go:67)
+
 // Adds one thread's traversal work to the job's counters (one atomic per warp).
 __device__ __forceinline__ void add_counts(unsigned long long* dst, uint32_t rays, const TraceStats& s) {
   unsigned long long v[4] = {rays, s.nodes, s.boxes, s.prims};
@@ -108,35 +134,84 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, uint32_t ray
   }
 }
 
+struct ExtendSource {
+  DevPaths P;
+  const uint32_t* q;
+  uint32_t n;
+  __device__ uint32_t count() const { return n; }
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
+    uint32_t p = q[i];
+    float4 a = P.ray_o[p], b = P.ray_d[p];
+    o = f3(a);
+    d = f3(b);
+    tmin = 0.001f;
+    tmax = kInfF;
+    skip = __float_as_uint(a.w);
+  }
+  __device__ void store(uint32_t i, const Hit& h) const {
+    uint32_t p = q[i];
+    bool any = h.prim != kNoHit;
+    P.hit[p] = make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), h.u, h.v);
+  }
+};
+
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_pt_extend(DevScene sc, DevPaths P, int cur) {
-  uint32_t n = P.counters[cur];
+__global__ void __launch_bounds__(128, 8) k_pt_extend(DevScene sc, DevPaths P, int cur) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[cur ^ 1] = 0;  // next queue and shadow queue start empty
     P.counters[2] = 0;
   }
-  const uint32_t* q = P.queue[cur];
+  ExtendSource src{P, P.queue[cur], P.counters[cur]};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
-  uint32_t stride = gridDim.x * blockDim.x;
-  uint32_t end = kCount ? ((n + 31) & ~31u) : n;  // whole warps stay in the loop for the reduction
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += stride) {
+  trace_persistent<false, kCount>(sc, src, P.counters + 4, reinterpret_cast<int*>(P.counters + 3), &ts, &rays);
+  if (kCount) add_counts(P.stats, rays, ts);
+}
+
+// One ray per thread (grid-stride), the variant GPRT_JOB_SIMPLE_EXTEND selects.
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_pt_extend_simple(DevScene sc, DevPaths P, int cur) {
+  uint32_t n = P.counters[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[cur ^ 1] = 0;
+    P.counters[2] = 0;
+  }
+  ExtendSource src{P, P.queue[cur], n};
+  TraceStats ts{0, 0, 0};
+  uint32_t rays = 0;
+  uint32_t end = kCount ? ((n + 31) & ~31u) : n;  // whole warps stay for the count reduction
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
     if (i < n) {
-      uint32_t p = q[i];
-      float4 o = P.ray_o[p], d = P.ray_d[p];
+      float3 o, d;
+      float tmin, tmax;
+      uint32_t skip;
+      src.load(i, o, d, tmin, tmax, skip);
       Hit h;
-      bool any = trace<false, kCount>(sc, f3(o), f3(d), 0.001f, kInfF, __float_as_uint(o.w), h,
-                                      reinterpret_cast<int*>(P.counters + 3), &ts);
-      P.hit[p] = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), h.u, h.v);
+      trace<false, kCount>(sc, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      src.store(i, h);
       rays++;
     }
   }
   if (kCount) add_counts(P.stats, rays, ts);
 }
 
+static int sm_count_current() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
-  if (P.stats) k_pt_extend<true><<<grid, block, 0, st>>>(sc, P, cur);
-  else k_pt_extend<false><<<grid, block, 0, st>>>(sc, P, cur);
+  if (P.variant & GPRT_JOB_SIMPLE_EXTEND) {
+    int b = std::min(block, 256);
+    if (P.stats) k_pt_extend_simple<true><<<grid, b, 0, st>>>(sc, P, cur);
+    else k_pt_extend_simple<false><<<grid, b, 0, st>>>(sc, P, cur);
+    return;
+  }
+  int g = persistent_grid(sm_count_current(), 128);
+  if (P.stats) k_pt_extend<true><<<g, 128, 0, st>>>(sc, P, cur);
+  else k_pt_extend<false><<<g, 128, 0, st>>>(sc, P, cur);
 }
 
 // ----------------------------------------------------------------- shade
@@ -146,6 +221,10 @@ void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block,
 // first at every level, as in the reference.
 __global__ void __launch_bounds__(256) k_pt_shade(DevScene sc, DevPaths P, ChunkDesc ch, int cur, int bounce) {
   uint32_t n = P.counters[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[4] = 0;  // ray-fetch counters of the next shadow and extend launches
+    P.counters[5] = 0;
+  }
   const uint32_t* q = P.queue[cur];
   uint32_t* qn = P.queue[cur ^ 1];
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -259,33 +338,69 @@ void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch,
 // ----------------------------------------------------------------- shadow
 // scene.BVH.Hit(shadowRay, 0.001, distance - 0.001) used as a boolean
 // (path_tracing.go:143-148): the contribution is kept when nothing is hit.
+struct ShadowSource {
+  DevPaths P;
+  uint32_t n;
+  __device__ uint32_t count() const { return n; }
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
+    float4 a = P.sh_o[i], b = P.sh_d[i];
+    o = f3(a);
+    d = f3(b);
+    tmin = 0.001f;
+    tmax = a.w;
+    skip = __float_as_uint(b.w);
+  }
+  __device__ void store(uint32_t i, const Hit& h) const {
+    if (h.prim != kNoHit) return;  // occluded
+    float4 c = P.sh_c[i];
+    uint32_t p = __float_as_uint(c.w);
+    float4 L = P.L[p];
+    P.L[p] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
+  }
+};
+
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_pt_shadow(DevScene sc, DevPaths P) {
+__global__ void __launch_bounds__(128, 8) k_pt_shadow(DevScene sc, DevPaths P) {
+  ShadowSource src{P, P.counters[2]};
+  TraceStats ts{0, 0, 0};
+  uint32_t rays = 0;
+  trace_persistent<true, kCount>(sc, src, P.counters + 5, reinterpret_cast<int*>(P.counters + 3), &ts, &rays);
+  if (kCount) add_counts(P.stats + 4, rays, ts);
+}
+
+// One shadow ray per thread (grid-stride), the variant GPRT_JOB_SIMPLE_SHADOW selects.
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_pt_shadow_simple(DevScene sc, DevPaths P) {
   uint32_t n = P.counters[2];
+  ShadowSource src{P, n};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
   uint32_t end = kCount ? ((n + 31) & ~31u) : n;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
     if (i < n) {
-      float4 o = P.sh_o[i], d = P.sh_d[i];
+      float3 o, d;
+      float tmin, tmax;
+      uint32_t skip;
+      src.load(i, o, d, tmin, tmax, skip);
       Hit h;
-      bool blocked = trace<true, kCount>(sc, f3(o), f3(d), 0.001f, o.w, __float_as_uint(d.w), h,
-                                         reinterpret_cast<int*>(P.counters + 3), &ts);
+      trace<true, kCount>(sc, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      src.store(i, h);
       rays++;
-      if (!blocked) {
-        float4 c = P.sh_c[i];
-        uint32_t p = __float_as_uint(c.w);
-        float4 L = P.L[p];
-        P.L[p] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
-      }
     }
   }
   if (kCount) add_counts(P.stats + 4, rays, ts);
 }
 
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int block, int grid, cudaStream_t st) {
-  if (P.stats) k_pt_shadow<true><<<grid, block, 0, st>>>(sc, P);
-  else k_pt_shadow<false><<<grid, block, 0, st>>>(sc, P);
+  if (P.variant & GPRT_JOB_SIMPLE_SHADOW) {
+    int b = std::min(block, 256);
+    if (P.stats) k_pt_shadow_simple<true><<<grid, b, 0, st>>>(sc, P);
+    else k_pt_shadow_simple<false><<<grid, b, 0, st>>>(sc, P);
+    return;
+  }
+  int g = persistent_grid(sm_count_current(), 128);
+  if (P.stats) k_pt_shadow<true><<<g, 128, 0, st>>>(sc, P);
+  else k_pt_shadow<false><<<g, 128, 0, st>>>(sc, P);
 }
 
 // ----------------------------------------------------------------- accumulate

@@ -2,10 +2,11 @@
 // builder (scene.cpp) and the kernels (device.cuh).
 //
 // HBM layout (all arrays 16-byte aligned, read with 16-byte vector loads):
-//   nodes      8 x float4 (128 B) per 4-wide BVH node:
-//                lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] meta[4]
-//              child = node index (meta == 0), first primitive of a leaf
-//              (meta = count | type << 8), or kEmptyChild.
+//   nodes      8 x float4 (128 B, one cache line) per 4-wide BVH node; child i
+//              is the pair (lo.x, lo.y, lo.z, ref) (hi.x, hi.y, hi.z, meta):
+//              ref = node index (meta == 0), first primitive of a leaf
+//              (meta = count | type << 8), or kEmptyChild.  Used slots come
+//              first, so a traversal stops at the first empty one.
 //   tris       3 x float4 (48 B): (v0, material) (e1 = v1 - v0, -) (e2 = v2 - v0, -)
 //   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64
 //   quads      5 x float4 (80 B): (corner, D) (u, material) (v, -) (normal, -) (W, -)

@@ -362,14 +362,10 @@ struct Emitter {
       }
     }
     float4* N = &out.nodes[(size_t)idx * 8];
-    N[0] = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
-    N[1] = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
-    N[2] = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
-    N[3] = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
-    N[4] = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
-    N[5] = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
-    N[6] = make_float4(i2f((uint32_t)child[0]), i2f((uint32_t)child[1]), i2f((uint32_t)child[2]), i2f((uint32_t)child[3]));
-    N[7] = make_float4(i2f((uint32_t)meta[0]), i2f((uint32_t)meta[1]), i2f((uint32_t)meta[2]), i2f((uint32_t)meta[3]));
+    for (int i = 0; i < 4; i++) {  // child i: (lo, ref) (hi, meta)
+      N[2 * i] = make_float4(lo[0][i], lo[1][i], lo[2][i], i2f((uint32_t)child[i]));
+      N[2 * i + 1] = make_float4(hi[0][i], hi[1][i], hi[2][i], i2f((uint32_t)meta[i]));
+    }
     return idx;
   }
 };
@@ -735,19 +731,25 @@ std::string validate_layout(const HostScene& s) {
     int n = todo.back();
     todo.pop_back();
     const float4* N = &s.nodes[(size_t)n * 8];
+    bool seen_empty = false;
     for (int i = 0; i < 4; i++) {
-      int ch = ri(N[6], i), mt = ri(N[7], i);
-      if (ch == kEmptyChild) continue;
-      float lo[3] = {rd(N[0], i), rd(N[2], i), rd(N[4], i)}, hi[3] = {rd(N[1], i), rd(N[3], i), rd(N[5], i)};
+      const float4 &A = N[2 * i], &B = N[2 * i + 1];
+      int ch = ri(A, 3), mt = ri(B, 3);
+      if (ch == kEmptyChild) {
+        seen_empty = true;
+        continue;
+      }
+      if (seen_empty) return "used child slot after an empty one";
+      float lo[3] = {A.x, A.y, A.z}, hi[3] = {B.x, B.y, B.z};
       auto inside = [&](float x, int k) { return x >= lo[k] && x <= hi[k]; };
       if (mt == 0) {
         if (ch <= 0 || (size_t)ch >= nn || node_seen[ch]) return "bad child node index";
         node_seen[ch] = 1;
         const float4* C = &s.nodes[(size_t)ch * 8];
         for (int j = 0; j < 4; j++) {
-          if (ri(C[6], j) == kEmptyChild) continue;
-          if (!(rd(C[0], j) >= lo[0] && rd(C[1], j) <= hi[0] && rd(C[2], j) >= lo[1] && rd(C[3], j) <= hi[1] &&
-                rd(C[4], j) >= lo[2] && rd(C[5], j) <= hi[2]))
+          const float4 &CA = C[2 * j], &CB = C[2 * j + 1];
+          if (ri(CA, 3) == kEmptyChild) continue;
+          if (!(CA.x >= lo[0] && CB.x <= hi[0] && CA.y >= lo[1] && CB.y <= hi[1] && CA.z >= lo[2] && CB.z <= hi[2]))
             return "child box not inside its parent slot";
         }
         todo.push_back(ch);
@@ -823,12 +825,12 @@ void count_traversal(const HostScene& s, const gprt_ray* rays, uint32_t n, bool 
       float itn[4];
       int nint = 0;
       for (int i = 0; i < 4 && !done; i++) {
-        int ch = ri(N[6], i), mt = ri(N[7], i);
-        if (ch == kEmptyChild) continue;
+        int ch = ri(N[2 * i], 3), mt = ri(N[2 * i + 1], 3);
+        if (ch == kEmptyChild) break;
         boxes++;
         float t0[3], t1[3];
         for (int k = 0; k < 3; k++) {
-          float lo = rd(N[2 * k], i), hi = rd(N[2 * k + 1], i);
+          float lo = rd(N[2 * i], k), hi = rd(N[2 * i + 1], k);
           bool neg = inv[k] < 0;
           t0[k] = std::fma(neg ? hi : lo, inv[k], -ood[k]);
           t1[k] = std::fma(neg ? lo : hi, inv[k], -ood[k]);

@@ -93,6 +93,13 @@ class JobDesc(C.Structure):
 
 JOB_TIME_KERNELS = 1
 JOB_COUNT_TRAVERSAL = 2
+JOB_SIMPLE_EXTEND = 4
+JOB_SIMPLE_SHADOW = 8
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("flags", C.c_uint32), ("block_size", C.c_uint32), ("chunk_paths", C.c_uint32),
+                ("candidates", C.c_uint32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
 
 
 class JobCounters(C.Structure):
@@ -144,6 +151,7 @@ SIGNATURES = {
     "gprt_job_reset_counters": (C.c_int, [P]),
     "gprt_job_stream": (C.c_int, [P, PP]),
     "gprt_render_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint64, P, P]),
+    "gprt_autotune": (C.c_int, [P, C.POINTER(JobDesc), C.c_uint32, C.POINTER(TuneResult)]),
 }
 
 _lib = None

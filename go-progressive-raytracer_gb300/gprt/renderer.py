@@ -94,6 +94,24 @@ class GpuScene:
             pass
 
 
+def autotune(gscene: "GpuScene", integrator=None, spp=1, config: Optional["ProgressiveConfig"] = None):
+    """gprt_autotune: the fastest wavefront size / traversal variant / block
+    size for this scene.  Returns (config with the choice applied, details)."""
+    cfg = config or ProgressiveConfig()
+    d = capi.JobDesc()
+    d.integrator = (integrator or PathTracingIntegrator()).kind
+    d.max_samples_per_pixel = max(cfg.max_samples_per_pixel, 2 * spp)
+    d.max_passes = 1
+    d.seed = cfg.seed
+    r = capi.TuneResult()
+    gscene.ctx.check(gscene.ctx.lib.gprt_autotune(gscene.h, C.byref(d), spp, C.byref(r)))
+    out = ProgressiveConfig(**cfg.__dict__)
+    out.flags = (cfg.flags & ~(capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW)) | r.flags
+    out.block_size = r.block_size
+    out.chunk_paths = r.chunk_paths
+    return out, {k: getattr(r, k) for k, _ in capi.TuneResult._fields_}
+
+
 @dataclass
 class PathTracingIntegrator:  # integrator.NewPathTracingIntegrator
     kind: int = capi.INTEGRATOR_PATH_TRACING

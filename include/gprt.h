@@ -212,6 +212,11 @@ typedef struct gprt_job_desc {
 
 #define GPRT_JOB_TIME_KERNELS 1u     /* CUDA-event timing of every kernel launch, per kernel class */
 #define GPRT_JOB_COUNT_TRAVERSAL 2u  /* count BVH node / box / primitive tests (slower kernels) */
+/* Kernel variants (normally chosen by gprt_autotune): the closest-hit and the
+ * shadow traversal run either persistent (warps refill finished lanes with
+ * new rays) or one ray per thread. */
+#define GPRT_JOB_SIMPLE_EXTEND 4u
+#define GPRT_JOB_SIMPLE_SHADOW 8u
 
 /* Instrumentation of a job (GPRT_JOB_* flags), summed since the last reset.
  * "extend" is the closest-hit traversal of the live paths (one launch per
@@ -321,6 +326,24 @@ int gprt_job_get_counters(gprt_job* job, gprt_job_counters* out);
 int gprt_job_reset_counters(gprt_job* job);
 /* The cudaStream_t every kernel of the job is launched on. */
 int gprt_job_stream(gprt_job* job, void** stream);
+
+/* ---- autotuning ------------------------------------------------------------
+ * No counterpart in the reference (its worker count is the only knob,
+ * pkg/renderer/worker_pool.go:49-52).  Times candidate wavefront sizes,
+ * traversal variants (GPRT_JOB_SIMPLE_*) and block sizes on tuning passes of
+ * `spp` samples per pixel of `scene` with the integrator of `base`
+ * (coordinate descent, each candidate timed with CUDA events after one
+ * warm-up pass) and returns the fastest configuration; apply it by copying
+ * flags / block_size / chunk_paths into the gprt_job_desc of later jobs. */
+typedef struct gprt_tune_result {
+  uint32_t flags;        /* GPRT_JOB_SIMPLE_* bits of the fastest configuration */
+  uint32_t block_size;
+  uint32_t chunk_paths;
+  uint32_t candidates;   /* configurations timed */
+  double best_ms;        /* one tuning pass with the chosen configuration */
+  double default_ms;     /* the same pass with the default configuration */
+} gprt_tune_result;
+int gprt_autotune(gprt_scene* scene, const gprt_job_desc* base, uint32_t spp, gprt_tune_result* out);
 
 /* ---- allocation-free rendering ---------------------------------------------
  * No counterpart in the reference: an entry point for callers that cannot
