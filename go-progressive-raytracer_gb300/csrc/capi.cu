@@ -1,124 +1,13 @@
 // capi.cu - the C ABI of include/gprt.h: context, scene and job handles and
 // the host orchestration of the kernels (chunked wavefront passes).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
-#include <memory>
-#include <mutex>
-#include <set>
-#include <string>
-#include <vector>
 
-#include "../../include/gprt.h"
-#include "kernels.h"
-#include "scene.h"
-
-using namespace gprt;
-
-// Ownership: a context owns its scenes and a scene owns its jobs, so
-// destroying a parent releases whatever children the caller did not.
-struct gprt_ctx {
-  int device = 0;
-  int sm_count = 0;
-  cudaStream_t stream = nullptr;
-  std::recursive_mutex mu;
-  std::string err;
-  std::set<gprt_scene*> scenes;
-};
-
-struct gprt_scene {
-  gprt_ctx* ctx = nullptr;
-  HostScene host;
-  DevScene dev{};
-  std::vector<void*> buffers;
-  size_t bytes = 0;
-  int* d_err = nullptr;
-  std::set<gprt_job*> jobs;
-};
-
-struct gprt_job {
-  gprt_scene* scene = nullptr;
-  gprt_job_desc desc{};
-  DevFilm film{};
-  DevPaths paths{};
-  std::vector<void*> buffers;
-  cudaStream_t stream = nullptr;
-  uint32_t* d_pix_list = nullptr;
-  uint32_t* d_active = nullptr;
-  uint64_t launches = 0;
-  int64_t uniform_count = 0;  // every pixel holds this many samples (-1: differs)
-  uint64_t sample_index_base = 0;
-  gprt_render_stats last{};
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // instrumentation (GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL)
-  struct Timed {
-    int cls;  // 0 extend, 1 shade, 2 shadow, 3 other
-    cudaEvent_t a, b;
-  };
-  std::vector<Timed> timed;
-  size_t timed_used = 0;
-  unsigned long long* d_stats = nullptr;
-  gprt_job_counters acc{};
-};
+#include "handles.h"
 
 namespace {
-
-int fail(gprt_ctx* ctx, int code, const std::string& msg) {
-  if (ctx) ctx->err = msg;
-  return code;
-}
-
-int cuda_fail(gprt_ctx* ctx, cudaError_t e, const char* what) {
-  return fail(ctx, GPRT_E_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define CK(ctx, call)                                  \
-  do {                                                 \
-    cudaError_t e_ = (call);                           \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
-
-template <class T>
-int dev_alloc(gprt_ctx* ctx, std::vector<void*>& bufs, T** out, size_t count, size_t* bytes = nullptr) {
-  *out = nullptr;
-  if (count == 0) return GPRT_OK;
-  void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return fail(ctx, GPRT_E_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-  }
-  bufs.push_back(p);
-  *out = static_cast<T*>(p);
-  if (bytes) *bytes += count * sizeof(T);
-  return GPRT_OK;
-}
-
-template <class T>
-int upload(gprt_ctx* ctx, std::vector<void*>& bufs, const std::vector<T>& src, const T** out, size_t* bytes) {
-  T* d = nullptr;
-  int rc = dev_alloc(ctx, bufs, &d, src.size(), bytes);
-  if (rc) return rc;
-  if (!src.empty()) CK(ctx, cudaMemcpyAsync(d, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
-  *out = d;
-  return GPRT_OK;
-}
-
-void free_all(std::vector<void*>& bufs) {
-  for (void* p : bufs) cudaFree(p);
-  bufs.clear();
-}
-
-// getSamplesForPass (pkg/renderer/progressive.go:98-123)
-uint32_t samples_for_pass(const gprt_job_desc& d, uint32_t pass) {
-  if (d.max_passes == 1) return d.max_samples_per_pixel;
-  if (pass == 1) return d.initial_samples;
-  uint32_t rem = d.max_samples_per_pixel - d.initial_samples;
-  uint32_t per = rem / (d.max_passes - 1);
-  uint32_t t = d.initial_samples + (pass - 1) * per;
-  if (pass == d.max_passes) t = d.max_samples_per_pixel;
-  return t;
-}
 
 int ensure_paths(gprt_job* j) {
   if (j->paths.capacity) return GPRT_OK;
@@ -329,6 +218,16 @@ int gprt_ctx_create(int device, gprt_ctx** out) {
 
 int gprt_ctx_destroy(gprt_ctx* ctx) {
   if (!ctx) return GPRT_E_INVALID;
+  // servers first: their loop threads take the context lock
+  for (;;) {
+    gprt_server* sv = nullptr;
+    {
+      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      if (ctx->servers.empty()) break;
+      sv = *ctx->servers.begin();
+    }
+    gprt_server_destroy(sv);
+  }
   {
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
@@ -349,6 +248,8 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   cudaSetDevice(ctx->device);
   auto s = std::make_unique<gprt_scene>();
   s->ctx = ctx;
+  static std::atomic<uint64_t> next_serial{1};
+  s->serial = next_serial++;
   std::string err;
   if (!build_scene(desc, s->host, err)) return fail(ctx, GPRT_E_INVALID, err);
   HostScene& h = s->host;
@@ -371,6 +272,7 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   }
   cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
   d.n_nodes = (int)(h.nodes.size() / 8);
+  d.root = d.n_nodes > 0 ? 0 : -1;
   d.n_lights = (int)h.lights.size();
   d.quad_base = h.n_tris;
   d.sphere_base = h.n_tris + h.n_quads;
@@ -396,6 +298,7 @@ int gprt_scene_destroy(gprt_scene* s) {
   gprt_ctx* ctx = s->ctx;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
+  for (gprt_server* sv : ctx->servers) server_forget_scene(sv, s);
   while (!s->jobs.empty()) gprt_job_destroy(*s->jobs.begin());
   cudaStreamSynchronize(ctx->stream);
   free_all(s->buffers);

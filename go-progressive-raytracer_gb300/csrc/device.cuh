@@ -254,8 +254,9 @@ struct Trav {
   Hit hit;
 };
 
+// `root` is the BVH node the ray starts at (-1: nothing to intersect).
 __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
-                                          int n_nodes) {
+                                          int root) {
   s.o = o;
   s.d = d;
   s.inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
@@ -265,7 +266,7 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmi
   s.tmin = tmin;
   s.best = tmax;
   s.skip = skip;
-  s.node = n_nodes > 0 ? 0 : -1;
+  s.node = root;
   s.sp = 0;
   s.hit.prim = kNoHit;
   s.hit.t = -1.f;
@@ -366,18 +367,25 @@ __device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* sta
   return false;
 }
 
-// Whole traversal of one ray (used inside the BDPT and shading kernels).
+// Whole traversal of one ray from BVH node `root`.
 template <bool kAnyHit, bool kCount>
-__device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
-                                      Hit& hit, int* err, TraceStats* st = nullptr) {
+__device__ __forceinline__ bool trace_from(const DevScene& sc, int root, float3 o, float3 d, float tmin, float tmax,
+                                           uint32_t skip, Hit& hit, int* err, TraceStats* st = nullptr) {
   Trav s;
-  trav_init(s, o, d, tmin, tmax, skip, sc.n_nodes);
+  trav_init(s, o, d, tmin, tmax, skip, root);
   int stack[kTraceStack];
   while (s.node >= 0) {
     if (trav_visit<kAnyHit, kCount>(sc, s, stack, err, st)) break;
   }
   hit = s.hit;
   return s.hit.prim != kNoHit;
+}
+
+// Whole traversal of one ray of the scene (used inside the BDPT kernel).
+template <bool kAnyHit, bool kCount>
+__device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
+                                      Hit& hit, int* err, TraceStats* st = nullptr) {
+  return trace_from<kAnyHit, kCount>(sc, sc.root, o, d, tmin, tmax, skip, hit, err, st);
 }
 
 // Persistent traversal of a batch of rays: every warp loops until its work
@@ -387,7 +395,7 @@ __device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, fl
 // `work` != null, chunks of 64 rays come from that counter (zeroed by the
 // previous kernel on the same stream); otherwise each warp owns a static
 // contiguous range of the batch.  Source provides count(),
-// load(i, o, d, tmin, tmax, skip) and store(i, hit).
+// load(i, o, d, tmin, tmax, skip, root) and store(i, hit).
 constexpr uint32_t kFetchChunk = 64;
 
 template <bool kAnyHit, bool kCount, class Source>
@@ -429,9 +437,10 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
           float3 o, d;
           float tmin, tmax;
           uint32_t skip;
+          int root;
           uint32_t mine = cur + rank;
-          src.load(mine, o, d, tmin, tmax, skip);
-          trav_init(s, o, d, tmin, tmax, skip, sc.n_nodes);
+          src.load(mine, o, d, tmin, tmax, skip, root);
+          trav_init(s, o, d, tmin, tmax, skip, root);
           ray = (int)mine;
           if (kCount) (*traced)++;
         }

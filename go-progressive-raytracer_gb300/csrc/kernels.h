@@ -20,7 +20,7 @@ struct DevFilm {
 // Wavefront path state (structure of arrays, capacity = paths per chunk)
 struct DevPaths {
   float4* ray_o;   // origin.xyz, skip primitive (as int bits)
-  float4* ray_d;   // direction.xyz
+  float4* ray_d;   // direction.xyz, BVH root node of the path's scene (as int bits)
   float4* weight;  // radiance weight (rgb)
   float4* thr;     // Russian-roulette throughput (rgb)
   float4* L;       // radiance gathered so far (rgb)
@@ -32,6 +32,8 @@ struct DevPaths {
   float4* sh_o;    // shadow ray origin.xyz, tmax
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
   float4* sh_c;    // contribution rgb, path index (int bits)
+  int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
+  uint32_t* item;  // work item (job) of each path (multi-job wavefronts; null otherwise)
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;

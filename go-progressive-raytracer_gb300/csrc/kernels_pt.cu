@@ -15,6 +15,7 @@
 
 #include "device.cuh"
 #include "kernels.h"
+#include "pt_shade.cuh"
 
 namespace gprt {
 
@@ -31,7 +32,9 @@ struct BatchSource {
   gprt_hit* hits;
   uint32_t n;
   __device__ uint32_t count() const { return n; }
-  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
+  int root;
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
+    rt = root;
     const float4* r = reinterpret_cast<const float4*>(rays + i);
     float4 a = __ldg(r), b = __ldg(r + 1);
     o = f3(a);
@@ -62,22 +65,9 @@ void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = launch_grid((n + 31) / 32 * 32, 128, persistent_grid(sms, 128));
-  BatchSource src{rays, hits, n};
+  BatchSource src{rays, hits, n, sc.root};
   if (any_hit) k_intersect<true><<<grid, 128, 0, st>>>(sc, src, err);
   else k_intersect<false><<<grid, 128, 0, st>>>(sc, src, err);
-}
-
-// ----------------------------------------------------------------- queues
-// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
-__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
-  unsigned mask = __ballot_sync(__activemask(), want);
-  if (!want) return 0;
-  int lane = threadIdx.x & 31;
-  int leader = __ffs(mask) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-  base = __shfl_sync(mask, base, leader);
-  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
 // ----------------------------------------------------------------- raygen
@@ -98,7 +88,7 @@ __global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch)
     float3 o, d;
     camera_ray(sc.cam, x, y, lens, jit, o, d);
     P.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
-    P.ray_d[p] = make_float4(d.x, d.y, d.z, 0.f);
+    P.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(sc.root));
     P.weight[p] = make_float4(1.f, 1.f, 1.f, 0.f);
     P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
     P.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -139,9 +129,10 @@ struct ExtendSource {
   const uint32_t* q;
   uint32_t n;
   __device__ uint32_t count() const { return n; }
-  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
     uint32_t p = q[i];
     float4 a = P.ray_o[p], b = P.ray_d[p];
+    rt = __float_as_int(b.w);
     o = f3(a);
     d = f3(b);
     tmin = 0.001f;
@@ -185,9 +176,10 @@ __global__ void __launch_bounds__(256) k_pt_extend_simple(DevScene sc, DevPaths 
       float3 o, d;
       float tmin, tmax;
       uint32_t skip;
-      src.load(i, o, d, tmin, tmax, skip);
+      int root;
+      src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace<false, kCount>(sc, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      trace_from<false, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
       src.store(i, h);
       rays++;
     }
@@ -226,107 +218,16 @@ __global__ void __launch_bounds__(256) k_pt_shade(DevScene sc, DevPaths P, Chunk
     P.counters[5] = 0;
   }
   const uint32_t* q = P.queue[cur];
-  uint32_t* qn = P.queue[cur ^ 1];
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     uint32_t i = base + threadIdx.x;
-    bool live = i < n;
-    bool cont = false, shadow = false;
+    ShadeOut o;
+    o.cont = o.shadow = false;
     uint32_t p = 0;
-    float3 sh_o, sh_d, sh_c;
-    float sh_t = 0.f;
-    uint32_t sh_skip = kNoHit;
-    if (live) {
+    if (i < n) {
       p = q[i];
-      float4 o4 = P.ray_o[p], d4 = P.ray_d[p], h4 = P.hit[p];
-      float3 d = f3(d4);
-      float3 W = f3(P.weight[p]), thr = f3(P.thr[p]), L = f3(P.L[p]);
-      Rng rng;
-      rng.init(ch.seed, P.pixel[p], P.sample[p], P.rng_pos[p]);
-      // ApplyRussianRoulette: currentBounce = MaxDepth - depth = bounce
-      float u = rng.next();
-      bool dead = false;
-      if (bounce >= sc.rr_min_bounces) {
-        float surv = fminf(0.95f, fmaxf(0.5f, luminance(thr)));
-        if (u > surv) dead = true;
-        else W *= 1.0f / surv;
-      }
-      if (!dead) {
-        uint32_t prim = __float_as_uint(h4.y);
-        if (prim == kNoHit) {
-          L += W * background(sc, d);  // infinite-light emission of a missed ray
-        } else {
-          Hit h{h4.x, prim, h4.z, h4.w};
-          Surface s;
-          surface_at(sc, f3(o4), d, h, s);
-          DevMaterial m = load_material(sc, s.mat);
-          L += W * emitted(m, s.front);  // getEmittedLight (:108-113)
-          Scatter sc_;
-          if (scatter(sc, m, d, s, rng, sc_)) {
-            if (sc_.pdf <= 0.f) {
-              // calculateSpecularColor (:88-97)
-              W *= sc_.att;
-              thr *= sc_.att;
-              cont = true;
-            } else {
-              // CalculateDirectLighting: light choice + light sample
-              if (sc.n_lights > 0) {
-                int li = pick_light(sc, rng.next());
-                DevLight Lt = sc.lights[li];
-                LightSample ls = light_sample(sc, Lt, s.p, s.n, rng.next2());
-                ls.pdf *= Lt.prob;
-                if (luminance(ls.emission) > 0.f && ls.pdf > 0.f) {
-                  float cosine = dot(ls.dir, s.n);
-                  bool delta;
-                  float mp = mat_pdf(sc, m, d, ls.dir, s.n, delta);
-                  if (cosine > 0.f && !delta) {
-                    float w = power_heuristic(ls.pdf, mp);
-                    float3 f = brdf(sc, m, d, ls.dir, s, true);
-                    float3 c = W * (f * ls.emission) * (cosine * w / ls.pdf);
-                    if (!is_zero(c)) {
-                      shadow = true;
-                      sh_o = s.p;
-                      sh_d = ls.dir;
-                      sh_t = ls.dist - 0.001f;
-                      sh_c = c;
-                      sh_skip = prim;
-                    }
-                  }
-                }
-              }
-              // CalculateIndirectLighting
-              float3 sd = normalize(sc_.dir);
-              float cosine = dot(sd, s.n);
-              if (cosine > 0.f) {
-                float lp = total_light_pdf(sc, s.p, s.n, sd);
-                float w = power_heuristic(sc_.pdf, lp);
-                W *= sc_.att * (cosine * w / sc_.pdf);
-                thr *= sc_.att * (cosine / sc_.pdf);
-                cont = true;
-              }
-            }
-            if (cont) {
-              P.ray_o[p] = make_float4(s.p.x, s.p.y, s.p.z, __uint_as_float(prim));
-              P.ray_d[p] = make_float4(sc_.dir.x, sc_.dir.y, sc_.dir.z, 0.f);
-            }
-          }
-        }
-      }
-      cont = cont && (bounce + 1 < sc.max_depth);
-      P.L[p] = make_float4(L.x, L.y, L.z, 0.f);
-      P.rng_pos[p] = rng.pos;
-      if (cont) {
-        P.weight[p] = make_float4(W.x, W.y, W.z, 0.f);
-        P.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
-      }
+      shade_path(sc, P, p, ch.seed, bounce, o);
     }
-    uint32_t slot = warp_append(&P.counters[cur ^ 1], cont);
-    if (cont) qn[slot] = p;
-    uint32_t ss = warp_append(&P.counters[2], shadow);
-    if (shadow) {
-      P.sh_o[ss] = make_float4(sh_o.x, sh_o.y, sh_o.z, sh_t);
-      P.sh_d[ss] = make_float4(sh_d.x, sh_d.y, sh_d.z, __uint_as_float(sh_skip));
-      P.sh_c[ss] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(p));
-    }
+    push_shade_out(P, cur, p, o);
   }
 }
 
@@ -342,7 +243,9 @@ struct ShadowSource {
   DevPaths P;
   uint32_t n;
   __device__ uint32_t count() const { return n; }
-  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip) const {
+  int root;
+  __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
+    rt = P.sh_root ? P.sh_root[i] : root;
     float4 a = P.sh_o[i], b = P.sh_d[i];
     o = f3(a);
     d = f3(b);
@@ -361,7 +264,7 @@ struct ShadowSource {
 
 template <bool kCount>
 __global__ void __launch_bounds__(128, 8) k_pt_shadow(DevScene sc, DevPaths P) {
-  ShadowSource src{P, P.counters[2]};
+  ShadowSource src{P, P.counters[2], sc.root};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
   trace_persistent<true, kCount>(sc, src, P.counters + 5, reinterpret_cast<int*>(P.counters + 3), &ts, &rays);
@@ -372,7 +275,7 @@ __global__ void __launch_bounds__(128, 8) k_pt_shadow(DevScene sc, DevPaths P) {
 template <bool kCount>
 __global__ void __launch_bounds__(256) k_pt_shadow_simple(DevScene sc, DevPaths P) {
   uint32_t n = P.counters[2];
-  ShadowSource src{P, n};
+  ShadowSource src{P, n, sc.root};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
   uint32_t end = kCount ? ((n + 31) & ~31u) : n;
@@ -381,9 +284,10 @@ __global__ void __launch_bounds__(256) k_pt_shadow_simple(DevScene sc, DevPaths 
       float3 o, d;
       float tmin, tmax;
       uint32_t skip;
-      src.load(i, o, d, tmin, tmax, skip);
+      int root;
+      src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace<true, kCount>(sc, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      trace_from<true, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
       src.store(i, h);
       rays++;
     }

@@ -70,6 +70,7 @@ struct DevScene {
   const DevMaterial* materials;
   const DevLight* lights;
   int n_nodes;
+  int root;  // BVH root node of the scene (-1: empty)
   int n_lights;
   uint32_t quad_base, sphere_base, n_prims;
   int has_infinite;

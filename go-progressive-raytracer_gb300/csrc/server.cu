@@ -1,0 +1,1320 @@
+// server.cu - gprt_server: a device-resident request loop with continuous
+// batching.  Many progressive path-tracing jobs of different scenes and
+// resolutions share every wavefront.
+//
+// Device data of the server:
+//   scene pool   one growable array per primitive type (BVH nodes, triangles +
+//                normals, quads, spheres, materials, lights).  A scene admitted
+//                for the first time is copied in from its gprt_scene and its
+//                node / leaf / light references are rebased to pool indices,
+//                so the unchanged traversal kernels walk any scene from its
+//                root.  Primitive ids of the pool: triangles [0, 2^30), quads
+//                [2^30, 2^31), spheres [2^31, 2^32 - 1).
+//   path state   one set of wavefront arrays (DevPaths) of step capacity,
+//                shared by all jobs; each path records its work item.
+//   item table   per step: prefix sums of the items' paths and pixels (for a
+//                binary search from a path or pixel index to its item) and one
+//                DevItem per item (the job's camera, film, seed, pool offsets).
+//   films        one per admitted job (sum rgb + lum, lum^2, count per pixel).
+// A step: raygen over all items -> [extend -> shade -> shadow] x depth ->
+// accumulate, replayed from a CUDA graph captured once per depth (kernel
+// arguments are fixed device pointers; what changes per step is the item
+// table, copied in before the replay).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <thread>
+#include <unordered_map>
+
+#include "device.cuh"
+#include "handles.h"
+#include "pt_shade.cuh"
+
+namespace gprt {
+namespace {
+
+constexpr uint32_t kPoolQuadBase = 1u << 30;
+constexpr uint32_t kPoolSphereBase = 1u << 31;
+
+struct StepHdr {
+  uint32_t n_items, total_paths, total_pix, dry;
+};
+
+struct DevItem {
+  uint32_t path0, pix0, npix, layers;
+  int root, mat_off, light_off, n_lights;
+  int has_infinite, max_depth, rr_min_bounces, width;
+  float3 world_center;
+  float world_radius;
+  unsigned long long seed;
+  float4* rgbl;
+  float* lum2;
+  uint32_t* count;
+  DevCamera cam;
+};
+
+// Largest k < n with start[k] <= x (start[0] = 0, start ascending).
+__device__ __forceinline__ uint32_t find_range(const uint32_t* start, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(start + mid) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Camera rays of every item: path p is sample `layer` of pixel i of its item,
+// drawn exactly as k_pt_raygen draws them for a single job.
+__global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* path0, const DevItem* items) {
+  uint32_t n = hdr->total_paths, ni = hdr->n_items;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    uint32_t k = find_range(path0, ni, p);
+    const DevItem& it = items[k];
+    uint32_t rel = p - it.path0;
+    uint32_t layer = rel / it.npix, pix = rel - layer * it.npix;
+    uint32_t sample = it.count[pix] + layer;
+    int x = (int)(pix % (uint32_t)it.width), y = (int)(pix / (uint32_t)it.width);
+    Rng rng;
+    rng.init(it.seed, pix, sample);
+    float2 lens = rng.next2();
+    float2 jit = rng.next2();
+    float3 o, d;
+    camera_ray(it.cam, x, y, lens, jit, o, d);
+    P.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
+    P.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(it.root));
+    P.weight[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.pixel[p] = pix;
+    P.sample[p] = sample;
+    P.rng_pos[p] = rng.pos;
+    P.item[p] = k;
+    P.queue[0][p] = p;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[0] = n;
+    P.counters[4] = 0;
+    P.counters[5] = 0;
+  }
+}
+
+// One bounce of every live path, each shaded with its own job's scene view
+// (materials, lights, infinite-light bounds, depth and Russian-roulette
+// settings) over the pooled geometry.
+__global__ void __launch_bounds__(256) k_srv_shade(DevScene pool, DevPaths P, const DevItem* items, int cur,
+                                                   int bounce) {
+  uint32_t n = P.counters[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[4] = 0;
+    P.counters[5] = 0;
+  }
+  const uint32_t* q = P.queue[cur];
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    ShadeOut o;
+    o.cont = o.shadow = false;
+    o.root = -1;
+    uint32_t p = 0;
+    if (i < n) {
+      p = q[i];
+      const DevItem& it = items[P.item[p]];
+      DevScene v = pool;
+      v.materials = pool.materials + it.mat_off;
+      v.lights = pool.lights + it.light_off;
+      v.n_lights = it.n_lights;
+      v.has_infinite = it.has_infinite;
+      v.world_center = it.world_center;
+      v.world_radius = it.world_radius;
+      v.max_depth = it.max_depth;
+      v.rr_min_bounces = it.rr_min_bounces;
+      v.root = it.root;
+      shade_path(v, P, p, it.seed, bounce, o);
+    }
+    push_shade_out(P, cur, p, o);
+  }
+}
+
+// PixelStats.AddSample for every pixel of every item, samples in order (the
+// same additions as k_accumulate).
+__global__ void k_srv_accumulate(DevPaths P, const StepHdr* hdr, const uint32_t* pix0, const DevItem* items) {
+  if (hdr->dry) return;
+  uint32_t n = hdr->total_pix, ni = hdr->n_items;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    uint32_t k = find_range(pix0, ni, t);
+    const DevItem& it = items[k];
+    uint32_t i = t - it.pix0;
+    float4 acc = it.rgbl[i];
+    float l2 = it.lum2[i];
+    for (uint32_t layer = 0; layer < it.layers; layer++) {
+      float4 c = P.L[it.path0 + layer * it.npix + i];
+      float lum = luminance(f3(c));
+      acc.x += c.x;
+      acc.y += c.y;
+      acc.z += c.z;
+      acc.w += lum;
+      l2 += lum * lum;
+    }
+    it.rgbl[i] = acc;
+    it.lum2[i] = l2;
+    it.count[i] += it.layers;
+  }
+}
+
+// Rebases the references of `n` nodes copied to pool index node_off: inner
+// children by node_off, leaves by the offset of their primitive type.
+__global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_off, int quad_off, int sph_off) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n * 4u; c += gridDim.x * blockDim.x) {
+    float4* a = nodes + (size_t)(c >> 2) * 8 + 2 * (c & 3);
+    int ref = __float_as_int(a->w);
+    if (ref == kEmptyChild) continue;
+    int meta = __float_as_int(a[1].w);
+    int off = node_off;
+    if (meta != 0) {
+      int type = (meta >> kLeafTypeShift) & 3;
+      off = type == kPrimTriangle ? tri_off : type == kPrimQuad ? quad_off : sph_off;
+    }
+    a->w = __int_as_float(ref + off);
+  }
+}
+
+__global__ void k_rebase_lights(DevLight* L, uint32_t n, int quad_off, int sph_off) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (L[i].kind == kLightQuad) L[i].prim += quad_off;
+    else if (L[i].kind == kLightSphere) L[i].prim += sph_off;
+  }
+}
+
+double now_ms(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// One growable device array (or two parallel ones) with a first-fit range
+// allocator over element indices.
+struct PoolArray {
+  size_t elem[2] = {0, 0};  // bytes per element of each parallel buffer (0: unused)
+  void* buf[2] = {nullptr, nullptr};
+  size_t cap = 0;
+  std::map<size_t, size_t> free_;  // offset -> length
+
+  size_t bytes_per() const { return elem[0] + elem[1]; }
+  size_t bytes() const { return cap * bytes_per(); }
+  bool take(size_t n, size_t* off) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        *off = it->first;
+        size_t rest = it->second - n, o = it->first + n;
+        free_.erase(it);
+        if (rest) free_[o] = rest;
+        return true;
+      }
+    }
+    return false;
+  }
+  void give(size_t off, size_t n) {
+    if (!n) return;
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + n == nx->first) {
+      n += nx->second;
+      free_.erase(nx);
+    }
+    auto pv = free_.lower_bound(off);
+    if (pv != free_.begin()) {
+      --pv;
+      if (pv->first + pv->second == off) {
+        pv->second += n;
+        return;
+      }
+    }
+    free_[off] = n;
+  }
+  // elements free at the end of the array
+  size_t tail_free() const {
+    if (free_.empty()) return 0;
+    auto last = std::prev(free_.end());
+    return last->first + last->second == cap ? last->second : 0;
+  }
+  bool empty_all() const { return cap == 0 || (free_.size() == 1 && free_.begin()->second == cap); }
+};
+
+}  // namespace
+}  // namespace gprt
+
+// A scene resident in the pool.
+struct PoolScene {
+  uint64_t serial = 0;
+  size_t off[6] = {0, 0, 0, 0, 0, 0};  // nodes, tris, quads, spheres, materials, lights
+  size_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  int refs = 0;
+  uint64_t last_use = 0;
+  size_t bytes = 0;
+  // per-job constants of the scene
+  int root = -1;
+  int has_infinite = 0, max_depth = 0, rr_min = 0;
+  float3 world_center{};
+  float world_radius = 0.f;
+  DevCamera cam{};
+  uint32_t width = 0, height = 0;
+};
+
+struct SrvRequest {
+  uint64_t ticket;
+  gprt_scene* scene;
+  uint64_t serial;
+  gprt_job_desc desc;
+  double submit_ms;
+};
+
+struct SrvJob {
+  uint64_t ticket = 0;
+  PoolScene* ps = nullptr;
+  gprt_job_desc desc{};
+  uint32_t npix = 0;
+  DevFilm film{};
+  std::vector<void*> bufs;
+  size_t film_bytes = 0;
+  uint32_t passes = 0, spp_done = 0, pass_target = 0;
+  bool running = true;
+  double submit_ms = 0, admit_ms = 0;
+  uint64_t last_served = 0;
+};
+
+struct gprt_server {
+  gprt_ctx* ctx = nullptr;
+  gprt_server_desc desc{};
+  std::chrono::steady_clock::time_point t0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // state (smu)
+  std::mutex smu;
+  gprt::PoolArray pool[6];
+  uint64_t pool_gen = 0;
+  std::vector<std::unique_ptr<PoolScene>> scenes;
+  std::map<uint64_t, std::unique_ptr<SrvJob>> jobs;  // admitted, by ticket
+  DevPaths P{};
+  std::vector<void*> path_bufs;
+  size_t path_bytes = 0;
+  size_t reserve = 0;      // bytes promised to the film being admitted
+  uint32_t capacity = 0;   // path capacity allocated
+  uint32_t step_paths = 0; // paths per step (<= capacity)
+  uint32_t block = 128;
+  uint32_t flags = 0;
+  // item table: [hdr | path0[max+1] | pix0[max+1]] then items[max]
+  unsigned char* d_table = nullptr;
+  unsigned char* h_table = nullptr;  // pinned
+  size_t table_bytes = 0, prefix_bytes = 0;
+  std::map<int, cudaGraphExec_t> graphs;  // by depth
+  uint64_t graph_gen = ~0ull;
+  gprt_server_stats st{};
+  // requests and events (qmu)
+  std::mutex qmu;
+  std::condition_variable cv_work, cv_ev;
+  std::deque<SrvRequest> pending;
+  std::deque<gprt_event> events;
+  uint64_t next_ticket = 1;
+  std::atomic<uint32_t> n_running{0};
+  uint64_t work_gen = 0;
+  // loop thread
+  std::thread loop;
+  bool stopping = false, loop_running = false;
+};
+
+using namespace gprt;
+
+namespace {
+
+constexpr int kNodes = 0, kTris = 1, kQuads = 2, kSpheres = 3, kMats = 4, kLights = 5;
+
+void emit(gprt_server* sv, uint64_t ticket, uint32_t kind, uint32_t passes, uint32_t spp, int status,
+          double submit_ms) {
+  gprt_event e{};
+  e.ticket = ticket;
+  e.kind = kind;
+  e.pass_number = passes;
+  e.samples_per_pixel = spp;
+  e.status = status;
+  e.t_ms = now_ms(sv->t0);
+  e.submit_ms = submit_ms;
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    sv->events.push_back(e);
+  }
+  sv->cv_ev.notify_all();
+}
+
+size_t film_bytes_for(uint32_t npix) { return (size_t)npix * (sizeof(float4) + sizeof(float) + sizeof(uint32_t)); }
+
+size_t bytes_in_use(gprt_server* sv) {
+  size_t b = sv->path_bytes + sv->table_bytes + sv->reserve;
+  for (auto& a : sv->pool) b += a.bytes();
+  for (auto& kv : sv->jobs) b += kv.second->film_bytes;
+  return b;
+}
+
+// Element counts of a gprt_scene in the pool's arrays.
+void scene_counts(const gprt_scene* s, size_t cnt[6]) {
+  const HostScene& h = s->host;
+  cnt[kNodes] = h.nodes.size() / 8;
+  cnt[kTris] = h.n_tris;
+  cnt[kQuads] = h.n_quads;
+  cnt[kSpheres] = h.n_spheres;
+  cnt[kMats] = h.materials.size();
+  cnt[kLights] = h.lights.size();
+}
+
+size_t scene_bytes(gprt_server* sv, const size_t cnt[6]) {
+  size_t b = 0;
+  for (int k = 0; k < 6; k++) b += cnt[k] * sv->pool[k].bytes_per();
+  return b;
+}
+
+DevScene pool_view(gprt_server* sv) {
+  DevScene d{};
+  d.nodes = static_cast<const float4*>(sv->pool[kNodes].buf[0]);
+  d.tris = static_cast<const float4*>(sv->pool[kTris].buf[0]);
+  d.tri_normals = static_cast<const float4*>(sv->pool[kTris].buf[1]);
+  d.quads = static_cast<const float4*>(sv->pool[kQuads].buf[0]);
+  d.spheres = static_cast<const float4*>(sv->pool[kSpheres].buf[0]);
+  d.materials = static_cast<const DevMaterial*>(sv->pool[kMats].buf[0]);
+  d.lights = static_cast<const DevLight*>(sv->pool[kLights].buf[0]);
+  d.n_nodes = (int)sv->pool[kNodes].cap;
+  d.root = -1;
+  d.quad_base = kPoolQuadBase;
+  d.sphere_base = kPoolSphereBase;
+  d.n_prims = 0xFFFFFFFEu;
+  return d;
+}
+
+// Grows pool array k to hold at least `need_cap` elements (copying what it
+// holds).  Returns false when the budget or the device refuses.
+bool grow(gprt_server* sv, int k, size_t need_cap) {
+  PoolArray& a = sv->pool[k];
+  size_t new_cap = std::max(need_cap, a.cap + a.cap / 2);
+  if (k == kTris || k == kQuads) new_cap = std::min<size_t>(new_cap, kPoolQuadBase);
+  if (k == kSpheres) new_cap = std::min<size_t>(new_cap, (size_t)0xFFFFFFFEu - kPoolSphereBase);
+  if (k == kNodes || k == kMats || k == kLights) new_cap = std::min<size_t>(new_cap, 0x7FFFFFFF);
+  if (new_cap < need_cap) return false;
+  size_t used = bytes_in_use(sv);
+  size_t extra = (new_cap - a.cap) * a.bytes_per();
+  if (used + extra > sv->desc.hbm_budget_bytes) {
+    new_cap = need_cap;  // exact fit
+    extra = (new_cap - a.cap) * a.bytes_per();
+    if (used + extra > sv->desc.hbm_budget_bytes) return false;
+  }
+  void* nb[2] = {nullptr, nullptr};
+  for (int b = 0; b < 2; b++) {
+    if (!a.elem[b]) continue;
+    if (cudaMalloc(&nb[b], new_cap * a.elem[b]) != cudaSuccess) {
+      cudaGetLastError();
+      if (nb[0] && b == 1) cudaFree(nb[0]);
+      return false;
+    }
+    if (a.cap) cudaMemcpyAsync(nb[b], a.buf[b], a.cap * a.elem[b], cudaMemcpyDeviceToDevice, sv->stream);
+  }
+  cudaStreamSynchronize(sv->stream);
+  for (int b = 0; b < 2; b++)
+    if (a.buf[b]) cudaFree(a.buf[b]);
+  size_t old = a.cap;
+  a.buf[0] = nb[0];
+  a.buf[1] = nb[1];
+  a.cap = new_cap;
+  a.give(old, new_cap - old);
+  sv->pool_gen++;
+  return true;
+}
+
+// Frees the pool's device arrays when no scene is resident.
+void shrink_if_empty(gprt_server* sv) {
+  if (!sv->scenes.empty()) return;
+  bool any = false;
+  for (auto& a : sv->pool) {
+    for (int b = 0; b < 2; b++)
+      if (a.buf[b]) {
+        cudaFree(a.buf[b]);
+        a.buf[b] = nullptr;
+        any = true;
+      }
+    a.cap = 0;
+    a.free_.clear();
+  }
+  if (any) sv->pool_gen++;
+}
+
+void evict(gprt_server* sv, PoolScene* ps) {
+  for (int k = 0; k < 6; k++) sv->pool[k].give(ps->off[k], ps->cnt[k]);
+  for (auto it = sv->scenes.begin(); it != sv->scenes.end(); ++it)
+    if (it->get() == ps) {
+      sv->scenes.erase(it);
+      break;
+    }
+}
+
+// Places the scene's arrays in the pool, evicting unreferenced scenes (least
+// recently used first) and growing arrays as the budget allows.
+bool place(gprt_server* sv, const size_t cnt[6], size_t off[6]) {
+  for (;;) {
+    bool ok = true;
+    size_t got[6] = {0, 0, 0, 0, 0, 0};
+    int k = 0;
+    for (; k < 6; k++) {
+      if (cnt[k] == 0) continue;
+      if (!sv->pool[k].take(cnt[k], &got[k])) {
+        ok = false;
+        break;
+      }
+    }
+    if (ok) {
+      for (int i = 0; i < 6; i++) off[i] = got[i];
+      return true;
+    }
+    for (int i = 0; i < k; i++) sv->pool[i].give(got[i], cnt[i]);
+    // grow array k by what its free tail lacks
+    PoolArray& a = sv->pool[k];
+    if (grow(sv, k, a.cap + cnt[k] - a.tail_free())) continue;
+    // evict the least recently used unreferenced scene and retry
+    PoolScene* lru = nullptr;
+    for (auto& s : sv->scenes)
+      if (s->refs == 0 && (!lru || s->last_use < lru->last_use)) lru = s.get();
+    if (!lru) return false;
+    evict(sv, lru);
+    shrink_if_empty(sv);
+  }
+}
+
+// Copies a gprt_scene into the pool (or finds it there).
+PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
+  for (auto& ps : sv->scenes)
+    if (ps->serial == s->serial) return ps.get();
+  size_t cnt[6], off[6];
+  scene_counts(s, cnt);
+  if (!place(sv, cnt, off)) return nullptr;
+  auto ps = std::make_unique<PoolScene>();
+  ps->serial = s->serial;
+  for (int k = 0; k < 6; k++) {
+    ps->off[k] = off[k];
+    ps->cnt[k] = cnt[k];
+  }
+  ps->bytes = scene_bytes(sv, cnt);
+  const DevScene& d = s->dev;
+  cudaStream_t st = sv->stream;
+  auto copy = [&](int k, int b, const void* src) {
+    if (!cnt[k]) return;
+    PoolArray& a = sv->pool[k];
+    cudaMemcpyAsync(static_cast<unsigned char*>(a.buf[b]) + off[k] * a.elem[b], src, cnt[k] * a.elem[b],
+                    cudaMemcpyDeviceToDevice, st);
+  };
+  copy(kNodes, 0, d.nodes);
+  copy(kTris, 0, d.tris);
+  copy(kTris, 1, d.tri_normals);
+  copy(kQuads, 0, d.quads);
+  copy(kSpheres, 0, d.spheres);
+  copy(kMats, 0, d.materials);
+  copy(kLights, 0, d.lights);
+  if (cnt[kNodes]) {
+    float4* nodes = static_cast<float4*>(sv->pool[kNodes].buf[0]) + off[kNodes] * 8;
+    uint32_t n = (uint32_t)cnt[kNodes];
+    k_rebase_nodes<<<launch_grid(n * 4, 256, 4096), 256, 0, st>>>(nodes, n, (int)off[kNodes], (int)off[kTris],
+                                                                   (int)off[kQuads], (int)off[kSpheres]);
+  }
+  if (cnt[kLights]) {
+    DevLight* L = static_cast<DevLight*>(sv->pool[kLights].buf[0]) + off[kLights];
+    k_rebase_lights<<<1, 128, 0, st>>>(L, (uint32_t)cnt[kLights], (int)off[kQuads], (int)off[kSpheres]);
+  }
+  ps->root = cnt[kNodes] ? (int)off[kNodes] : -1;
+  ps->has_infinite = d.has_infinite;
+  ps->max_depth = d.max_depth;
+  ps->rr_min = d.rr_min_bounces;
+  ps->world_center = d.world_center;
+  ps->world_radius = d.world_radius;
+  ps->cam = d.cam;
+  ps->width = s->host.sampling.width;
+  ps->height = s->host.sampling.height;
+  PoolScene* raw = ps.get();
+  sv->scenes.push_back(std::move(ps));
+  return raw;
+}
+
+void release_job(gprt_server* sv, SrvJob* j) {
+  if (j->running) {
+    j->running = false;
+    sv->n_running--;
+  }
+  if (j->ps) {
+    j->ps->refs--;
+    j->ps = nullptr;
+  }
+  free_all(j->bufs);
+}
+
+// Moves the job past passes that need no new samples; finishes it after its
+// last pass (RenderProgressive stops at max passes or when the average
+// sample count reaches the maximum, progressive.go:339-361).
+void advance(gprt_server* sv, SrvJob* j, bool emit_pass) {
+  if (emit_pass) {
+    j->passes++;
+    emit(sv, j->ticket, GPRT_EV_PASS, j->passes, j->spp_done, GPRT_OK, j->submit_ms);
+  }
+  for (;;) {
+    if (j->passes >= j->desc.max_passes || j->spp_done >= j->desc.max_samples_per_pixel) {
+      emit(sv, j->ticket, GPRT_EV_DONE, j->passes, j->spp_done, GPRT_OK, j->submit_ms);
+      sv->st.finished++;
+      if (j->running) {
+        j->running = false;
+        sv->n_running--;
+      }
+      if (j->ps) {
+        j->ps->refs--;
+        j->ps->last_use = sv->st.steps;
+        j->ps = nullptr;
+      }
+      return;
+    }
+    j->pass_target = samples_for_pass(j->desc, j->passes + 1);
+    if (j->pass_target > j->spp_done) return;
+    j->passes++;
+    emit(sv, j->ticket, GPRT_EV_PASS, j->passes, j->spp_done, GPRT_OK, j->submit_ms);
+  }
+}
+
+// Admits pending requests in arrival order while they fit.
+void admit(gprt_server* sv) {
+  gprt_ctx* ctx = sv->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);  // keeps pending scenes alive
+  for (;;) {
+    SrvRequest r;
+    {
+      std::lock_guard<std::mutex> q(sv->qmu);
+      if (sv->pending.empty()) return;
+      r = sv->pending.front();
+    }
+    if (sv->jobs.size() >= sv->desc.max_jobs) return;
+    gprt_scene* s = r.scene;
+    uint32_t npix = s->host.sampling.width * s->host.sampling.height;
+    size_t cnt[6];
+    scene_counts(s, cnt);
+    bool resident = false;
+    for (auto& ps : sv->scenes) resident |= ps->serial == r.serial;
+    size_t fixed = sv->path_bytes + sv->table_bytes;
+    size_t need = film_bytes_for(npix) + (resident ? 0 : scene_bytes(sv, cnt));
+    auto pop = [&]() {
+      std::lock_guard<std::mutex> q(sv->qmu);
+      sv->pending.pop_front();
+    };
+    if (npix > sv->capacity || fixed + need > sv->desc.hbm_budget_bytes) {
+      pop();
+      sv->st.refused++;
+      emit(sv, r.ticket, GPRT_EV_REFUSED, 0, 0, GPRT_E_ADMISSION, r.submit_ms);
+      continue;
+    }
+    // films must fit beside everything held now (scene bytes are checked as the pool grows)
+    if (bytes_in_use(sv) + film_bytes_for(npix) > sv->desc.hbm_budget_bytes) {
+      // unreferenced cached scenes go first
+      bool freed = false;
+      for (auto& ps : sv->scenes)
+        if (ps->refs == 0 && ps->serial != r.serial) {
+          evict(sv, ps.get());
+          freed = true;
+          break;
+        }
+      if (freed) {
+        shrink_if_empty(sv);
+        continue;
+      }
+      return;
+    }
+    auto j = std::make_unique<SrvJob>();
+    j->ticket = r.ticket;
+    j->desc = r.desc;
+    j->npix = npix;
+    j->submit_ms = r.submit_ms;
+    DevFilm& f = j->film;
+    f.width = (int)s->host.sampling.width;
+    f.height = (int)s->host.sampling.height;
+    int rc = 0;
+    rc |= dev_alloc(ctx, j->bufs, &f.rgbl, npix);
+    rc |= dev_alloc(ctx, j->bufs, &f.lum2, npix);
+    rc |= dev_alloc(ctx, j->bufs, &f.count, npix);
+    if (rc) {
+      free_all(j->bufs);
+      return;  // device full: retry next step
+    }
+    sv->reserve = film_bytes_for(npix);  // the scene may not take the film's room
+    PoolScene* ps = make_resident(sv, s);
+    sv->reserve = 0;
+    if (!ps) {
+      free_all(j->bufs);
+      return;  // waits for films and scenes to be released
+    }
+    cudaMemsetAsync(f.rgbl, 0, (size_t)npix * sizeof(float4), sv->stream);
+    cudaMemsetAsync(f.lum2, 0, (size_t)npix * sizeof(float), sv->stream);
+    cudaMemsetAsync(f.count, 0, (size_t)npix * sizeof(uint32_t), sv->stream);
+    j->film_bytes = film_bytes_for(npix);
+    ps->refs++;
+    ps->last_use = sv->st.steps;
+    j->ps = ps;
+    j->admit_ms = now_ms(sv->t0);
+    pop();
+    sv->st.admitted++;
+    sv->n_running++;
+    emit(sv, r.ticket, GPRT_EV_ADMITTED, 0, 0, GPRT_OK, r.submit_ms);
+    SrvJob* raw = j.get();
+    sv->jobs[r.ticket] = std::move(j);
+    advance(sv, raw, false);
+  }
+}
+
+int grid_for(gprt_server* sv, int block) { return std::max(1, sv->ctx->sm_count * (2048 / block)); }
+
+// The kernel sequence of one step of depth D on the server stream.
+void launch_step(gprt_server* sv, int D, cudaStream_t st) {
+  DevScene pool = pool_view(sv);
+  DevPaths P = sv->P;
+  P.variant = sv->flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  const StepHdr* hdr = reinterpret_cast<const StepHdr*>(sv->d_table);
+  const uint32_t* path0 = reinterpret_cast<const uint32_t*>(sv->d_table + 16);
+  const uint32_t* pix0 = path0 + (sv->desc.max_jobs + 1);
+  const DevItem* items = reinterpret_cast<const DevItem*>(sv->d_table + sv->prefix_bytes);
+  int block = (int)sv->block;
+  int grid = grid_for(sv, block);
+  k_srv_raygen<<<grid, block, 0, st>>>(P, hdr, path0, items);
+  int cur = 0;
+  for (int b = 0; b < D; b++) {
+    launch_pt_extend(pool, P, cur, block, grid, st);
+    k_srv_shade<<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
+    launch_pt_shadow(pool, P, block, grid, st);
+    cur ^= 1;
+  }
+  k_srv_accumulate<<<grid, block, 0, st>>>(P, hdr, pix0, items);
+}
+
+void drop_graphs(gprt_server* sv) {
+  for (auto& kv : sv->graphs) cudaGraphExecDestroy(kv.second);
+  sv->graphs.clear();
+}
+
+int run_step(gprt_server* sv, int D) {
+  gprt_ctx* ctx = sv->ctx;
+  if (sv->flags & GPRT_SERVER_NO_GRAPHS) {
+    launch_step(sv, D, sv->stream);
+    return GPRT_OK;
+  }
+  if (sv->graph_gen != sv->pool_gen) {
+    drop_graphs(sv);
+    sv->graph_gen = sv->pool_gen;
+  }
+  auto it = sv->graphs.find(D);
+  if (it == sv->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    CK(ctx, cudaStreamBeginCapture(sv->stream, cudaStreamCaptureModeThreadLocal));
+    launch_step(sv, D, sv->stream);
+    CK(ctx, cudaStreamEndCapture(sv->stream, &g));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+    it = sv->graphs.emplace(D, ex).first;
+  }
+  CK(ctx, cudaGraphLaunch(it->second, sv->stream));
+  sv->st.graph_launches++;
+  return GPRT_OK;
+}
+
+struct Item {
+  SrvJob* j;
+  uint32_t layers;
+};
+
+// Packs the next samples of the running jobs (least recently served first)
+// into one wavefront of at most step_paths paths.
+std::vector<Item> pack(gprt_server* sv) {
+  std::vector<SrvJob*> order;
+  for (auto& kv : sv->jobs)
+    if (kv.second->running) order.push_back(kv.second.get());
+  std::stable_sort(order.begin(), order.end(),
+                   [](const SrvJob* a, const SrvJob* b) { return a->last_served < b->last_served; });
+  std::vector<Item> items;
+  uint64_t used = 0;
+  for (SrvJob* j : order) {
+    if (items.size() >= sv->desc.max_jobs) break;
+    uint32_t want = j->pass_target - j->spp_done;
+    uint64_t fit = (sv->step_paths - used) / j->npix;
+    uint32_t layers = (uint32_t)std::min<uint64_t>(want, fit);
+    if (layers == 0) continue;
+    items.push_back({j, layers});
+    used += (uint64_t)layers * j->npix;
+  }
+  return items;
+}
+
+// Uploads the item table of a step; returns the depth of the step.
+int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint64_t* paths) {
+  uint32_t nmax = sv->desc.max_jobs;
+  StepHdr* hdr = reinterpret_cast<StepHdr*>(sv->h_table);
+  uint32_t* path0 = reinterpret_cast<uint32_t*>(sv->h_table + 16);
+  uint32_t* pix0 = path0 + (nmax + 1);
+  DevItem* it = reinterpret_cast<DevItem*>(sv->h_table + sv->prefix_bytes);
+  uint32_t pp = 0, px = 0;
+  int D = 0;
+  for (size_t k = 0; k < items.size(); k++) {
+    SrvJob* j = items[k].j;
+    PoolScene* ps = j->ps;
+    DevItem& d = it[k];
+    std::memset(&d, 0, sizeof(d));
+    path0[k] = pp;
+    pix0[k] = px;
+    d.path0 = pp;
+    d.pix0 = px;
+    d.npix = j->npix;
+    d.layers = items[k].layers;
+    d.root = ps->root;
+    d.mat_off = (int)ps->off[kMats];
+    d.light_off = (int)ps->off[kLights];
+    d.n_lights = (int)ps->cnt[kLights];
+    d.has_infinite = ps->has_infinite;
+    d.max_depth = ps->max_depth;
+    d.rr_min_bounces = ps->rr_min;
+    d.width = (int)ps->width;
+    d.world_center = ps->world_center;
+    d.world_radius = ps->world_radius;
+    d.seed = j->desc.seed;
+    d.rgbl = j->film.rgbl;
+    d.lum2 = j->film.lum2;
+    d.count = j->film.count;
+    d.cam = ps->cam;
+    pp += items[k].layers * j->npix;
+    px += j->npix;
+    D = std::max(D, ps->max_depth);
+  }
+  uint32_t n = (uint32_t)items.size();
+  path0[n] = pp;
+  pix0[n] = px;
+  hdr->n_items = n;
+  hdr->total_paths = pp;
+  hdr->total_pix = px;
+  hdr->dry = dry ? 1u : 0u;
+  *paths = pp;
+  cudaMemcpyAsync(sv->d_table, sv->h_table, sv->prefix_bytes, cudaMemcpyHostToDevice, sv->stream);
+  cudaMemcpyAsync(sv->d_table + sv->prefix_bytes, sv->h_table + sv->prefix_bytes, n * sizeof(DevItem),
+                  cudaMemcpyHostToDevice, sv->stream);
+  return D;
+}
+
+// One step: admission, one batched wavefront, events.  Returns the number of
+// items run (0: nothing to do) or a negative status.
+int step_impl(gprt_server* sv, bool dry, double* ms_out) {
+  gprt_ctx* ctx = sv->ctx;
+  if (!dry) admit(sv);
+  std::vector<Item> items = pack(sv);
+  if (items.empty()) return 0;
+  uint64_t paths = 0;
+  int D = upload_items(sv, items, dry, &paths);
+  CK(ctx, cudaEventRecord(sv->ev0, sv->stream));
+  int rc = run_step(sv, D);
+  if (rc) return rc;
+  CK(ctx, cudaEventRecord(sv->ev1, sv->stream));
+  uint32_t err = 0;
+  CK(ctx, cudaMemcpyAsync(&err, sv->P.counters + 3, 4, cudaMemcpyDeviceToHost, sv->stream));
+  CK(ctx, cudaStreamSynchronize(sv->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, sv->ev0, sv->ev1);
+  if (ms_out) *ms_out = ms;
+  if (dry) return (int)items.size();
+  sv->st.steps++;
+  sv->st.busy_ms += ms;
+  sv->st.last_step_ms = ms;
+  sv->st.paths += paths;
+  if (err) {
+    cudaMemsetAsync(sv->P.counters + 3, 0, 4, sv->stream);
+    for (const Item& it : items) {
+      emit(sv, it.j->ticket, GPRT_EV_FAILED, it.j->passes, it.j->spp_done, GPRT_E_BOUND, it.j->submit_ms);
+      release_job(sv, it.j);
+    }
+    return fail(ctx, GPRT_E_BOUND, "device bound exceeded in a batched step");
+  }
+  for (const Item& it : items) {
+    SrvJob* j = it.j;
+    j->spp_done += it.layers;
+    j->last_served = sv->st.steps;
+    sv->st.samples += (uint64_t)it.layers * j->npix;
+    if (j->ps) j->ps->last_use = sv->st.steps;
+    if (j->spp_done >= j->pass_target) advance(sv, j, true);
+  }
+  return (int)items.size();
+}
+
+SrvJob* find_job(gprt_server* sv, uint64_t ticket) {
+  auto it = sv->jobs.find(ticket);
+  return it == sv->jobs.end() ? nullptr : it->second.get();
+}
+
+void loop_main(gprt_server* sv) {
+  cudaSetDevice(sv->ctx->device);
+  for (;;) {
+    uint64_t gen;
+    {
+      std::unique_lock<std::mutex> lk(sv->qmu);
+      sv->cv_work.wait(lk, [&] { return sv->stopping || !sv->pending.empty() || sv->n_running.load() > 0; });
+      if (sv->stopping) return;
+      gen = sv->work_gen;
+    }
+    int did;
+    {
+      std::lock_guard<std::mutex> g(sv->smu);
+      did = step_impl(sv, false, nullptr);
+    }
+    if (did <= 0) {
+      // nothing could run (requests wait for memory): sleep until something changes
+      std::unique_lock<std::mutex> lk(sv->qmu);
+      sv->cv_work.wait_for(lk, std::chrono::milliseconds(5), [&] { return sv->stopping || sv->work_gen != gen; });
+    }
+  }
+}
+
+void notify_work(gprt_server* sv) {
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    sv->work_gen++;
+  }
+  sv->cv_work.notify_all();
+}
+
+int stop_loop(gprt_server* sv) {
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    if (!sv->loop_running) return GPRT_OK;
+    sv->stopping = true;
+  }
+  sv->cv_work.notify_all();
+  sv->loop.join();
+  std::lock_guard<std::mutex> lk(sv->qmu);
+  sv->stopping = false;
+  sv->loop_running = false;
+  return GPRT_OK;
+}
+
+int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out) {
+  std::lock_guard<std::mutex> g(sv->smu);
+  gprt_ctx* ctx = sv->ctx;
+  cudaSetDevice(ctx->device);
+  SrvJob* j = find_job(sv, ticket);
+  if (!j) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
+  if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
+  size_t npix = j->npix;
+  size_t bytes = kind == 0 ? npix * 4 : npix * 3 * sizeof(float);
+  std::vector<void*> tmp;
+  uint8_t* d = nullptr;
+  if (dev_alloc(ctx, tmp, &d, bytes)) return GPRT_E_OOM;
+  if (kind == 0) launch_resolve_rgba8(j->film, d, sv->stream);
+  else launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->stream);
+  cudaError_t e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, sv->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+  free_all(tmp);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "server read-back");
+  return GPRT_OK;
+}
+
+}  // namespace
+
+namespace gprt {
+void server_forget_scene(gprt_server* sv, gprt_scene* s) {
+  std::vector<SrvRequest> gone;
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    for (auto it = sv->pending.begin(); it != sv->pending.end();) {
+      if (it->scene == s) {
+        gone.push_back(*it);
+        it = sv->pending.erase(it);
+      } else {
+        ++it;
+      }
+    }
+  }
+  for (auto& r : gone) {
+    sv->st.cancelled++;
+    emit(sv, r.ticket, GPRT_EV_CANCELLED, 0, 0, GPRT_E_CANCELLED, r.submit_ms);
+  }
+}
+}  // namespace gprt
+
+extern "C" {
+
+int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server** out) {
+  if (!ctx || !out) return GPRT_E_INVALID;
+  *out = nullptr;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  auto sv = std::make_unique<gprt_server>();
+  sv->ctx = ctx;
+  if (desc) sv->desc = *desc;
+  gprt_server_desc& d = sv->desc;
+  if (d.hbm_budget_bytes == 0) d.hbm_budget_bytes = 60ull << 30;
+  if (d.max_jobs == 0) d.max_jobs = 1024;
+  if (d.step_paths == 0) d.step_paths = 1u << 22;
+  if (d.block_size == 0) d.block_size = 128;
+  if (d.block_size % 32 || d.block_size > 1024) return fail(ctx, GPRT_E_INVALID, "block_size must be a multiple of 32, <= 1024");
+  if (d.max_jobs > (1u << 20)) return fail(ctx, GPRT_E_INVALID, "max_jobs above 2^20");
+  sv->t0 = std::chrono::steady_clock::now();
+  sv->capacity = d.step_paths;
+  sv->step_paths = d.step_paths;
+  sv->block = d.block_size;
+  sv->flags = d.flags;
+  sv->pool[kNodes].elem[0] = 8 * sizeof(float4);
+  sv->pool[kTris].elem[0] = 3 * sizeof(float4);
+  sv->pool[kTris].elem[1] = sizeof(float4);
+  sv->pool[kQuads].elem[0] = 5 * sizeof(float4);
+  sv->pool[kSpheres].elem[0] = 2 * sizeof(float4);
+  sv->pool[kMats].elem[0] = sizeof(DevMaterial);
+  sv->pool[kLights].elem[0] = sizeof(DevLight);
+  // path state of one step
+  DevPaths& P = sv->P;
+  auto& b = sv->path_bufs;
+  uint32_t cap = sv->capacity;
+  size_t bytes = 0;
+  int rc = 0;
+  rc |= dev_alloc(ctx, b, &P.ray_o, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.ray_d, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.weight, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.thr, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.L, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.hit, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.pixel, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.sample, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.rng_pos, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.queue[0], cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.queue[1], cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.sh_o, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.sh_d, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.sh_c, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.sh_root, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.item, cap, &bytes);
+  rc |= dev_alloc(ctx, b, &P.counters, 8, &bytes);
+  if (rc) {
+    free_all(b);
+    return GPRT_E_OOM;
+  }
+  P.capacity = cap;
+  P.stats = nullptr;
+  sv->path_bytes = bytes;
+  sv->prefix_bytes = (16 + 2 * (size_t)(d.max_jobs + 1) * 4 + 255) & ~(size_t)255;
+  sv->table_bytes = sv->prefix_bytes + (size_t)d.max_jobs * sizeof(DevItem);
+  if (sv->path_bytes + sv->table_bytes > d.hbm_budget_bytes) {
+    free_all(b);
+    return fail(ctx, GPRT_E_ADMISSION, "the budget does not cover the path state of one step");
+  }
+  if (dev_alloc(ctx, b, &sv->d_table, sv->table_bytes) ||
+      cudaMallocHost(reinterpret_cast<void**>(&sv->h_table), sv->table_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    free_all(b);
+    return fail(ctx, GPRT_E_OOM, "item table allocation failed");
+  }
+  if (cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    free_all(b);
+    cudaFreeHost(sv->h_table);
+    return fail(ctx, GPRT_E_DEVICE, "stream creation failed");
+  }
+  cudaEventCreate(&sv->ev0);
+  cudaEventCreate(&sv->ev1);
+  cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), sv->stream);
+  cudaError_t e = cudaStreamSynchronize(sv->stream);
+  if (e != cudaSuccess) {
+    free_all(b);
+    cudaFreeHost(sv->h_table);
+    return cuda_fail(ctx, e, "server init");
+  }
+  ctx->servers.insert(sv.get());
+  *out = sv.release();
+  return GPRT_OK;
+}
+
+int gprt_server_destroy(gprt_server* sv) {
+  if (!sv) return GPRT_E_INVALID;
+  gprt_ctx* ctx = sv->ctx;
+  stop_loop(sv);
+  {
+    std::lock_guard<std::mutex> g(sv->smu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(sv->stream);
+    for (auto& kv : sv->jobs) free_all(kv.second->bufs);
+    sv->jobs.clear();
+    sv->scenes.clear();
+    for (auto& a : sv->pool)
+      for (int b = 0; b < 2; b++)
+        if (a.buf[b]) cudaFree(a.buf[b]);
+    drop_graphs(sv);
+    free_all(sv->path_bufs);
+    if (sv->h_table) cudaFreeHost(sv->h_table);
+    cudaEventDestroy(sv->ev0);
+    cudaEventDestroy(sv->ev1);
+    cudaStreamDestroy(sv->stream);
+  }
+  {
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    ctx->servers.erase(sv);
+  }
+  delete sv;
+  return GPRT_OK;
+}
+
+int gprt_server_submit(gprt_server* sv, gprt_scene* s, const gprt_job_desc* desc, uint64_t* ticket) {
+  if (!sv || !s || !desc || s->ctx != sv->ctx) return GPRT_E_INVALID;
+  gprt_ctx* ctx = sv->ctx;
+  if (desc->integrator != GPRT_INTEGRATOR_PATH_TRACING)
+    return fail(ctx, GPRT_E_INVALID, "the batched server runs path tracing only");
+  gprt_job_desc d = *desc;
+  if (d.initial_samples == 0) d.initial_samples = 1;
+  if (d.max_samples_per_pixel == 0) d.max_samples_per_pixel = 50;
+  if (d.max_passes == 0) d.max_passes = 7;
+  if (d.max_samples_per_pixel < d.initial_samples) return fail(ctx, GPRT_E_INVALID, "max samples below initial samples");
+  SrvRequest r;
+  r.scene = s;
+  r.serial = s->serial;
+  r.desc = d;
+  r.submit_ms = now_ms(sv->t0);
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    r.ticket = sv->next_ticket++;
+    sv->pending.push_back(r);
+    sv->st.submitted++;
+    sv->work_gen++;
+  }
+  sv->cv_work.notify_all();
+  if (ticket) *ticket = r.ticket;
+  return GPRT_OK;
+}
+
+int gprt_server_cancel(gprt_server* sv, uint64_t ticket) {
+  if (!sv) return GPRT_E_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    for (auto it = sv->pending.begin(); it != sv->pending.end(); ++it)
+      if (it->ticket == ticket) {
+        double sm = it->submit_ms;
+        sv->pending.erase(it);
+        sv->st.cancelled++;
+        gprt_event e{};
+        e.ticket = ticket;
+        e.kind = GPRT_EV_CANCELLED;
+        e.status = GPRT_E_CANCELLED;
+        e.t_ms = now_ms(sv->t0);
+        e.submit_ms = sm;
+        sv->events.push_back(e);
+        sv->cv_ev.notify_all();
+        return GPRT_OK;
+      }
+  }
+  std::lock_guard<std::mutex> g(sv->smu);
+  SrvJob* j = find_job(sv, ticket);
+  if (!j) return fail(sv->ctx, GPRT_E_NOT_FOUND, "unknown ticket");
+  if (j->running) {
+    sv->st.cancelled++;
+    emit(sv, ticket, GPRT_EV_CANCELLED, j->passes, j->spp_done, GPRT_E_CANCELLED, j->submit_ms);
+  }
+  cudaSetDevice(sv->ctx->device);
+  cudaStreamSynchronize(sv->stream);
+  release_job(sv, j);
+  sv->jobs.erase(ticket);
+  notify_work(sv);
+  return GPRT_OK;
+}
+
+int gprt_server_step(gprt_server* sv, uint32_t* busy) {
+  if (!sv) return GPRT_E_INVALID;
+  int rc;
+  {
+    std::lock_guard<std::mutex> g(sv->smu);
+    cudaSetDevice(sv->ctx->device);
+    rc = step_impl(sv, false, nullptr);
+  }
+  if (busy) {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    *busy = sv->n_running.load() + (uint32_t)sv->pending.size();
+  }
+  return rc < 0 ? rc : GPRT_OK;
+}
+
+int gprt_server_start(gprt_server* sv) {
+  if (!sv) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> lk(sv->qmu);
+  if (sv->loop_running) return GPRT_OK;
+  sv->stopping = false;
+  sv->loop_running = true;
+  sv->loop = std::thread(loop_main, sv);
+  return GPRT_OK;
+}
+
+int gprt_server_stop(gprt_server* sv) {
+  if (!sv) return GPRT_E_INVALID;
+  return stop_loop(sv);
+}
+
+int gprt_server_poll(gprt_server* sv, gprt_event* events, uint32_t max, uint32_t timeout_ms, uint32_t* n) {
+  if (!sv || (max && !events)) return GPRT_E_INVALID;
+  std::unique_lock<std::mutex> lk(sv->qmu);
+  if (sv->events.empty() && timeout_ms)
+    sv->cv_ev.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !sv->events.empty(); });
+  uint32_t k = 0;
+  while (k < max && !sv->events.empty()) {
+    events[k++] = sv->events.front();
+    sv->events.pop_front();
+  }
+  if (n) *n = k;
+  return GPRT_OK;
+}
+
+int gprt_server_read_film(gprt_server* sv, uint64_t ticket, float* rgb_sum, float* lum_sum, float* lum2_sum,
+                          uint32_t* count) {
+  if (!sv) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> g(sv->smu);
+  gprt_ctx* ctx = sv->ctx;
+  cudaSetDevice(ctx->device);
+  SrvJob* j = find_job(sv, ticket);
+  if (!j || j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
+  uint32_t npix = j->npix;
+  CK(ctx, cudaStreamSynchronize(sv->stream));
+  if (rgb_sum || lum_sum) {
+    std::vector<float4> v(npix);
+    CK(ctx, cudaMemcpy(v.data(), j->film.rgbl, (size_t)npix * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < npix; i++) {
+      if (rgb_sum) {
+        rgb_sum[3 * i] = v[i].x;
+        rgb_sum[3 * i + 1] = v[i].y;
+        rgb_sum[3 * i + 2] = v[i].z;
+      }
+      if (lum_sum) lum_sum[i] = v[i].w;
+    }
+  }
+  if (lum2_sum) CK(ctx, cudaMemcpy(lum2_sum, j->film.lum2, (size_t)npix * 4, cudaMemcpyDeviceToHost));
+  if (count) CK(ctx, cudaMemcpy(count, j->film.count, (size_t)npix * 4, cudaMemcpyDeviceToHost));
+  return GPRT_OK;
+}
+
+int gprt_server_read_image(gprt_server* sv, uint64_t ticket, float* rgb_mean) {
+  if (!sv || !rgb_mean) return GPRT_E_INVALID;
+  return read_job(sv, ticket, 1, rgb_mean);
+}
+
+int gprt_server_read_rgba8(gprt_server* sv, uint64_t ticket, uint8_t* rgba) {
+  if (!sv || !rgba) return GPRT_E_INVALID;
+  return read_job(sv, ticket, 0, rgba);
+}
+
+int gprt_server_release(gprt_server* sv, uint64_t ticket) { return gprt_server_cancel(sv, ticket); }
+
+int gprt_server_get_stats(gprt_server* sv, gprt_server_stats* out) {
+  if (!sv || !out) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> g(sv->smu);
+  gprt_server_stats s = sv->st;
+  {
+    std::lock_guard<std::mutex> lk(sv->qmu);
+    s.pending_jobs = (uint32_t)sv->pending.size();
+    s.submitted = sv->st.submitted;
+    s.cancelled = sv->st.cancelled;
+  }
+  s.active_jobs = sv->n_running.load();
+  s.resident_scenes = (uint32_t)sv->scenes.size();
+  s.bytes_in_use = bytes_in_use(sv);
+  s.bytes_budget = sv->desc.hbm_budget_bytes;
+  s.pool_bytes = 0;
+  for (auto& a : sv->pool) s.pool_bytes += a.bytes();
+  s.path_state_bytes = sv->path_bytes;
+  s.step_paths = sv->step_paths;
+  s.block_size = sv->block;
+  s.flags = sv->flags;
+  s.max_jobs = sv->desc.max_jobs;
+  *out = s;
+  return GPRT_OK;
+}
+
+int gprt_server_configure(gprt_server* sv, uint32_t step_paths, uint32_t block_size, uint32_t flags) {
+  if (!sv) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> g(sv->smu);
+  if (step_paths == 0 || step_paths > sv->capacity) return fail(sv->ctx, GPRT_E_INVALID, "step_paths above the capacity");
+  if (block_size == 0 || block_size % 32 || block_size > 1024) return fail(sv->ctx, GPRT_E_INVALID, "bad block_size");
+  sv->step_paths = step_paths;
+  if (sv->block != block_size || sv->flags != flags) {
+    sv->block = block_size;
+    sv->flags = flags;
+    drop_graphs(sv);
+  }
+  return GPRT_OK;
+}
+
+int gprt_server_autotune(gprt_server* sv, double max_step_ms, gprt_tune_result* out) {
+  if (!sv || !out) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> g(sv->smu);
+  gprt_ctx* ctx = sv->ctx;
+  cudaSetDevice(ctx->device);
+  admit(sv);
+  if (pack(sv).empty()) return fail(ctx, GPRT_E_INVALID, "autotune needs admitted, unfinished jobs");
+  uint32_t keep_paths = sv->step_paths, keep_block = sv->block, keep_flags = sv->flags;
+  // samples per ms of dry steps (no film is changed) of the current jobs
+  auto rate = [&](uint32_t paths, uint32_t block, uint32_t flags, double* step_ms) -> double {
+    sv->step_paths = paths;
+    if (sv->block != block || sv->flags != flags) {
+      sv->block = block;
+      sv->flags = flags;
+      drop_graphs(sv);
+    }
+    std::vector<Item> items = pack(sv);
+    uint64_t n = 0;
+    for (auto& it : items) n += (uint64_t)it.layers * it.j->npix;
+    double ms = 0;
+    if (step_impl(sv, true, &ms) <= 0) return -1.0;  // warm-up (and graph capture)
+    double total = 0;
+    for (int r = 0; r < 2; r++) {
+      if (step_impl(sv, true, &ms) <= 0) return -1.0;
+      total += ms;
+    }
+    *step_ms = total / 2;
+    return *step_ms > 0 ? (double)n / *step_ms : -1.0;
+  };
+  std::vector<uint32_t> sizes;
+  for (uint32_t p = sv->capacity; p >= (1u << 18) && sizes.size() < 5; p >>= 1) sizes.push_back(p);
+  double step_ms = 0;
+  double best = rate(keep_paths, keep_block, keep_flags, &step_ms);
+  double default_ms = step_ms;
+  uint32_t bp = keep_paths, bb = keep_block, bf = keep_flags;
+  bool best_ok = max_step_ms <= 0 || step_ms <= max_step_ms;
+  uint32_t tried = 1;
+  auto consider = [&](uint32_t p, uint32_t b, uint32_t f) {
+    double ms = 0;
+    double r = rate(p, b, f, &ms);
+    tried++;
+    if (r <= 0) return;
+    bool ok = max_step_ms <= 0 || ms <= max_step_ms;
+    if ((ok && !best_ok) || (ok == best_ok && r > best)) {
+      best = r;
+      best_ok = ok;
+      bp = p;
+      bb = b;
+      bf = f;
+      out->best_ms = ms;
+    }
+  };
+  out->best_ms = step_ms;
+  for (uint32_t p : sizes)
+    if (p != keep_paths) consider(p, bb, bf);
+  for (uint32_t b : {64u, 128u, 256u})
+    if (b != bb) consider(bp, b, bf);
+  uint32_t variant_bits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW;
+  for (uint32_t v : {0u, (uint32_t)GPRT_JOB_SIMPLE_EXTEND, (uint32_t)GPRT_JOB_SIMPLE_SHADOW})
+    if (v != (bf & variant_bits)) consider(bp, bb, (bf & ~variant_bits) | v);
+  sv->step_paths = bp;
+  if (sv->block != bb || sv->flags != bf) {
+    sv->block = bb;
+    sv->flags = bf;
+    drop_graphs(sv);
+  }
+  (void)keep_block;
+  out->flags = bf;
+  out->block_size = bb;
+  out->chunk_paths = bp;
+  out->candidates = tried;
+  out->default_ms = default_ms;
+  return GPRT_OK;
+}
+
+}  // extern "C"

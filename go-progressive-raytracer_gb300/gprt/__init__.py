@@ -10,3 +10,4 @@ from .renderer import (BDPTIntegrator, Context, GpuScene, PassResult, PathTracin
 from .scene import (Box, CameraConfig, Dielectric, Emissive, Lambertian, Layered, MaterialTable, Mesh,  # noqa: F401
                     Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, Triangle, TriangleMesh)
 from . import scenes  # noqa: F401
+from .server import RenderServer, ServerEvent, latency_summary  # noqa: F401

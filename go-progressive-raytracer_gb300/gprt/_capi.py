@@ -115,6 +115,32 @@ class RenderStats(C.Structure):
                 ("pass_number", C.c_uint32), ("pass_ms", C.c_double), ("splats", C.c_uint64)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_jobs", C.c_uint32), ("step_paths", C.c_uint32),
+                ("block_size", C.c_uint32), ("flags", C.c_uint32)]
+
+
+SERVER_NO_GRAPHS = 16
+EV_ADMITTED, EV_PASS, EV_DONE, EV_REFUSED, EV_CANCELLED, EV_FAILED = range(1, 7)
+EVENT_NAMES = {EV_ADMITTED: "admitted", EV_PASS: "pass", EV_DONE: "done", EV_REFUSED: "refused",
+               EV_CANCELLED: "cancelled", EV_FAILED: "failed"}
+
+
+class Event(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("kind", C.c_uint32), ("pass_number", C.c_uint32),
+                ("samples_per_pixel", C.c_uint32), ("status", C.c_int32), ("t_ms", C.c_double),
+                ("submit_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("steps", "graph_launches", "samples", "paths", "submitted", "admitted",
+                                           "finished", "refused", "cancelled")] + \
+        [(n, C.c_uint32) for n in ("active_jobs", "pending_jobs", "resident_scenes", "reserved")] + \
+        [(n, C.c_uint64) for n in ("bytes_in_use", "bytes_budget", "pool_bytes", "path_state_bytes")] + \
+        [(n, C.c_double) for n in ("busy_ms", "last_step_ms")] + \
+        [(n, C.c_uint32) for n in ("step_paths", "block_size", "flags", "max_jobs")]
+
+
 P = C.c_void_p
 PP = C.POINTER(C.c_void_p)
 F32P = C.POINTER(C.c_float)
@@ -152,6 +178,21 @@ SIGNATURES = {
     "gprt_job_stream": (C.c_int, [P, PP]),
     "gprt_render_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint64, P, P]),
     "gprt_autotune": (C.c_int, [P, C.POINTER(JobDesc), C.c_uint32, C.POINTER(TuneResult)]),
+    "gprt_server_create": (C.c_int, [P, C.POINTER(ServerDesc), PP]),
+    "gprt_server_destroy": (C.c_int, [P]),
+    "gprt_server_submit": (C.c_int, [P, P, C.POINTER(JobDesc), U64P]),
+    "gprt_server_cancel": (C.c_int, [P, C.c_uint64]),
+    "gprt_server_step": (C.c_int, [P, U32P]),
+    "gprt_server_start": (C.c_int, [P]),
+    "gprt_server_stop": (C.c_int, [P]),
+    "gprt_server_poll": (C.c_int, [P, C.POINTER(Event), C.c_uint32, C.c_uint32, U32P]),
+    "gprt_server_read_film": (C.c_int, [P, C.c_uint64, F32P, F32P, F32P, U32P]),
+    "gprt_server_read_image": (C.c_int, [P, C.c_uint64, F32P]),
+    "gprt_server_read_rgba8": (C.c_int, [P, C.c_uint64, U8P]),
+    "gprt_server_release": (C.c_int, [P, C.c_uint64]),
+    "gprt_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "gprt_server_configure": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "gprt_server_autotune": (C.c_int, [P, C.c_double, C.POINTER(TuneResult)]),
 }
 
 _lib = None

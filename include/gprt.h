@@ -246,6 +246,7 @@ typedef struct gprt_render_stats {
 typedef struct gprt_ctx gprt_ctx;
 typedef struct gprt_scene gprt_scene;
 typedef struct gprt_job gprt_job;
+typedef struct gprt_server gprt_server;
 
 /* ---- context ------------------------------------------------------------ */
 int gprt_version(void);
@@ -365,6 +366,105 @@ int gprt_autotune(gprt_scene* scene, const gprt_job_desc* base, uint32_t spp, gp
  * `stream` (NULL = the context stream). */
 #define GPRT_NOALLOC_MAX_PATHS 131072u
 int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* rgb_out, void* stream);
+
+/* ---- serving ---------------------------------------------------------------
+ * The reference serves concurrent progressive renders from its web server:
+ * one ProgressiveRaytracer per HTTP request, each with its own NumCPU worker
+ * pool, no admission control and no batching (web/server/render.go:45-82,
+ * 183-227; the pass loop is RenderProgressive, progressive.go:286-368).
+ * A gprt_server is the device-resident equivalent with continuous batching:
+ *   - requests (a scene + a gprt_job_desc pass schedule) are submitted from
+ *     any thread and queue in arrival order;
+ *   - admission copies the scene's BVH and primitives into a device pool
+ *     shared by all jobs (scenes submitted several times are held once) and
+ *     gives the job its film; a request is admitted when its bytes fit the
+ *     HBM budget (refused at once when they never can);
+ *   - every step packs the next samples of many admitted jobs into ONE
+ *     wavefront (raygen -> [extend -> shade -> shadow] x depth ->
+ *     accumulate, the bounce sequence replayed as a captured CUDA graph),
+ *     so jobs of any size share each launch; jobs admitted while others are
+ *     in flight join the next step;
+ *   - a pass of a job completes when all its samples are accumulated; events
+ *     report admission, every pass (with host timestamps for time-to-first-
+ *     pass and per-pass latency), completion, refusal and cancellation.
+ * Passes follow getSamplesForPass (progressive.go:98-123) over
+ * initial_samples / max_samples_per_pixel / max_passes of the request's
+ * gprt_job_desc, every pixel taking every sample (the scene's adaptive
+ * stopping is not applied).  A job's film equals, bit for bit, the film of a
+ * gprt_job with the same scene, seed and sample count: each sample is keyed
+ * by (seed, pixel, sample index) and each pixel accumulates its samples in
+ * order, whatever else shares the wavefront.  Path tracing only
+ * (integrator = GPRT_INTEGRATOR_PATH_TRACING). */
+typedef struct gprt_server_desc {
+  uint64_t hbm_budget_bytes; /* device bytes held at most: path state + scene pool + films (0: 60 GiB) */
+  uint32_t max_jobs;         /* admitted (unreleased) jobs at most (0: 1024) */
+  uint32_t step_paths;       /* path capacity of one step's wavefront (0: 1 << 22) */
+  uint32_t block_size;       /* threads per block of raygen / shade / accumulate (0: 128) */
+  uint32_t flags;            /* GPRT_SERVER_* and GPRT_JOB_SIMPLE_* bits */
+} gprt_server_desc;
+#define GPRT_SERVER_NO_GRAPHS 16u /* launch each bounce kernel instead of replaying a captured graph */
+
+enum {
+  GPRT_EV_ADMITTED = 1,  /* the request holds a film and its scene is resident */
+  GPRT_EV_PASS = 2,      /* a pass completed (PassResult, progressive.go:258-263) */
+  GPRT_EV_DONE = 3,      /* the last pass completed; the film stays until released */
+  GPRT_EV_REFUSED = 4,   /* never fits the budget, or invalid (status = GPRT_E_*) */
+  GPRT_EV_CANCELLED = 5, /* gprt_server_cancel, or its scene was destroyed before admission */
+  GPRT_EV_FAILED = 6     /* a device error ended the job (status = GPRT_E_*) */
+};
+typedef struct gprt_event {
+  uint64_t ticket;
+  uint32_t kind;              /* GPRT_EV_* */
+  uint32_t pass_number;       /* passes completed */
+  uint32_t samples_per_pixel; /* samples every pixel of the film holds */
+  int32_t status;
+  double t_ms;                /* host time of the event, ms since the server was created */
+  double submit_ms;           /* host time the request was submitted */
+} gprt_event;
+
+typedef struct gprt_server_stats {
+  uint64_t steps, graph_launches, samples, paths;
+  uint64_t submitted, admitted, finished, refused, cancelled;
+  uint32_t active_jobs, pending_jobs, resident_scenes, reserved;
+  uint64_t bytes_in_use, bytes_budget, pool_bytes, path_state_bytes;
+  double busy_ms;             /* device time of all steps (CUDA events) */
+  double last_step_ms;
+  uint32_t step_paths, block_size, flags, max_jobs;
+} gprt_server_stats;
+
+int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server** out);
+/* Stops the loop thread, cancels what is pending and frees every film and the pool. */
+int gprt_server_destroy(gprt_server* server);
+/* Queues a request; the scene must stay alive until the request is admitted
+ * (destroying it earlier cancels the request).  Thread-safe. */
+int gprt_server_submit(gprt_server* server, gprt_scene* scene, const gprt_job_desc* desc, uint64_t* ticket);
+/* Cancels a pending or running request (its film is released). */
+int gprt_server_cancel(gprt_server* server, uint64_t ticket);
+/* Runs one step on the calling thread: admission, one batched wavefront,
+ * events.  *busy = admitted-but-unfinished plus pending requests after it. */
+int gprt_server_step(gprt_server* server, uint32_t* busy);
+/* Starts / stops a loop thread that steps whenever there is work. */
+int gprt_server_start(gprt_server* server);
+int gprt_server_stop(gprt_server* server);
+/* Takes up to `max` events, waiting up to timeout_ms for the first one. */
+int gprt_server_poll(gprt_server* server, gprt_event* events, uint32_t max, uint32_t timeout_ms, uint32_t* n);
+/* Film / image of an admitted job (in flight or done), as gprt_job_read_*. */
+int gprt_server_read_film(gprt_server* server, uint64_t ticket, float* rgb_sum, float* lum_sum, float* lum2_sum,
+                          uint32_t* count);
+int gprt_server_read_image(gprt_server* server, uint64_t ticket, float* rgb_mean);
+int gprt_server_read_rgba8(gprt_server* server, uint64_t ticket, uint8_t* rgba);
+/* Frees the film of a finished (or cancels and frees a running) job. */
+int gprt_server_release(gprt_server* server, uint64_t ticket);
+int gprt_server_get_stats(gprt_server* server, gprt_server_stats* stats);
+/* Changes the step size / block size / GPRT_JOB_SIMPLE_* variant between steps
+ * (step_paths up to the capacity given at creation). */
+int gprt_server_configure(gprt_server* server, uint32_t step_paths, uint32_t block_size, uint32_t flags);
+/* Autotuner of the batched loop: times candidate step sizes, block sizes and
+ * traversal variants on steps of the jobs currently admitted, without adding
+ * their samples to any film, and applies the configuration with the highest
+ * samples per second among those whose step takes at most max_step_ms
+ * (0: no limit).  Needs admitted, unfinished jobs. */
+int gprt_server_autotune(gprt_server* server, double max_step_ms, gprt_tune_result* out);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,203 @@
+"""The batched render server (gprt_server_*).
+
+A job's film must be the same, bit for bit, whether it runs alone through the
+plain per-job path (gprt_job_add_samples), alone in the server, or in the
+server beside other scenes and resolutions: every sample is keyed by (seed,
+pixel, sample index) and each pixel adds its samples in order.  The
+tolerance is therefore exact equality."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _plain_film(g, seed, spp):
+    import gprt
+    r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=spp, max_passes=1, seed=seed))
+    r.add_samples(spp)
+    f = r.film()
+    r.close()
+    return f
+
+
+def _cfg(spp, per_pass, seed):
+    import gprt
+    passes = max(1, spp // per_pass)
+    return gprt.ProgressiveConfig(initial_samples=per_pass, max_samples_per_pixel=spp, max_passes=passes, seed=seed)
+
+
+def _same(a, b):
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+@pytest.fixture(scope="module")
+def scenes(ctx):
+    import gprt
+    from gprt import scenes as S
+    out = {
+        "cornell": gprt.GpuScene(ctx, S.cornell_baseline(48).to_desc()),
+        "ico": gprt.GpuScene(ctx, S.icosphere_scene(level=4, width=40).to_desc()),
+        "spheres_a": gprt.GpuScene(ctx, S.default_style_scene(5, width=64, height=48).to_desc()),
+        "spheres_b": gprt.GpuScene(ctx, S.default_style_scene(9, width=32, height=32).to_desc()),
+    }
+    yield out
+    for g in out.values():
+        g.close()
+
+
+def test_job_alone_in_server_equals_plain_job(ctx, scenes):
+    import gprt
+    g = scenes["cornell"]
+    plain = _plain_film(g, 3, 8)
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    t = sv.submit(g, _cfg(8, 4, 3))
+    ev = sv.run_until_idle()
+    kinds = [e.kind for e in ev if e.ticket == t]
+    assert kinds == ["admitted", "pass", "pass", "done"]
+    _same(sv.film(t), plain)
+    sv.close()
+
+
+def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
+    import gprt
+    jobs = [("cornell", 3, 8, 4), ("ico", 5, 6, 2), ("spheres_a", 7, 12, 4), ("spheres_b", 11, 4, 1),
+            ("cornell", 13, 4, 4)]
+    plain = [_plain_film(scenes[n], seed, spp) for n, seed, spp, _ in jobs]
+    # a small step capacity forces jobs to share steps and to be split across them
+    sv = gprt.RenderServer(ctx, step_paths=3 * 64 * 48)
+    tickets = [sv.submit(scenes[n], _cfg(spp, per, seed)) for n, seed, spp, per in jobs]
+    ev = sv.run_until_idle()
+    done = {e.ticket for e in ev if e.kind == "done"}
+    assert done == set(tickets)
+    for t, p in zip(tickets, plain):
+        _same(sv.film(t), p)
+    st = sv.stats()
+    assert st["resident_scenes"] == 4  # the two cornell requests share one pooled copy
+    assert st["samples"] == sum(scenes[n].width * scenes[n].height * spp for n, _, spp, _ in jobs)
+    sv.close()
+
+
+def test_graphs_and_direct_launches_agree(ctx, scenes):
+    import gprt
+    from gprt import capi
+    out = []
+    for flags in (0, capi.SERVER_NO_GRAPHS, capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW):
+        sv = gprt.RenderServer(ctx, step_paths=1 << 15, flags=flags)
+        ts = [sv.submit(scenes["spheres_a"], _cfg(4, 2, 1)), sv.submit(scenes["ico"], _cfg(4, 2, 2))]
+        sv.run_until_idle()
+        out.append([sv.film(t) for t in ts])
+        st = sv.stats()
+        assert (st["graph_launches"] > 0) == (not flags & capi.SERVER_NO_GRAPHS)
+        sv.close()
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            _same(a, b)
+
+
+def test_pass_events_follow_the_progressive_schedule(ctx, scenes):
+    import gprt
+    g = scenes["spheres_b"]
+    sv = gprt.RenderServer(ctx)
+    # getSamplesForPass: initial 1, max 10 over 4 passes -> 1, 4, 7, 10
+    t = sv.submit(g, gprt.ProgressiveConfig(initial_samples=1, max_samples_per_pixel=10, max_passes=4, seed=2))
+    ev = [e for e in sv.run_until_idle() if e.ticket == t]
+    passes = [e for e in ev if e.kind == "pass"]
+    assert [e.samples_per_pixel for e in passes] == [1, 4, 7, 10]
+    assert [e.pass_number for e in passes] == [1, 2, 3, 4]
+    assert all(b.t_ms >= a.t_ms for a, b in zip(passes, passes[1:]))
+    assert passes[0].t_ms >= passes[0].submit_ms
+    _same(sv.film(t), _plain_film(g, 2, 10))
+    img = sv.rgba8(t)
+    assert img.shape == (g.height, g.width, 4) and img[..., 3].min() == 255
+    sv.close()
+
+
+def test_admission_by_budget(ctx, scenes):
+    import gprt
+    g = scenes["spheres_a"]
+    film = g.width * g.height * 24  # sum rgb + lum, lum^2, count
+    sv0 = gprt.RenderServer(ctx, step_paths=1 << 12)
+    sv0.submit(g, _cfg(2, 2, 1))
+    sv0.step()
+    used = sv0.stats()["bytes_in_use"]  # path state + pooled scene + one film
+    sv0.close()
+    budget = used + film // 2  # room for one film, not two
+    sv = gprt.RenderServer(ctx, hbm_budget_bytes=budget, step_paths=1 << 12)
+    big = sv.submit(scenes["ico"], _cfg(2, 2, 1))  # its pooled BVH never fits
+    a = sv.submit(g, _cfg(2, 2, 1))
+    b = sv.submit(g, _cfg(2, 2, 2))
+    sv.step()
+    ev = sv.poll()
+    assert any(e.ticket == big and e.kind == "refused" for e in ev)
+    assert any(e.ticket == a and e.kind == "admitted" for e in ev)
+    assert not any(e.ticket == b for e in ev)
+    while sv.step():
+        ev += sv.poll()
+        if any(e.ticket == a and e.kind == "done" for e in ev):
+            break
+    ev += sv.poll()
+    assert any(e.ticket == a and e.kind == "done" for e in ev)
+    assert not any(e.ticket == b for e in ev)  # waits: a's film is still held
+    assert sv.stats()["pending_jobs"] == 1
+    sv.release(a)
+    ev = sv.run_until_idle()
+    assert any(e.ticket == b and e.kind == "done" for e in ev)
+    _same(sv.film(b), _plain_film(g, 2, 2))
+    assert sv.stats()["bytes_in_use"] <= budget
+    sv.close()
+
+
+def test_cancel_and_scene_destroy(ctx, scenes):
+    import gprt
+    from gprt import scenes as S
+    sv = gprt.RenderServer(ctx, max_jobs=1)
+    t1 = sv.submit(scenes["spheres_b"], _cfg(64, 1, 1))
+    tmp = gprt.GpuScene(ctx, S.default_style_scene(21, width=16, height=16).to_desc())
+    t2 = sv.submit(tmp, _cfg(4, 4, 1))  # pending: max_jobs = 1
+    sv.step()
+    tmp.close()  # destroyed before admission -> cancelled
+    sv.cancel(t1)  # running -> cancelled, film released
+    ev = sv.poll()
+    assert any(e.ticket == t2 and e.kind == "cancelled" for e in ev)
+    assert any(e.ticket == t1 and e.kind == "cancelled" for e in ev)
+    assert sv.step() == 0
+    with pytest.raises(gprt.capi.GprtError):
+        sv.film(t1)
+    sv.close()
+
+
+def test_loop_thread_serves_concurrent_submissions(ctx, scenes):
+    import time
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 14)
+    sv.start()
+    reqs = [("spheres_a", 1, 4), ("ico", 2, 4), ("cornell", 3, 4), ("spheres_b", 4, 8)]
+    tickets = []
+    for n, seed, spp in reqs:
+        tickets.append(sv.submit(scenes[n], _cfg(spp, 2, seed)))
+        time.sleep(0.002)  # arrivals while earlier jobs are on the GPU
+    ev, deadline = [], time.time() + 60
+    while time.time() < deadline and len({e.ticket for e in ev if e.kind == "done"}) < len(tickets):
+        ev += sv.poll(timeout_ms=100)
+    sv.stop()
+    assert {e.ticket for e in ev if e.kind == "done"} == set(tickets)
+    for t, (n, seed, spp) in zip(tickets, reqs):
+        _same(sv.film(t), _plain_film(scenes[n], seed, spp))
+    lat = gprt.latency_summary(ev)
+    assert lat["jobs"] == 4 and lat["ttfp_p99_ms"] > 0
+    sv.close()
+
+
+def test_server_autotune_keeps_films_and_picks_a_valid_config(ctx, scenes):
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 18)
+    ts = [sv.submit(scenes["spheres_a"], _cfg(4, 4, 1)), sv.submit(scenes["ico"], _cfg(4, 4, 2))]
+    r = sv.autotune()
+    assert r["candidates"] >= 5 and 0 < r["chunk_paths"] <= 1 << 18 and r["block_size"] in (64, 128, 256)
+    st = sv.stats()
+    assert st["step_paths"] == r["chunk_paths"] and st["samples"] == 0  # tuning steps add no samples
+    sv.run_until_idle()
+    _same(sv.film(ts[0]), _plain_film(scenes["spheres_a"], 1, 4))
+    _same(sv.film(ts[1]), _plain_film(scenes["ico"], 2, 4))
+    sv.close()
