@@ -1,17 +1,30 @@
-"""Benchmark of the GB300 rendering path on the BVH-stress workload.
+"""Benchmark of the GB300 rendering path: batched serving vs the plain path.
 
-Workload (one step): 16 samples per pixel of the 1024x1024 path-traced image
-of a level-8 displaced icosphere (1,310,720 triangles, one material per
-face) on a ground quad under a uniform infinite light, max depth 8 -- one
-pass of the hot path over 16,777,216 pixel samples.  Metric: Msamples/s.
+Headline workload (one step): the heterogeneous batch -- 256 seeded
+default-style sphere scenes (ground sphere, 3 feature spheres, 10-500 small
+spheres of 60/25/15 % Lambertian / metal / glass, gradient sky) at
+resolutions drawn from {128^2, 256^2, 512^2, 1024x768}, spp ~ U[1,64], max
+depth 8, about 2.14 G pixel samples -- rendered to completion by the batched
+render server (many jobs per wavefront, bounce sequences replayed from CUDA
+graphs, autotuned step size / block size / traversal variant).  Metric:
+aggregate Msamples/s.  Beside it, on the same GPU:
+  plain      the same 256 jobs one at a time through the per-job path;
+  serving    Poisson request streams mixing the Cornell (400^2), icosphere
+             (1024^2, 1.3 M triangles), Cornell-boxes (512^2) and
+             default-style scenes, target spp 16-256 in passes of 4 spp:
+             p50/p99 time-to-first-pass and per-pass latency, aggregate
+             Msamples/s, batched server vs plain one-job-at-a-time;
+  bvh_stress the 1024^2 icosphere at 16 spp through the per-job path.
+Every job's film is the same alone and in the batch (bit for bit), so the
+comparison is at equal image RMSE.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 N > 1 runs under torchrun as N independent replicas (one per GPU, weak
 scaling, no data-path collective); rank 0 prints one JSON line.
 `--impl reference` times the reference algorithm on the host cores (the
-float64 restatement in oracle/, 64x64 tiles on all host threads, scene build
-excluded) on a bounded sample of the same workload.
+float64 restatement in oracle/, 64x64 tiles on all host threads) on a bounded
+sample of the same batch.
 """
 import argparse
 import json
@@ -29,23 +42,27 @@ for _p in (PKG, ROOT):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-WIDTH = 1024
-SPP = 16
+NJOBS = 256
+JOB_SEED = 17
 DEPTH = 8
-LEVEL = 8
 METRIC = "Msamples/s at fixed image RMSE, batched-serving vs plain; p50/p99 first-pass ms"
-WORKLOAD = "icosphere-L8 displaced (1,310,720 tris, per-face Lambertian/metal), ground quad, uniform sky; " \
-           "1024x1024, 16 spp per step, max depth 8, path tracing"
+WORKLOAD = "256 heterogeneous default-style sphere scenes (seed 17; 10-500 spheres each; 128^2/256^2/512^2/1024x768; " \
+           "spp U[1,64]; max depth 8), path tracing, batched render server"
+ICO_WIDTH, ICO_SPP, ICO_LEVEL = 1024, 16, 8
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gprt", choices=["gprt", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--stream-requests", type=int, default=48)
+    ap.add_argument("--rates", default="20,100,200")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-bvh-stress", action="store_true")
+    ap.add_argument("--no-stream", action="store_true")
     return ap.parse_args()
 
 
@@ -60,11 +77,6 @@ def build_libs():
         m = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(m)
         m.build()
-
-
-def make_scene():
-    from gprt import scenes
-    return scenes.icosphere_scene(level=LEVEL, width=WIDTH, max_depth=DEPTH)
 
 
 class ClockSampler:
@@ -126,36 +138,78 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per extend launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "extend_traffic.json")
+def committed_traffic(name, rays_per_launch):
+    """DRAM bytes per launch of the extend kernel: the committed ncu capture's
+    DRAM bytes per ray (a smaller case of the same kernel) x rays per launch."""
+    p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
         d = json.load(open(p))
-        return d.get("dram_bytes_per_launch"), d
+        return d["dram_bytes_per_ray"] * rays_per_launch, d
     return None, None
 
 
-def cpu_baseline(flat, seconds=15.0, threads=None, seed=101):
-    """The oracle (float64 restatement of the reference's CPU path) on a
-    bounded sample of the workload: whole 64x64 tiles at 16 spp."""
+def aggregate_over_ranks(ms, samples_per_rank, steps, dist=None, device="cpu"):
+    """Max timed-region duration over the replicas and the whole-job rate
+    (weak scaling: every rank renders its own copy of the workload, no
+    data-path collective).  Returns (ms, Msamples/s)."""
+    world = 1
+    if dist is not None and dist.is_initialized():
+        import torch
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        world = dist.get_world_size()
+    return ms, world * samples_per_rank * steps / (ms / 1e3) / 1e6
+
+
+def batch_jobs():
+    from gprt import scenes
+    return [(s.to_desc(), spp) for s, spp in scenes.batched_jobs(NJOBS, JOB_SEED, DEPTH)]
+
+
+def job_config(spp, seed=1):
+    import gprt
+    return gprt.ProgressiveConfig(initial_samples=spp, max_samples_per_pixel=spp, max_passes=1, seed=seed)
+
+
+# ----------------------------------------------------------------- CPU side
+def oracle_sample(jobs, seconds, threads, seed):
+    """Renders whole 64x64 tiles of the batch's jobs (in order, at each job's
+    spp) with the oracle until about `seconds` of work; returns
+    (samples, seconds, description)."""
     from oracle import client
-    threads = threads or os.cpu_count()
-    t0 = time.time()
-    sc = client.OracleScene(flat)
-    build_s = time.time() - t0
-    r = client.OracleRenderer(sc, 0, max_spp=SPP, max_passes=1, seed=seed, threads=threads)
-    probe = max(1, threads)
-    secs, st = r.render_pass(1, only_tiles=probe)
-    rate = st[1] / max(secs, 1e-9)  # samples/s (tiles beyond `probe` hold 0 samples)
-    tiles = int(min(256, max(probe, probe * seconds / max(secs, 1e-3))))
-    r2 = client.OracleRenderer(sc, 0, max_spp=SPP, max_passes=1, seed=seed + 1, threads=threads)
-    secs2, st2 = r2.render_pass(1, only_tiles=tiles)
-    r.close()
-    r2.close()
-    sc.close()
-    return {"value": st2[1] / secs2 / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": "%d of 256 64x64 tiles of the 1024x1024 image at 16 spp (%d samples, %.1f s); scene build "
-                      "%.1f s excluded" % (tiles, st2[1], secs2, build_s)}
+    done_s, done_n, parts = 0.0, 0, []
+    for k, (flat, spp) in enumerate(jobs):
+        if done_s >= seconds:
+            break
+        sc = client.OracleScene(flat)
+        ntiles = ((sc.width + 63) // 64) * ((sc.height + 63) // 64)
+        r = client.OracleRenderer(sc, 0, max_spp=spp, max_passes=1, seed=seed + k, threads=threads)
+        probe = min(ntiles, threads)
+        secs, st = r.render_pass(1, only_tiles=probe)
+        r.close()
+        per_tile = secs / probe
+        want = int(min(ntiles, max(probe, (seconds - done_s) / max(per_tile, 1e-6))))
+        used = probe
+        if want > probe:
+            r = client.OracleRenderer(sc, 0, max_spp=spp, max_passes=1, seed=seed + k, threads=threads)
+            secs, st = r.render_pass(1, only_tiles=want)
+            r.close()
+            used = want
+        sc.close()
+        done_s += secs
+        done_n += st[1]
+        parts.append("job %d: %d tiles at %d spp" % (k, used, spp))
+    return done_n, done_s, "; ".join(parts)
+
+
+def cpu_baseline(jobs, seconds=15.0):
+    threads = os.cpu_count()
+    n, s, desc = oracle_sample(jobs, seconds, threads, 101)
+    return {"value": n / s / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": "oracle (float64 restatement of the reference CPU path), %d host threads, %d samples in %.1f s "
+                      "of whole 64x64 tiles of the batch's first jobs (%s); scene builds excluded"
+                      % (threads, n, s, desc)}
 
 
 def run_reference(args):
@@ -163,29 +217,187 @@ def run_reference(args):
     if rank != 0:
         return 0
     build_libs()
-    from oracle import client
-    flat = make_scene().to_desc()
-    sc = client.OracleScene(flat)
+    jobs = batch_jobs()
     threads = os.cpu_count()
-    tiles = max(threads, 16)
+    per_step = 4.0  # seconds of host work per step
     times, samples = [], []
     for i in range(args.warmup + args.steps):
-        r = client.OracleRenderer(sc, 0, max_spp=SPP, max_passes=1, seed=1000 + i, threads=threads)
-        secs, st = r.render_pass(1, only_tiles=tiles)
-        r.close()
+        n, s, desc = oracle_sample(jobs[i % 8:], per_step, threads, 1000 + 17 * i)
         if i >= args.warmup:
-            times.append(secs)
-            samples.append(st[1])
+            times.append(s)
+            samples.append(n)
     v = sum(samples) / sum(times) / 1e6
     line = {"metric": METRIC, "value": v, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "parallelism": "host threads", "sample": "%d tiles per step" % tiles},
+            "config": {"workload": WORKLOAD, "parallelism": "%d host threads" % threads,
+                       "sample": "about %.0f s of whole 64x64 tiles of the batch's jobs per step" % per_step},
             "cpu_baseline": {"value": v, "unit": "Msamples/s", "cores": threads, "kind": "port",
-                             "sample": "%d of 256 64x64 tiles at 16 spp per step" % tiles},
+                             "sample": "about %.0f s of whole 64x64 tiles of the batch's jobs per step" % per_step},
             "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+# ----------------------------------------------------------------- GPU side
+def run_batch(sv, gscenes, spps, seed=1):
+    """Submits every job, steps the server until all are done and releases
+    them; returns the jobs' sample total."""
+    tickets = [sv.submit(g, job_config(s, seed)) for g, s in zip(gscenes, spps)]
+    sv.run_until_idle()
+    for t in tickets:
+        sv.release(t)
+    return sum(g.width * g.height * s for g, s in zip(gscenes, spps))
+
+
+def run_plain_batch(gscenes, spps, seed=1):
+    """The same jobs one at a time through the per-job path."""
+    import gprt
+    n = 0
+    for g, s in zip(gscenes, spps):
+        r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=s, max_passes=1, seed=seed))
+        r.add_samples(s)
+        r.sync()
+        r.close()
+        n += g.width * g.height * s
+    return n
+
+
+def stream_batched(ctx, server_kw, tune, reqs, arrivals, gs):
+    """Serves a request stream with the batched server's loop thread."""
+    import gprt
+    sv = gprt.RenderServer(ctx, **server_kw)
+    sv.configure(tune["chunk_paths"], tune["block_size"], tune["flags"])
+    sv.start()
+    t0 = time.perf_counter()
+    tickets = []
+    for (kind, spp), at in zip(reqs, arrivals):
+        while time.perf_counter() - t0 < at:
+            time.sleep(0.0002)
+        cfg = gprt.ProgressiveConfig(initial_samples=4, max_samples_per_pixel=spp, max_passes=spp // 4, seed=5)
+        tickets.append(sv.submit(gs[kind], cfg))
+    ev = []
+    deadline = time.perf_counter() + 600
+    while len({e.ticket for e in ev if e.kind == "done"}) < len(tickets) and time.perf_counter() < deadline:
+        ev += sv.poll(1024, timeout_ms=20)
+    sv.stop()
+    st = sv.stats()
+    for t in tickets:
+        sv.release(t)
+    sv.close()
+    first_submit = min((e.submit_ms for e in ev), default=0.0)
+    last_done = max((e.t_ms for e in ev if e.kind == "done"), default=first_submit)
+    return ev, tickets, (last_done - first_submit) / 1e3, st
+
+
+def stream_plain(reqs, arrivals, gs):
+    """The same stream served one job at a time, in arrival order, by the
+    per-job path (passes of 4 spp)."""
+    import gprt
+    ev = []
+    t0 = time.perf_counter()
+    for k, ((kind, spp), at) in enumerate(zip(reqs, arrivals)):
+        now = time.perf_counter() - t0
+        if now < at:
+            time.sleep(at - now)
+        r = gprt.ProgressiveRaytracer(gs[kind], gprt.ProgressiveConfig(max_samples_per_pixel=spp, max_passes=spp // 4,
+                                                                       seed=5))
+        for p in range(spp // 4):
+            r.add_samples(4)
+            r.sync()
+            ev.append(gprt.ServerEvent(k, "pass", p + 1, 4 * (p + 1), 0, 1e3 * (time.perf_counter() - t0), 1e3 * at))
+        r.close()
+        ev.append(gprt.ServerEvent(k, "done", spp // 4, spp, 0, 1e3 * (time.perf_counter() - t0), 1e3 * at))
+    last = max(e.t_ms for e in ev) / 1e3
+    return ev, last - arrivals[0]
+
+
+def serving_section(ctx, args, server_kw, tune, flats):
+    """Request streams at each rate, batched and (at the middle rate) plain."""
+    import gprt
+    from gprt import scenes
+    gs = [gprt.GpuScene(ctx, f) for f in flats]
+    sizes = [g.width * g.height for g in gs]
+    reqs = scenes.serving_requests(args.stream_requests)
+    samples = sum(sizes[k] * spp for k, spp in reqs)
+    out = {"requests": len(reqs), "mix": "Cornell 400^2 / icosphere 1024^2 / Cornell boxes 512^2 / default-style "
+                                         "scene, target spp U{16..256} in passes of 4 spp",
+           "samples_per_stream": samples, "rates": {}}
+    rates = [float(x) for x in args.rates.split(",") if x]
+    for rate in rates:
+        arr = scenes.poisson_arrivals(len(reqs), rate)
+        ev, tickets, span, st = stream_batched(ctx, server_kw, tune, reqs, arr, gs)
+        t512 = [t for t, (k, _) in zip(tickets, reqs) if gs[k].width == 512 and gs[k].height == 512]
+        out["rates"][str(int(rate))] = {
+            "batched": {"msamples_per_s": samples / span / 1e6, "makespan_s": span,
+                        **gprt.latency_summary(ev),
+                        "ttfp_p99_ms_512sq": gprt.latency_summary(ev, t512)["ttfp_p99_ms"],
+                        "steps": st["steps"], "graph_launches": st["graph_launches"]}}
+    mid = rates[len(rates) // 2] if rates else None
+    if mid is not None:
+        arr = scenes.poisson_arrivals(len(reqs), mid)
+        ev, span = stream_plain(reqs, arr, gs)
+        idx512 = [k for k, (kind, _) in enumerate(reqs) if gs[kind].width == 512 and gs[kind].height == 512]
+        out["rates"][str(int(mid))]["plain"] = {"msamples_per_s": samples / span / 1e6, "makespan_s": span,
+                                                **gprt.latency_summary(ev),
+                                                "ttfp_p99_ms_512sq": gprt.latency_summary(ev, idx512)["ttfp_p99_ms"]}
+    for g in gs:
+        g.close()
+    return out
+
+
+def bvh_stress(ctx, flat, torch):
+    """The icosphere at 1024^2, 16 spp through the autotuned per-job path."""
+    import gprt
+    from gprt import capi
+    g = gprt.GpuScene(ctx, flat)
+    cj = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=ICO_SPP, max_passes=1, seed=1,
+                                                             flags=capi.JOB_COUNT_TRAVERSAL | capi.JOB_TIME_KERNELS))
+    cj.add_samples(ICO_SPP)
+    cnt = cj.counters()
+    cj.close()
+    tuned, tune = gprt.renderer.autotune(g, spp=ICO_SPP, config=gprt.ProgressiveConfig(max_samples_per_pixel=ICO_SPP))
+    job = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1,
+                                                              flags=capi.JOB_TIME_KERNELS | tuned.flags,
+                                                              block_size=tuned.block_size,
+                                                              chunk_paths=tuned.chunk_paths))
+    stream = torch.cuda.ExternalStream(job.stream())
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        job.add_samples(ICO_SPP)
+    job.sync()
+    job.counters(reset=True)
+    steps = 10
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        job.add_samples(ICO_SPP)
+    ev1.record(stream)
+    job.sync()
+    ms = ev0.elapsed_time(ev1)
+    kc = job.counters()
+    peak, _ = measured_peaks()
+    alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 36 * cnt["extend_prims"]
+    per_launch = alg / max(1, cnt["extend_launches"])
+    avg_ms = kc["extend_ms"] / max(1, kc["extend_launches"])
+    achieved = per_launch / (avg_ms / 1e3) / 1e9
+    traffic, _ = committed_traffic("extend_traffic.json", cnt["extend_rays"] / max(1, cnt["extend_launches"]))
+    npix = g.width * g.height
+    out = {"workload": "icosphere-L8 displaced (1,310,720 tris), ground quad, uniform sky; 1024x1024, 16 spp, depth 8",
+           "msamples_per_s": npix * ICO_SPP * steps / (ms / 1e3) / 1e6, "ms_per_frame": ms / steps,
+           "mrays_per_s": (cnt["extend_rays"] + cnt["shadow_rays"]) * steps / (ms / 1e3) / 1e6,
+           "extend_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                               "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms},
+           "host_bvh_build_ms": g.info.build_ms,
+           "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
+    job.close()
+    g.close()
+    del flush
+    return out
 
 
 def run_gprt(args):
@@ -200,35 +412,38 @@ def run_gprt(args):
     import gprt
     from gprt import capi
 
-    scene = make_scene()
-    flat = scene.to_desc()
+    jobs = batch_jobs()
     ctx = gprt.Context(local)
-    g = gprt.GpuScene(ctx, flat)
-    npix = g.width * g.height
-    samples_per_step = npix * SPP
+    gscenes = [gprt.GpuScene(ctx, f) for f, _ in jobs]
+    spps = [s for _, s in jobs]
+    samples_per_step = sum(g.width * g.height * s for g, s in zip(gscenes, spps))
+    cap = 1 << 24
 
-    # work per extend launch, counted once on the same inputs (not timed)
-    cj = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=SPP, max_passes=1, seed=1,
-                                                             flags=capi.JOB_COUNT_TRAVERSAL | capi.JOB_TIME_KERNELS))
-    cj.add_samples(SPP)
-    cnt = cj.counters()
-    cj.close()
+    # work per extend launch, counted once on the same batch (not timed)
+    sv = gprt.RenderServer(ctx, step_paths=cap,
+                           flags=capi.JOB_COUNT_TRAVERSAL | capi.JOB_TIME_KERNELS | capi.SERVER_NO_GRAPHS)
+    run_batch(sv, gscenes, spps)
+    cnt = sv.counters()
+    sv.close()
+    launches_counted = cnt["extend_launches"]
 
-    # autotuned wavefront size / traversal variants / block size (not timed)
-    tuned, tune = gprt.renderer.autotune(g, spp=SPP, config=gprt.ProgressiveConfig(max_samples_per_pixel=SPP))
-    job = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1,
-                                                              flags=capi.JOB_TIME_KERNELS | tuned.flags,
-                                                              block_size=tuned.block_size,
-                                                              chunk_paths=tuned.chunk_paths))
-    stream = torch.cuda.ExternalStream(job.stream())
+    # the batched server, autotuned on the admitted batch (tuning steps change no film)
+    sv = gprt.RenderServer(ctx, step_paths=cap)
+    tickets = [sv.submit(g, job_config(s)) for g, s in zip(gscenes, spps)]
+    tune = sv.autotune()
+    sv.run_until_idle()
+    film0 = sv.film(tickets[0])
+    for t in tickets:
+        sv.release(t)
+    sv.configure(tune["chunk_paths"], tune["block_size"], tune["flags"] | capi.JOB_TIME_KERNELS)
+    stream = torch.cuda.ExternalStream(sv.stream())
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         with torch.cuda.stream(stream):
             flush.zero_()
-        job.add_samples(SPP)
-    job.sync()
-    job.counters(reset=True)
-    launches0 = job.launches()
+        run_batch(sv, gscenes, spps)
+    sv.counters(reset=True)
+    st0 = sv.stats()
     clocks = ClockSampler(local)
     if dist:
         dist.barrier()
@@ -239,96 +454,136 @@ def run_gprt(args):
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()  # L2 flush: 512 MB write before every step
-        job.add_samples(SPP)
+        run_batch(sv, gscenes, spps)
     ev1.record(stream)
-    job.sync()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    timed_launches = job.launches() - launches0 + args.steps  # + the flush kernels
-    kc = job.counters()
+    st1 = sv.stats()
+    kc = sv.counters()
+    timed_kernels = st1["kernels"] - st0["kernels"] + args.steps  # + the flush kernels
+    ms, value = aggregate_over_ranks(ms, samples_per_step, args.steps, dist, "cuda")
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
+    server_kw = {"step_paths": cap, "block_size": tune["block_size"], "flags": tune["flags"]}
+    timing_source = "CUDA events captured in the step graphs of the timed region"
+    if kc["extend_launches"] == 0:
+        # no event-record nodes fired: time one more batch with direct launches
+        sv.configure(tune["chunk_paths"], tune["block_size"],
+                     tune["flags"] | capi.JOB_TIME_KERNELS | capi.SERVER_NO_GRAPHS)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        sv.counters(reset=True)
+        run_batch(sv, gscenes, spps)
+        kc = sv.counters()
+        kc = {k: (v * args.steps if k.endswith("_ms") else v) for k, v in kc.items()}
+        timing_source = "CUDA events around direct launches, one batch after the timed region"
+    sv.close()
+    del flush
 
-    # roofline of the dominant kernel: closest-hit traversal ("extend")
+    # roofline of the dominant kernel: closest-hit traversal ("extend") over
+    # the pooled sphere BVHs.  Algorithmic bytes per ray: ray in (32 B) + hit
+    # out (16 B) + 24 B per child-box test + 16 B (center, radius) per sphere test.
     peak, peak_kind = measured_peaks()
-    ray_b = 32 + 16
-    alg_bytes = cnt["extend_rays"] * ray_b + 24 * cnt["extend_boxes"] + 36 * cnt["extend_prims"]
-    per_launch = alg_bytes / max(1, cnt["extend_launches"])
+    alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 16 * cnt["extend_prims"]
+    per_launch = alg / max(1, launches_counted)
     avg_ms = kc["extend_ms"] / max(1, kc["extend_launches"])
-    achieved = per_launch / (avg_ms / 1e3) / 1e9
-    traffic, _ = committed_traffic()
-    roof = {"bound": "hbm", "kernel": "k_pt_extend (closest-hit BVH4 traversal)", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
-            "rays_per_launch": cnt["extend_rays"] / max(1, cnt["extend_launches"]),
+    achieved = per_launch / (avg_ms / 1e3) / 1e9 if kc["extend_launches"] else None
+    traffic, _ = committed_traffic("extend_batch_traffic.json", cnt["extend_rays"] / max(1, launches_counted))
+    roof = {"bound": "hbm", "kernel": "k_pt_extend (closest-hit BVH4 traversal, all jobs of a step)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "traffic": traffic,
+            "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launch_timing": timing_source,
+            "rays_per_launch": cnt["extend_rays"] / max(1, launches_counted),
             "box_tests_per_ray": cnt["extend_boxes"] / max(1, cnt["extend_rays"]),
-            "tri_tests_per_ray": cnt["extend_prims"] / max(1, cnt["extend_rays"])}
-    kernel_share = {k: kc[k + "_ms"] for k in ("extend", "shade", "shadow", "other")}
-    rays_total = (cnt["extend_rays"] + cnt["shadow_rays"]) * args.steps  # per-step rays x steps (same workload)
+            "sphere_tests_per_ray": cnt["extend_prims"] / max(1, cnt["extend_rays"])}
+    kernel_ms = {k: kc[k + "_ms"] / args.steps for k in ("extend", "shade", "shadow", "other")}
 
-    # end to end through the C ABI with host buffers
+    # the plain per-job path on the same batch (host clock around device-synchronised jobs)
+    plain = None
+    if rank == 0:
+        run_plain_batch(gscenes[:16], spps[:16])  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n = run_plain_batch(gscenes, spps)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        r = gprt.ProgressiveRaytracer(gscenes[0], gprt.ProgressiveConfig(max_samples_per_pixel=spps[0], max_passes=1,
+                                                                         seed=1))
+        r.add_samples(spps[0])
+        same = all(np.array_equal(a, b) for a, b in zip(r.film(), film0))
+        r.close()
+        plain = {"msamples_per_s": n / tp / 1e6, "s_per_batch": tp, "timing": "host clock, device-synchronised",
+                 "batched_over_plain": value / world / (n / tp / 1e6), "film_of_job0_identical": bool(same)}
+
+    # end to end through the public API with host buffers: scene descriptions
+    # in (host BVH build + upload), every job's RGBA8 image out
     e2e = None
-    if args.e2e_steps > 0:
-        rgba = np.zeros((g.height, g.width, 4), dtype=np.uint8)
-        h2d = 0
-        t_total = 0.0
-        parts = {"scene_create_ms": 0.0, "render_ms": 0.0, "readback_ms": 0.0}
+    if args.e2e_steps > 0 and rank == 0:
+        sv = gprt.RenderServer(ctx, **server_kw)
+        sv.configure(tune["chunk_paths"], tune["block_size"], tune["flags"])
+        total_t, h2d, d2h = 0.0, 0, 0
         for i in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s2 = gprt.GpuScene(ctx, flat)
+            gs2 = [gprt.GpuScene(ctx, f) for f, _ in jobs]
+            tickets = [sv.submit(g, job_config(s, 7 + i)) for g, s in zip(gs2, spps)]
+            sv.run_until_idle()
+            imgs = [sv.rgba8(t) for t in tickets]
+            for t in tickets:
+                sv.release(t)
             t1 = time.perf_counter()
-            j2 = gprt.ProgressiveRaytracer(s2, gprt.ProgressiveConfig(max_samples_per_pixel=SPP, max_passes=1, seed=7 + i))
-            j2.add_samples(SPP)
-            j2.sync()
-            t2 = time.perf_counter()
-            ctx.check(ctx.lib.gprt_job_read_rgba8(j2.h, rgba.ctypes.data_as(capi.U8P)))
-            t3 = time.perf_counter()
-            h2d = s2.info.device_bytes
-            j2.close()
-            s2.close()
-            if i == 0:
-                continue  # first call warms allocations
-            t_total += t3 - t0
-            parts["scene_create_ms"] += 1e3 * (t1 - t0) / args.e2e_steps
-            parts["render_ms"] += 1e3 * (t2 - t1) / args.e2e_steps
-            parts["readback_ms"] += 1e3 * (t3 - t2) / args.e2e_steps
-        e2e = {"value": samples_per_step * args.e2e_steps / t_total / 1e6, "unit": "Msamples/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(rgba.nbytes),
-               "includes": "scene upload + host BVH build, job create, 16 spp, RGBA8 read-back", **parts}
+            h2d = sum(g.info.device_bytes for g in gs2)
+            d2h = sum(im.nbytes for im in imgs)
+            for g in gs2:
+                g.close()
+            if i > 0:
+                total_t += t1 - t0
+        sv.close()
+        e2e = {"value": samples_per_step * args.e2e_steps / total_t / 1e6, "unit": "Msamples/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "includes": "256 scene builds (host BVH) + uploads, submit, batched render, 256 RGBA8 read-backs"}
+
+    ico_flat = None
+    serving = None
+    if rank == 0 and not args.no_stream:
+        from gprt import scenes
+        ico_flat = scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH).to_desc()
+        flats = [scenes.cornell_baseline(400).to_desc(), ico_flat, scenes.cornell_boxes_bdpt(512).to_desc(), jobs[0][0]]
+        serving = serving_section(ctx, args, server_kw, tune, flats)
+
+    stress = None
+    if rank == 0 and not args.no_bvh_stress:
+        from gprt import scenes
+        if ico_flat is None:
+            ico_flat = scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH).to_desc()
+        stress = bvh_stress(ctx, ico_flat, torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(flat)
+            cpu = cpu_baseline(jobs)
         except Exception as e:  # the baseline never blocks the GPU line
             cpu = {"value": None, "error": str(e)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere, no dataset)",
-                "config": {"workload": WORKLOAD, "samples_per_step": samples_per_step, "triangles": 1310720,
-                           "l2": "flushed (512 MB write before every timed step)",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, no dataset)",
+                "config": {"workload": WORKLOAD, "jobs": NJOBS, "samples_per_step": samples_per_step,
+                           "l2": "flushed (512 MB write before every timed step); path state 4.6 GB > L2",
                            "parallelism": "replicas" if world > 1 else "single GPU",
-                           "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size,
-                                         "simple_extend": bool(tuned.flags & capi.JOB_SIMPLE_EXTEND),
-                                         "simple_shadow": bool(tuned.flags & capi.JOB_SIMPLE_SHADOW),
-                                         "candidates": tune["candidates"], "tuning_pass_ms": tune["best_ms"],
-                                         "default_pass_ms": tune["default_ms"]}},
-                "mrays_per_s": rays_total * world / (ms / 1e3) / 1e6,
-                "roofline": roof, "kernel_ms": kernel_share, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": int(timed_launches), "clocks": clk,
-                "scene": {"nodes": int(g.info.n_nodes), "device_mb": g.info.device_bytes / 2 ** 20,
-                          "host_bvh_build_ms": g.info.build_ms}}
+                           "autotuned": {"step_paths": tune["chunk_paths"], "block_size": tune["block_size"],
+                                         "simple_extend": bool(tune["flags"] & capi.JOB_SIMPLE_EXTEND),
+                                         "simple_shadow": bool(tune["flags"] & capi.JOB_SIMPLE_SHADOW),
+                                         "candidates": tune["candidates"]},
+                           "server_steps_per_batch": (st1["steps"] - st0["steps"]) / args.steps},
+                "plain": plain, "serving": serving, "bvh_stress": stress,
+                "roofline": roof, "kernel_ms_per_step": kernel_ms, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": int(timed_kernels), "clocks": clk}
         print(json.dumps(line))
-    job.close()
-    g.close()
+    for g in gscenes:
+        g.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -14,30 +14,15 @@ int ensure_paths(gprt_job* j) {
   gprt_ctx* ctx = j->scene->ctx;
   uint32_t cap = j->desc.chunk_paths;
   DevPaths& P = j->paths;
-  auto& b = j->buffers;
-  int rc = 0;
-  rc |= dev_alloc(ctx, b, &P.ray_o, cap);
-  rc |= dev_alloc(ctx, b, &P.ray_d, cap);
-  rc |= dev_alloc(ctx, b, &P.weight, cap);
-  rc |= dev_alloc(ctx, b, &P.thr, cap);
-  rc |= dev_alloc(ctx, b, &P.L, cap);
-  rc |= dev_alloc(ctx, b, &P.hit, cap);
-  rc |= dev_alloc(ctx, b, &P.pixel, cap);
-  rc |= dev_alloc(ctx, b, &P.sample, cap);
-  rc |= dev_alloc(ctx, b, &P.rng_pos, cap);
-  rc |= dev_alloc(ctx, b, &P.queue[0], cap);
-  rc |= dev_alloc(ctx, b, &P.queue[1], cap);
-  rc |= dev_alloc(ctx, b, &P.sh_o, cap);
-  rc |= dev_alloc(ctx, b, &P.sh_d, cap);
-  rc |= dev_alloc(ctx, b, &P.sh_c, cap);
-  rc |= dev_alloc(ctx, b, &P.counters, 8);
-  if (j->desc.flags & GPRT_JOB_COUNT_TRAVERSAL) rc |= dev_alloc(ctx, b, &j->d_stats, 8);
+  unsigned char* region = nullptr;
+  int rc = dev_alloc(ctx, j->buffers, &region, path_region_bytes(cap, false));
+  if (!rc && (j->desc.flags & GPRT_JOB_COUNT_TRAVERSAL)) rc = dev_alloc(ctx, j->buffers, &j->d_stats, 8);
   if (rc) return GPRT_E_OOM;
+  carve_paths(region, cap, false, P);
   P.stats = j->d_stats;
-  P.variant = j->desc.flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  P.variant = j->desc.flags & kVariantBits;
   CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), j->stream));
   if (j->d_stats) CK(ctx, cudaMemsetAsync(j->d_stats, 0, 8 * sizeof(unsigned long long), j->stream));
-  P.capacity = cap;
   return GPRT_OK;
 }
 
@@ -129,7 +114,7 @@ void run_chunk(gprt_job* j, const ChunkDesc& ch) {
     }
     {
       TimedLaunch t(j, 2);
-      launch_pt_shadow(sc, j->paths, block, g, j->stream);
+      launch_pt_shadow(sc, j->paths, cur, block, g, j->stream);
     }
     cur ^= 1;
   }
@@ -713,12 +698,9 @@ int gprt_job_stream(gprt_job* j, void** stream) {
 namespace {
 
 constexpr size_t kNoAllocPaths = GPRT_NOALLOC_MAX_PATHS;
-constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-// per-path arrays: 9 float4 (ray o/d, weight, thr, L, hit, shadow o/d/c) and
-// 5 uint32 (pixel, sample, rng position, two queues), plus 8 counters
-constexpr size_t kNoAllocF4 = align256(kNoAllocPaths * sizeof(float4));
-constexpr size_t kNoAllocU32 = align256(kNoAllocPaths * sizeof(uint32_t));
-constexpr size_t kNoAllocBytes = 256 + 9 * kNoAllocF4 + 5 * kNoAllocU32;
+// the path state of kNoAllocPaths paths (two compacted queues of ray, weight,
+// throughput, radiance and sampler ids; hits; origin radiance; shadow rays)
+constexpr size_t kNoAllocBytes = path_region_bytes((uint32_t)kNoAllocPaths, false);
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -748,7 +730,7 @@ __global__ void k_noalloc_mean(DevPaths P, uint32_t npix, uint32_t layers, float
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint32_t l = 0; l < layers; l++) {
-      float4 c = P.L[l * npix + i];
+      float4 c = P.Lout[l * npix + i];
       acc.x += c.x;
       acc.y += c.y;
       acc.z += c.z;
@@ -784,23 +766,17 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
   if (rc) return rc;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   DevPaths P{};
-  P.counters = reinterpret_cast<uint32_t*>(base);
-  unsigned char* f4 = base + 256;
-  float4** f4s[9] = {&P.ray_o, &P.ray_d, &P.weight, &P.thr, &P.L, &P.hit, &P.sh_o, &P.sh_d, &P.sh_c};
-  for (int k = 0; k < 9; k++) *f4s[k] = reinterpret_cast<float4*>(f4 + k * kNoAllocF4);
-  unsigned char* u = f4 + 9 * kNoAllocF4;
-  uint32_t** u32s[5] = {&P.pixel, &P.sample, &P.rng_pos, &P.queue[0], &P.queue[1]};
-  for (int k = 0; k < 5; k++) *u32s[k] = reinterpret_cast<uint32_t*>(u + k * kNoAllocU32);
+  carve_paths(base, (uint32_t)kNoAllocPaths, false, P);
   P.stats = nullptr;
-  P.capacity = (uint32_t)kNoAllocPaths;
   // queue counters and the error word start at zero
   CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), st));
-  // a film view whose sample counts are zero: the queue[1] array holds them
-  // until the first bounce (raygen reads them before any path is queued there)
+  // a film view whose sample counts are zero: the ids array of the second
+  // queue holds them until the first bounce (raygen reads them before any
+  // path is moved there)
   DevFilm film{};
   film.width = (int)s->host.sampling.width;
   film.height = (int)s->host.sampling.height;
-  film.count = P.queue[1];
+  film.count = reinterpret_cast<uint32_t*>(P.q[1].ids);
   k_noalloc_zero<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(film.count, (uint32_t)npix);
   ChunkDesc ch{};
   ch.pix0 = 0;
@@ -817,7 +793,7 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
   for (int b = 0; b < sc.max_depth; b++) {
     launch_pt_extend(sc, P, cur, block, grid, st);
     launch_pt_shade(sc, P, ch, cur, b, block, grid, st);
-    launch_pt_shadow(sc, P, block, grid, st);
+    launch_pt_shadow(sc, P, cur, block, grid, st);
     cur ^= 1;
   }
   k_noalloc_mean<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(P, (uint32_t)npix, spp, rgb_out);
@@ -862,7 +838,7 @@ extern "C" int gprt_autotune(gprt_scene* s, const gprt_job_desc* base, uint32_t 
   cudaSetDevice(ctx->device);
   std::memset(out, 0, sizeof(*out));
   gprt_job_desc d = *base;
-  d.flags &= ~(GPRT_JOB_TIME_KERNELS | GPRT_JOB_COUNT_TRAVERSAL | GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  d.flags &= ~(GPRT_JOB_TIME_KERNELS | GPRT_JOB_COUNT_TRAVERSAL | kVariantBits);
   d.max_samples_per_pixel = std::max(d.max_samples_per_pixel, 2 * spp);
   uint64_t npix = (uint64_t)s->host.sampling.width * s->host.sampling.height;
   uint64_t work = npix * spp;
@@ -897,6 +873,10 @@ extern "C" int gprt_autotune(gprt_scene* s, const gprt_job_desc* base, uint32_t 
       cand.flags = fl0 | v;
       consider(cand);
     }
+    // shading kernel with fewer registers
+    gprt_job_desc cand = d;
+    cand.flags ^= GPRT_JOB_SHADE_OCCUPANCY;
+    consider(cand);
   }
   // block size of the non-persistent kernels
   for (uint32_t b : {64u, 256u}) {
@@ -904,7 +884,7 @@ extern "C" int gprt_autotune(gprt_scene* s, const gprt_job_desc* base, uint32_t 
     cand.block_size = b;
     consider(cand);
   }
-  out->flags = d.flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  out->flags = d.flags & kVariantBits;
   out->block_size = d.block_size;
   out->chunk_paths = d.chunk_paths;
   out->best_ms = best;

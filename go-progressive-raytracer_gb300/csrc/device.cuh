@@ -153,23 +153,38 @@ struct Hit {
   float u, v;
 };
 
+// The primitive tests below spell out every rounding (explicit fma / mul /
+// add / div intrinsics): kernels that inline them in different contexts -- the
+// traversal variants, the single-job and the batched wavefronts -- then
+// return bit-identical hits.
+__device__ __forceinline__ float dot_rn(float3 a, float3 b) {
+  return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, __fmul_rn(a.z, b.z)));
+}
+__device__ __forceinline__ float3 cross_rn(float3 a, float3 b) {
+  return make_float3(__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)), __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+                     __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float3 sub_rn(float3 a, float3 b) {
+  return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+
 // ----------------------------------------------------------------- primitives
 // Triangle.Hit, Moller-Trumbore, epsilon 1e-8 (pkg/geometry/triangle.go:107-175)
 // Triangles are stored as (v0, e1 = v1 - v0, e2 = v2 - v0).
 __device__ __forceinline__ bool hit_triangle(float3 o, float3 d, float4 a, float4 b, float4 c, float tmin,
                                              float tmax, float& t, float& uu, float& vv) {
   float3 v0 = f3(a), e1 = f3(b), e2 = f3(c);
-  float3 h = cross(d, e2);
-  float det = dot(e1, h);
+  float3 h = cross_rn(d, e2);
+  float det = dot_rn(e1, h);
   if (det > -1e-8f && det < 1e-8f) return false;
-  float f = 1.0f / det;
-  float3 s = o - v0;
-  float u = f * dot(s, h);
+  float f = __frcp_rn(det);
+  float3 s = sub_rn(o, v0);
+  float u = __fmul_rn(f, dot_rn(s, h));
   if (u < 0.f || u > 1.f) return false;
-  float3 q = cross(s, e1);
-  float v = f * dot(d, q);
-  if (v < 0.f || u + v > 1.f) return false;
-  float tt = f * dot(e2, q);
+  float3 q = cross_rn(s, e1);
+  float v = __fmul_rn(f, dot_rn(d, q));
+  if (v < 0.f || __fadd_rn(u, v) > 1.f) return false;
+  float tt = __fmul_rn(f, dot_rn(e2, q));
   if (tt < tmin || tt > tmax) return false;
   t = tt;
   uu = u;
@@ -183,15 +198,15 @@ __device__ __forceinline__ bool hit_quad(float3 o, float3 d, const float4* q, fl
                                          float& alpha, float& beta) {
   float4 c = q[0];
   float3 n = f3(q[3]);
-  float den = dot(d, n);
+  float den = dot_rn(d, n);
   if (fabsf(den) < 1e-8f) return false;
-  float tt = (c.w - dot(o, n)) / den;
+  float tt = __fdiv_rn(__fsub_rn(c.w, dot_rn(o, n)), den);
   if (tt < tmin || tt > tmax) return false;
-  float3 p = o + d * tt;
-  float3 hv = p - f3(c);
+  float3 p = make_float3(__fmaf_rn(d.x, tt, o.x), __fmaf_rn(d.y, tt, o.y), __fmaf_rn(d.z, tt, o.z));
+  float3 hv = sub_rn(p, f3(c));
   float3 U = f3(q[1]), V = f3(q[2]), W = f3(q[4]);
-  float a = dot(W, cross(hv, V));
-  float b = dot(W, cross(U, hv));
+  float a = dot_rn(W, cross_rn(hv, V));
+  float b = dot_rn(W, cross_rn(U, hv));
   if (a < 0.f || a > 1.f || b < 0.f || b > 1.f) return false;
   t = tt;
   alpha = a;
@@ -205,21 +220,22 @@ __device__ __forceinline__ bool hit_quad(float3 o, float3 d, const float4* q, fl
 // (Ray Tracing Gems, 2019, ch. 7) to keep FP32 usable for radius-1000
 // spheres; the roots are the same quantities as (-halfB -/+ sqrt(D)) / a.
 __device__ __forceinline__ bool hit_sphere(float3 o, float3 d, float4 s, float tmin, float tmax, float& t) {
-  float3 f = o - f3(s);
-  float a = dot(d, d);
-  float halfB = dot(f, d);
-  float3 l = f - d * (halfB / a);
-  float r2 = s.w * s.w;
-  float disc = a * (r2 - dot(l, l));
+  float3 f = sub_rn(o, f3(s));
+  float a = dot_rn(d, d);
+  float halfB = dot_rn(f, d);
+  float k = __fdiv_rn(halfB, a);
+  float3 l = make_float3(__fmaf_rn(-d.x, k, f.x), __fmaf_rn(-d.y, k, f.y), __fmaf_rn(-d.z, k, f.z));
+  float r2 = __fmul_rn(s.w, s.w);
+  float disc = __fmul_rn(a, __fsub_rn(r2, dot_rn(l, l)));
   if (disc < 0.f) return false;
-  float sq = sqrtf(disc);
-  float qq = -halfB - copysignf(sq, halfB);
-  float c = dot(f, f) - r2;
+  float sq = __fsqrt_rn(disc);
+  float qq = __fsub_rn(-halfB, copysignf(sq, halfB));
+  float c = __fsub_rn(dot_rn(f, f), r2);
   float t0, t1;
   if (qq == 0.f) {
-    t0 = t1 = -halfB / a;
+    t0 = t1 = __fdiv_rn(-halfB, a);
   } else {
-    float ra = c / qq, rb = qq / a;
+    float ra = __fdiv_rn(c, qq), rb = __fdiv_rn(qq, a);
     t0 = fminf(ra, rb);
     t1 = fmaxf(ra, rb);
   }

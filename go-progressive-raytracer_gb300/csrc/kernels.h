@@ -17,28 +17,52 @@ struct DevFilm {
   int width, height;
 };
 
-// Wavefront path state (structure of arrays, capacity = paths per chunk)
+// Live paths of one bounce, compacted: slot i of the queue holds the whole
+// state of one path (structure of arrays), so every kernel of a bounce reads
+// and writes contiguous slots.
+struct PathBuf {
+  float4* ray_o;   // origin.xyz, primitive the ray leaves (uint bits)
+  float4* ray_d;   // direction.xyz, BVH root node of the path's scene (int bits)
+  float4* weight;  // radiance weight rgb, origin index of the path (uint bits)
+  float4* thr;     // Russian-roulette throughput rgb
+  float4* L;       // radiance gathered so far rgb
+  uint4* ids;      // pixel, sample index, sampler position, work item
+};
+
+// Wavefront path state (capacity = paths per chunk).  Paths are generated in
+// origin order (origin index = layer * npix + pixel of the chunk) into q[0];
+// each shade kernel compacts the continuing paths of q[cur] into q[cur ^ 1]
+// and writes the radiance of finished paths to Lout at their origin index.
 struct DevPaths {
-  float4* ray_o;   // origin.xyz, skip primitive (as int bits)
-  float4* ray_d;   // direction.xyz, BVH root node of the path's scene (as int bits)
-  float4* weight;  // radiance weight (rgb)
-  float4* thr;     // Russian-roulette throughput (rgb)
-  float4* L;       // radiance gathered so far (rgb)
-  float4* hit;     // t, prim, u, v
-  uint32_t* pixel;
-  uint32_t* sample;
-  uint32_t* rng_pos;  // uniform numbers consumed so far by the path's sample
-  uint32_t* queue[2];
+  PathBuf q[2];
+  float4* hit;     // closest hit of slot i of the current queue: t, prim, u, v
+  float4* Lout;    // radiance of every finished path, by origin index
   float4* sh_o;    // shadow ray origin.xyz, tmax
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
-  float4* sh_c;    // contribution rgb, path index (int bits)
+  float4* sh_c;    // contribution rgb, target: slot of the next queue, or origin index | kShadowToOrigin
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
-  uint32_t* item;  // work item (job) of each path (multi-job wavefronts; null otherwise)
-  uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits
+  uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
-  uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW
+  uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY
 };
+
+constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;
+
+constexpr uint32_t kShadowToOrigin = 0x80000000u;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Device bytes of the path state of `cap` paths (one region: counters, two
+// queues, hits, origin radiance, shadow rays; sh_root when multi-scene).
+constexpr size_t path_region_bytes(uint32_t cap, bool multi) {
+  return 256 + 2 * (5 * align256((size_t)cap * sizeof(float4)) + align256((size_t)cap * sizeof(uint4))) +
+         5 * align256((size_t)cap * sizeof(float4)) + (multi ? align256((size_t)cap * sizeof(int)) : 0);
+}
+
+// Points the arrays of P at consecutive 256-byte-aligned ranges of `base`
+// (path_region_bytes(cap, multi) bytes, 256-byte aligned).
+void carve_paths(unsigned char* base, uint32_t cap, bool multi, DevPaths& P);
 
 // Pixels a chunk covers: `layers` consecutive samples of `npix` pixels,
 // pixel i = pix_list ? pix_list[pix0 + i] : pix0 + i.
@@ -60,7 +84,7 @@ void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st);
-void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int block, int grid, cudaStream_t st);
+void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
 void launch_accumulate(const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block, cudaStream_t st);
 
 // bidirectional path tracing (pkg/integrator/bdpt.go), one sample per thread

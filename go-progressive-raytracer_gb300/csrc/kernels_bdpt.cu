@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(128) k_bdpt(DevScene sc, DevFilm film, DevPath
         }
       }
     }
-    PS.L[p] = make_float4(total.x, total.y, total.z, 0.f);
+    PS.Lout[p] = make_float4(total.x, total.y, total.z, 0.f);
   }
 }
 

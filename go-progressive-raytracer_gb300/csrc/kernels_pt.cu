@@ -87,15 +87,14 @@ __global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch)
     float2 jit = rng.next2();
     float3 o, d;
     camera_ray(sc.cam, x, y, lens, jit, o, d);
-    P.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
-    P.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(sc.root));
-    P.weight[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.pixel[p] = pix;
-    P.sample[p] = sample;
-    P.rng_pos[p] = rng.pos;
-    P.queue[0][p] = p;
+    const PathBuf& Q = P.q[0];
+    Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
+    Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(sc.root));
+    Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
+    Q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    Q.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, 0u);
+    P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[0] = n;
@@ -124,14 +123,16 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, uint32_t ray
   }
 }
 
+// The rays of the current queue; built on the host and passed as a kernel
+// argument, so its pointers stay in the constant bank.
 struct ExtendSource {
-  DevPaths P;
-  const uint32_t* q;
-  uint32_t n;
-  __device__ uint32_t count() const { return n; }
+  const float4* ray_o;
+  const float4* ray_d;
+  float4* hit;
+  const uint32_t* n;
+  __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
-    uint32_t p = q[i];
-    float4 a = P.ray_o[p], b = P.ray_d[p];
+    float4 a = ray_o[i], b = ray_d[i];
     rt = __float_as_int(b.w);
     o = f3(a);
     d = f3(b);
@@ -140,34 +141,33 @@ struct ExtendSource {
     skip = __float_as_uint(a.w);
   }
   __device__ void store(uint32_t i, const Hit& h) const {
-    uint32_t p = q[i];
     bool any = h.prim != kNoHit;
-    P.hit[p] = make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), h.u, h.v);
+    hit[i] = make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), h.u, h.v);
   }
 };
 
 template <bool kCount>
-__global__ void __launch_bounds__(128, 8) k_pt_extend(DevScene sc, DevPaths P, int cur) {
+__global__ void __launch_bounds__(128, 8)
+    k_pt_extend(DevScene sc, ExtendSource src, uint32_t* counters, int cur, unsigned long long* stats) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.counters[cur ^ 1] = 0;  // next queue and shadow queue start empty
-    P.counters[2] = 0;
+    counters[cur ^ 1] = 0;  // next queue and shadow queue start empty
+    counters[2] = 0;
   }
-  ExtendSource src{P, P.queue[cur], P.counters[cur]};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
-  trace_persistent<false, kCount>(sc, src, P.counters + 4, reinterpret_cast<int*>(P.counters + 3), &ts, &rays);
-  if (kCount) add_counts(P.stats, rays, ts);
+  trace_persistent<false, kCount>(sc, src, counters + 4, reinterpret_cast<int*>(counters + 3), &ts, &rays);
+  if (kCount) add_counts(stats, rays, ts);
 }
 
 // One ray per thread (grid-stride), the variant GPRT_JOB_SIMPLE_EXTEND selects.
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_pt_extend_simple(DevScene sc, DevPaths P, int cur) {
-  uint32_t n = P.counters[cur];
+__global__ void __launch_bounds__(256)
+    k_pt_extend_simple(DevScene sc, ExtendSource src, uint32_t* counters, int cur, unsigned long long* stats) {
+  uint32_t n = src.count();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.counters[cur ^ 1] = 0;
-    P.counters[2] = 0;
+    counters[cur ^ 1] = 0;
+    counters[2] = 0;
   }
-  ExtendSource src{P, P.queue[cur], n};
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
   uint32_t end = kCount ? ((n + 31) & ~31u) : n;  // whole warps stay for the count reduction
@@ -179,12 +179,12 @@ __global__ void __launch_bounds__(256) k_pt_extend_simple(DevScene sc, DevPaths 
       int root;
       src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace_from<false, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      trace_from<false, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(counters + 3), &ts);
       src.store(i, h);
       rays++;
     }
   }
-  if (kCount) add_counts(P.stats, rays, ts);
+  if (kCount) add_counts(stats, rays, ts);
 }
 
 static int sm_count_current() {
@@ -195,15 +195,16 @@ static int sm_count_current() {
 }
 
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
+  ExtendSource src{P.q[cur].ray_o, P.q[cur].ray_d, P.hit, P.counters + cur};
   if (P.variant & GPRT_JOB_SIMPLE_EXTEND) {
     int b = std::min(block, 256);
-    if (P.stats) k_pt_extend_simple<true><<<grid, b, 0, st>>>(sc, P, cur);
-    else k_pt_extend_simple<false><<<grid, b, 0, st>>>(sc, P, cur);
+    if (P.stats) k_pt_extend_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, cur, P.stats);
+    else k_pt_extend_simple<false><<<grid, b, 0, st>>>(sc, src, P.counters, cur, P.stats);
     return;
   }
   int g = persistent_grid(sm_count_current(), 128);
-  if (P.stats) k_pt_extend<true><<<g, 128, 0, st>>>(sc, P, cur);
-  else k_pt_extend<false><<<g, 128, 0, st>>>(sc, P, cur);
+  if (P.stats) k_pt_extend<true><<<g, 128, 0, st>>>(sc, src, P.counters, cur, P.stats);
+  else k_pt_extend<false><<<g, 128, 0, st>>>(sc, src, P.counters, cur, P.stats);
 }
 
 // ----------------------------------------------------------------- shade
@@ -211,42 +212,50 @@ void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block,
 // CalculateDirectLighting (:116-157), CalculateIndirectLighting (:160-189)
 // and ApplyRussianRoulette (:193-220).  The Russian-roulette draw happens
 // first at every level, as in the reference.
-__global__ void __launch_bounds__(256) k_pt_shade(DevScene sc, DevPaths P, ChunkDesc ch, int cur, int bounce) {
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    k_pt_shade(DevScene sc, DevPaths P, ChunkDesc ch, int cur, int bounce) {
   uint32_t n = P.counters[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[4] = 0;  // ray-fetch counters of the next shadow and extend launches
     P.counters[5] = 0;
   }
-  const uint32_t* q = P.queue[cur];
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     uint32_t i = base + threadIdx.x;
     ShadeOut o;
     o.cont = o.shadow = false;
-    uint32_t p = 0;
-    if (i < n) {
-      p = q[i];
-      shade_path(sc, P, p, ch.seed, bounce, o);
-    }
-    push_shade_out(P, cur, p, o);
+    bool live = i < n;
+    if (live) shade_path(sc, P.q[cur], P.hit, i, ch.seed, bounce, o);
+    push_shade_out(P, cur, live, o);
   }
 }
 
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st) {
-  k_pt_shade<<<grid, block, 0, st>>>(sc, P, ch, cur, bounce);
+  if (P.variant & GPRT_JOB_SHADE_OCCUPANCY) {
+    int g = std::max(1, (int)((int64_t)grid * block / 128));
+    k_pt_shade<128, 6><<<g, 128, 0, st>>>(sc, P, ch, cur, bounce);
+  } else {
+    k_pt_shade<256, 1><<<grid, std::min(block, 256), 0, st>>>(sc, P, ch, cur, bounce);
+  }
 }
 
 // ----------------------------------------------------------------- shadow
 // scene.BVH.Hit(shadowRay, 0.001, distance - 0.001) used as a boolean
 // (path_tracing.go:143-148): the contribution is kept when nothing is hit.
 struct ShadowSource {
-  DevPaths P;
-  uint32_t n;
-  __device__ uint32_t count() const { return n; }
+  const float4* sh_o;
+  const float4* sh_d;
+  const float4* sh_c;
+  const int* sh_root;  // null: every ray starts at `root`
+  float4* Lnext;       // radiance of the continuing paths (the next queue)
+  float4* Lout;        // radiance of finished paths, by origin index
+  const uint32_t* n;
   int root;
+  __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
-    rt = P.sh_root ? P.sh_root[i] : root;
-    float4 a = P.sh_o[i], b = P.sh_d[i];
+    rt = sh_root ? sh_root[i] : root;
+    float4 a = sh_o[i], b = sh_d[i];
     o = f3(a);
     d = f3(b);
     tmin = 0.001f;
@@ -255,27 +264,28 @@ struct ShadowSource {
   }
   __device__ void store(uint32_t i, const Hit& h) const {
     if (h.prim != kNoHit) return;  // occluded
-    float4 c = P.sh_c[i];
-    uint32_t p = __float_as_uint(c.w);
-    float4 L = P.L[p];
-    P.L[p] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
+    float4 c = sh_c[i];
+    uint32_t t = __float_as_uint(c.w);
+    float4* dst = (t & kShadowToOrigin) ? Lout + (t & ~kShadowToOrigin) : Lnext + t;
+    float4 L = *dst;
+    *dst = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
   }
 };
 
 template <bool kCount>
-__global__ void __launch_bounds__(128, 8) k_pt_shadow(DevScene sc, DevPaths P) {
-  ShadowSource src{P, P.counters[2], sc.root};
+__global__ void __launch_bounds__(128, 8)
+    k_pt_shadow(DevScene sc, ShadowSource src, uint32_t* counters, unsigned long long* stats) {
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
-  trace_persistent<true, kCount>(sc, src, P.counters + 5, reinterpret_cast<int*>(P.counters + 3), &ts, &rays);
-  if (kCount) add_counts(P.stats + 4, rays, ts);
+  trace_persistent<true, kCount>(sc, src, counters + 5, reinterpret_cast<int*>(counters + 3), &ts, &rays);
+  if (kCount) add_counts(stats + 4, rays, ts);
 }
 
 // One shadow ray per thread (grid-stride), the variant GPRT_JOB_SIMPLE_SHADOW selects.
 template <bool kCount>
-__global__ void __launch_bounds__(256) k_pt_shadow_simple(DevScene sc, DevPaths P) {
-  uint32_t n = P.counters[2];
-  ShadowSource src{P, n, sc.root};
+__global__ void __launch_bounds__(256)
+    k_pt_shadow_simple(DevScene sc, ShadowSource src, uint32_t* counters, unsigned long long* stats) {
+  uint32_t n = src.count();
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
   uint32_t end = kCount ? ((n + 31) & ~31u) : n;
@@ -287,24 +297,25 @@ __global__ void __launch_bounds__(256) k_pt_shadow_simple(DevScene sc, DevPaths 
       int root;
       src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace_from<true, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(P.counters + 3), &ts);
+      trace_from<true, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(counters + 3), &ts);
       src.store(i, h);
       rays++;
     }
   }
-  if (kCount) add_counts(P.stats + 4, rays, ts);
+  if (kCount) add_counts(stats + 4, rays, ts);
 }
 
-void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int block, int grid, cudaStream_t st) {
+void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
+  ShadowSource src{P.sh_o, P.sh_d, P.sh_c, P.sh_root, P.q[cur ^ 1].L, P.Lout, P.counters + 2, sc.root};
   if (P.variant & GPRT_JOB_SIMPLE_SHADOW) {
     int b = std::min(block, 256);
-    if (P.stats) k_pt_shadow_simple<true><<<grid, b, 0, st>>>(sc, P);
-    else k_pt_shadow_simple<false><<<grid, b, 0, st>>>(sc, P);
+    if (P.stats) k_pt_shadow_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, P.stats);
+    else k_pt_shadow_simple<false><<<grid, b, 0, st>>>(sc, src, P.counters, P.stats);
     return;
   }
   int g = persistent_grid(sm_count_current(), 128);
-  if (P.stats) k_pt_shadow<true><<<g, 128, 0, st>>>(sc, P);
-  else k_pt_shadow<false><<<g, 128, 0, st>>>(sc, P);
+  if (P.stats) k_pt_shadow<true><<<g, 128, 0, st>>>(sc, src, P.counters, P.stats);
+  else k_pt_shadow<false><<<g, 128, 0, st>>>(sc, src, P.counters, P.stats);
 }
 
 // ----------------------------------------------------------------- accumulate
@@ -315,7 +326,7 @@ __global__ void k_accumulate(DevFilm film, DevPaths P, ChunkDesc ch) {
     float4 acc = film.rgbl[pix];
     float l2 = film.lum2[pix];
     for (uint32_t layer = 0; layer < ch.layers; layer++) {
-      float4 c = P.L[layer * ch.npix + i];
+      float4 c = P.Lout[layer * ch.npix + i];
       float lum = luminance(f3(c));
       acc.x += c.x;
       acc.y += c.y;
@@ -331,6 +342,37 @@ __global__ void k_accumulate(DevFilm film, DevPaths P, ChunkDesc ch) {
 
 void launch_accumulate(const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block, cudaStream_t st) {
   k_accumulate<<<launch_grid(ch.npix, block, 0), block, 0, st>>>(film, P, ch);
+}
+
+}  // namespace gprt
+
+namespace gprt {
+
+void carve_paths(unsigned char* base, uint32_t cap, bool multi, DevPaths& P) {
+  size_t f4 = align256((size_t)cap * sizeof(float4)), u4 = align256((size_t)cap * sizeof(uint4));
+  unsigned char* p = base;
+  auto take = [&](size_t n) {
+    unsigned char* r = p;
+    p += n;
+    return r;
+  };
+  P.counters = reinterpret_cast<uint32_t*>(take(256));
+  for (int k = 0; k < 2; k++) {
+    PathBuf& Q = P.q[k];
+    Q.ray_o = reinterpret_cast<float4*>(take(f4));
+    Q.ray_d = reinterpret_cast<float4*>(take(f4));
+    Q.weight = reinterpret_cast<float4*>(take(f4));
+    Q.thr = reinterpret_cast<float4*>(take(f4));
+    Q.L = reinterpret_cast<float4*>(take(f4));
+    Q.ids = reinterpret_cast<uint4*>(take(u4));
+  }
+  P.hit = reinterpret_cast<float4*>(take(f4));
+  P.Lout = reinterpret_cast<float4*>(take(f4));
+  P.sh_o = reinterpret_cast<float4*>(take(f4));
+  P.sh_d = reinterpret_cast<float4*>(take(f4));
+  P.sh_c = reinterpret_cast<float4*>(take(f4));
+  P.sh_root = multi ? reinterpret_cast<int*>(take(align256((size_t)cap * sizeof(int)))) : nullptr;
+  P.capacity = cap;
 }
 
 }  // namespace gprt

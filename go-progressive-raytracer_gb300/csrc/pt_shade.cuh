@@ -8,34 +8,37 @@
 
 namespace gprt {
 
-// What one shading step asks of the queues: continue the path, and/or trace
-// a shadow ray whose contribution is added when it is unoccluded.
+// The state a shading step leaves: the continuing path (when `cont`) and the
+// shadow ray whose contribution is added when it is unoccluded.
 struct ShadeOut {
   bool cont, shadow;
+  float4 o, d, w;  // next ray origin (+ skip prim), direction (+ BVH root), weight (+ origin index)
+  float3 thr, L;
+  uint4 ids;
   float3 sh_o, sh_d, sh_c;
   float sh_t;
   uint32_t sh_skip;
-  int root;  // BVH root of the path's scene
 };
 
 // One level of rayColorRecursive (pkg/integrator/path_tracing.go:35-104) with
 // CalculateDirectLighting (:116-157), CalculateIndirectLighting (:160-189)
-// and ApplyRussianRoulette (:193-220), for path p at depth index `bounce`
-// (= MaxDepth - depth).  The Russian-roulette draw happens first at every
-// level, as in the reference.  Updates the path's radiance, weights, ray and
-// sampler position in P.
-__device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P, uint32_t p, uint64_t seed,
-                                           int bounce, ShadeOut& out) {
+// and ApplyRussianRoulette (:193-220), for slot i of queue Q at depth index
+// `bounce` (= MaxDepth - depth).  The Russian-roulette draw happens first at
+// every level, as in the reference.
+__device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q, const float4* hits, uint32_t i,
+                                           uint64_t seed, int bounce, ShadeOut& out) {
   out.cont = false;
   out.shadow = false;
   out.sh_skip = kNoHit;
   out.sh_t = 0.f;
-  float4 o4 = P.ray_o[p], d4 = P.ray_d[p], h4 = P.hit[p];
+  float4 o4 = Q.ray_o[i], d4 = Q.ray_d[i], h4 = hits[i], w4 = Q.weight[i];
+  uint4 ids = Q.ids[i];
   float3 d = f3(d4);
-  out.root = __float_as_int(d4.w);
-  float3 W = f3(P.weight[p]), thr = f3(P.thr[p]), L = f3(P.L[p]);
+  float3 W = f3(w4), thr = f3(Q.thr[i]), L = f3(Q.L[i]);
+  out.o = o4;
+  out.d = d4;
   Rng rng;
-  rng.init(seed, P.pixel[p], P.sample[p], P.rng_pos[p]);
+  rng.init(seed, ids.x, ids.y, ids.z);
   // ApplyRussianRoulette: currentBounce = MaxDepth - depth = bounce
   float u = rng.next();
   bool dead = false;
@@ -100,20 +103,17 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P
           }
         }
         if (cont) {
-          P.ray_o[p] = make_float4(s.p.x, s.p.y, s.p.z, __uint_as_float(prim));
-          P.ray_d[p] = make_float4(sc_.dir.x, sc_.dir.y, sc_.dir.z, d4.w);
+          out.o = make_float4(s.p.x, s.p.y, s.p.z, __uint_as_float(prim));
+          out.d = make_float4(sc_.dir.x, sc_.dir.y, sc_.dir.z, d4.w);
         }
       }
     }
   }
-  cont = cont && (bounce + 1 < sc.max_depth);
-  P.L[p] = make_float4(L.x, L.y, L.z, 0.f);
-  P.rng_pos[p] = rng.pos;
-  if (cont) {
-    P.weight[p] = make_float4(W.x, W.y, W.z, 0.f);
-    P.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
-  }
-  out.cont = cont;
+  out.cont = cont && (bounce + 1 < sc.max_depth);
+  out.L = L;
+  out.w = make_float4(W.x, W.y, W.z, w4.w);
+  out.thr = thr;
+  out.ids = make_uint4(ids.x, ids.y, rng.pos, ids.w);
 }
 
 // Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
@@ -128,16 +128,32 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
   return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-// Queues the continuation of path p and its shadow ray.
-__device__ __forceinline__ void push_shade_out(const DevPaths& P, int cur, uint32_t p, const ShadeOut& o) {
-  uint32_t slot = warp_append(&P.counters[cur ^ 1], o.cont);
-  if (o.cont) P.queue[cur ^ 1][slot] = p;
-  uint32_t ss = warp_append(&P.counters[2], o.shadow);
-  if (o.shadow) {
+// Moves a continuing path to the next queue (a finished path leaves its
+// radiance at its origin index) and queues its shadow ray.  Called by every
+// lane of the warp; `live` is false for lanes without a path.
+__device__ __forceinline__ void push_shade_out(const DevPaths& P, int cur, bool live, const ShadeOut& o) {
+  bool cont = live && o.cont;
+  uint32_t slot = warp_append(&P.counters[cur ^ 1], cont);
+  uint32_t origin = __float_as_uint(o.w.w);
+  if (cont) {
+    const PathBuf& N = P.q[cur ^ 1];
+    N.ray_o[slot] = o.o;
+    N.ray_d[slot] = o.d;
+    N.weight[slot] = o.w;
+    N.thr[slot] = make_float4(o.thr.x, o.thr.y, o.thr.z, 0.f);
+    N.L[slot] = make_float4(o.L.x, o.L.y, o.L.z, 0.f);
+    N.ids[slot] = o.ids;
+  } else if (live) {
+    P.Lout[origin] = make_float4(o.L.x, o.L.y, o.L.z, 0.f);
+  }
+  bool sh = live && o.shadow;
+  uint32_t ss = warp_append(&P.counters[2], sh);
+  if (sh) {
+    uint32_t target = cont ? slot : (origin | kShadowToOrigin);
     P.sh_o[ss] = make_float4(o.sh_o.x, o.sh_o.y, o.sh_o.z, o.sh_t);
     P.sh_d[ss] = make_float4(o.sh_d.x, o.sh_d.y, o.sh_d.z, __uint_as_float(o.sh_skip));
-    P.sh_c[ss] = make_float4(o.sh_c.x, o.sh_c.y, o.sh_c.z, __uint_as_float(p));
-    if (P.sh_root) P.sh_root[ss] = o.root;
+    P.sh_c[ss] = make_float4(o.sh_c.x, o.sh_c.y, o.sh_c.z, __uint_as_float(target));
+    if (P.sh_root) P.sh_root[ss] = __float_as_int(o.d.w);
   }
 }
 

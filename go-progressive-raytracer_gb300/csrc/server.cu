@@ -84,16 +84,14 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
     float2 jit = rng.next2();
     float3 o, d;
     camera_ray(it.cam, x, y, lens, jit, o, d);
-    P.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
-    P.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(it.root));
-    P.weight[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.pixel[p] = pix;
-    P.sample[p] = sample;
-    P.rng_pos[p] = rng.pos;
-    P.item[p] = k;
-    P.queue[0][p] = p;
+    const PathBuf& Q = P.q[0];
+    Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
+    Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(it.root));
+    Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
+    Q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    Q.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, k);
+    P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[0] = n;
@@ -105,23 +103,22 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
 // One bounce of every live path, each shaded with its own job's scene view
 // (materials, lights, infinite-light bounds, depth and Russian-roulette
 // settings) over the pooled geometry.
-__global__ void __launch_bounds__(256) k_srv_shade(DevScene pool, DevPaths P, const DevItem* items, int cur,
-                                                   int bounce) {
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    k_srv_shade(DevScene pool, DevPaths P, const DevItem* items, int cur, int bounce) {
   uint32_t n = P.counters[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[4] = 0;
     P.counters[5] = 0;
   }
-  const uint32_t* q = P.queue[cur];
+  const PathBuf Q = P.q[cur];
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     uint32_t i = base + threadIdx.x;
     ShadeOut o;
     o.cont = o.shadow = false;
-    o.root = -1;
-    uint32_t p = 0;
-    if (i < n) {
-      p = q[i];
-      const DevItem& it = items[P.item[p]];
+    bool live = i < n;
+    if (live) {
+      const DevItem& it = items[Q.ids[i].w];
       DevScene v = pool;
       v.materials = pool.materials + it.mat_off;
       v.lights = pool.lights + it.light_off;
@@ -132,9 +129,9 @@ __global__ void __launch_bounds__(256) k_srv_shade(DevScene pool, DevPaths P, co
       v.max_depth = it.max_depth;
       v.rr_min_bounces = it.rr_min_bounces;
       v.root = it.root;
-      shade_path(v, P, p, it.seed, bounce, o);
+      shade_path(v, Q, P.hit, i, it.seed, bounce, o);
     }
-    push_shade_out(P, cur, p, o);
+    push_shade_out(P, cur, live, o);
   }
 }
 
@@ -150,7 +147,7 @@ __global__ void k_srv_accumulate(DevPaths P, const StepHdr* hdr, const uint32_t*
     float4 acc = it.rgbl[i];
     float l2 = it.lum2[i];
     for (uint32_t layer = 0; layer < it.layers; layer++) {
-      float4 c = P.L[it.path0 + layer * it.npix + i];
+      float4 c = P.Lout[it.path0 + layer * it.npix + i];
       float lum = luminance(f3(c));
       acc.x += c.x;
       acc.y += c.y;
@@ -308,6 +305,12 @@ struct gprt_server {
   size_t table_bytes = 0, prefix_bytes = 0;
   std::map<int, cudaGraphExec_t> graphs;  // by depth
   uint64_t graph_gen = ~0ull;
+  // instrumentation (GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL in flags):
+  // event pairs around every kernel of a step, by depth (captured into the
+  // graph of that depth), and the device traversal counters
+  std::map<int, std::vector<cudaEvent_t>> step_events;
+  unsigned long long* d_stats = nullptr;
+  gprt_job_counters acc{};
   gprt_server_stats st{};
   // requests and events (qmu)
   std::mutex qmu;
@@ -668,37 +671,115 @@ void admit(gprt_server* sv) {
 
 int grid_for(gprt_server* sv, int block) { return std::max(1, sv->ctx->sm_count * (2048 / block)); }
 
-// The kernel sequence of one step of depth D on the server stream.
-void launch_step(gprt_server* sv, int D, cudaStream_t st) {
+// Kernels of a step of depth D: raygen, D x (extend, shade, shadow), accumulate.
+int kernels_per_step(int D) { return 2 + 3 * D; }
+
+// Kernel class of launch k of a step (0 extend, 1 shade, 2 shadow, 3 other).
+int kernel_class(int k, int D) { return (k == 0 || k == kernels_per_step(D) - 1) ? 3 : (k - 1) % 3; }
+
+// Event pairs bracketing every kernel of a depth-D step (created once).
+std::vector<cudaEvent_t>* events_for(gprt_server* sv, int D) {
+  auto& v = sv->step_events[D];
+  if (v.empty()) {
+    v.resize(2 * kernels_per_step(D));
+    for (auto& e : v) cudaEventCreate(&e);
+  }
+  return &v;
+}
+
+// The kernel sequence of one step of depth D on the server stream.  While
+// the stream is being captured, the timing events become event-record nodes
+// of the graph (cudaEventRecordExternal), so they fire on every replay.
+void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
   DevScene pool = pool_view(sv);
   DevPaths P = sv->P;
-  P.variant = sv->flags & (GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW);
+  P.variant = sv->flags & kVariantBits;
+  P.stats = (sv->flags & GPRT_JOB_COUNT_TRAVERSAL) ? sv->d_stats : nullptr;
   const StepHdr* hdr = reinterpret_cast<const StepHdr*>(sv->d_table);
   const uint32_t* path0 = reinterpret_cast<const uint32_t*>(sv->d_table + 16);
   const uint32_t* pix0 = path0 + (sv->desc.max_jobs + 1);
   const DevItem* items = reinterpret_cast<const DevItem*>(sv->d_table + sv->prefix_bytes);
   int block = (int)sv->block;
   int grid = grid_for(sv, block);
+  std::vector<cudaEvent_t>* ev = (sv->flags & GPRT_JOB_TIME_KERNELS) ? events_for(sv, D) : nullptr;
+  int k = 0;
+  unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  auto open = [&]() {
+    if (ev) cudaEventRecordWithFlags((*ev)[2 * k], st, rec);
+  };
+  auto close = [&]() {
+    if (ev) cudaEventRecordWithFlags((*ev)[2 * k + 1], st, rec);
+    k++;
+  };
+  open();
   k_srv_raygen<<<grid, block, 0, st>>>(P, hdr, path0, items);
+  close();
   int cur = 0;
   for (int b = 0; b < D; b++) {
+    open();
     launch_pt_extend(pool, P, cur, block, grid, st);
-    k_srv_shade<<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
-    launch_pt_shadow(pool, P, block, grid, st);
+    close();
+    open();
+    if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
+      k_srv_shade<128, 6><<<std::max(1, grid * block / 128), 128, 0, st>>>(pool, P, items, cur, b);
+    else
+      k_srv_shade<256, 1><<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
+    close();
+    open();
+    launch_pt_shadow(pool, P, cur, block, grid, st);
+    close();
     cur ^= 1;
   }
+  open();
   k_srv_accumulate<<<grid, block, 0, st>>>(P, hdr, pix0, items);
+  close();
+}
+
+// Folds the kernel times of the step just synchronised (and the traversal
+// counters) into sv->acc.
+void collect_step_counters(gprt_server* sv, int D) {
+  if (sv->flags & GPRT_JOB_TIME_KERNELS) {
+    auto& ev = *events_for(sv, D);
+    for (int k = 0; k < kernels_per_step(D); k++) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      switch (kernel_class(k, D)) {
+        case 0: sv->acc.extend_ms += ms; sv->acc.extend_launches++; break;
+        case 1: sv->acc.shade_ms += ms; sv->acc.shade_launches++; break;
+        case 2: sv->acc.shadow_ms += ms; sv->acc.shadow_launches++; break;
+        default: sv->acc.other_ms += ms; sv->acc.other_launches++; break;
+      }
+    }
+  }
+  if ((sv->flags & GPRT_JOB_COUNT_TRAVERSAL) && sv->d_stats) {
+    unsigned long long v[8];
+    cudaMemcpy(v, sv->d_stats, sizeof(v), cudaMemcpyDeviceToHost);
+    cudaMemset(sv->d_stats, 0, sizeof(v));
+    sv->acc.extend_rays += v[0];
+    sv->acc.extend_nodes += v[1];
+    sv->acc.extend_boxes += v[2];
+    sv->acc.extend_prims += v[3];
+    sv->acc.shadow_rays += v[4];
+    sv->acc.shadow_nodes += v[5];
+    sv->acc.shadow_boxes += v[6];
+    sv->acc.shadow_prims += v[7];
+  }
 }
 
 void drop_graphs(gprt_server* sv) {
   for (auto& kv : sv->graphs) cudaGraphExecDestroy(kv.second);
   sv->graphs.clear();
+  cudaGetLastError();
 }
 
 int run_step(gprt_server* sv, int D) {
   gprt_ctx* ctx = sv->ctx;
+  sv->st.kernels += (uint64_t)kernels_per_step(D);
   if (sv->flags & GPRT_SERVER_NO_GRAPHS) {
-    launch_step(sv, D, sv->stream);
+    launch_step(sv, D, sv->stream, false);
     return GPRT_OK;
   }
   if (sv->graph_gen != sv->pool_gen) {
@@ -707,9 +788,10 @@ int run_step(gprt_server* sv, int D) {
   }
   auto it = sv->graphs.find(D);
   if (it == sv->graphs.end()) {
+    if (sv->flags & GPRT_JOB_TIME_KERNELS) events_for(sv, D);  // created outside the capture
     cudaGraph_t g = nullptr;
     CK(ctx, cudaStreamBeginCapture(sv->stream, cudaStreamCaptureModeThreadLocal));
-    launch_step(sv, D, sv->stream);
+    launch_step(sv, D, sv->stream, true);
     CK(ctx, cudaStreamEndCapture(sv->stream, &g));
     cudaGraphExec_t ex = nullptr;
     cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
@@ -822,6 +904,7 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
   cudaEventElapsedTime(&ms, sv->ev0, sv->ev1);
   if (ms_out) *ms_out = ms;
   if (dry) return (int)items.size();
+  collect_step_counters(sv, D);
   sv->st.steps++;
   sv->st.busy_ms += ms;
   sv->st.last_step_ms = ms;
@@ -972,29 +1055,15 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   DevPaths& P = sv->P;
   auto& b = sv->path_bufs;
   uint32_t cap = sv->capacity;
-  size_t bytes = 0;
-  int rc = 0;
-  rc |= dev_alloc(ctx, b, &P.ray_o, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.ray_d, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.weight, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.thr, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.L, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.hit, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.pixel, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.sample, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.rng_pos, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.queue[0], cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.queue[1], cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.sh_o, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.sh_d, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.sh_c, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.sh_root, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.item, cap, &bytes);
-  rc |= dev_alloc(ctx, b, &P.counters, 8, &bytes);
+  size_t bytes = path_region_bytes(cap, true);
+  unsigned char* region = nullptr;
+  int rc = dev_alloc(ctx, b, &region, bytes);
+  if (!rc && (d.flags & GPRT_JOB_COUNT_TRAVERSAL)) rc = dev_alloc(ctx, b, &sv->d_stats, 8);
   if (rc) {
     free_all(b);
     return GPRT_E_OOM;
   }
+  carve_paths(region, cap, true, P);
   P.capacity = cap;
   P.stats = nullptr;
   sv->path_bytes = bytes;
@@ -1018,6 +1087,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   cudaEventCreate(&sv->ev0);
   cudaEventCreate(&sv->ev1);
   cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), sv->stream);
+  if (sv->d_stats) cudaMemsetAsync(sv->d_stats, 0, 8 * sizeof(unsigned long long), sv->stream);
   cudaError_t e = cudaStreamSynchronize(sv->stream);
   if (e != cudaSuccess) {
     free_all(b);
@@ -1044,6 +1114,8 @@ int gprt_server_destroy(gprt_server* sv) {
       for (int b = 0; b < 2; b++)
         if (a.buf[b]) cudaFree(a.buf[b]);
     drop_graphs(sv);
+    for (auto& kv : sv->step_events)
+      for (auto e : kv.second) cudaEventDestroy(e);
     free_all(sv->path_bufs);
     if (sv->h_table) cudaFreeHost(sv->h_table);
     cudaEventDestroy(sv->ev0);
@@ -1228,9 +1300,27 @@ int gprt_server_get_stats(gprt_server* sv, gprt_server_stats* out) {
   return GPRT_OK;
 }
 
+int gprt_server_get_counters(gprt_server* sv, gprt_job_counters* out, int reset) {
+  if (!sv || !out) return GPRT_E_INVALID;
+  std::lock_guard<std::mutex> g(sv->smu);
+  *out = sv->acc;
+  if (reset) sv->acc = gprt_job_counters{};
+  return GPRT_OK;
+}
+
+int gprt_server_stream(gprt_server* sv, void** stream) {
+  if (!sv || !stream) return GPRT_E_INVALID;
+  *stream = sv->stream;
+  return GPRT_OK;
+}
+
 int gprt_server_configure(gprt_server* sv, uint32_t step_paths, uint32_t block_size, uint32_t flags) {
   if (!sv) return GPRT_E_INVALID;
   std::lock_guard<std::mutex> g(sv->smu);
+  if ((flags & GPRT_JOB_COUNT_TRAVERSAL) && !sv->d_stats) {
+    if (dev_alloc(sv->ctx, sv->path_bufs, &sv->d_stats, 8)) return GPRT_E_OOM;
+    cudaMemset(sv->d_stats, 0, 8 * sizeof(unsigned long long));
+  }
   if (step_paths == 0 || step_paths > sv->capacity) return fail(sv->ctx, GPRT_E_INVALID, "step_paths above the capacity");
   if (block_size == 0 || block_size % 32 || block_size > 1024) return fail(sv->ctx, GPRT_E_INVALID, "bad block_size");
   sv->step_paths = step_paths;
@@ -1299,9 +1389,10 @@ int gprt_server_autotune(gprt_server* sv, double max_step_ms, gprt_tune_result* 
     if (p != keep_paths) consider(p, bb, bf);
   for (uint32_t b : {64u, 128u, 256u})
     if (b != bb) consider(bp, b, bf);
-  uint32_t variant_bits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW;
+  uint32_t trav_bits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW;
   for (uint32_t v : {0u, (uint32_t)GPRT_JOB_SIMPLE_EXTEND, (uint32_t)GPRT_JOB_SIMPLE_SHADOW})
-    if (v != (bf & variant_bits)) consider(bp, bb, (bf & ~variant_bits) | v);
+    if (v != (bf & trav_bits)) consider(bp, bb, (bf & ~trav_bits) | v);
+  consider(bp, bb, bf ^ GPRT_JOB_SHADE_OCCUPANCY);
   sv->step_paths = bp;
   if (sv->block != bb || sv->flags != bf) {
     sv->block = bb;

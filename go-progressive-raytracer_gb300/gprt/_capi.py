@@ -95,6 +95,7 @@ JOB_TIME_KERNELS = 1
 JOB_COUNT_TRAVERSAL = 2
 JOB_SIMPLE_EXTEND = 4
 JOB_SIMPLE_SHADOW = 8
+JOB_SHADE_OCCUPANCY = 32
 
 
 class TuneResult(C.Structure):
@@ -133,7 +134,8 @@ class Event(C.Structure):
 
 
 class ServerStats(C.Structure):
-    _fields_ = [(n, C.c_uint64) for n in ("steps", "graph_launches", "samples", "paths", "submitted", "admitted",
+    _fields_ = [(n, C.c_uint64) for n in ("steps", "graph_launches", "kernels", "samples", "paths", "submitted",
+                                           "admitted",
                                            "finished", "refused", "cancelled")] + \
         [(n, C.c_uint32) for n in ("active_jobs", "pending_jobs", "resident_scenes", "reserved")] + \
         [(n, C.c_uint64) for n in ("bytes_in_use", "bytes_budget", "pool_bytes", "path_state_bytes")] + \
@@ -191,6 +193,8 @@ SIGNATURES = {
     "gprt_server_read_rgba8": (C.c_int, [P, C.c_uint64, U8P]),
     "gprt_server_release": (C.c_int, [P, C.c_uint64]),
     "gprt_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "gprt_server_get_counters": (C.c_int, [P, C.POINTER(JobCounters), C.c_int]),
+    "gprt_server_stream": (C.c_int, [P, PP]),
     "gprt_server_configure": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "gprt_server_autotune": (C.c_int, [P, C.c_double, C.POINTER(TuneResult)]),
 }

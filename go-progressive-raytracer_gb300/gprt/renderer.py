@@ -106,7 +106,7 @@ def autotune(gscene: "GpuScene", integrator=None, spp=1, config: Optional["Progr
     r = capi.TuneResult()
     gscene.ctx.check(gscene.ctx.lib.gprt_autotune(gscene.h, C.byref(d), spp, C.byref(r)))
     out = ProgressiveConfig(**cfg.__dict__)
-    out.flags = (cfg.flags & ~(capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW)) | r.flags
+    out.flags = (cfg.flags & ~(capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW | capi.JOB_SHADE_OCCUPANCY)) | r.flags
     out.block_size = r.block_size
     out.chunk_paths = r.chunk_paths
     return out, {k: getattr(r, k) for k, _ in capi.TuneResult._fields_}

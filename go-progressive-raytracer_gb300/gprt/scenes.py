@@ -302,3 +302,32 @@ def ray_batch(scene_vertices, scene_faces, n, seed=13, width=1024, camera=None):
     rays[half:, 4:7] = d2
     rays[half:, 7] = np.inf
     return rays
+
+
+# ---------------------------------------------------------------- job streams
+def batched_jobs(n=256, seed=17, max_depth=8):
+    """The heterogeneous batch: n seeded default-style scenes (resolution from
+    {128^2, 256^2, 512^2, 1024x768}) with spp ~ U[1,64], max depth 8.
+    Returns [(Scene, spp)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        sseed = int(rng.integers(0, 2 ** 31 - 1))
+        spp = int(rng.integers(1, 65))
+        out.append((default_style_scene(sseed, max_depth=max_depth), spp))
+    return out
+
+
+def serving_requests(n, seed=23, kinds=4):
+    """A request stream mixing the workloads: (kind, target spp) per request,
+    kind uniform over 0..kinds-1 (0 Cornell 400^2, 1 icosphere 1024^2,
+    2 Cornell boxes 512^2, 3 default-style scene), target spp uniform over
+    {16, 20, ..., 256} (passes of 4 spp)."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(0, kinds)), int(4 * rng.integers(4, 65))) for _ in range(n)]
+
+
+def poisson_arrivals(n, rate, seed=23):
+    """Arrival times (s) of a Poisson process of `rate` requests per second."""
+    rng = np.random.default_rng(seed + 1)
+    return np.cumsum(rng.exponential(1.0 / rate, n))

@@ -119,6 +119,17 @@ class RenderServer:
         self.ctx.check(self.ctx.lib.gprt_server_get_stats(self.h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in capi.ServerStats._fields_}
 
+    def counters(self, reset=False) -> dict:
+        c = capi.JobCounters()
+        self.ctx.check(self.ctx.lib.gprt_server_get_counters(self.h, C.byref(c), 1 if reset else 0))
+        return {k: getattr(c, k) for k, _ in capi.JobCounters._fields_}
+
+    def stream(self) -> int:
+        """The cudaStream_t (as an int) the server runs on."""
+        s = C.c_void_p()
+        self.ctx.check(self.ctx.lib.gprt_server_stream(self.h, C.byref(s)))
+        return s.value or 0
+
     def configure(self, step_paths: int, block_size: int, flags: int):
         self.ctx.check(self.ctx.lib.gprt_server_configure(self.h, step_paths, block_size, flags))
 

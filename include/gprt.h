@@ -217,6 +217,9 @@ typedef struct gprt_job_desc {
  * new rays) or one ray per thread. */
 #define GPRT_JOB_SIMPLE_EXTEND 4u
 #define GPRT_JOB_SIMPLE_SHADOW 8u
+/* Shading kernel compiled for 6 resident 128-thread blocks per SM (fewer
+ * registers, some spilled to L1) instead of unconstrained registers. */
+#define GPRT_JOB_SHADE_OCCUPANCY 32u
 
 /* Instrumentation of a job (GPRT_JOB_* flags), summed since the last reset.
  * "extend" is the closest-hit traversal of the live paths (one launch per
@@ -356,7 +359,7 @@ int gprt_autotune(gprt_scene* scene, const gprt_job_desc* base, uint32_t spp, gp
  * that seed takes) and writes the per-pixel mean radiance, 3 floats per pixel
  * (PixelStats.GetColor), into the caller's DEVICE buffer `rgb_out`.  The
  * path state lives in one statically sized device array inside the library
- * (GPRT_NOALLOC_MAX_PATHS paths, about 22 MB, held by every GPU that loads
+ * (GPRT_NOALLOC_MAX_PATHS paths, about 34 MB, held by every GPU that loads
  * the library until the process exits); requests with
  * width * height * spp > GPRT_NOALLOC_MAX_PATHS return GPRT_E_INVALID.  It
  * calls no cudaMalloc or cudaFree.  The first call on a device looks up the
@@ -400,7 +403,7 @@ typedef struct gprt_server_desc {
   uint32_t max_jobs;         /* admitted (unreleased) jobs at most (0: 1024) */
   uint32_t step_paths;       /* path capacity of one step's wavefront (0: 1 << 22) */
   uint32_t block_size;       /* threads per block of raygen / shade / accumulate (0: 128) */
-  uint32_t flags;            /* GPRT_SERVER_* and GPRT_JOB_SIMPLE_* bits */
+  uint32_t flags;            /* GPRT_SERVER_* and GPRT_JOB_* bits (variants and instrumentation) */
 } gprt_server_desc;
 #define GPRT_SERVER_NO_GRAPHS 16u /* launch each bounce kernel instead of replaying a captured graph */
 
@@ -423,7 +426,7 @@ typedef struct gprt_event {
 } gprt_event;
 
 typedef struct gprt_server_stats {
-  uint64_t steps, graph_launches, samples, paths;
+  uint64_t steps, graph_launches, kernels, samples, paths;
   uint64_t submitted, admitted, finished, refused, cancelled;
   uint32_t active_jobs, pending_jobs, resident_scenes, reserved;
   uint64_t bytes_in_use, bytes_budget, pool_bytes, path_state_bytes;
@@ -456,6 +459,12 @@ int gprt_server_read_rgba8(gprt_server* server, uint64_t ticket, uint8_t* rgba);
 /* Frees the film of a finished (or cancels and frees a running) job. */
 int gprt_server_release(gprt_server* server, uint64_t ticket);
 int gprt_server_get_stats(gprt_server* server, gprt_server_stats* stats);
+/* Per-kernel-class launch times and traversal counters of the steps run with
+ * GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL in the server's flags
+ * (summed since the last reset; reset != 0 clears them after reading). */
+int gprt_server_get_counters(gprt_server* server, gprt_job_counters* out, int reset);
+/* The cudaStream_t every kernel and copy of the server runs on. */
+int gprt_server_stream(gprt_server* server, void** stream);
 /* Changes the step size / block size / GPRT_JOB_SIMPLE_* variant between steps
  * (step_paths up to the capacity given at creation). */
 int gprt_server_configure(gprt_server* server, uint32_t step_paths, uint32_t block_size, uint32_t flags);

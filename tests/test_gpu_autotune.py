@@ -21,10 +21,19 @@ def _film(ctx, g, cfg, spp):
 def test_variants_render_identically(ctx):
     import gprt
     from gprt import capi, scenes
-    g = gprt.GpuScene(ctx, scenes.icosphere_scene(level=5, width=64).to_desc())
+    for desc in (scenes.icosphere_scene(level=5, width=64).to_desc(),
+                 scenes.default_style_scene(3, width=48, height=32).to_desc()):
+        _variants_agree(ctx, desc)
+
+
+def _variants_agree(ctx, desc):
+    import gprt
+    from gprt import capi
+    g = gprt.GpuScene(ctx, desc)
     base = _film(ctx, g, gprt.ProgressiveConfig(max_samples_per_pixel=8, max_passes=1, seed=3), 8)
     for flags, block, chunk in [(capi.JOB_SIMPLE_EXTEND, 64, 0), (capi.JOB_SIMPLE_SHADOW, 256, 5000),
-                                (capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW, 128, 20000), (0, 128, 3000)]:
+                                (capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW, 128, 20000), (0, 128, 3000),
+                                (capi.JOB_SHADE_OCCUPANCY, 256, 0)]:
         f = _film(ctx, g, gprt.ProgressiveConfig(max_samples_per_pixel=8, max_passes=1, seed=3, flags=flags,
                                                   block_size=block, chunk_paths=chunk), 8)
         for a, b in zip(base, f):

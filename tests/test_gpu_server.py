@@ -82,7 +82,8 @@ def test_graphs_and_direct_launches_agree(ctx, scenes):
     import gprt
     from gprt import capi
     out = []
-    for flags in (0, capi.SERVER_NO_GRAPHS, capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW):
+    for flags in (0, capi.SERVER_NO_GRAPHS, capi.JOB_SIMPLE_EXTEND | capi.JOB_SIMPLE_SHADOW,
+                  capi.JOB_SHADE_OCCUPANCY):
         sv = gprt.RenderServer(ctx, step_paths=1 << 15, flags=flags)
         ts = [sv.submit(scenes["spheres_a"], _cfg(4, 2, 1)), sv.submit(scenes["ico"], _cfg(4, 2, 2))]
         sv.run_until_idle()
