@@ -9,8 +9,33 @@
 
 namespace {
 
+// BDPT working set: counters, per-sample radiance and the strategy buffers.
+int ensure_bdpt(gprt_job* j) {
+  gprt_ctx* ctx = j->scene->ctx;
+  uint32_t ns = j->desc.chunk_paths;
+  DevPaths& P = j->paths;
+  DevBdpt& B = P.bd;
+  B.maxv = bdpt_maxv(j->scene->dev.max_depth);
+  B.ns = ns;
+  auto& b = j->buffers;
+  int rc = 0;
+  rc |= dev_alloc(ctx, b, &P.counters, 64);
+  rc |= dev_alloc(ctx, b, &P.Lout, ns);
+  for (int k = 0; k < 5; k++) rc |= dev_alloc(ctx, b, &B.v[k], (size_t)ns * 2 * B.maxv);
+  rc |= dev_alloc(ctx, b, &B.meta, ns);
+  rc |= dev_alloc(ctx, b, &B.masks, ns);
+  rc |= dev_alloc(ctx, b, &B.contrib, (size_t)ns * (B.maxv + 1) * B.maxv);
+  if (rc) return GPRT_E_OOM;
+  P.stats = nullptr;
+  P.variant = 0;
+  CK(ctx, cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), j->stream));
+  P.capacity = ns;
+  return GPRT_OK;
+}
+
 int ensure_paths(gprt_job* j) {
   if (j->paths.capacity) return GPRT_OK;
+  if (j->desc.integrator == GPRT_INTEGRATOR_BDPT) return ensure_bdpt(j);
   gprt_ctx* ctx = j->scene->ctx;
   uint32_t cap = j->desc.chunk_paths;
   DevPaths& P = j->paths;
@@ -415,13 +440,15 @@ int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
   uint32_t npix = s->host.sampling.width * s->host.sampling.height;
   if (d.chunk_paths == 0) {
     uint64_t want = (uint64_t)npix * std::max(1u, d.max_samples_per_pixel);
-    // path tracing: up to 2^24 paths per wavefront (about 3 GB of path state);
-    // BDPT keeps its subpaths per thread, 2^20 samples per launch
+    // path tracing: up to 2^24 paths per wavefront (about 4.6 GB of path
+    // state); BDPT: 2^20 samples per chunk (3.5 GB of vertices and strategy
+    // contributions at depth <= 9, 8.4 GB up to depth 17)
     d.chunk_paths = (uint32_t)std::min<uint64_t>(want, d.integrator == GPRT_INTEGRATOR_BDPT ? (1u << 20) : (1u << 24));
   }
+  if (d.integrator == GPRT_INTEGRATOR_BDPT) d.chunk_paths = std::min(d.chunk_paths, 1u << 20);
   if (d.max_samples_per_pixel < d.initial_samples) return fail(ctx, GPRT_E_INVALID, "max samples below initial samples");
   if (d.integrator == GPRT_INTEGRATOR_BDPT && s->host.sampling.max_depth > 17)
-    return fail(ctx, GPRT_E_INVALID, "BDPT supports max_depth <= 17 (subpath vertices are kept per thread)");
+    return fail(ctx, GPRT_E_INVALID, "BDPT supports max_depth <= 17 (18 stored vertices per subpath)");
   DevFilm& f = j->film;
   f.width = (int)s->host.sampling.width;
   f.height = (int)s->host.sampling.height;

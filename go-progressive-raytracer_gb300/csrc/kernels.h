@@ -33,6 +33,19 @@ struct PathBuf {
 // origin order (origin index = layer * npix + pixel of the chunk) into q[0];
 // each shade kernel compacts the continuing paths of q[cur] into q[cur ^ 1]
 // and writes the radiance of finished paths to Lout at their origin index.
+// BDPT working set of one chunk of samples (see kernels_bdpt.cu): subpath
+// vertices as 5 float4 fields, each indexed [vertex * ns + sample] (camera
+// vertices 0..maxv-1, light vertices maxv..2 maxv-1), per-sample metadata,
+// and one contribution slot per (strategy, sample).
+struct DevBdpt {
+  float4* v[5];
+  uint4* meta;    // nc | nl << 8, sampler position after the subpaths, pixel, sample index
+  uint2* masks;   // strategies that draw samples: light-tracing (bit s), direct-lighting (bit t)
+  float4* contrib;
+  uint32_t ns;    // samples per chunk
+  int maxv;       // vertices per subpath (10 or 18)
+};
+
 struct DevPaths {
   PathBuf q[2];
   float4* hit;     // closest hit of slot i of the current queue: t, prim, u, v
@@ -45,7 +58,15 @@ struct DevPaths {
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
   uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY
+  DevBdpt bd;        // BDPT jobs only
 };
+
+// Subpath vertices per BDPT subpath for a scene depth, and the device bytes
+// of the BDPT working set of `ns` samples.
+inline int bdpt_maxv(int max_depth) { return max_depth <= 9 ? 10 : 18; }
+inline size_t bdpt_bytes(uint32_t ns, int maxv) {
+  return (size_t)ns * (5 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16) + 8 * 256;
+}
 
 constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;
 
@@ -87,7 +108,8 @@ void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch,
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
 void launch_accumulate(const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block, cudaStream_t st);
 
-// bidirectional path tracing (pkg/integrator/bdpt.go), one sample per thread
+// bidirectional path tracing (pkg/integrator/bdpt.go): subpaths per sample,
+// then one thread per (strategy, sample), then the per-sample sums
 void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
                  cudaStream_t st);
 

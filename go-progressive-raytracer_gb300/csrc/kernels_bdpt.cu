@@ -1,4 +1,4 @@
-// kernels_bdpt.cu - bidirectional path tracing, one pixel sample per thread.
+// kernels_bdpt.cu - bidirectional path tracing.
 //
 // Restates BDPTIntegrator.RayColor (pkg/integrator/bdpt.go:73-102): a camera
 // subpath and a light subpath are generated (generateCameraPath :106-135,
@@ -7,14 +7,27 @@
 // (pkg/integrator/bdpt_mis.go:13-335).  t=1 light-tracing contributions are
 // splatted into the film's splat buffer with atomic adds and applied after
 // the pass (processSplats, pkg/renderer/progressive.go:371-391).
-// The subpath vertices live in per-thread local arrays (the compiler
-// interleaves local memory per thread, so the accesses are coalesced).
+//
+// Three kernels per chunk of samples:
+//   k_bdpt_subpaths    one thread per sample builds both subpaths into a
+//                      global vertex store (fields indexed [vertex][sample]);
+//   k_bdpt_strategies  one thread per (strategy, sample), the samples of a
+//                      strategy in consecutive threads: each warp runs a
+//                      single (s,t) for 32 samples, so control flow is uniform
+//                      and vertex reads coalesce; its sampler position is the
+//                      sample's position after the subpaths plus the draws of
+//                      the strategies before it (draws_before);
+//   k_bdpt_sum         adds each sample's strategy contributions in the
+//                      reference's s-major order.
+#include <algorithm>
+
 #include "device.cuh"
 #include "kernels.h"
 
 namespace gprt {
 
 namespace {
+
 
 constexpr int kFlagLight = 1, kFlagCamera = 2, kFlagSpecular = 4, kFlagInfinite = 8, kFlagFront = 16;
 
@@ -88,7 +101,7 @@ __device__ __forceinline__ float camera_importance(const DevCamera& c, float3 d)
 // ---------------------------------------------------------------- lights
 // SampleEmission (quad_light.go:113-145, sphere_light.go:169-184,
 // light_sampling.go:58-115 for the infinite lights)
-__device__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp, float2 sd, float3& p, float3& n,
+__device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp, float2 sd, float3& p, float3& n,
                                 float3& dir, float3& Le, float& area_pdf, float& dir_pdf) {
   if (L.kind == kLightQuad) {
     const float4* Q = sc.quads + (size_t)L.prim * 5;
@@ -134,7 +147,7 @@ __device__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp
 
 // PDF_Le direction pdf (quad_light.go:148-185, sphere_light.go:187-209,
 // uniform_infinite_light.go:94-106); pos receives the position pdf
-__device__ float pdf_le(const DevScene& sc, const DevLight& L, float3 p, float3 dir, float& pos) {
+__device__ __noinline__ float pdf_le(const DevScene& sc, const DevLight& L, float3 p, float3 dir, float& pos) {
   pos = 0.f;
   if (L.kind == kLightQuad) {
     const float4* Q = sc.quads + (size_t)L.prim * 5;
@@ -182,7 +195,7 @@ __device__ float infinite_density(const DevScene& sc, float3 p, float3 n, float3
 
 // ---------------------------------------------------------------- BRDF at a vertex
 // evaluateBRDF (bdpt.go:564-583)
-__device__ float3 vertex_brdf(const DevScene& sc, const BVert& v, float3 out, bool radiance) {
+__device__ __noinline__ float3 vertex_brdf(const DevScene& sc, const BVert& v, float3 out, bool radiance) {
   if (v.is(kFlagInfinite)) return f3(0.f, 0.f, 0.f);
   if (v.is(kFlagLight) && v.mat < 0) return f3(1.f, 1.f, 1.f);
   if (v.mat < 0) return f3(0.f, 0.f, 0.f);
@@ -194,81 +207,8 @@ __device__ float3 vertex_brdf(const DevScene& sc, const BVert& v, float3 out, bo
   return brdf(sc, load_material(sc, v.mat), v.wi, out, s, radiance);
 }
 
-template <int MAXV>
-struct Paths {
-  BVert cam[MAXV];
-  BVert lgt[MAXV];
-  int nc, nl;
-};
-
-// extendPath (bdpt.go:206-291)
-template <int MAXV>
-__device__ void extend_path(const DevScene& sc, BVert* path, int& len, float3 o, float3 d, float3 beta, float pdf_fwd,
-                            int max_bounces, bool camera, Rng& rng, uint32_t skip, int* err) {
-  for (int b = 0; b < max_bounces && len < MAXV; b++) {
-    BVert& prev = path[len - 1];
-    Hit h;
-    if (!trace<false, false>(sc, o, d, 0.001f, kInfF, skip, h, err)) {
-      if (camera) {
-        // createBackgroundVertex (bdpt.go:585-601)
-        float3 bg = background(sc, d);
-        BVert& v = path[len++];
-        v.p = o + d * 1000.f;
-        v.n = -d;
-        v.wi = -d;
-        v.fwd = pdf_fwd;
-        v.rev = 0.f;
-        v.beta = beta;
-        v.Le = bg;
-        v.mat = -1;
-        v.light = -1;
-        v.prim = kNoHit;
-        v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
-      }
-      break;
-    }
-    Surface s;
-    surface_at(sc, o, d, h, s);
-    DevMaterial m = load_material(sc, s.mat);
-    BVert& v = path[len];
-    v.p = s.p;
-    v.n = s.n;
-    v.wi = -d;
-    v.beta = beta;
-    v.Le = emitted(m, s.front);
-    v.mat = s.mat;
-    v.light = -1;
-    v.prim = h.prim;
-    v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
-    v.rev = 0.f;
-    v.fwd = to_area(sc, prev, v, pdf_fwd);
-    Scatter scn;
-    if (!scatter(sc, m, d, s, rng, scn)) {
-      len++;
-      break;
-    }
-    pdf_fwd = scn.pdf;
-    if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
-    float ct = fabsf(dot(scn.dir, s.n));
-    if (scn.pdf <= 0.f) beta = beta * scn.att;
-    else beta = beta * scn.att * (ct / scn.pdf);
-    bool rdelta;
-    float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
-    if (rdelta) {
-      v.flags |= kFlagSpecular;
-      pdf_rev = 0.f;
-      pdf_fwd = 0.f;
-    }
-    prev.rev = to_area(sc, v, prev, pdf_rev);
-    len++;
-    o = s.p;
-    d = scn.dir;
-    skip = h.prim;
-  }
-}
-
 // calculateLightPdf (bdpt_mis.go:239-272)
-__device__ float vertex_light_pdf(const DevScene& sc, const BVert& cur, const BVert& to) {
+__device__ __noinline__ float vertex_light_pdf(const DevScene& sc, const BVert& cur, const BVert& to) {
   float3 w = to.p - cur.p;
   float inv = 1.0f / dot(w, w);
   w = w * sqrtf(inv);
@@ -287,7 +227,9 @@ __device__ float vertex_light_pdf(const DevScene& sc, const BVert& cur, const BV
 }
 
 // calculateVertexPdf (bdpt_mis.go:186-236)
-__device__ float vertex_pdf(const DevScene& sc, const BVert& cur, const BVert* prev, const BVert& next) {
+// (out of line: inlined into the weight walk it makes the strategy kernel
+// slower, instruction fetch dominating)
+__device__ __noinline__ float vertex_pdf(const DevScene& sc, const BVert& cur, const BVert* prev, const BVert& next) {
   if (cur.is(kFlagLight)) return vertex_light_pdf(sc, cur, next);
   float3 wn = next.p - cur.p;
   if (dot(wn, wn) == 0.f) return 0.f;
@@ -315,7 +257,7 @@ __device__ float vertex_pdf(const DevScene& sc, const BVert& cur, const BVert* p
 }
 
 // calculateLightOriginPdf (bdpt_mis.go:275-308)
-__device__ float light_origin_pdf(const DevScene& sc, const BVert& lv, const BVert& to) {
+__device__ __noinline__ float light_origin_pdf(const DevScene& sc, const BVert& lv, const BVert& to) {
   float3 w = to.p - lv.p;
   if (dot(w, w) == 0.f) return 0.f;
   w = normalize(w);
@@ -329,23 +271,147 @@ __device__ float light_origin_pdf(const DevScene& sc, const BVert& lv, const BVe
 
 __device__ __forceinline__ float remap0(float f) { return f != 0.f ? f : 1.f; }
 
-// calculateMISWeight (bdpt_mis.go:13-181)
+// Any-hit test of a connection / shadow ray (one call site for all strategies).
+__device__ __noinline__ bool occluded(const DevScene& sc, float3 o, float3 d, float tmax, uint32_t skip, int* err) {
+  Hit hh;
+  return trace<true, false>(sc, o, d, 0.001f, tmax, skip, hh, err);
+}
+
+// ---------------------------------------------------------------- vertex store
+// Subpath vertices live in global memory as 5 float4 fields indexed
+// [vertex * ns + sample], so the 32 lanes of a warp (32 consecutive samples)
+// read one field of one vertex in a single coalesced access.
+__device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, const BVert& x) {
+  size_t k = (size_t)v * B.ns + i;
+  B.v[0][k] = make_float4(x.p.x, x.p.y, x.p.z, x.fwd);
+  B.v[1][k] = make_float4(x.n.x, x.n.y, x.n.z, x.rev);
+  B.v[2][k] = make_float4(x.beta.x, x.beta.y, x.beta.z, x.wi.x);
+  B.v[3][k] = make_float4(x.Le.x, x.Le.y, x.Le.z, x.wi.y);
+  B.v[4][k] = make_float4(x.wi.z, __int_as_float((x.mat + 1) | (x.flags << 24)), __int_as_float(x.light),
+                          __uint_as_float(x.prim));
+}
+
+__device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
+  size_t k = (size_t)v * B.ns + i;
+  float4 a = B.v[0][k], b = B.v[1][k], c = B.v[2][k], d = B.v[3][k], e = B.v[4][k];
+  BVert x;
+  x.p = f3(a);
+  x.fwd = a.w;
+  x.n = f3(b);
+  x.rev = b.w;
+  x.beta = f3(c);
+  x.Le = f3(d);
+  x.wi = make_float3(c.w, d.w, e.x);
+  int mf = __float_as_int(e.y);
+  x.mat = (mf & 0xFFFFFF) - 1;
+  x.flags = (mf >> 24) & 0xFF;
+  x.light = __float_as_int(e.z);
+  x.prim = __float_as_uint(e.w);
+  return x;
+}
+
+// The vertices of one sample's subpath (camera: base 0, light: base maxv).
+struct SubpathRef {
+  const DevBdpt* B;
+  uint32_t i;
+  int base;
+  __device__ BVert operator[](int k) const { return get_vert(*B, base + k, i); }
+};
+
+// extendPath (bdpt.go:206-291), writing vertex `len-1` once its reverse pdf
+// is final; `prev` enters as the subpath's first vertex.  Returns the length.
 template <int MAXV>
-__device__ float mis_weight(const DevScene& sc, const Paths<MAXV>& P, const BVert* sampled, int s, int t) {
+__device__ __noinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, uint32_t i, int base, BVert prev,
+                                        float3 o, float3 d, float3 beta, float pdf_fwd, int max_bounces, bool camera,
+                                        Rng& rng, uint32_t skip, int* err) {
+  int len = 1;
+  for (int b = 0; b < max_bounces && len < MAXV; b++) {
+    Hit h;
+    if (!trace<false, false>(sc, o, d, 0.001f, kInfF, skip, h, err)) {
+      if (camera) {
+        // createBackgroundVertex (bdpt.go:585-601)
+        float3 bg = background(sc, d);
+        BVert v;
+        v.p = o + d * 1000.f;
+        v.n = -d;
+        v.wi = -d;
+        v.fwd = pdf_fwd;
+        v.rev = 0.f;
+        v.beta = beta;
+        v.Le = bg;
+        v.mat = -1;
+        v.light = -1;
+        v.prim = kNoHit;
+        v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
+        put_vert(B, base + len - 1, i, prev);
+        prev = v;
+        len++;
+      }
+      break;
+    }
+    Surface s;
+    surface_at(sc, o, d, h, s);
+    DevMaterial m = load_material(sc, s.mat);
+    BVert v;
+    v.p = s.p;
+    v.n = s.n;
+    v.wi = -d;
+    v.beta = beta;
+    v.Le = emitted(m, s.front);
+    v.mat = s.mat;
+    v.light = -1;
+    v.prim = h.prim;
+    v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
+    v.rev = 0.f;
+    v.fwd = to_area(sc, prev, v, pdf_fwd);
+    Scatter scn;
+    if (!scatter(sc, m, d, s, rng, scn)) {
+      put_vert(B, base + len - 1, i, prev);
+      prev = v;
+      len++;
+      break;
+    }
+    pdf_fwd = scn.pdf;
+    if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
+    float ct = fabsf(dot(scn.dir, s.n));
+    if (scn.pdf <= 0.f) beta = beta * scn.att;
+    else beta = beta * scn.att * (ct / scn.pdf);
+    bool rdelta;
+    float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
+    if (rdelta) {
+      v.flags |= kFlagSpecular;
+      pdf_rev = 0.f;
+      pdf_fwd = 0.f;
+    }
+    prev.rev = to_area(sc, v, prev, pdf_rev);
+    put_vert(B, base + len - 1, i, prev);
+    prev = v;
+    len++;
+    o = s.p;
+    d = scn.dir;
+    skip = h.prim;
+  }
+  put_vert(B, base + len - 1, i, prev);
+  return len;
+}
+
+// calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
+__device__ __noinline__ float mis_weight(const DevScene& sc, const SubpathRef& C, const SubpathRef& Lp,
+                                         const BVert* sampled, int s, int t) {
   if (s + t == 2) return 1.f;
-  const BVert* C = P.cam;
-  const BVert* Lp = P.lgt;
   float sum = 0.f, ri = 1.f;
   for (int i = t - 1; i > 0; i--) {
-    const BVert& v = C[i];
+    BVert v = C[i];
     float fwd = v.fwd, rev = v.rev;
     bool conn = !v.is(kFlagSpecular);
     if (s == 0) {
       if (i == t - 1 && t > 1) {
-        rev = light_origin_pdf(sc, C[t - 1], C[t - 2]);
+        BVert a = C[t - 1], b = C[t - 2];
+        rev = light_origin_pdf(sc, a, b);
         conn = true;
       } else if (i == t - 2 && t > 2) {
-        rev = vertex_pdf(sc, C[t - 1], nullptr, C[t - 2]);
+        BVert a = C[t - 1], b = C[t - 2];
+        rev = vertex_pdf(sc, a, nullptr, b);
       }
     } else if (t == 1) {
       if (i == 0) {
@@ -355,17 +421,21 @@ __device__ float mis_weight(const DevScene& sc, const Paths<MAXV>& P, const BVer
       }
     } else if (s == 1) {
       if (i == t - 1 && t > 0) {
-        rev = vertex_pdf(sc, *sampled, nullptr, C[t - 1]);
+        BVert a = C[t - 1];
+        rev = vertex_pdf(sc, *sampled, nullptr, a);
         conn = true;
       } else if (i == t - 2 && t > 1) {
-        rev = vertex_pdf(sc, C[t - 1], sampled, C[t - 2]);
+        BVert a = C[t - 1], b = C[t - 2];
+        rev = vertex_pdf(sc, a, sampled, b);
       }
     } else {
       if (i == t - 1) {
-        rev = vertex_pdf(sc, Lp[s - 1], &Lp[s - 2], C[t - 1]);
+        BVert a = Lp[s - 1], b = Lp[s - 2], c = C[t - 1];
+        rev = vertex_pdf(sc, a, &b, c);
         conn = true;
       } else if (i == t - 2 && t > 1) {
-        rev = vertex_pdf(sc, C[t - 1], &Lp[s - 1], C[t - 2]);
+        BVert a = C[t - 1], b = Lp[s - 1], c = C[t - 2];
+        rev = vertex_pdf(sc, a, &b, c);
       }
     }
     if (i > 0) conn = conn && !C[i - 1].is(kFlagSpecular);
@@ -374,29 +444,34 @@ __device__ float mis_weight(const DevScene& sc, const Paths<MAXV>& P, const BVer
   }
   ri = 1.f;
   for (int i = s - 1; i >= 0; i--) {
-    const BVert& v = Lp[i];
+    BVert v = Lp[i];
     float fwd = v.fwd, rev = v.rev;
     bool conn = !v.is(kFlagSpecular);  // no point lights on this path
     if (i > 0) conn = conn && !Lp[i - 1].is(kFlagSpecular);
     if (t == 1) {
       if (i == s - 1 && s > 1) {
-        rev = vertex_pdf(sc, *sampled, nullptr, Lp[s - 1]);
+        BVert a = Lp[s - 1];
+        rev = vertex_pdf(sc, *sampled, nullptr, a);
         conn = true;
       } else if (i == s - 2 && s > 1) {
-        rev = vertex_pdf(sc, Lp[s - 1], sampled, Lp[s - 2]);
+        BVert a = Lp[s - 1], b = Lp[s - 2];
+        rev = vertex_pdf(sc, a, sampled, b);
       }
     } else if (s == 1) {
       if (i == s - 1 && sampled) {
         fwd = sampled->fwd;
-        rev = vertex_pdf(sc, C[t - 1], &C[t - 2], *sampled);
+        BVert a = C[t - 1], b = C[t - 2];
+        rev = vertex_pdf(sc, a, &b, *sampled);
         conn = true;
       }
     } else {
       if (i == s - 1) {
-        rev = vertex_pdf(sc, C[t - 1], &C[t - 2], Lp[s - 1]);
+        BVert a = C[t - 1], b = C[t - 2], c = Lp[s - 1];
+        rev = vertex_pdf(sc, a, &b, c);
         conn = true;
       } else if (i == s - 2 && s > 1) {
-        rev = vertex_pdf(sc, Lp[s - 1], &C[t - 1], Lp[s - 2]);
+        BVert a = Lp[s - 1], b = C[t - 1], c = Lp[s - 2];
+        rev = vertex_pdf(sc, a, &b, c);
       }
     }
     ri *= remap0(rev) / remap0(fwd);
@@ -405,8 +480,162 @@ __device__ float mis_weight(const DevScene& sc, const Paths<MAXV>& P, const BVer
   return 1.f / (1.f + sum);
 }
 
+// Uniform numbers the strategies before (s, t) draw, in the reference's
+// s-major order: light tracing (s >= 2, t = 1) draws 2 when its light vertex
+// is not specular (mask bit s); direct lighting (s = 1, t >= 2) draws 3 when
+// its camera vertex is a non-specular surface and the scene has lights (mask
+// bit t); every other strategy draws nothing.
+__device__ __forceinline__ uint32_t draws_before(int s, int t, uint2 m) {
+  if (s == 0) return 0;
+  uint32_t lo_t = ((1u << t) - 1u) & ~3u;  // bits 2 .. t-1
+  if (s == 1) return 3u * __popc(m.y & lo_t);
+  uint32_t lo_s = ((1u << s) - 1u) & ~3u;  // bits 2 .. s-1
+  return 3u * __popc(m.y) + 2u * __popc(m.x & lo_s) + (t > 1 ? 2u * ((m.x >> s) & 1u) : 0u);
+}
+
+// evaluateBDPTStrategy (bdpt.go:294-561) for strategy (s, t) of sample i;
+// returns the weighted contribution to the sample (t = 1 splats instead).
+__device__ __noinline__ float3 eval_strategy(const DevScene& sc, const DevFilm& film, const DevBdpt& B, uint32_t i,
+                                             int s, int t, Rng& rs, int* err) {
+  const float3 zero = f3(0.f, 0.f, 0.f);
+  SubpathRef C{&B, i, 0}, Lp{&B, i, B.maxv};
+  float3 Lc = zero;
+  BVert sampled;
+  bool has = false, splat = false;
+  int spx = 0, spy = 0;
+  bool test = false;
+  float3 ro = zero, rd = f3(0.f, 0.f, 1.f);
+  float rt = 0.f;
+  uint32_t rskip = kNoHit;
+  if (s == 0) {
+    // evaluatePathTracingStrategy (bdpt.go:317-332): the caller passes t == nc only
+    BVert last = C[t - 1];
+    Lc = last.Le * last.beta;
+  } else if (t == 1) {
+    // evaluateLightTracingStrategy (bdpt.go:398-486)
+    BVert lv = Lp[s - 1];
+    if (s <= 1 || lv.is(kFlagSpecular)) return zero;
+    float2 cs = rs.next2();
+    float2 lens2 = sample_unit_disk(cs);
+    float3 lp = sc.cam.center + sc.cam.u * (lens2.x * sc.cam.lens_radius) + sc.cam.v * (lens2.y * sc.cam.lens_radius);
+    float3 toRef = lv.p - lp;
+    float dist = length(toRef);
+    float3 dir = normalize(toRef);
+    float cpdf = (dist * dist) / (fabsf(dot(sc.cam.forward, dir)) * sc.cam.lens_area);
+    float imp = camera_importance(sc.cam, dir);
+    if (imp == 0.f) return zero;  // SampleCameraFromPoint returns nil
+    float3 toCam = -dir;
+    float3 f = vertex_brdf(sc, lv, toCam, false);
+    float cb = imp / cpdf;
+    float cosine = dot(toCam, lv.n);
+    if (cosine <= 0.f) return zero;
+    float3 c = f * cb * lv.beta;
+    if (on_surface(sc, lv)) c = c * cosine;
+    if (is_zero(c)) return zero;
+    test = true;
+    ro = lv.p;
+    rd = toCam;
+    rt = dist - 0.001f;
+    rskip = lv.prim;
+    sampled.p = lp;
+    sampled.n = toCam;
+    sampled.wi = dir;  // (scratch: the lens-to-vertex direction)
+    sampled.beta = f3(cb, cb, cb);
+    sampled.Le = zero;
+    sampled.fwd = cpdf;
+    sampled.rev = 0.f;
+    sampled.mat = -1;
+    sampled.light = -1;
+    sampled.prim = kNoHit;
+    sampled.flags = kFlagCamera;
+    has = true;
+    splat = true;
+    Lc = c;
+  } else if (s == 1) {
+    // evaluateDirectLightingStrategy (bdpt.go:334-394)
+    BVert cv = C[t - 1];
+    if (cv.is(kFlagSpecular) || cv.mat < 0) return zero;
+    if (sc.n_lights == 0) return zero;
+    int li = pick_light(sc, rs.next());
+    DevLight L = sc.lights[li];
+    LightSample ls = light_sample(sc, L, cv.p, cv.n, rs.next2());
+    ls.pdf *= L.prob;
+    if (is_zero(ls.emission) || ls.pdf <= 0.f) return zero;
+    float ct = fabsf(dot(ls.dir, cv.n));
+    if (ct <= 0.f) return zero;
+    float3 f = vertex_brdf(sc, cv, ls.dir, true);
+    float3 lb = ls.emission * (1.f / ls.pdf);
+    float3 c = f * cv.beta * lb * ct;
+    if (is_zero(c)) return zero;
+    test = true;
+    ro = cv.p;
+    rd = ls.dir;
+    rt = ls.dist - 0.001f;
+    rskip = cv.prim;
+    sampled.p = ls.point;
+    sampled.n = ls.normal;
+    sampled.wi = zero;
+    sampled.light = li;
+    sampled.mat = -1;
+    sampled.prim = kNoHit;
+    sampled.fwd = ls.pdf;
+    sampled.rev = 0.f;
+    bool inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
+    sampled.flags = kFlagLight | (inf ? kFlagInfinite : 0);
+    sampled.beta = lb;
+    sampled.Le = ls.emission;
+    has = true;
+    Lc = c;
+  } else {
+    // evaluateConnectionStrategy (bdpt.go:502-561)
+    BVert lv = Lp[s - 1];
+    BVert cv = C[t - 1];
+    if (lv.is(kFlagSpecular) || cv.is(kFlagSpecular)) return zero;
+    float3 dd = lv.p - cv.p;
+    float dist = length(dd);
+    if (dist < 0.001f) return zero;
+    dd = dd * (1.f / dist);
+    float cc = dot(dd, cv.n), cl = dot(-dd, lv.n);
+    if (cc <= 0.f || cl <= 0.f) return zero;
+    float g = (cc * cl) / (dist * dist);
+    float3 cb = vertex_brdf(sc, cv, dd, true);
+    float3 lb = vertex_brdf(sc, lv, -dd, false);
+    float3 c = lv.beta * lb * cb * cv.beta * g;
+    if (is_zero(c)) return zero;
+    test = true;
+    ro = cv.p;
+    rd = dd;
+    rt = dist - 0.001f;
+    rskip = cv.prim;
+    Lc = c;
+  }
+  if (test && occluded(sc, ro, rd, rt, rskip, err)) return zero;
+  if (splat) {
+    // MapRayToPixel, then the light pdf of the camera vertex (bdpt.go:440-470)
+    float3 dir = sampled.wi;
+    sampled.wi = zero;
+    if (!map_ray_to_pixel(sc.cam, sampled.p, dir, spx, spy)) return zero;
+    sampled.rev = total_light_pdf(sc, sampled.p, sampled.n, normalize(Lp[s - 1].p - sampled.p));
+  }
+  if (is_zero(Lc) && !splat) return zero;
+  float w = mis_weight(sc, C, Lp, has ? &sampled : nullptr, s, t);
+  if (splat) {
+    float3 c = Lc * w;
+    float4* dst = film.splat + (size_t)spy * film.width + spx;
+    atomicAdd(&dst->x, c.x);
+    atomicAdd(&dst->y, c.y);
+    atomicAdd(&dst->z, c.z);
+    return zero;
+  }
+  return Lc * w;
+}
+
+// generateCameraPath + generateLightPath (bdpt.go:106-202) for every sample
+// of the chunk, in the reference's draw order; records the subpath lengths,
+// the sampler position the strategies start from and the strategy draw masks.
 template <int MAXV>
-__global__ void __launch_bounds__(128) k_bdpt(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+__global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+  const DevBdpt& B = PS.bd;
   uint32_t n = ch.npix * ch.layers;
   int* err = reinterpret_cast<int*>(PS.counters + 3);
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
@@ -414,47 +643,40 @@ __global__ void __launch_bounds__(128) k_bdpt(DevScene sc, DevFilm film, DevPath
     uint32_t pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
     uint32_t sample = film.count[pix] + layer;
     int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
-    // one sequential stream per sample, drawn in the reference's order:
-    // GetRay, camera subpath, light subpath, then the strategies
     Rng rng;
     rng.init(ch.seed, pix, sample);
     float2 lens = rng.next2();
     float2 jit = rng.next2();
     float3 o, d;
     camera_ray(sc.cam, x, y, lens, jit, o, d);
-    Paths<MAXV> P;
     // generateCameraPath (bdpt.go:106-135)
-    {
-      BVert& c = P.cam[0];
-      c.p = o;
-      c.n = -d;
-      c.wi = f3(0.f, 0.f, 0.f);
-      c.beta = f3(1.f, 1.f, 1.f);
-      c.Le = f3(0.f, 0.f, 0.f);
-      c.fwd = 0.f;
-      c.rev = 0.f;
-      c.mat = -1;
-      c.light = -1;
-      c.prim = kNoHit;
-      c.flags = kFlagCamera;
-      P.nc = 1;
-      float dir_pdf = camera_dir_pdf(sc.cam, o, d);
-      extend_path<MAXV>(sc, P.cam, P.nc, o, d, f3(1.f, 1.f, 1.f), dir_pdf, sc.max_depth, true, rng, kNoHit, err);
-    }
+    BVert c;
+    c.p = o;
+    c.n = -d;
+    c.wi = f3(0.f, 0.f, 0.f);
+    c.beta = f3(1.f, 1.f, 1.f);
+    c.Le = f3(0.f, 0.f, 0.f);
+    c.fwd = 0.f;
+    c.rev = 0.f;
+    c.mat = -1;
+    c.light = -1;
+    c.prim = kNoHit;
+    c.flags = kFlagCamera;
+    float dir_pdf = camera_dir_pdf(sc.cam, o, d);
+    int nc = gen_subpath<MAXV>(sc, B, p, 0, c, o, d, f3(1.f, 1.f, 1.f), dir_pdf, sc.max_depth, true, rng, kNoHit, err);
     // generateLightPath (bdpt.go:139-202)
-    P.nl = 0;
+    int nl = 0;
     if (sc.n_lights > 0) {
-      Rng& rl = rng;
-      float ul = rl.next();
+      float ul = rng.next();
       int li = pick_light(sc, ul);
       DevLight L = sc.lights[li];
-      float2 sp = rl.next2();
-      float2 sd = rl.next2();
+      float2 sp = rng.next2();
+      float2 sd = rng.next2();
       float3 ep, en, ed, Le;
       float apdf, dpdf;
       sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
       float ct = fabsf(dot(ed, en));
-      BVert& lv = P.lgt[0];
+      BVert lv;
       lv.p = ep;
       lv.n = en;
       lv.wi = f3(0.f, 0.f, 0.f);
@@ -468,140 +690,78 @@ __global__ void __launch_bounds__(128) k_bdpt(DevScene sc, DevFilm film, DevPath
       lv.flags = kFlagLight | (inf ? kFlagInfinite : 0);
       lv.beta = Le;
       lv.Le = Le;
-      P.nl = 1;
       float3 beta = Le * (ct / (L.prob * apdf * dpdf));
-      extend_path<MAXV>(sc, P.lgt, P.nl, ep, ed, beta, dpdf, sc.max_depth - 1, false, rl, lv.prim, err);
+      nl = gen_subpath<MAXV>(sc, B, p, MAXV, lv, ep, ed, beta, dpdf, sc.max_depth - 1, false, rng, lv.prim, err);
       if (inf) {
-        if (P.nl > 1) {
-          BVert& fb = P.lgt[1];
+        if (nl > 1) {
+          BVert fb = get_vert(B, MAXV + 1, p);
           fb.fwd = apdf * L.prob;
           if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
+          put_vert(B, MAXV + 1, p, fb);
         }
-        P.lgt[0].fwd = infinite_density(sc, ep, en, ed);
+        BVert l0 = get_vert(B, MAXV, p);
+        l0.fwd = infinite_density(sc, ep, en, ed);
+        put_vert(B, MAXV, p, l0);
       }
     }
-    // all strategies (bdpt.go:83-99)
+    // which strategies draw uniform numbers (draws_before)
+    uint32_t lm = 0, cm = 0;
+    for (int s = 2; s <= nl; s++)
+      if (!get_vert(B, MAXV + s - 1, p).is(kFlagSpecular)) lm |= 1u << s;
+    if (sc.n_lights > 0)
+      for (int t = 2; t <= nc; t++) {
+        BVert v = get_vert(B, t - 1, p);
+        if (!v.is(kFlagSpecular) && v.mat >= 0) cm |= 1u << t;
+      }
+    B.meta[p] = make_uint4((uint32_t)nc | ((uint32_t)nl << 8), rng.pos, pix, sample);
+    B.masks[p] = make_uint2(lm, cm);
+  }
+}
+
+// One thread per (strategy, sample): strategy k = s * MAXV + (t - 1); the
+// samples of one strategy are consecutive threads, so a warp evaluates one
+// (s, t) for 32 samples (uniform control flow and coalesced vertex reads).
+template <int MAXV>
+__global__ void __launch_bounds__(128) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+  const DevBdpt& B = PS.bd;
+  const uint32_t n = ch.npix * ch.layers;
+  const uint64_t total = (uint64_t)(MAXV + 1) * MAXV * n;
+  int* err = reinterpret_cast<int*>(PS.counters + 3);
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < total;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t k = (uint32_t)(g / n), i = (uint32_t)(g - (uint64_t)k * n);
+    int s = (int)(k / MAXV), t = (int)(k % MAXV) + 1;
+    uint4 m = B.meta[i];
+    int nc = (int)(m.x & 0xFF), nl = (int)(m.x >> 8);
+    if (s > nl || t > nc) continue;
+    float3 c = f3(0.f, 0.f, 0.f);
+    // (1,1) is skipped (bdpt.go:300-301); s = 0 contributes only at t = nc
+    if (!(s == 1 && t == 1) && !(s == 0 && t != nc)) {
+      Rng rs;
+      rs.init(ch.seed, m.z, m.w, m.y + draws_before(s, t, B.masks[i]));
+      c = eval_strategy(sc, film, B, i, s, t, rs, err);
+    }
+    B.contrib[(size_t)k * n + i] = make_float4(c.x, c.y, c.z, 0.f);
+  }
+}
+
+// The sample's radiance: its strategies' contributions summed in the
+// reference's s-major order (the same additions as its RayColor loop).
+template <int MAXV>
+__global__ void k_bdpt_sum(DevPaths PS, ChunkDesc ch) {
+  const DevBdpt& B = PS.bd;
+  uint32_t n = ch.npix * ch.layers;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint4 m = B.meta[i];
+    int nc = (int)(m.x & 0xFF), nl = (int)(m.x >> 8);
     float3 total = f3(0.f, 0.f, 0.f);
-    Rng& rs = rng;
-    for (int s = 0; s <= P.nl; s++) {
-      for (int t = 1; t <= P.nc; t++) {
+    for (int s = 0; s <= nl; s++)
+      for (int t = 1; t <= nc; t++) {
         if (s == 1 && t == 1) continue;
-        float3 Lc = f3(0.f, 0.f, 0.f);
-        BVert sampled;
-        bool has = false;
-        bool splat = false;
-        int spx = 0, spy = 0;
-        if (s == 0) {
-          // evaluatePathTracingStrategy (bdpt.go:317-332)
-          if (t == P.nc) {
-            const BVert& last = P.cam[t - 1];
-            Lc = last.Le * last.beta;
-          }
-        } else if (t == 1) {
-          // evaluateLightTracingStrategy (bdpt.go:398-486)
-          const BVert& lv = P.lgt[s - 1];
-          if (s <= 1 || lv.is(kFlagSpecular)) continue;
-          float2 cs = rs.next2();
-          float2 lens2 = sample_unit_disk(cs);
-          float3 lp = sc.cam.center + sc.cam.u * (lens2.x * sc.cam.lens_radius) + sc.cam.v * (lens2.y * sc.cam.lens_radius);
-          float3 toRef = lv.p - lp;
-          float dist = length(toRef);
-          float3 dir = normalize(toRef);
-          float cpdf = (dist * dist) / (fabsf(dot(sc.cam.forward, dir)) * sc.cam.lens_area);
-          float imp = camera_importance(sc.cam, dir);
-          if (imp == 0.f) continue;  // SampleCameraFromPoint returns nil
-          float3 toCam = -dir;
-          float3 f = vertex_brdf(sc, lv, toCam, false);
-          float cb = imp / cpdf;
-          float cosine = dot(toCam, lv.n);
-          if (cosine <= 0.f) continue;
-          float3 c = f * cb * lv.beta;
-          if (on_surface(sc, lv)) c = c * cosine;
-          if (is_zero(c)) continue;
-          Hit hh;
-          if (trace<true, false>(sc, lv.p, toCam, 0.001f, dist - 0.001f, lv.prim, hh, err)) continue;
-          if (!map_ray_to_pixel(sc.cam, lp, dir, spx, spy)) continue;
-          float lpdf = total_light_pdf(sc, lp, toCam, normalize(lv.p - lp));
-          sampled.p = lp;
-          sampled.n = toCam;
-          sampled.wi = f3(0.f, 0.f, 0.f);
-          sampled.beta = f3(cb, cb, cb);
-          sampled.Le = f3(0.f, 0.f, 0.f);
-          sampled.fwd = cpdf;
-          sampled.rev = lpdf;
-          sampled.mat = -1;
-          sampled.light = -1;
-          sampled.prim = kNoHit;
-          sampled.flags = kFlagCamera;
-          has = true;
-          splat = true;
-          Lc = c;
-        } else if (s == 1) {
-          // evaluateDirectLightingStrategy (bdpt.go:334-394)
-          const BVert& cv = P.cam[t - 1];
-          if (cv.is(kFlagSpecular) || cv.mat < 0) continue;
-          if (sc.n_lights == 0) continue;
-          int li = pick_light(sc, rs.next());
-          DevLight L = sc.lights[li];
-          LightSample ls = light_sample(sc, L, cv.p, cv.n, rs.next2());
-          ls.pdf *= L.prob;
-          if (is_zero(ls.emission) || ls.pdf <= 0.f) continue;
-          float ct = fabsf(dot(ls.dir, cv.n));
-          if (ct <= 0.f) continue;
-          float3 f = vertex_brdf(sc, cv, ls.dir, true);
-          float3 lb = ls.emission * (1.f / ls.pdf);
-          float3 c = f * cv.beta * lb * ct;
-          if (is_zero(c)) continue;
-          Hit hh;
-          if (trace<true, false>(sc, cv.p, ls.dir, 0.001f, ls.dist - 0.001f, cv.prim, hh, err)) continue;
-          sampled.p = ls.point;
-          sampled.n = ls.normal;
-          sampled.wi = f3(0.f, 0.f, 0.f);
-          sampled.light = li;
-          sampled.mat = -1;
-          sampled.prim = kNoHit;
-          sampled.fwd = ls.pdf;
-          sampled.rev = 0.f;
-          bool inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
-          sampled.flags = kFlagLight | (inf ? kFlagInfinite : 0);
-          sampled.beta = lb;
-          sampled.Le = ls.emission;
-          has = true;
-          Lc = c;
-        } else {
-          // evaluateConnectionStrategy (bdpt.go:502-561)
-          const BVert& lv = P.lgt[s - 1];
-          const BVert& cv = P.cam[t - 1];
-          if (lv.is(kFlagSpecular) || cv.is(kFlagSpecular)) continue;
-          float3 dd = lv.p - cv.p;
-          float dist = length(dd);
-          if (dist < 0.001f) continue;
-          dd = dd * (1.f / dist);
-          float cc = dot(dd, cv.n), cl = dot(-dd, lv.n);
-          if (cc <= 0.f || cl <= 0.f) continue;
-          float g = (cc * cl) / (dist * dist);
-          float3 cb = vertex_brdf(sc, cv, dd, true);
-          float3 lb = vertex_brdf(sc, lv, -dd, false);
-          float3 c = lv.beta * lb * cb * cv.beta * g;
-          if (is_zero(c)) continue;
-          Hit hh;
-          if (trace<true, false>(sc, cv.p, dd, 0.001f, dist - 0.001f, cv.prim, hh, err)) continue;
-          Lc = c;
-        }
-        if (is_zero(Lc) && !splat) continue;
-        float w = mis_weight<MAXV>(sc, P, has ? &sampled : nullptr, s, t);
-        if (splat) {
-          float3 c = Lc * w;
-          float4* dst = film.splat + (size_t)spy * film.width + spx;
-          atomicAdd(&dst->x, c.x);
-          atomicAdd(&dst->y, c.y);
-          atomicAdd(&dst->z, c.z);
-        } else {
-          total += Lc * w;
-        }
+        float4 c = B.contrib[(size_t)(s * MAXV + t - 1) * n + i];
+        total += f3(c);
       }
-    }
-    PS.Lout[p] = make_float4(total.x, total.y, total.z, 0.f);
+    PS.Lout[i] = make_float4(total.x, total.y, total.z, 0.f);
   }
 }
 
@@ -611,9 +771,21 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
                  cudaStream_t st) {
   uint32_t n = ch.npix * ch.layers;
   (void)block;
-  int grid = launch_grid(n, 128, 0);
-  if (sc.max_depth <= 9) k_bdpt<10><<<grid, 128, 0, st>>>(sc, film, P, ch);
-  else k_bdpt<18><<<grid, 128, 0, st>>>(sc, film, P, ch);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int g1 = launch_grid(n, 128, 0);
+  int g2 = std::max(1, sms * 16);
+  int g3 = launch_grid(n, 256, 0);
+  if (P.bd.maxv == 10) {
+    k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<10><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_sum<10><<<g3, 256, 0, st>>>(P, ch);
+  } else {
+    k_bdpt_subpaths<18><<<g1, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<18><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_sum<18><<<g3, 256, 0, st>>>(P, ch);
+  }
 }
 
 }  // namespace gprt

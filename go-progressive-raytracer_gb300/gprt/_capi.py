@@ -1,8 +1,8 @@
 """ctypes binding of include/gprt.h.
 
-Loads the in-tree ``_build/libgprt.so``; there is no other implementation, so
-a missing library is an error (build it with ``build.py`` or
-``__graft_entry__.build()``).
+Loads the in-tree ``_build/libgprt.so`` (or the build named by the GPRT_LIB
+environment variable); there is no other implementation, so a missing
+library is an error (build it with ``build.py`` or ``__graft_entry__.build()``).
 """
 import ctypes as C
 import os
@@ -207,7 +207,7 @@ def load(path=None):
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("GPRT_LIB") or LIB_PATH
     if not os.path.exists(p):
         raise RuntimeError("libgprt.so is not built (%s); run go-progressive-raytracer_gb300/build.py" % p)
     lib = C.CDLL(p)

@@ -101,19 +101,24 @@ def main(argv=None):
     _setup()
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--only", default="", help="comma list of: cornell, spheres, icosphere, bdpt, raw")
     a = ap.parse_args(argv)
+    only = set(x for x in a.only.split(",") if x)
     import torch
     import gprt
     from gprt import scenes
     ctx = gprt.Context(0)
     PT, BD = gprt.PathTracingIntegrator, gprt.BDPTIntegrator
-    cases = [("cornell (path-tracing workload), PT", scenes.cornell_baseline(400), 64, PT),
-             ("reference cornell with spheres, PT", scenes.cornell_scene(), 64, PT),
-             ("icosphere L8 (1,310,720 tris), PT", scenes.icosphere_scene(level=8, width=1024), 16, PT),
-             ("cornell-boxes, BDPT", scenes.cornell_boxes_bdpt(512), 64, BD)]
-    for name, sc, spp, integ in cases:
-        print(json.dumps(_render(ctx, torch, name, sc, spp, integ, a.steps)), flush=True)
-    print(json.dumps(_raw_batch(ctx, torch, a.steps)), flush=True)
+    cases = [("cornell", "cornell (path-tracing workload), PT", lambda: scenes.cornell_baseline(400), 64, PT),
+             ("spheres", "reference cornell with spheres, PT", lambda: scenes.cornell_scene(), 64, PT),
+             ("icosphere", "icosphere L8 (1,310,720 tris), PT", lambda: scenes.icosphere_scene(level=8, width=1024), 16,
+              PT),
+             ("bdpt", "cornell-boxes, BDPT", lambda: scenes.cornell_boxes_bdpt(512), 64, BD)]
+    for key, name, make, spp, integ in cases:
+        if not only or key in only:
+            print(json.dumps(_render(ctx, torch, name, make(), spp, integ, a.steps)), flush=True)
+    if not only or "raw" in only:
+        print(json.dumps(_raw_batch(ctx, torch, a.steps)), flush=True)
     ctx.close()
     return 0
 
