@@ -1,0 +1,97 @@
+"""The workloads at their full sizes, checked through properties that do not
+depend on size (the oracle checks a sample of each against its own result):
+
+- the raw batch: 2^24 rays (half camera rays at 1024^2, half incoherent
+  surface rays) on the level-8 icosphere (1,310,720 triangles) -- any-hit and
+  closest-hit agree on every ray, a repeated call is bit-identical, and 8,192
+  rays drawn across the batch match the oracle under the hit-parity rule;
+- the BVH-stress render (1024^2, 16 spp): deterministic, every pixel holds
+  16 samples, radiance finite and non-negative, mean below the sky's 1.0;
+- the Cornell path-tracing render at 400^2, 64 spp: chunk-size invariant
+  (one wavefront vs. 64 small ones give the same film bit for bit).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ico8():
+    from gprt import scenes
+    return scenes.icosphere_scene(level=8, width=1024)
+
+
+def test_raw_batch_2_24_rays(ctx, oracle, ico8):
+    import gprt
+    from gprt import scenes
+    from test_gpu_intersect import REL
+    mesh = ico8.shapes[0].mesh
+    n = 1 << 24
+    rays = scenes.ray_batch(mesh.vertices, mesh.faces, n, seed=13, width=1024)
+    flat = ico8.to_desc()
+    g = gprt.GpuScene(ctx, flat)
+    hits = g.intersect(rays)
+    anyh = g.intersect(rays, any_hit=True)
+    hit = hits["prim"] != gprt.capi.NO_HIT
+    assert np.array_equal(hit, anyh["prim"] != gprt.capi.NO_HIT)
+    assert np.array_equal(hits, g.intersect(rays))
+    assert 0.5 < hit.mean() < 1.0
+    # a sample of the batch against the oracle
+    idx = np.random.default_rng(5).choice(n, 8192, replace=False)
+    sub = rays[idx]
+    shape_map, sub_map = g.primitive_map()
+    o = oracle.OracleScene(flat)
+    t_o, shape_o, sub_o, _, nrm_o = o.intersect(sub)
+    h = hits[idx]
+    g_hit = h["prim"] != gprt.capi.NO_HIT
+    o_hit = shape_o >= 0
+    assert (g_hit != o_hit).sum() <= 2
+    both = g_hit & o_hit
+    pid = h["prim"][both]
+    same = (shape_map[pid] == shape_o[both]) & (sub_map[pid] == sub_o[both])
+    o_len = np.linalg.norm(sub[both, 0:3].astype(np.float64), axis=1)
+    rel = np.abs(h["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), np.maximum(o_len, 1e-30))
+    d = sub[both, 4:7].astype(np.float64)
+    cosg = np.abs(np.sum(d * nrm_o[both], axis=1)) / np.linalg.norm(d, axis=1)
+    rel_c = rel * np.minimum(1.0, np.maximum(cosg, 1e-6))
+    assert (~same & (rel_c > REL)).sum() <= 2
+    assert (rel_c[same] > REL).sum() <= 2
+    g.close()
+
+
+def test_bvh_stress_render_full_size(ctx, ico8):
+    import gprt
+    g = gprt.GpuScene(ctx, ico8.to_desc())
+    films = []
+    for _ in range(2):
+        r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=16, max_passes=1, seed=3))
+        r.add_samples(16)
+        films.append(r.film())
+        img = r.image()
+        r.close()
+    for a, b in zip(*films):
+        assert np.array_equal(a, b)
+    rgb, lum, lum2, cnt = films[0]
+    assert cnt.min() == 16 and cnt.max() == 16
+    assert np.isfinite(img).all() and img.min() >= 0.0
+    # the environment is radiance 1 and every surface albedo is < 1
+    assert 0.05 < img.mean() < 1.0
+    g.close()
+
+
+def test_cornell_400_64spp_chunk_invariant(ctx):
+    import gprt
+    from gprt import scenes
+    g = gprt.GpuScene(ctx, scenes.cornell_baseline(400).to_desc())
+    out = []
+    for chunk in (0, 400 * 400 // 4):
+        r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=64, max_passes=1, seed=9,
+                                                                chunk_paths=chunk))
+        r.add_samples(64)
+        out.append(r.film())
+        r.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+    assert out[0][3].min() == 64
+    g.close()
