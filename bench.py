@@ -395,6 +395,29 @@ def bvh_stress(ctx, flat, torch):
            "host_bvh_build_ms": g.info.build_ms,
            "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
     job.close()
+    # the same scene built on the GPU (GPRT_BUILD_DEVICE): creation time and frame time
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gd = gprt.GpuScene(ctx, flat, device_bvh=True)
+    create_dev = (time.perf_counter() - t0) * 1e3
+    jd = gprt.ProgressiveRaytracer(gd, gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1,
+                                                              flags=tuned.flags, block_size=tuned.block_size,
+                                                              chunk_paths=tuned.chunk_paths))
+    sd = torch.cuda.ExternalStream(jd.stream())
+    jd.add_samples(ICO_SPP)
+    jd.sync()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(sd)
+    for _ in range(3):
+        jd.add_samples(ICO_SPP)
+    e3.record(sd)
+    jd.sync()
+    out["scene_build"] = {"host_sah_ms": g.info.build_ms, "host_sah_flatten_ms": g.info.flatten_ms,
+                          "device_lbvh_create_ms": create_dev, "device_lbvh_build_ms": gd.info.build_ms,
+                          "device_lbvh_nodes": int(gd.info.n_nodes), "host_sah_nodes": int(g.info.n_nodes),
+                          "device_lbvh_ms_per_frame": e2.elapsed_time(e3) / 3}
+    jd.close()
+    gd.close()
     g.close()
     del flush
     return out

@@ -2,6 +2,7 @@
 // the host orchestration of the kernels (chunked wavefront passes).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -261,15 +262,34 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   static std::atomic<uint64_t> next_serial{1};
   s->serial = next_serial++;
   std::string err;
-  if (!build_scene(desc, s->host, err)) return fail(ctx, GPRT_E_INVALID, err);
+  if (!build_scene(desc, s->host, err, (desc->build_flags & GPRT_BUILD_DEVICE) != 0))
+    return fail(ctx, GPRT_E_INVALID, err);
   HostScene& h = s->host;
   DevScene& d = s->dev;
   int rc = 0;
-  rc |= upload(ctx, s->buffers, h.nodes, &d.nodes, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.tris, &d.tris, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
+  if (h.device_bvh) {
+    // BVH and primitive arrays built on the GPU (also remaps the light indices)
+    rc = device_build_bvh(ctx, h, d, s->buffers, &s->bytes);
+    if (rc) {
+      free_all(s->buffers);
+      return rc;
+    }
+    // the tree is checked on the host copy before any kernel walks it
+    auto tc = std::chrono::steady_clock::now();
+    std::string bad = validate_layout(h);
+    h.check_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tc).count();
+    h.build_ms += h.check_ms;
+    if (!bad.empty()) {
+      free_all(s->buffers);
+      return fail(ctx, GPRT_E_DEVICE, "device BVH build produced an invalid tree: " + bad);
+    }
+  } else {
+    rc |= upload(ctx, s->buffers, h.nodes, &d.nodes, &s->bytes);
+    rc |= upload(ctx, s->buffers, h.tris, &d.tris, &s->bytes);
+    rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
+    rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
+    rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
+  }
   rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
   rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
   if (rc) {
@@ -332,6 +352,9 @@ int gprt_scene_get_info(const gprt_scene* s, gprt_scene_info* info) {
   info->image_width = h.sampling.width;
   info->image_height = h.sampling.height;
   info->build_ms = h.build_ms;
+  info->flatten_ms = h.flatten_ms;
+  info->bvh_ms = h.bvh_ms;
+  info->check_ms = h.check_ms;
   return GPRT_OK;
 }
 
@@ -357,6 +380,8 @@ int gprt_scene_validate(const gprt_scene_desc* desc, gprt_scene_info* info, char
     info->image_width = h.sampling.width;
     info->image_height = h.sampling.height;
     info->build_ms = h.build_ms;
+    info->flatten_ms = h.flatten_ms;
+    info->bvh_ms = h.bvh_ms;
   }
   return GPRT_OK;
 }

@@ -114,6 +114,10 @@ inline void free_all(std::vector<void*>& bufs) {
 }
 
 // getSamplesForPass (pkg/renderer/progressive.go:98-123)
+// Builds the BVH and the primitive arrays of `h` on the GPU from h.pending
+// (bvh_build.cu); the device arrays are allocated into `bufs`.
+int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*>& bufs, size_t* bytes);
+
 // Cancels the server's pending requests for a scene that is being destroyed
 // (server.cu).  Called with the scene's context locked.
 void server_forget_scene(gprt_server* sv, gprt_scene* s);

@@ -14,11 +14,14 @@
 #include "scene.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <future>
 #include <memory>
+#include <mutex>
+#include <thread>
 
 namespace gprt {
 namespace {
@@ -100,6 +103,21 @@ void box_faces(const D3& center, const D3& size, const D3& rot, D3 corner[6], D3
   bbox = box_of(cs, 8);
 }
 
+// Runs f(begin, end) over [0, n) in contiguous chunks on the host's cores
+// (one chunk when n is small).
+template <class F>
+void parallel_for(size_t n, F f) {
+  unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  unsigned T = (unsigned)std::min<size_t>(hw, n / 32768 + 1);
+  if (T <= 1) {
+    f((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; t++) th.emplace_back([=]() { f(n * t / T, n * (t + 1) / T); });
+  for (auto& x : th) x.join();
+}
+
 float4 mk4(const D3& a, float w) { return make_float4((float)a.x, (float)a.y, (float)a.z, w); }
 float i2f(uint32_t i) {
   float f;
@@ -112,6 +130,31 @@ struct Prim {
   int type;
   uint32_t shape, sub, material;
   D3 a, b, c;  // tri: v0,v1,v2 ; quad: corner,u,v ; sphere: center,(r,_,_)
+};
+
+// Primitive storage that grows without initialising: the slots of a mesh are
+// filled in parallel, so the pages are first touched by the filling threads.
+struct PrimArray {
+  std::unique_ptr<Prim[]> p;
+  size_t n = 0, cap = 0;
+  void reserve(size_t c) {
+    if (c <= cap) return;
+    std::unique_ptr<Prim[]> q(static_cast<Prim*>(::operator new[](c * sizeof(Prim))));
+    if (n) std::memcpy(static_cast<void*>(q.get()), p.get(), n * sizeof(Prim));
+    p.reset(q.release());
+    cap = c;
+  }
+  void push_back(const Prim& x) {
+    if (n == cap) reserve(std::max<size_t>(16, cap * 2));
+    p[n++] = x;
+  }
+  void grow_uninit(size_t k) {
+    reserve(n + k);
+    n += k;
+  }
+  size_t size() const { return n; }
+  Prim& operator[](size_t i) { return p[i]; }
+  const Prim& operator[](size_t i) const { return p[i]; }
 };
 
 struct Ref {
@@ -135,8 +178,8 @@ struct BNode {
 
 struct Builder {
   std::vector<Ref>& refs;
-  const std::vector<Prim>& prims;
-  explicit Builder(std::vector<Ref>& r, const std::vector<Prim>& p) : refs(r), prims(p) {}
+  const PrimArray& prims;
+  explicit Builder(std::vector<Ref>& r, const PrimArray& p) : refs(r), prims(p) {}
 
   static int max_leaf(int type) { return type == kPrimQuad ? 2 : 4; }
 
@@ -270,7 +313,7 @@ std::unique_ptr<BNode> join(std::unique_ptr<BNode> a, std::unique_ptr<BNode> b) 
 struct Emitter {
   HostScene& out;
   const std::vector<Ref>& refs;
-  const std::vector<Prim>& prims;
+  const PrimArray& prims;
   std::vector<uint32_t>& final_index;  // prim -> index in its type array
   int max_depth = 0;
 
@@ -382,7 +425,7 @@ void pad_box(float lo[3], float hi[3], float extent) {
 
 }  // namespace
 
-bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
+bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, bool device_bvh) {
   auto t0 = std::chrono::steady_clock::now();
   if (!d) {
     err = "null scene description";
@@ -429,7 +472,16 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
     return true;
   };
   // primitives and the reference's world box
-  std::vector<Prim> prims;
+  PrimArray prims;
+  {
+    size_t total = 0;
+    for (uint32_t i = 0; i < d->n_shapes; i++) {
+      const gprt_shape_desc& s = d->shapes[i];
+      if (s.kind == GPRT_SHAPE_MESH && d->meshes && s.mesh < d->n_meshes) total += d->meshes[s.mesh].n_triangles;
+      else total += s.kind == GPRT_SHAPE_BOX ? 6 : 1;
+    }
+    prims.reserve(total);
+  }
   std::vector<int> shape_quad_prim(d->n_shapes, -1), shape_sphere_prim(d->n_shapes, -1);
   DBox world{};
   bool have_world = false;
@@ -493,21 +545,50 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
           err = "mesh arrays are null";
           return false;
         }
-        DBox mb{};
-        for (uint32_t t = 0; t < m.n_triangles; t++) {
-          uint32_t ia = m.indices[3 * t], ib = m.indices[3 * t + 1], ic = m.indices[3 * t + 2];
-          if (ia >= m.n_vertices || ib >= m.n_vertices || ic >= m.n_vertices) {
-            err = "Face index out of bounds";  // NewTriangleMesh panics (triangle_mesh.go:73-76)
-            return false;
+        // the triangles on all host cores; a bad face index (NewTriangleMesh
+        // panics, triangle_mesh.go:73-76) or material is reported after
+        size_t first = prims.size();
+        prims.grow_uninit(m.n_triangles);
+        std::vector<DBox> part(std::max(1u, std::thread::hardware_concurrency()));
+        std::vector<uint8_t> used(part.size(), 0);
+        std::atomic<unsigned> slot{0};
+        std::atomic<int> bad{0};  // 1: face index, 2: material
+        parallel_for(m.n_triangles, [&](size_t b0, size_t b1) {
+          if (b0 == b1) return;
+          unsigned me = slot++;
+          DBox mb{};
+          for (size_t t = b0; t < b1; t++) {
+            uint32_t ia = m.indices[3 * t], ib = m.indices[3 * t + 1], ic = m.indices[3 * t + 2];
+            uint32_t mat = m.tri_materials ? m.tri_materials[t] : s.material;
+            if (ia >= m.n_vertices || ib >= m.n_vertices || ic >= m.n_vertices) {
+              bad |= 1;
+              ia = ib = ic = 0;
+            }
+            if (mat >= d->n_materials) bad |= 2;
+            D3 a(m.vertices + 3 * ia), b(m.vertices + 3 * ib), c(m.vertices + 3 * ic);
+            prims[first + t] = {kPrimTriangle, i, (uint32_t)t, mat, a, b, c};
+            D3 v3[3] = {a, b, c};
+            DBox tb = box_of(v3, 3);
+            mb = t == b0 ? tb : mb.unite(tb);
           }
-          uint32_t mat = m.tri_materials ? m.tri_materials[t] : s.material;
-          if (!check_mat(mat)) return false;
-          D3 a(m.vertices + 3 * ia), b(m.vertices + 3 * ib), c(m.vertices + 3 * ic);
-          prims.push_back({kPrimTriangle, i, t, mat, a, b, c});
-          D3 v3[3] = {a, b, c};
-          DBox tb = box_of(v3, 3);
-          mb = t == 0 ? tb : mb.unite(tb);
+          part[me] = mb;
+          used[me] = 1;
+        });
+        if (bad & 1) {
+          err = "Face index out of bounds";
+          return false;
         }
+        if (bad & 2) {
+          err = "material index out of range";
+          return false;
+        }
+        DBox mb{};
+        bool have = false;
+        for (size_t k = 0; k < part.size(); k++)
+          if (used[k]) {
+            mb = have ? mb.unite(part[k]) : part[k];
+            have = true;
+          }
         add_world(mb);
         break;
       }
@@ -528,9 +609,18 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
   if (have_world) ext = std::max({std::fabs(world.mx.x - world.mn.x), std::fabs(world.mx.y - world.mn.y),
                                   std::fabs(world.mx.z - world.mn.z)});
   float fext = (float)std::min(ext, 1e30);
-  // references per type
+  // references per type (rank of each primitive within its type, then the
+  // boxes on all host cores)
   std::vector<Ref> refs[3];
-  for (uint32_t k = 0; k < prims.size(); k++) {
+  std::vector<uint32_t> rank(prims.size());
+  {
+    uint32_t cnt[3] = {0, 0, 0};
+    for (size_t k = 0; k < prims.size(); k++) rank[k] = cnt[prims[k].type]++;
+    for (int t = 0; t < 3; t++) refs[t].resize(cnt[t]);
+  }
+  parallel_for(prims.size(), [&](size_t b0, size_t b1) {
+   for (size_t kk = b0; kk < b1; kk++) {
+    uint32_t k = (uint32_t)kk;
     const Prim& p = prims[k];
     Ref r;
     r.prim = k;
@@ -553,11 +643,57 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
     r.hi[0] = (float)b.mx.x, r.hi[1] = (float)b.mx.y, r.hi[2] = (float)b.mx.z;
     pad_box(r.lo, r.hi, fext);
     for (int j = 0; j < 3; j++) r.ct[j] = 0.5f * (r.lo[j] + r.hi[j]);
-    refs[p.type].push_back(r);
-  }
+    refs[p.type][rank[k]] = r;
+   }
+  });
   out.n_tris = (uint32_t)refs[kPrimTriangle].size();
   out.n_quads = (uint32_t)refs[kPrimQuad].size();
   out.n_spheres = (uint32_t)refs[kPrimSphere].size();
+  std::vector<uint32_t> final_index(prims.size(), 0);
+  out.device_bvh = device_bvh && prims.size() >= 8;
+  if (out.device_bvh) {
+    // the device builder takes the primitives in flattened order
+    BuildPrims& bp = out.pending;
+    size_t np = prims.size();
+    bp.box.resize(2 * np);
+    bp.geo.resize(9 * np);
+    bp.shape.resize(np);
+    bp.sub.resize(np);
+    for (int k = 0; k < 3; k++) {
+      bp.clo[k] = INFINITY;
+      bp.chi[k] = -INFINITY;
+    }
+    std::mutex mu;
+    parallel_for(np, [&](size_t b0, size_t b1) {
+      float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (size_t k = b0; k < b1; k++) {
+        const Prim& p = prims[k];
+        const Ref& r = refs[p.type][rank[k]];
+        bp.box[2 * k] = make_float4(r.lo[0], r.lo[1], r.lo[2], i2f((uint32_t)p.type));
+        bp.box[2 * k + 1] = make_float4(r.hi[0], r.hi[1], r.hi[2], i2f(p.material));
+        const D3* v[3] = {&p.a, &p.b, &p.c};
+        for (int q = 0; q < 3; q++) {
+          bp.geo[9 * k + 3 * q] = v[q]->x;
+          bp.geo[9 * k + 3 * q + 1] = v[q]->y;
+          bp.geo[9 * k + 3 * q + 2] = v[q]->z;
+        }
+        bp.shape[k] = p.shape;
+        bp.sub[k] = p.sub;
+        for (int j = 0; j < 3; j++) {
+          lo[j] = std::min(lo[j], r.ct[j]);
+          hi[j] = std::max(hi[j], r.ct[j]);
+        }
+        final_index[k] = (uint32_t)k;  // flattened order until the build
+      }
+      std::lock_guard<std::mutex> g(mu);
+      for (int j = 0; j < 3; j++) {
+        bp.clo[j] = std::min(bp.clo[j], lo[j]);
+        bp.chi[j] = std::max(bp.chi[j], hi[j]);
+      }
+    });
+  }
+  auto t_flat = std::chrono::steady_clock::now();
+  out.flatten_ms = std::chrono::duration<double, std::milli>(t_flat - t0).count();
   std::vector<Ref> all;
   all.reserve(prims.size());
   uint32_t off[3];
@@ -565,25 +701,27 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
     off[t] = (uint32_t)all.size();
     all.insert(all.end(), refs[t].begin(), refs[t].end());
   }
-  Builder bld(all, prims);
-  std::unique_ptr<BNode> roots[3];
-  for (int t = 0; t < 3; t++)
-    if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
-  std::unique_ptr<BNode> root = join(std::move(roots[0]), join(std::move(roots[1]), std::move(roots[2])));
-  std::vector<uint32_t> final_index(prims.size(), 0);
-  if (root) {
-    Emitter em{out, all, prims, final_index};
-    em.emit(root.get(), 0);
-    out.bvh_depth = em.max_depth;
-  }
-  // primitive id maps
-  out.prim_shape.assign(prims.size(), 0);
-  out.prim_sub.assign(prims.size(), 0);
-  uint32_t base[3] = {0, out.n_tris, out.n_tris + out.n_quads};
-  for (uint32_t k = 0; k < prims.size(); k++) {
-    uint32_t gid = base[prims[k].type] + final_index[k];
-    out.prim_shape[gid] = prims[k].shape;
-    out.prim_sub[gid] = prims[k].sub;
+  if (!out.device_bvh) {
+    Builder bld(all, prims);
+    std::unique_ptr<BNode> roots[3];
+    for (int t = 0; t < 3; t++)
+      if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
+    std::unique_ptr<BNode> root = join(std::move(roots[0]), join(std::move(roots[1]), std::move(roots[2])));
+    if (root) {
+      Emitter em{out, all, prims, final_index};
+      em.emit(root.get(), 0);
+      out.bvh_depth = em.max_depth;
+    }
+    out.bvh_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_flat).count();
+    // primitive id maps
+    out.prim_shape.assign(prims.size(), 0);
+    out.prim_sub.assign(prims.size(), 0);
+    uint32_t base[3] = {0, out.n_tris, out.n_tris + out.n_quads};
+    for (uint32_t k = 0; k < prims.size(); k++) {
+      uint32_t gid = base[prims[k].type] + final_index[k];
+      out.prim_shape[gid] = prims[k].shape;
+      out.prim_sub[gid] = prims[k].sub;
+    }
   }
   // lights (pkg/scene/scene.go:102-141) and the light sampler
   // (weighted_light_sampler.go:22-78)
@@ -642,6 +780,10 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
         return false;
     }
     out.lights.push_back(L);
+    if (out.device_bvh)  // remapped to leaf order by the device builder
+      out.pending.light_prim.push_back(l.kind == GPRT_LIGHT_QUAD     ? shape_quad_prim[l.shape]
+                                       : l.kind == GPRT_LIGHT_SPHERE ? shape_sphere_prim[l.shape]
+                                                                     : -1);
   }
   // camera (NewCamera, pkg/geometry/camera.go:70-170) in float64
   const gprt_camera_desc& c = d->camera;
@@ -710,86 +852,104 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err) {
 }
 
 // ---------------------------------------------------------------- invariants
+// Every node is checked independently (on all host cores): used child slots
+// come first; an inner child has a larger index than its parent (both
+// builders number children after their parent, so the tree is acyclic) and
+// lies inside the parent's slot box; a leaf names a valid range of one
+// primitive array whose primitives lie inside its box.  Then every node but
+// the root must be referenced exactly once and every primitive exactly once.
 std::string validate_layout(const HostScene& s) {
   size_t nn = s.nodes.size() / 8;
-  std::vector<uint8_t> seen[3];
-  seen[kPrimTriangle].assign(s.n_tris, 0);
-  seen[kPrimQuad].assign(s.n_quads, 0);
-  seen[kPrimSphere].assign(s.n_spheres, 0);
-  std::vector<uint8_t> node_seen(nn, 0);
-  auto rd = [](const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; };
-  auto ri = [&](const float4& v, int i) {
-    float f = rd(v, i);
+  if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres) ? "primitives without a BVH" : "";
+  size_t np[3] = {s.n_tris, s.n_quads, s.n_spheres};
+  std::unique_ptr<std::atomic<uint8_t>[]> pseen[3];
+  for (int t = 0; t < 3; t++) {
+    pseen[t].reset(new std::atomic<uint8_t>[np[t] ? np[t] : 1]);
+    for (size_t k = 0; k < np[t]; k++) pseen[t][k].store(0, std::memory_order_relaxed);
+  }
+  std::unique_ptr<std::atomic<uint8_t>[]> nseen(new std::atomic<uint8_t>[nn]);
+  for (size_t k = 0; k < nn; k++) nseen[k].store(0, std::memory_order_relaxed);
+  std::mutex mu;
+  std::string first_err;
+  auto ri = [](float f) {
     int x;
     std::memcpy(&x, &f, 4);
     return x;
   };
-  if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres) ? "primitives without a BVH" : "";
-  std::vector<int> todo = {0};
-  node_seen[0] = 1;
-  while (!todo.empty()) {
-    int n = todo.back();
-    todo.pop_back();
-    const float4* N = &s.nodes[(size_t)n * 8];
-    bool seen_empty = false;
-    for (int i = 0; i < 4; i++) {
-      const float4 &A = N[2 * i], &B = N[2 * i + 1];
-      int ch = ri(A, 3), mt = ri(B, 3);
-      if (ch == kEmptyChild) {
-        seen_empty = true;
-        continue;
-      }
-      if (seen_empty) return "used child slot after an empty one";
-      float lo[3] = {A.x, A.y, A.z}, hi[3] = {B.x, B.y, B.z};
-      auto inside = [&](float x, int k) { return x >= lo[k] && x <= hi[k]; };
-      if (mt == 0) {
-        if (ch <= 0 || (size_t)ch >= nn || node_seen[ch]) return "bad child node index";
-        node_seen[ch] = 1;
-        const float4* C = &s.nodes[(size_t)ch * 8];
-        for (int j = 0; j < 4; j++) {
-          const float4 &CA = C[2 * j], &CB = C[2 * j + 1];
-          if (ri(CA, 3) == kEmptyChild) continue;
-          if (!(CA.x >= lo[0] && CB.x <= hi[0] && CA.y >= lo[1] && CB.y <= hi[1] && CA.z >= lo[2] && CB.z <= hi[2]))
-            return "child box not inside its parent slot";
+  parallel_for(nn, [&](size_t b0, size_t b1) {
+    auto bad = [&](const char* m) {
+      std::lock_guard<std::mutex> g(mu);
+      if (first_err.empty()) first_err = m;
+    };
+    for (size_t n = b0; n < b1; n++) {
+      const float4* N = &s.nodes[n * 8];
+      bool seen_empty = false;
+      for (int i = 0; i < 4; i++) {
+        const float4 &A = N[2 * i], &B = N[2 * i + 1];
+        int ch = ri(A.w), mt = ri(B.w);
+        if (ch == kEmptyChild) {
+          seen_empty = true;
+          continue;
         }
-        todo.push_back(ch);
-        continue;
-      }
-      int cnt = mt & kLeafCountMask, type = (mt >> kLeafTypeShift) & 3;
-      if (type > kPrimSphere || cnt <= 0) return "bad leaf meta";
-      if (ch < 0 || (size_t)ch + cnt > seen[type].size()) return "leaf range out of bounds";
-      for (int k = 0; k < cnt; k++) {
-        int p = ch + k;
-        if (seen[type][p]++) return "primitive referenced twice";
-        if (type == kPrimTriangle) {
-          const float4* T = &s.tris[(size_t)p * 3];
-          float v[3][3] = {{T[0].x, T[0].y, T[0].z}, {T[0].x + T[1].x, T[0].y + T[1].y, T[0].z + T[1].z},
-                           {T[0].x + T[2].x, T[0].y + T[2].y, T[0].z + T[2].z}};
-          for (auto& q : v)
+        if (seen_empty) return bad("used child slot after an empty one");
+        float lo[3] = {A.x, A.y, A.z}, hi[3] = {B.x, B.y, B.z};
+        auto inside = [&](float x, int k) { return x >= lo[k] && x <= hi[k]; };
+        if (mt == 0) {
+          if (ch <= (int)n || (size_t)ch >= nn) return bad("bad child node index");
+          nseen[ch].fetch_add(1, std::memory_order_relaxed);
+          const float4* C = &s.nodes[(size_t)ch * 8];
+          for (int j = 0; j < 4; j++) {
+            const float4 &CA = C[2 * j], &CB = C[2 * j + 1];
+            if (ri(CA.w) == kEmptyChild) continue;
+            if (!(CA.x >= lo[0] && CB.x <= hi[0] && CA.y >= lo[1] && CB.y <= hi[1] && CA.z >= lo[2] && CB.z <= hi[2]))
+              return bad("child box not inside its parent slot");
+          }
+          continue;
+        }
+        int cnt = mt & kLeafCountMask, type = (mt >> kLeafTypeShift) & 3;
+        if (type > kPrimSphere || cnt <= 0 || (mt & ~0x3FF)) return bad("bad leaf meta");
+        if (ch < 0 || (size_t)ch + cnt > np[type]) return bad("leaf range out of bounds");
+        for (int k = 0; k < cnt; k++) {
+          size_t p = (size_t)ch + k;
+          pseen[type][p].fetch_add(1, std::memory_order_relaxed);
+          if (type == kPrimTriangle) {
+            const float4* T = &s.tris[p * 3];
+            float v[3][3] = {{T[0].x, T[0].y, T[0].z}, {T[0].x + T[1].x, T[0].y + T[1].y, T[0].z + T[1].z},
+                             {T[0].x + T[2].x, T[0].y + T[2].y, T[0].z + T[2].z}};
+            for (auto& q : v)
+              for (int a = 0; a < 3; a++)
+                if (!inside(q[a], a)) return bad("triangle outside its leaf box");
+          } else if (type == kPrimSphere) {
+            const float4& S = s.spheres[p * 2];
+            float r = std::fabs(S.w), c[3] = {S.x, S.y, S.z};
             for (int a = 0; a < 3; a++)
-              if (!inside(q[a], a)) return "triangle outside its leaf box";
-        } else if (type == kPrimSphere) {
-          const float4& S = s.spheres[(size_t)p * 2];
-          float r = std::fabs(S.w), c[3] = {S.x, S.y, S.z};
-          for (int a = 0; a < 3; a++)
-            if (!inside(c[a] - r, a) || !inside(c[a] + r, a)) return "sphere outside its leaf box";
-        } else {
-          const float4* Q = &s.quads[(size_t)p * 5];
-          float c[3] = {Q[0].x, Q[0].y, Q[0].z}, u[3] = {Q[1].x, Q[1].y, Q[1].z}, v[3] = {Q[2].x, Q[2].y, Q[2].z};
-          for (int a = 0; a < 3; a++) {
-            float xs[4] = {c[a], c[a] + u[a], c[a] + v[a], c[a] + u[a] + v[a]};
-            for (float x : xs)
-              if (!inside(x, a)) return "quad outside its leaf box";
+              if (!inside(c[a] - r, a) || !inside(c[a] + r, a)) return bad("sphere outside its leaf box");
+          } else {
+            const float4* Q = &s.quads[p * 5];
+            float c[3] = {Q[0].x, Q[0].y, Q[0].z}, u[3] = {Q[1].x, Q[1].y, Q[1].z}, v[3] = {Q[2].x, Q[2].y, Q[2].z};
+            for (int a = 0; a < 3; a++) {
+              float xs[4] = {c[a], c[a] + u[a], c[a] + v[a], c[a] + u[a] + v[a]};
+              for (float x : xs)
+                if (!inside(x, a)) return bad("quad outside its leaf box");
+            }
           }
         }
       }
     }
+  });
+  if (!first_err.empty()) return first_err;
+  if (nseen[0].load()) return "the root is referenced as a child";
+  for (size_t i = 1; i < nn; i++) {
+    uint8_t c = nseen[i].load(std::memory_order_relaxed);
+    if (c == 0) return "unreachable node";
+    if (c > 1) return "node referenced twice";
   }
   for (int t = 0; t < 3; t++)
-    for (uint8_t x : seen[t])
-      if (!x) return "primitive missing from the BVH";
-  for (size_t i = 0; i < nn; i++)
-    if (!node_seen[i]) return "unreachable node";
+    for (size_t k = 0; k < np[t]; k++) {
+      uint8_t c = pseen[t][k].load(std::memory_order_relaxed);
+      if (c == 0) return "primitive missing from the BVH";
+      if (c > 1) return "primitive referenced twice";
+    }
   return "";
 }
 

@@ -9,6 +9,16 @@
 
 namespace gprt {
 
+// Input of the device BVH builder (bvh_build.cu): every primitive in
+// flattened order.
+struct BuildPrims {
+  std::vector<float4> box;           // 2 per primitive: (lo.xyz, type bits) (hi.xyz, material bits), padded
+  std::vector<double> geo;           // 9 per primitive: tri v0 v1 v2 / quad corner u v / sphere centre (r,0,0)
+  std::vector<uint32_t> shape, sub;  // index in scene.Shapes, box face / mesh triangle
+  std::vector<int> light_prim;       // per light: flattened index of its primitive, -1 for infinite lights
+  float clo[3], chi[3];              // centroid bounds
+};
+
 struct HostScene {
   // device layout (host copies, uploaded by the C ABI layer)
   std::vector<float4> nodes, tris, tri_normals, quads, spheres;
@@ -23,12 +33,17 @@ struct HostScene {
   DevCamera cam{};
   gprt_sampling_desc sampling{};
   int bvh_depth = 0;
-  double build_ms = 0;
+  double build_ms = 0, flatten_ms = 0, bvh_ms = 0, check_ms = 0;
+  bool device_bvh = false;  // the BVH and primitive arrays are built on the GPU from `pending`
+  BuildPrims pending;
 };
 
 // Flattens `desc` into `out`.  Returns false with `err` set on invalid or
-// unsupported content.
-bool build_scene(const gprt_scene_desc* desc, HostScene& out, std::string& err);
+// unsupported content.  With device_bvh (and at least 8 primitives) the BVH
+// and the primitive arrays are left to the device builder: `out.pending`
+// holds the primitives, light indices refer to the flattened order, and the
+// primitive maps are filled by the builder.
+bool build_scene(const gprt_scene_desc* desc, HostScene& out, std::string& err, bool device_bvh = false);
 
 // Checks the layout invariants of a built scene; returns "" when valid.
 std::string validate_layout(const HostScene& s);

@@ -25,6 +25,7 @@ LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE = rang
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
 CLOSEST, ANY = 0, 1
 NO_HIT = 0xFFFFFFFF
+BUILD_DEVICE = 1
 NOALLOC_MAX_PATHS = 131072  # GPRT_NOALLOC_MAX_PATHS
 
 
@@ -65,7 +66,7 @@ class SceneDesc(C.Structure):
     _fields_ = [("materials", C.POINTER(MaterialDesc)), ("shapes", C.POINTER(ShapeDesc)),
                 ("meshes", C.POINTER(MeshDesc)), ("lights", C.POINTER(LightDesc)),
                 ("n_materials", C.c_uint32), ("n_shapes", C.c_uint32), ("n_meshes", C.c_uint32),
-                ("n_lights", C.c_uint32), ("weighted_sampler", C.c_uint32), ("reserved", C.c_uint32),
+                ("n_lights", C.c_uint32), ("weighted_sampler", C.c_uint32), ("build_flags", C.c_uint32),
                 ("camera", CameraDesc), ("sampling", SamplingDesc)]
 
 
@@ -82,7 +83,8 @@ class SceneInfo(C.Structure):
     _fields_ = [("world_center", C.c_double * 3), ("world_radius", C.c_double), ("n_primitives", C.c_uint64),
                 ("n_triangles", C.c_uint64), ("n_quads", C.c_uint64), ("n_spheres", C.c_uint64),
                 ("n_nodes", C.c_uint64), ("device_bytes", C.c_uint64), ("image_width", C.c_uint32),
-                ("image_height", C.c_uint32), ("build_ms", C.c_double)]
+                ("image_height", C.c_uint32), ("build_ms", C.c_double), ("flatten_ms", C.c_double),
+                ("bvh_ms", C.c_double), ("check_ms", C.c_double)]
 
 
 class JobDesc(C.Structure):

@@ -44,9 +44,12 @@ class Context:
 class GpuScene:
     """scene.Scene after Preprocess, resident on the device."""
 
-    def __init__(self, ctx: Context, scene):
+    def __init__(self, ctx: Context, scene, device_bvh: bool = False):
+        """device_bvh: build the BVH on the GPU (GPRT_BUILD_DEVICE) instead of
+        the host SAH builder."""
         self.ctx = ctx
         self.flat = scene.to_desc() if hasattr(scene, "to_desc") else scene
+        self.flat.desc.build_flags = capi.BUILD_DEVICE if device_bvh else 0
         h = C.c_void_p()
         ctx.check(ctx.lib.gprt_scene_create(ctx.h, self.flat.ptr(), C.byref(h)))
         self.h = h

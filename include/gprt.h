@@ -150,7 +150,7 @@ typedef struct gprt_scene_desc {
   uint32_t n_meshes;
   uint32_t n_lights;
   uint32_t weighted_sampler; /* 0: lights.NewUniformLightSampler; 1: NewWeightedLightSampler(weights) */
-  uint32_t reserved;
+  uint32_t build_flags;      /* GPRT_BUILD_* */
   gprt_camera_desc camera;
   gprt_sampling_desc sampling;
 } gprt_scene_desc;
@@ -159,6 +159,14 @@ typedef struct gprt_scene_desc {
  * Layout of a ray batch for gprt_intersect: 32 bytes per ray, two 16-byte
  * vectors per ray.  tmin/tmax are the Hit(ray, tMin, tMax) interval of
  * geometry.BVH.Hit. */
+/* BVH construction.  Default: binned-SAH BVH built on the host (best
+ * traversal speed).  GPRT_BUILD_DEVICE builds it on the GPU instead: Morton
+ * codes, radix sort, a linear BVH (Karras 2012) collapsed to the same
+ * 4-wide node layout, in milliseconds for millions of triangles (for scenes
+ * that arrive while a server is running); its tree traverses somewhat
+ * slower.  Scenes of fewer than 8 primitives always build on the host. */
+#define GPRT_BUILD_DEVICE 1u
+
 typedef struct gprt_ray {
   float ox, oy, oz, tmin;
   float dx, dy, dz, tmax;
@@ -187,7 +195,10 @@ typedef struct gprt_scene_info {
   uint64_t device_bytes;  /* device memory held by the scene */
   uint32_t image_width;
   uint32_t image_height;
-  double build_ms;        /* host BVH build time */
+  double build_ms;        /* scene construction time (flatten + BVH + checks) */
+  double flatten_ms;      /* of which: flattening the description into primitives */
+  double bvh_ms;          /* of which: BVH build and primitive arrays (host SAH or device) */
+  double check_ms;        /* of which: layout check of a device-built tree */
 } gprt_scene_info;
 
 /* ---- progressive jobs ---------------------------------------------------- */
