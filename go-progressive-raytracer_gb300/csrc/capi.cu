@@ -674,21 +674,20 @@ int gprt_job_read_rgba8(gprt_job* j, uint8_t* rgba) {
 int gprt_job_read_tile(gprt_job* j, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint8_t* rgba) {
   if (!j || !rgba || x1 <= x0 || y1 <= y0 || x1 > (uint32_t)j->film.width || y1 > (uint32_t)j->film.height)
     return GPRT_E_INVALID;
-  std::lock_guard<std::recursive_mutex> lk(j->scene->ctx->mu);
-  size_t npix = (size_t)j->film.width * j->film.height;
-  std::vector<uint8_t> full(npix * 4);
-  int rc = gprt_job_read_rgba8(j, full.data());
-  if (rc) return rc;
-  // extractTileImage leaves pixels with no samples at zero (progressive.go:242-250)
-  std::vector<uint32_t> cnt(npix);
-  if (cudaMemcpy(cnt.data(), j->film.count, npix * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return fail(j->scene->ctx, GPRT_E_DEVICE, "tile read-back");
-  uint32_t tw = x1 - x0;
-  for (uint32_t y = y0; y < y1; y++)
-    for (uint32_t x = x0; x < x1; x++) {
-      size_t si = (size_t)y * j->film.width + x, di = (size_t)(y - y0) * tw + (x - x0);
-      for (int k = 0; k < 4; k++) rgba[4 * di + k] = cnt[si] ? full[4 * si + k] : 0;
-    }
+  gprt_ctx* ctx = j->scene->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  // resolved on the device: only the tile's bytes cross to the host
+  size_t bytes = (size_t)(x1 - x0) * (y1 - y0) * 4;
+  std::vector<void*> tmp;
+  uint8_t* d = nullptr;
+  if (dev_alloc(ctx, tmp, &d, bytes)) return GPRT_E_OOM;
+  launch_resolve_tile(j->film, x0, y0, x1, y1, d, j->stream);
+  j->launches++;
+  cudaError_t e = cudaMemcpyAsync(rgba, d, bytes, cudaMemcpyDeviceToHost, j->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->stream);
+  free_all(tmp);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tile read-back");
   return GPRT_OK;
 }
 

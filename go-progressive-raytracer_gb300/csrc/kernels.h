@@ -116,6 +116,8 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
 // film
 void launch_apply_splats(const DevFilm& film, cudaStream_t st);
 void launch_resolve_rgba8(const DevFilm& film, uint8_t* out, cudaStream_t st);
+void launch_resolve_tile(const DevFilm& film, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint8_t* out,
+                         cudaStream_t st);
 void launch_image_mean(const DevFilm& film, float* out, cudaStream_t st);
 void launch_active_pixels(const DevFilm& film, uint32_t target, uint32_t min_samples, float threshold,
                           uint32_t* list, uint32_t* count, cudaStream_t st);

@@ -51,6 +51,31 @@ void launch_resolve_rgba8(const DevFilm& film, uint8_t* out, cudaStream_t st) {
   k_resolve_rgba8<<<launch_grid(n, 256, 0), 256, 0, st>>>(film, reinterpret_cast<uchar4*>(out));
 }
 
+// extractTileImage (progressive.go:225-255): the tile's pixels resolved on
+// the device, pixels without samples left at zero (alpha included)
+__global__ void k_resolve_tile(DevFilm film, uint32_t x0, uint32_t y0, uint32_t tw, uint32_t th, uchar4* out) {
+  uint32_t n = tw * th;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    uint32_t tx = k % tw, ty = k / tw;
+    uint32_t i = (y0 + ty) * (uint32_t)film.width + (x0 + tx);
+    if (film.count[i] == 0) {
+      out[k] = make_uchar4(0, 0, 0, 0);
+      continue;
+    }
+    float3 c = pixel_color(film, i);
+    float r = fminf(1.f, fmaxf(0.f, sqrtf(c.x)));
+    float g = fminf(1.f, fmaxf(0.f, sqrtf(c.y)));
+    float b = fminf(1.f, fmaxf(0.f, sqrtf(c.z)));
+    out[k] = make_uchar4((unsigned char)(255.f * r), (unsigned char)(255.f * g), (unsigned char)(255.f * b), 255);
+  }
+}
+
+void launch_resolve_tile(const DevFilm& film, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint8_t* out,
+                         cudaStream_t st) {
+  uint32_t tw = x1 - x0, th = y1 - y0;
+  k_resolve_tile<<<launch_grid(tw * th, 256, 0), 256, 0, st>>>(film, x0, y0, tw, th, reinterpret_cast<uchar4*>(out));
+}
+
 __global__ void k_image_mean(DevFilm film, float* out) {
   uint32_t n = (uint32_t)film.width * film.height;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
