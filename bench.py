@@ -212,6 +212,33 @@ def cpu_baseline(jobs, seconds=15.0):
                       % (threads, n, s, desc)}
 
 
+def cpu_per_config(seconds=5.0):
+    """The oracle on each of the other workloads, about `seconds` of whole
+    64x64 tiles each (scene builds excluded): the CPU figure beside each
+    per-config GPU number."""
+    from gprt import scenes
+    from oracle import client
+    threads = os.cpu_count()
+    out = {}
+    for name, scene, spp, integ in (("cornell_400_64spp_pt", scenes.cornell_baseline(400), 64, 0),
+                                    ("cornell_spheres_400_64spp_pt", scenes.cornell_scene(), 64, 0),
+                                    ("icosphere_1024_16spp_pt", scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH),
+                                     16, 0),
+                                    ("cornell_boxes_512_64spp_bdpt", scenes.cornell_boxes_bdpt(512), 64, 1)):
+        sc = client.OracleScene(scene.to_desc())
+        r = client.OracleRenderer(sc, integ, max_spp=spp, max_passes=1, seed=11, threads=threads)
+        secs, st = r.render_pass(1, only_tiles=threads)
+        r.close()
+        ntiles = ((sc.width + 63) // 64) * ((sc.height + 63) // 64)
+        want = int(min(ntiles, max(threads, threads * seconds / max(secs, 1e-3))))
+        r = client.OracleRenderer(sc, integ, max_spp=spp, max_passes=1, seed=12, threads=threads)
+        secs, st = r.render_pass(1, only_tiles=want)
+        r.close()
+        sc.close()
+        out[name] = {"msamples_per_s": st[1] / secs / 1e6, "tiles": want, "seconds": secs}
+    return {"cores": threads, "kind": "port", "configs": out}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -586,6 +613,7 @@ def run_gprt(args):
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(jobs)
+            cpu["per_config"] = cpu_per_config()
         except Exception as e:  # the baseline never blocks the GPU line
             cpu = {"value": None, "error": str(e)}
 
