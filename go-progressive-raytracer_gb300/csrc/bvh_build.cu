@@ -47,7 +47,7 @@ __global__ void k_keys(uint32_t n, const float4* box, float3 clo, float3 cinv, u
                        uint32_t* idx) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     float4 lo = box[2 * k], hi = box[2 * k + 1];
-    uint32_t type = __float_as_uint(lo.w);
+    uint32_t type = __float_as_uint(lo.w) & 3u;
     float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
     float o[3] = {clo.x, clo.y, clo.z}, s[3] = {cinv.x, cinv.y, cinv.z};
     uint64_t m = 0;
@@ -142,7 +142,7 @@ struct TreeView {
   const uint32_t* idx;
   const uint32_t *left, *right, *first, *last;
   const float4* ibox;
-  uint32_t off[3];  // first sorted position of each primitive type
+  uint32_t off[4];  // first sorted position of each primitive type
 };
 
 __device__ __forceinline__ void range_of(const TreeView& T, uint32_t c, uint32_t& f, uint32_t& l) {
@@ -159,7 +159,7 @@ __device__ __forceinline__ bool leafable(const TreeView& T, uint32_t c) {
   uint32_t f = T.first[c], l = T.last[c];
   uint32_t tf = (uint32_t)(T.K[f] >> 62), tl = (uint32_t)(T.K[l] >> 62);
   if (tf != tl) return false;
-  return l - f + 1 <= (tf == (uint32_t)kPrimQuad ? 2u : 4u);
+  return l - f + 1 <= (tf == (uint32_t)kPrimQuad || tf == (uint32_t)kPrimQuadric ? 2u : 4u);
 }
 
 __device__ __forceinline__ float area(const Box3& b) {
@@ -228,11 +228,12 @@ __global__ void k_collapse(TreeView T, const uint2* qin, const uint32_t* qin_n, 
 
 // The primitive arrays in sorted (leaf) order, precomputed as the host
 // emitter does (NewQuad, quad.go:109-130; computeNormal, triangle.go:92-99).
-__global__ void k_gather(uint32_t n, const float4* box, const double* geo, const uint32_t* idx, uint3 off,
-                         float4* tris, float4* tri_normals, float4* quads, float4* spheres, uint32_t* final_index) {
+__global__ void k_gather(uint32_t n, const float4* box, const double* geo, const uint32_t* idx, uint4 off,
+                         float4* tris, float4* tri_normals, float4* quads, float4* spheres, float4* quadrics,
+                         uint32_t* final_index) {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     uint32_t k = idx[j];
-    uint32_t type = __float_as_uint(box[2 * k].w);
+    uint32_t tw = __float_as_uint(box[2 * k].w), type = tw & 3u;
     float mat = box[2 * k + 1].w;  // material index as int bits
     const double* g = geo + (size_t)9 * k;
     double ax = g[0], ay = g[1], az = g[2], bx = g[3], by = g[4], bz = g[5], cx = g[6], cy = g[7], cz = g[8];
@@ -260,10 +261,35 @@ __global__ void k_gather(uint32_t n, const float4* box, const double* geo, const
       Q[2] = make_float4((float)cx, (float)cy, (float)cz, 0.f);
       Q[3] = make_float4((float)nx, (float)ny, (float)nz, 0.f);
       Q[4] = make_float4((float)(nx * w), (float)(ny * w), (float)(nz * w), 0.f);
-    } else {
+    } else if (type == (uint32_t)kPrimSphere) {
       local = j - off.z;
       spheres[(size_t)local * 2] = make_float4((float)ax, (float)ay, (float)az, (float)bx);
       spheres[(size_t)local * 2 + 1] = make_float4(mat, 0.f, 0.f, 0.f);
+    } else {
+      // disc / cylinder / cone record (layout.h), as the host's quadric_record
+      local = j - off.w;
+      int kind = (int)(tw >> 4);
+      float4* R = quadrics + (size_t)local * 5;
+      float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      R[2] = R[3] = z;
+      R[4] = make_float4(__int_as_float(kind), mat, kind == kQuadricDisc ? 0.f : (float)cz, 0.f);
+      if (kind == kQuadricDisc) {
+        double inv = 1.0 / sqrt(bx * bx + by * by + bz * bz);
+        R[0] = make_float4((float)ax, (float)ay, (float)az, (float)cx);
+        R[1] = make_float4((float)(bx * inv), (float)(by * inv), (float)(bz * inv), 0.f);
+      } else {
+        double vx = bx - ax, vy = by - ay, vz = bz - az;
+        double hgt = sqrt(vx * vx + vy * vy + vz * vz), inv = 1.0 / hgt;
+        double ux = vx * inv, uy = vy * inv, uz = vz * inv;
+        double r0 = cx, r1 = kind == kQuadricCylinder ? cx : cy;
+        R[0] = make_float4((float)ax, (float)ay, (float)az, (float)r0);
+        R[1] = make_float4((float)ux, (float)uy, (float)uz, (float)hgt);
+        R[2] = make_float4((float)bx, (float)by, (float)bz, (float)r1);
+        if (kind == kQuadricCone) {
+          double s = r1 == 0 ? 0.0 : r1 * hgt / (r0 - r1), ta = (r0 - r1) / hgt;
+          R[3] = make_float4((float)(bx + ux * s), (float)(by + uy * s), (float)(bz + uz * s), (float)(ta * ta));
+        }
+      }
     }
     final_index[k] = local;
   }
@@ -341,7 +367,8 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   k_radix_tree<<<grid, 256, 0, st>>>((int)n, keys2, left, right, first, last, pint, pleaf);
   k_bounds<<<grid, 256, 0, st>>>((int)n, box, idx2, left, right, pint, pleaf, ibox, visits);
   // 5. collapse, level by level from the root (n >= 8: the root is not a leaf)
-  TreeView T{keys2, box, idx2, left, right, first, last, ibox, {0, h.n_tris, h.n_tris + h.n_quads}};
+  TreeView T{keys2, box, idx2, left, right, first, last, ibox,
+             {0, h.n_tris, h.n_tris + h.n_quads, h.n_tris + h.n_quads + h.n_spheres}};
   uint2 root = make_uint2(0, 0);
   uint32_t one[3] = {1, 0, 1};  // one queued item; the root occupies BVH4 node 0
   CK(ctx, cudaMemcpyAsync(qa, &root, sizeof(root), cudaMemcpyHostToDevice, st));
@@ -367,17 +394,19 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   CK(ctx, cudaStreamSynchronize(st));
   if (e) return cleanup(fail(ctx, GPRT_E_BOUND, "device BVH build exceeded its node capacity"));
   // 6. primitive arrays in leaf order, and the node array at its final size
-  float4 *nodes = nullptr, *tris = nullptr, *normals = nullptr, *quads = nullptr, *spheres = nullptr;
+  float4 *nodes = nullptr, *tris = nullptr, *normals = nullptr, *quads = nullptr, *spheres = nullptr,
+         *quadrics = nullptr;
   rc = 0;
   rc |= dev_alloc(ctx, bufs, &nodes, (size_t)n4 * 8, bytes);
   rc |= dev_alloc(ctx, bufs, &tris, (size_t)h.n_tris * 3, bytes);
   rc |= dev_alloc(ctx, bufs, &normals, (size_t)h.n_tris, bytes);
   rc |= dev_alloc(ctx, bufs, &quads, (size_t)h.n_quads * 5, bytes);
   rc |= dev_alloc(ctx, bufs, &spheres, (size_t)h.n_spheres * 2, bytes);
+  rc |= dev_alloc(ctx, bufs, &quadrics, (size_t)h.n_quadrics * 5, bytes);
   if (rc) return cleanup(GPRT_E_OOM);
   CK(ctx, cudaMemcpyAsync(nodes, nodes_tmp, (size_t)n4 * 128, cudaMemcpyDeviceToDevice, st));
-  uint3 off = make_uint3(0, h.n_tris, h.n_tris + h.n_quads);
-  k_gather<<<grid, 256, 0, st>>>(n, box, geo, idx2, off, tris, normals, quads, spheres, final_index);
+  uint4 off = make_uint4(0, h.n_tris, h.n_tris + h.n_quads, h.n_tris + h.n_quads + h.n_spheres);
+  k_gather<<<grid, 256, 0, st>>>(n, box, geo, idx2, off, tris, normals, quads, spheres, quadrics, final_index);
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cleanup(cuda_fail(ctx, le, "device BVH build launch"));
   // host copies (layout checks, traversal counts) and the primitive maps
@@ -387,6 +416,7 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   h.tri_normals.resize(h.n_tris);
   h.quads.resize((size_t)h.n_quads * 5);
   h.spheres.resize((size_t)h.n_spheres * 2);
+  h.quadrics.resize((size_t)h.n_quadrics * 5);
   CK(ctx, cudaMemcpyAsync(fi.data(), final_index, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaMemcpyAsync(h.nodes.data(), nodes, h.nodes.size() * 16, cudaMemcpyDeviceToHost, st));
   if (h.n_tris) {
@@ -396,14 +426,17 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   if (h.n_quads) CK(ctx, cudaMemcpyAsync(h.quads.data(), quads, h.quads.size() * 16, cudaMemcpyDeviceToHost, st));
   if (h.n_spheres)
     CK(ctx, cudaMemcpyAsync(h.spheres.data(), spheres, h.spheres.size() * 16, cudaMemcpyDeviceToHost, st));
+  if (h.n_quadrics)
+    CK(ctx, cudaMemcpyAsync(h.quadrics.data(), quadrics, h.quadrics.size() * 16, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaStreamSynchronize(st));
   free_all(tmp);
   h.prim_shape.assign(n, 0);
   h.prim_sub.assign(n, 0);
-  uint32_t base[3] = {0, h.n_tris, h.n_tris + h.n_quads};
+  uint32_t base[4] = {0, h.n_tris, h.n_tris + h.n_quads, h.n_tris + h.n_quads + h.n_spheres};
   for (uint32_t k = 0; k < n; k++) {
     uint32_t type = 0;
     std::memcpy(&type, &bp.box[2 * k].w, 4);
+    type &= 3u;
     uint32_t gid = base[type] + fi[k];
     h.prim_shape[gid] = bp.shape[k];
     h.prim_sub[gid] = bp.sub[k];
@@ -416,6 +449,7 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   d.tri_normals = normals;
   d.quads = quads;
   d.spheres = spheres;
+  d.quadrics = quadrics;
   h.pending = BuildPrims{};
   h.bvh_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   h.build_ms += h.bvh_ms;

@@ -289,6 +289,7 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
     rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
     rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
     rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
+    rc |= upload(ctx, s->buffers, h.quadrics, &d.quadrics, &s->bytes);
   }
   rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
   rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
@@ -306,7 +307,8 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   d.n_lights = (int)h.lights.size();
   d.quad_base = h.n_tris;
   d.sphere_base = h.n_tris + h.n_quads;
-  d.n_prims = h.n_tris + h.n_quads + h.n_spheres;
+  d.quadric_base = h.n_tris + h.n_quads + h.n_spheres;
+  d.n_prims = h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
   d.has_infinite = h.has_infinite;
   d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
   d.world_radius = (float)h.world_radius;
@@ -346,7 +348,8 @@ int gprt_scene_get_info(const gprt_scene* s, gprt_scene_info* info) {
   info->n_triangles = h.n_tris;
   info->n_quads = h.n_quads;
   info->n_spheres = h.n_spheres;
-  info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres;
+  info->n_quadrics = h.n_quadrics;
+  info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
   info->n_nodes = h.nodes.size() / 8;
   info->device_bytes = s->bytes;
   info->image_width = h.sampling.width;
@@ -375,7 +378,8 @@ int gprt_scene_validate(const gprt_scene_desc* desc, gprt_scene_info* info, char
     info->n_triangles = h.n_tris;
     info->n_quads = h.n_quads;
     info->n_spheres = h.n_spheres;
-    info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres;
+    info->n_quadrics = h.n_quadrics;
+    info->n_primitives = (uint64_t)h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
     info->n_nodes = h.nodes.size() / 8;
     info->image_width = h.sampling.width;
     info->image_height = h.sampling.height;

@@ -248,6 +248,154 @@ __device__ __forceinline__ bool hit_sphere(float3 o, float3 d, float4 s, float t
   return true;
 }
 
+// Disc (disc.go:49-92) and the circular caps of cylinders and cones
+// (cylinder.go:224-266, cone.go:306-350): plane hit, |n.d| < eps rejected,
+// inside when |p - c|^2 <= r^2.
+__device__ __forceinline__ bool hit_cap_plane(float3 o, float3 d, float3 c, float3 n, float r, float eps, float tmin,
+                                              float tmax, float& t) {
+  float den = dot_rn(d, n);
+  if (fabsf(den) < eps) return false;
+  float tt = __fdiv_rn(dot_rn(sub_rn(c, o), n), den);
+  if (tt < tmin || tt > tmax) return false;
+  float3 p = make_float3(__fmaf_rn(d.x, tt, o.x), __fmaf_rn(d.y, tt, o.y), __fmaf_rn(d.z, tt, o.z));
+  float3 cp = sub_rn(p, c);
+  if (dot_rn(cp, cp) > __fmul_rn(r, r)) return false;
+  t = tt;
+  return true;
+}
+
+__device__ __forceinline__ float axial_height(float3 o, float3 d, float t, float3 base, float3 axis) {
+  float3 p = make_float3(__fmaf_rn(d.x, t, o.x), __fmaf_rn(d.y, t, o.y), __fmaf_rn(d.z, t, o.z));
+  return dot_rn(sub_rn(p, base), axis);
+}
+
+// Cylinder, cone and disc (cylinder.go:97-221, cone.go:128-303, disc.go:49).
+// The quadratics are solved in the plane normal to the axis (cylinder) or
+// with the half-b form and q = -(b' + sign(b') sqrt(D)) (cone), which keep
+// FP32 roots accurate when the ray starts far away; the candidate order and
+// the height / nappe checks are the reference's.  `part` tells the surface
+// code which piece was hit: 0 body (or disc), 1 base cap, 2 top cap.
+__device__ __forceinline__ bool hit_quadric(float3 o, float3 d, const float4* Q, float tmin, float tmax, float& t,
+                                            float& part) {
+  float4 g0 = __ldg(Q), g1 = __ldg(Q + 1), g4 = __ldg(Q + 4);
+  int kind = __float_as_int(g4.x);
+  float3 p0 = f3(g0), axis = f3(g1);
+  if (kind == kQuadricDisc) {
+    if (!hit_cap_plane(o, d, p0, axis, g0.w, 1e-6f, tmin, tmax, t)) return false;
+    part = 0.f;
+    return true;
+  }
+  float4 g2 = __ldg(Q + 2);
+  float height = g1.w, best = tmax;
+  bool any = false;
+  if (kind == kQuadricCylinder) {
+    float3 delta = sub_rn(o, p0);
+    float DV = dot_rn(d, axis), dV = dot_rn(delta, axis);
+    float3 dp = make_float3(__fmaf_rn(-axis.x, DV, d.x), __fmaf_rn(-axis.y, DV, d.y), __fmaf_rn(-axis.z, DV, d.z));
+    float3 Dp = make_float3(__fmaf_rn(-axis.x, dV, delta.x), __fmaf_rn(-axis.y, dV, delta.y),
+                            __fmaf_rn(-axis.z, dV, delta.z));
+    float A = dot_rn(dp, dp);
+    if (A >= 1e-8f) {
+      float hb = dot_rn(Dp, dp);
+      float k = __fdiv_rn(hb, A);
+      float3 l = make_float3(__fmaf_rn(-dp.x, k, Dp.x), __fmaf_rn(-dp.y, k, Dp.y), __fmaf_rn(-dp.z, k, Dp.z));
+      float r2 = __fmul_rn(g0.w, g0.w);
+      float disc = __fmul_rn(A, __fsub_rn(r2, dot_rn(l, l)));
+      if (disc >= 0.f) {
+        float sq = __fsqrt_rn(disc);
+        float q = __fsub_rn(-hb, copysignf(sq, hb));
+        float C = __fsub_rn(dot_rn(Dp, Dp), r2);
+        float t1, t2;
+        if (q == 0.f) {
+          t1 = t2 = __fdiv_rn(-hb, A);
+        } else {
+          float ra = __fdiv_rn(C, q), rb = __fdiv_rn(q, A);
+          t1 = fminf(ra, rb);
+          t2 = fmaxf(ra, rb);
+        }
+        float tc = t1;
+        bool ok = true;
+        if (tc < tmin || tc > best) {
+          tc = t2;
+          if (tc < tmin || tc > best) ok = false;
+        }
+        if (ok) {
+          float h = axial_height(o, d, tc, p0, axis);
+          if (h < 0.f || h > height) {
+            ok = false;
+            if (tc == t1) {
+              tc = t2;
+              if (!(tc < tmin || tc > best)) {
+                h = axial_height(o, d, tc, p0, axis);
+                ok = !(h < 0.f || h > height);
+              }
+            }
+          }
+        }
+        if (ok) {
+          best = tc;
+          part = 0.f;
+          any = true;
+        }
+      }
+    }
+  } else {
+    float4 g3 = __ldg(Q + 3);
+    float3 apex = f3(g3);
+    float kk = __fadd_rn(1.f, g3.w);  // 1 + tan^2
+    float3 CO = sub_rn(o, apex);
+    float DV = dot_rn(d, axis), COV = dot_rn(CO, axis);
+    float A = __fsub_rn(dot_rn(d, d), __fmul_rn(kk, __fmul_rn(DV, DV)));
+    if (fabsf(A) >= 1e-8f) {
+      float hb = __fsub_rn(dot_rn(d, CO), __fmul_rn(kk, __fmul_rn(DV, COV)));
+      float C = __fsub_rn(dot_rn(CO, CO), __fmul_rn(kk, __fmul_rn(COV, COV)));
+      float disc = __fmaf_rn(hb, hb, -__fmul_rn(A, C));
+      if (disc >= 0.f) {
+        float sq = __fsqrt_rn(disc);
+        float q = __fsub_rn(-hb, copysignf(sq, hb));
+        float ra, rb;
+        if (q == 0.f) {
+          ra = rb = __fdiv_rn(-hb, A);
+        } else {
+          ra = __fdiv_rn(C, q);
+          rb = __fdiv_rn(q, A);
+        }
+        // the reference tries (-b - sqrt D) / 2a first: the smaller root when
+        // a > 0, the larger when a < 0
+        float first = A > 0.f ? fminf(ra, rb) : fmaxf(ra, rb);
+        float second = A > 0.f ? fmaxf(ra, rb) : fminf(ra, rb);
+        for (int pass = 0; pass < 2 && !any; pass++) {
+          float tc = pass == 0 ? first : second;
+          if (tc < tmin || tc > best) continue;
+          float3 p = make_float3(__fmaf_rn(d.x, tc, o.x), __fmaf_rn(d.y, tc, o.y), __fmaf_rn(d.z, tc, o.z));
+          float h = dot_rn(sub_rn(p, p0), axis);
+          if (h < -1e-8f || h > height + 1e-8f) continue;
+          if (dot_rn(sub_rn(p, apex), axis) > 1e-8f) continue;
+          best = tc;
+          part = 0.f;
+          any = true;
+        }
+      }
+    }
+  }
+  if (g4.z != 0.f) {  // caps: base (-axis), top (+axis) when it has a radius
+    float tc;
+    float3 na = make_float3(-axis.x, -axis.y, -axis.z);
+    if (hit_cap_plane(o, d, p0, na, g0.w, 1e-8f, tmin, best, tc)) {
+      best = tc;
+      part = 1.f;
+      any = true;
+    }
+    if (g2.w > 0.f && hit_cap_plane(o, d, f3(g2), axis, g2.w, 1e-8f, tmin, best, tc)) {
+      best = tc;
+      part = 2.f;
+      any = true;
+    }
+  }
+  if (any) t = best;
+  return any;
+}
+
 // ----------------------------------------------------------------- BVH traversal
 // Replaces geometry.BVH.Hit / hitNode (pkg/geometry/bvh.go:183-239).  The
 // tree is this library's own 4-wide SAH BVH (layout.h) instead of the
@@ -332,7 +480,11 @@ __device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* sta
     int type = (meta >> kLeafTypeShift) & 3;
     for (int k = 0; k < cnt; k++) {
       int p = ref + k;
-      uint32_t gid = (type == kPrimTriangle ? 0u : type == kPrimQuad ? sc.quad_base : sc.sphere_base) + (uint32_t)p;
+      uint32_t gid = (type == kPrimTriangle ? 0u
+                      : type == kPrimQuad   ? sc.quad_base
+                      : type == kPrimSphere ? sc.sphere_base
+                                            : sc.quadric_base) +
+                     (uint32_t)p;
       float t, u = 0.f, v = 0.f;
       bool h;
       if (kCount) st->prims++;
@@ -345,10 +497,21 @@ __device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* sta
         const float4* Q = sc.quads + (size_t)p * 5;
         float4 qq[5] = {__ldg(Q), __ldg(Q + 1), __ldg(Q + 2), __ldg(Q + 3), __ldg(Q + 4)};
         h = hit_quad(s.o, s.d, qq, s.tmin, s.best, t, u, v);
-      } else {
+      } else if (type == kPrimSphere) {
         float4 S = __ldg(sc.spheres + (size_t)p * 2);
         float lo = gid == s.skip ? fmaxf(s.tmin, 2e-4f * fabsf(S.w)) : s.tmin;
         h = hit_sphere(s.o, s.d, S, lo, s.best, t);
+      } else {
+        // a ray leaving a quadric may hit it again (the other side of a
+        // cylinder); hits closer than 2e-4 x radius are its own surface
+        const float4* Q = sc.quadrics + (size_t)p * 5;
+        float lo = s.tmin;
+        if (gid == s.skip) {
+          float4 g0 = __ldg(Q);
+          if (__float_as_int(__ldg(Q + 4).x) == kQuadricDisc) continue;  // planar
+          lo = fmaxf(s.tmin, 2e-4f * g0.w);
+        }
+        h = hit_quadric(s.o, s.d, Q, lo, s.best, t, u);
       }
       if (h) {
         s.best = t;
@@ -498,11 +661,30 @@ __device__ __forceinline__ void surface_at(const DevScene& sc, float3 o, float3 
     const float4* Q = sc.quads + (size_t)(p - sc.quad_base) * 5;
     outward = f3(__ldg(Q + 3));
     s.mat = __float_as_int(__ldg(Q + 1).w);
-  } else {
+  } else if (p < sc.quadric_base) {
     const float4* S = sc.spheres + (size_t)(p - sc.sphere_base) * 2;
     float4 c = __ldg(S);
     outward = (s.p - f3(c)) * (1.0f / c.w);  // (p - c) / r (sphere.go:62)
     s.mat = __float_as_int(__ldg(S + 1).x);
+  } else {
+    const float4* Q = sc.quadrics + (size_t)(p - sc.quadric_base) * 5;
+    float4 g0 = __ldg(Q), g1 = __ldg(Q + 1), g4 = __ldg(Q + 4);
+    float3 axis = f3(g1);
+    int kind = __float_as_int(g4.x);
+    s.mat = __float_as_int(g4.y);
+    if (kind == kQuadricDisc || h.u == 2.f) {
+      outward = axis;  // disc normal, top cap
+    } else if (h.u == 1.f) {
+      outward = -axis;  // base cap
+    } else {
+      // body: radial from the axis (cylinder.go:188-191), tilted by the
+      // cone's slope (cone.go:240-248)
+      float3 base = f3(g0);
+      float hh = dot(s.p - base, axis);
+      float3 radial = s.p - (base + axis * hh);
+      if (kind == kQuadricCone) radial = radial + axis * ((g0.w - __ldg(Q + 2).w) / g1.w);
+      outward = normalize(radial);
+    }
   }
   s.front = dot(d, outward) < 0.f;
   s.n = s.front ? outward : -outward;

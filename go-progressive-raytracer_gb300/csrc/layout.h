@@ -11,8 +11,14 @@
 //   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64
 //   quads      5 x float4 (80 B): (corner, D) (u, material) (v, -) (normal, -) (W, -)
 //   spheres    2 x float4 (32 B): (center, radius) (material, -, -, -)
+//   quadrics   5 x float4 (80 B): discs, cylinders and cones
+//              (p0, r0) (axis, height) (p1, r1) (apex, tan^2) (kind, material, capped, -)
+//              disc: p0 = centre, axis = unit normal, r0 = radius;
+//              cylinder: p0 = base, p1 = top, r0 = r1 = radius;
+//              cone: p0 = base (radius r0), p1 = top (radius r1), apex of the extended cone
 // Primitive ids: triangles [0, quad_base), quads [quad_base, sphere_base),
-// spheres [sphere_base, n_prims); each type array is in BVH leaf order.
+// spheres [sphere_base, quadric_base), quadrics [quadric_base, n_prims); each
+// type array is in BVH leaf order.
 #pragma once
 
 #include <cstdint>
@@ -25,7 +31,8 @@ constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 constexpr int kEmptyChild = -1;
 constexpr int kLeafCountMask = 0xFF;
 constexpr int kLeafTypeShift = 8;
-constexpr int kPrimTriangle = 0, kPrimQuad = 1, kPrimSphere = 2;
+constexpr int kPrimTriangle = 0, kPrimQuad = 1, kPrimSphere = 2, kPrimQuadric = 3;
+constexpr int kQuadricDisc = 0, kQuadricCylinder = 1, kQuadricCone = 2;
 constexpr int kTraceStack = 64;
 
 // device error bits (status word read by the host after each pass)
@@ -67,12 +74,13 @@ struct DevScene {
   const float4* tri_normals;
   const float4* quads;
   const float4* spheres;
+  const float4* quadrics;
   const DevMaterial* materials;
   const DevLight* lights;
   int n_nodes;
   int root;  // BVH root node of the scene (-1: empty)
   int n_lights;
-  uint32_t quad_base, sphere_base, n_prims;
+  uint32_t quad_base, sphere_base, quadric_base, n_prims;
   int has_infinite;
   float3 world_center;
   float world_radius;

@@ -129,8 +129,55 @@ float i2f(uint32_t i) {
 struct Prim {
   int type;
   uint32_t shape, sub, material;
-  D3 a, b, c;  // tri: v0,v1,v2 ; quad: corner,u,v ; sphere: center,(r,_,_)
+  D3 a, b, c;  // tri: v0,v1,v2 ; quad: corner,u,v ; sphere: center,(r,_,_) ;
+               // quadric: disc centre,normal,(r,_,_) / cylinder base,top,(r,_,capped) /
+               // cone base,top,(r0,r1,capped)
+  int qkind;   // kQuadric* of a quadric
 };
+
+// The reference BoundingBox of a disc, cylinder or cone (disc.go:95-118,
+// cylinder.go:42-94, cone.go:79-126): conservative, flat along an axis the
+// cylinder or cone is parallel to.
+DBox quadric_box(const Prim& p) {
+  if (p.qkind == kQuadricDisc) {
+    D3 n = p.b.norm();
+    D3 right = (std::fabs(n.x) > 0.1 ? D3(0, 1, 0) : D3(1, 0, 0)).cross(n).norm();
+    D3 up = n.cross(right).norm();
+    D3 re = right * p.c.x, ue = up * p.c.x;
+    D3 cs[4] = {p.a + re + ue, p.a + re - ue, p.a - re + ue, p.a - re - ue};
+    return box_of(cs, 4);
+  }
+  D3 axis = (p.b - p.a).norm();
+  double r = p.c.x;
+  double e[3];
+  for (int k = 0; k < 3; k++) e[k] = std::fabs(axis.at(k)) > 0.9999 ? 0.0 : r;
+  return DBox{{std::min(p.a.x, p.b.x) - e[0], std::min(p.a.y, p.b.y) - e[1], std::min(p.a.z, p.b.z) - e[2]},
+              {std::max(p.a.x, p.b.x) + e[0], std::max(p.a.y, p.b.y) + e[1], std::max(p.a.z, p.b.z) + e[2]}};
+}
+
+// The device record of a quadric (layout.h), precomputed in float64.
+void quadric_record(const Prim& p, float4 out[5]) {
+  float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  out[0] = out[1] = out[2] = out[3] = z;
+  out[4] = make_float4(i2f((uint32_t)p.qkind), i2f(p.material), p.qkind == kQuadricDisc ? 0.f : (float)p.c.z, 0.f);
+  if (p.qkind == kQuadricDisc) {
+    out[0] = mk4(p.a, (float)p.c.x);
+    out[1] = mk4(p.b.norm(), 0.f);
+    return;
+  }
+  D3 av = p.b - p.a;
+  double height = av.len();
+  D3 axis = av.norm();
+  double r0 = p.c.x, r1 = p.qkind == kQuadricCylinder ? p.c.x : p.c.y;
+  out[0] = mk4(p.a, (float)r0);
+  out[1] = mk4(axis, (float)height);
+  out[2] = mk4(p.b, (float)r1);
+  if (p.qkind == kQuadricCone) {
+    D3 apex = r1 == 0 ? p.b : p.b + axis * (r1 * height / (r0 - r1));
+    double tan_a = (r0 - r1) / height;
+    out[3] = mk4(apex, (float)(tan_a * tan_a));
+  }
+}
 
 // Primitive storage that grows without initialising: the slots of a mesh are
 // filled in parallel, so the pages are first touched by the filling threads.
@@ -181,7 +228,7 @@ struct Builder {
   const PrimArray& prims;
   explicit Builder(std::vector<Ref>& r, const PrimArray& p) : refs(r), prims(p) {}
 
-  static int max_leaf(int type) { return type == kPrimQuad ? 2 : 4; }
+  static int max_leaf(int type) { return type == kPrimQuad || type == kPrimQuadric ? 2 : 4; }
 
   std::unique_ptr<BNode> build(uint32_t b, uint32_t e, int depth) {
     auto n = std::make_unique<BNode>();
@@ -343,12 +390,19 @@ struct Emitter {
         out.quads.push_back(mk4(p.c, 0.f));
         out.quads.push_back(mk4(n, 0.f));
         out.quads.push_back(mk4(w, 0.f));
-      } else {
+      } else if (p.type == kPrimSphere) {
         uint32_t idx = (uint32_t)(out.spheres.size() / 2);
         if (i == 0) first = (int)idx;
         final_index[pid] = idx;
         out.spheres.push_back(mk4(p.a, (float)p.b.x));
         out.spheres.push_back(make_float4(i2f(p.material), 0.f, 0.f, 0.f));
+      } else {
+        uint32_t idx = (uint32_t)(out.quadrics.size() / 5);
+        if (i == 0) first = (int)idx;
+        final_index[pid] = idx;
+        float4 rec[5];
+        quadric_record(p, rec);
+        out.quadrics.insert(out.quadrics.end(), rec, rec + 5);
       }
     }
   }
@@ -523,6 +577,38 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
         add_world(bb);
         break;
       }
+      case GPRT_SHAPE_DISC:
+      case GPRT_SHAPE_CYLINDER:
+      case GPRT_SHAPE_CONE: {
+        if (!check_mat(s.material)) return false;
+        Prim q{kPrimQuadric, i, 0, s.material, D3(p), D3(p + 3), D3(p[6], p[7], p[8]), 0};
+        if (s.kind == GPRT_SHAPE_DISC) {
+          q.qkind = kQuadricDisc;
+          q.c = D3(p[6], 0, 0);
+          if (q.b.len() == 0) {
+            err = "disc normal must be non-zero";
+            return false;
+          }
+        } else if (s.kind == GPRT_SHAPE_CYLINDER) {
+          q.qkind = kQuadricCylinder;
+          q.c = D3(p[6], 0, p[7] != 0 ? 1 : 0);
+          if ((q.b - q.a).len() == 0) {
+            err = "cylinder base and top must differ";
+            return false;
+          }
+        } else {
+          q.qkind = kQuadricCone;
+          q.c = D3(p[6], p[7], p[8] != 0 ? 1 : 0);
+          // NewCone's checks (cone.go:28-50)
+          if (!(p[6] > 0) || p[7] < 0 || p[6] <= p[7] || !((q.b - q.a).len() > 0)) {
+            err = "invalid cone: need base radius > top radius >= 0 and distinct centres";
+            return false;
+          }
+        }
+        prims.push_back(q);
+        add_world(quadric_box(q));
+        break;
+      }
       case GPRT_SHAPE_TRIANGLE: {
         if (!check_mat(s.material)) return false;
         D3 a(p), b(p + 3), c(p + 6);
@@ -611,12 +697,12 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
   float fext = (float)std::min(ext, 1e30);
   // references per type (rank of each primitive within its type, then the
   // boxes on all host cores)
-  std::vector<Ref> refs[3];
+  std::vector<Ref> refs[4];
   std::vector<uint32_t> rank(prims.size());
   {
-    uint32_t cnt[3] = {0, 0, 0};
+    uint32_t cnt[4] = {0, 0, 0, 0};
     for (size_t k = 0; k < prims.size(); k++) rank[k] = cnt[prims[k].type]++;
-    for (int t = 0; t < 3; t++) refs[t].resize(cnt[t]);
+    for (int t = 0; t < 4; t++) refs[t].resize(cnt[t]);
   }
   parallel_for(prims.size(), [&](size_t b0, size_t b1) {
    for (size_t kk = b0; kk < b1; kk++) {
@@ -632,10 +718,15 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     } else if (p.type == kPrimQuad) {
       pts[0] = p.a, pts[1] = p.a + p.b, pts[2] = p.a + p.c, pts[3] = p.a + p.b + p.c;
       np = 4;
-    } else {
+    } else if (p.type == kPrimSphere) {
       double ar = std::fabs(p.b.x);
       pts[0] = p.a - D3(ar, ar, ar);
       pts[1] = p.a + D3(ar, ar, ar);
+      np = 2;
+    } else {
+      DBox qb = quadric_box(p);
+      pts[0] = qb.mn;
+      pts[1] = qb.mx;
       np = 2;
     }
     DBox b = box_of(pts, np);
@@ -649,6 +740,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
   out.n_tris = (uint32_t)refs[kPrimTriangle].size();
   out.n_quads = (uint32_t)refs[kPrimQuad].size();
   out.n_spheres = (uint32_t)refs[kPrimSphere].size();
+  out.n_quadrics = (uint32_t)refs[kPrimQuadric].size();
   std::vector<uint32_t> final_index(prims.size(), 0);
   out.device_bvh = device_bvh && prims.size() >= 8;
   if (out.device_bvh) {
@@ -669,7 +761,8 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
       for (size_t k = b0; k < b1; k++) {
         const Prim& p = prims[k];
         const Ref& r = refs[p.type][rank[k]];
-        bp.box[2 * k] = make_float4(r.lo[0], r.lo[1], r.lo[2], i2f((uint32_t)p.type));
+        uint32_t tw = (uint32_t)p.type | (p.type == kPrimQuadric ? (uint32_t)p.qkind << 4 : 0u);
+        bp.box[2 * k] = make_float4(r.lo[0], r.lo[1], r.lo[2], i2f(tw));
         bp.box[2 * k + 1] = make_float4(r.hi[0], r.hi[1], r.hi[2], i2f(p.material));
         const D3* v[3] = {&p.a, &p.b, &p.c};
         for (int q = 0; q < 3; q++) {
@@ -696,17 +789,18 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
   out.flatten_ms = std::chrono::duration<double, std::milli>(t_flat - t0).count();
   std::vector<Ref> all;
   all.reserve(prims.size());
-  uint32_t off[3];
-  for (int t = 0; t < 3; t++) {
+  uint32_t off[4];
+  for (int t = 0; t < 4; t++) {
     off[t] = (uint32_t)all.size();
     all.insert(all.end(), refs[t].begin(), refs[t].end());
   }
   if (!out.device_bvh) {
     Builder bld(all, prims);
-    std::unique_ptr<BNode> roots[3];
-    for (int t = 0; t < 3; t++)
+    std::unique_ptr<BNode> roots[4];
+    for (int t = 0; t < 4; t++)
       if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
-    std::unique_ptr<BNode> root = join(std::move(roots[0]), join(std::move(roots[1]), std::move(roots[2])));
+    std::unique_ptr<BNode> root =
+        join(std::move(roots[0]), join(std::move(roots[1]), join(std::move(roots[2]), std::move(roots[3]))));
     if (root) {
       Emitter em{out, all, prims, final_index};
       em.emit(root.get(), 0);
@@ -716,7 +810,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     // primitive id maps
     out.prim_shape.assign(prims.size(), 0);
     out.prim_sub.assign(prims.size(), 0);
-    uint32_t base[3] = {0, out.n_tris, out.n_tris + out.n_quads};
+    uint32_t base[4] = {0, out.n_tris, out.n_tris + out.n_quads, out.n_tris + out.n_quads + out.n_spheres};
     for (uint32_t k = 0; k < prims.size(); k++) {
       uint32_t gid = base[prims[k].type] + final_index[k];
       out.prim_shape[gid] = prims[k].shape;
@@ -860,10 +954,10 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
 // the root must be referenced exactly once and every primitive exactly once.
 std::string validate_layout(const HostScene& s) {
   size_t nn = s.nodes.size() / 8;
-  if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres) ? "primitives without a BVH" : "";
-  size_t np[3] = {s.n_tris, s.n_quads, s.n_spheres};
-  std::unique_ptr<std::atomic<uint8_t>[]> pseen[3];
-  for (int t = 0; t < 3; t++) {
+  if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres + s.n_quadrics) ? "primitives without a BVH" : "";
+  size_t np[4] = {s.n_tris, s.n_quads, s.n_spheres, s.n_quadrics};
+  std::unique_ptr<std::atomic<uint8_t>[]> pseen[4];
+  for (int t = 0; t < 4; t++) {
     pseen[t].reset(new std::atomic<uint8_t>[np[t] ? np[t] : 1]);
     for (size_t k = 0; k < np[t]; k++) pseen[t][k].store(0, std::memory_order_relaxed);
   }
@@ -907,7 +1001,7 @@ std::string validate_layout(const HostScene& s) {
           continue;
         }
         int cnt = mt & kLeafCountMask, type = (mt >> kLeafTypeShift) & 3;
-        if (type > kPrimSphere || cnt <= 0 || (mt & ~0x3FF)) return bad("bad leaf meta");
+        if (cnt <= 0 || (mt & ~0x3FF)) return bad("bad leaf meta");
         if (ch < 0 || (size_t)ch + cnt > np[type]) return bad("leaf range out of bounds");
         for (int k = 0; k < cnt; k++) {
           size_t p = (size_t)ch + k;
@@ -924,6 +1018,14 @@ std::string validate_layout(const HostScene& s) {
             float r = std::fabs(S.w), c[3] = {S.x, S.y, S.z};
             for (int a = 0; a < 3; a++)
               if (!inside(c[a] - r, a) || !inside(c[a] + r, a)) return bad("sphere outside its leaf box");
+          } else if (type == kPrimQuadric) {
+            const float4* Q = &s.quadrics[p * 5];
+            int kind;
+            std::memcpy(&kind, &Q[4].x, 4);
+            if (kind < kQuadricDisc || kind > kQuadricCone) return bad("bad quadric kind");
+            float c[3] = {Q[0].x, Q[0].y, Q[0].z};
+            for (int a = 0; a < 3; a++)
+              if (!inside(c[a], a)) return bad("quadric outside its leaf box");
           } else {
             const float4* Q = &s.quads[p * 5];
             float c[3] = {Q[0].x, Q[0].y, Q[0].z}, u[3] = {Q[1].x, Q[1].y, Q[1].z}, v[3] = {Q[2].x, Q[2].y, Q[2].z};
@@ -944,7 +1046,7 @@ std::string validate_layout(const HostScene& s) {
     if (c == 0) return "unreachable node";
     if (c > 1) return "node referenced twice";
   }
-  for (int t = 0; t < 3; t++)
+  for (int t = 0; t < 4; t++)
     for (size_t k = 0; k < np[t]; k++) {
       uint8_t c = pseen[t][k].load(std::memory_order_relaxed);
       if (c == 0) return "primitive missing from the BVH";
@@ -954,6 +1056,72 @@ std::string validate_layout(const HostScene& s) {
 }
 
 // ---------------------------------------------------------------- CPU walk
+namespace {
+// Closest hit distance of a quadric record in float64 (counts only), -1 when
+// missed: body, then the caps, as the device routine.
+double quadric_t(const float4* Q, const float o3[3], const float d3[3], double tmin, double tmax) {
+  D3 o(o3[0], o3[1], o3[2]), d(d3[0], d3[1], d3[2]);
+  D3 p0(Q[0].x, Q[0].y, Q[0].z), axis(Q[1].x, Q[1].y, Q[1].z), p1(Q[2].x, Q[2].y, Q[2].z), apex(Q[3].x, Q[3].y, Q[3].z);
+  int kind;
+  std::memcpy(&kind, &Q[4].x, 4);
+  double r0 = Q[0].w, r1 = Q[2].w, height = Q[1].w, best = tmax;
+  bool any = false;
+  auto cap = [&](const D3& c, const D3& nrm, double r, double eps) {
+    double den = d.dot(nrm);
+    if (std::fabs(den) < eps) return;
+    double t = (c - o).dot(nrm) / den;
+    if (t < tmin || t > best) return;
+    D3 cp = o + d * t - c;
+    if (cp.dot(cp) > r * r) return;
+    best = t;
+    any = true;
+  };
+  if (kind == kQuadricDisc) {
+    cap(p0, axis, r0, 1e-6);
+    return any ? best : -1;
+  }
+  auto height_ok = [&](double t, double eps) {
+    double h = (o + d * t - p0).dot(axis);
+    return h >= -eps && h <= height + eps;
+  };
+  if (kind == kQuadricCylinder) {
+    D3 delta = o - p0;
+    double DV = d.dot(axis), dV = delta.dot(axis);
+    double a = d.dot(d) - DV * DV, b = 2 * (delta.dot(d) - dV * DV), c = delta.dot(delta) - dV * dV - r0 * r0;
+    double disc = b * b - 4 * a * c;
+    if (std::fabs(a) >= 1e-8 && disc >= 0) {
+      double t1 = (-b - std::sqrt(disc)) / (2 * a), t2 = (-b + std::sqrt(disc)) / (2 * a);
+      for (double t : {t1, t2})
+        if (t >= tmin && t <= best && height_ok(t, 0)) {
+          best = t;
+          any = true;
+          break;
+        }
+    }
+  } else {
+    D3 CO = o - apex;
+    double k = 1.0 + Q[3].w;
+    double DV = d.dot(axis), COV = CO.dot(axis);
+    double a = d.dot(d) - k * DV * DV, b = 2 * (d.dot(CO) - k * DV * COV), c = CO.dot(CO) - k * COV * COV;
+    double disc = b * b - 4 * a * c;
+    if (std::fabs(a) >= 1e-8 && disc >= 0) {
+      double ts[2] = {(-b - std::sqrt(disc)) / (2 * a), (-b + std::sqrt(disc)) / (2 * a)};
+      for (double t : ts)
+        if (t >= tmin && t <= best && height_ok(t, 1e-8) && (o + d * t - apex).dot(axis) <= 1e-8) {
+          best = t;
+          any = true;
+          break;
+        }
+    }
+  }
+  if (Q[4].z != 0.f) {
+    cap(p0, axis * -1.0, r0, 1e-8);
+    if (r1 > 0) cap(p1, axis, r1, 1e-8);
+  }
+  return any ? best : -1;
+}
+}  // namespace
+
 void count_traversal(const HostScene& s, const gprt_ray* rays, uint32_t n, bool any_hit, uint64_t& nodes,
                      uint64_t& boxes, uint64_t& prims) {
   nodes = boxes = prims = 0;
@@ -1040,7 +1208,7 @@ void count_traversal(const HostScene& s, const gprt_ray* rays, uint32_t n, bool 
             double uh[3] = {U[1] * hp[2] - U[2] * hp[1], U[2] * hp[0] - U[0] * hp[2], U[0] * hp[1] - U[1] * hp[0]};
             double al = W[0] * hv[0] + W[1] * hv[1] + W[2] * hv[2], be = W[0] * uh[0] + W[1] * uh[1] + W[2] * uh[2];
             if (al < 0 || al > 1 || be < 0 || be > 1) continue;
-          } else {
+          } else if (type == kPrimSphere) {
             const float4& S = s.spheres[(size_t)p * 2];
             double f[3] = {o[0] - S.x, o[1] - S.y, o[2] - S.z};
             double a = (double)d[0] * d[0] + (double)d[1] * d[1] + (double)d[2] * d[2];
@@ -1050,6 +1218,8 @@ void count_traversal(const HostScene& s, const gprt_ray* rays, uint32_t n, bool 
             if (disc < 0) continue;
             t = (-hb - std::sqrt(disc)) / a;
             if (t < ray.tmin || t > best) t = (-hb + std::sqrt(disc)) / a;
+          } else {
+            t = quadric_t(&s.quadrics[(size_t)p * 5], o, d, ray.tmin, best);
           }
           if (t >= ray.tmin && t <= best) {
             best = (float)t;

@@ -12,8 +12,9 @@ namespace gprt {
 // Input of the device BVH builder (bvh_build.cu): every primitive in
 // flattened order.
 struct BuildPrims {
-  std::vector<float4> box;           // 2 per primitive: (lo.xyz, type bits) (hi.xyz, material bits), padded
-  std::vector<double> geo;           // 9 per primitive: tri v0 v1 v2 / quad corner u v / sphere centre (r,0,0)
+  std::vector<float4> box;           // 2 per primitive: (lo.xyz, type | quadric kind << 4) (hi.xyz, material), padded
+  std::vector<double> geo;           // 9 per primitive: tri v0 v1 v2 / quad corner u v / sphere centre (r,0,0) /
+                                     // quadric p0 p1 (r0, r1, capped) -- disc: centre normal (r, 0, 0)
   std::vector<uint32_t> shape, sub;  // index in scene.Shapes, box face / mesh triangle
   std::vector<int> light_prim;       // per light: flattened index of its primitive, -1 for infinite lights
   float clo[3], chi[3];              // centroid bounds
@@ -21,12 +22,12 @@ struct BuildPrims {
 
 struct HostScene {
   // device layout (host copies, uploaded by the C ABI layer)
-  std::vector<float4> nodes, tris, tri_normals, quads, spheres;
+  std::vector<float4> nodes, tris, tri_normals, quads, spheres, quadrics;
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights;
   // primitive id -> (index in scene.Shapes, box face / mesh triangle)
   std::vector<uint32_t> prim_shape, prim_sub;
-  uint32_t n_tris = 0, n_quads = 0, n_spheres = 0;
+  uint32_t n_tris = 0, n_quads = 0, n_spheres = 0, n_quadrics = 0;
   int has_infinite = 0;
   double world_center[3] = {0, 0, 0};
   double world_radius = 0;

@@ -9,7 +9,8 @@
 //                node / leaf / light references are rebased to pool indices,
 //                so the unchanged traversal kernels walk any scene from its
 //                root.  Primitive ids of the pool: triangles [0, 2^30), quads
-//                [2^30, 2^31), spheres [2^31, 2^32 - 1).
+//                [2^30, 2^31), spheres [2^31, 3 x 2^30), discs / cylinders /
+//                cones [3 x 2^30, 2^32 - 1).
 //   path state   one set of wavefront arrays (DevPaths) of step capacity,
 //                shared by all jobs; each path records its work item.
 //   item table   per step: prefix sums of the items' paths and pixels (for a
@@ -37,7 +38,8 @@ namespace gprt {
 namespace {
 
 constexpr uint32_t kPoolQuadBase = 1u << 30;
-constexpr uint32_t kPoolSphereBase = 1u << 31;
+constexpr uint32_t kPoolSphereBase = 2u << 30;
+constexpr uint32_t kPoolQuadricBase = 3u << 30;
 
 struct StepHdr {
   uint32_t n_items, total_paths, total_pix, dry;
@@ -163,7 +165,8 @@ __global__ void k_srv_accumulate(DevPaths P, const StepHdr* hdr, const uint32_t*
 
 // Rebases the references of `n` nodes copied to pool index node_off: inner
 // children by node_off, leaves by the offset of their primitive type.
-__global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_off, int quad_off, int sph_off) {
+__global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_off, int quad_off, int sph_off,
+                               int qdr_off) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n * 4u; c += gridDim.x * blockDim.x) {
     float4* a = nodes + (size_t)(c >> 2) * 8 + 2 * (c & 3);
     int ref = __float_as_int(a->w);
@@ -172,7 +175,7 @@ __global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_
     int off = node_off;
     if (meta != 0) {
       int type = (meta >> kLeafTypeShift) & 3;
-      off = type == kPrimTriangle ? tri_off : type == kPrimQuad ? quad_off : sph_off;
+      off = type == kPrimTriangle ? tri_off : type == kPrimQuad ? quad_off : type == kPrimSphere ? sph_off : qdr_off;
     }
     a->w = __int_as_float(ref + off);
   }
@@ -243,8 +246,8 @@ struct PoolArray {
 // A scene resident in the pool.
 struct PoolScene {
   uint64_t serial = 0;
-  size_t off[6] = {0, 0, 0, 0, 0, 0};  // nodes, tris, quads, spheres, materials, lights
-  size_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  size_t off[7] = {0, 0, 0, 0, 0, 0, 0};  // nodes, tris, quads, spheres, quadrics, materials, lights
+  size_t cnt[7] = {0, 0, 0, 0, 0, 0, 0};
   int refs = 0;
   uint64_t last_use = 0;
   size_t bytes = 0;
@@ -287,7 +290,7 @@ struct gprt_server {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // state (smu)
   std::mutex smu;
-  gprt::PoolArray pool[6];
+  gprt::PoolArray pool[7];
   uint64_t pool_gen = 0;
   std::vector<std::unique_ptr<PoolScene>> scenes;
   std::map<uint64_t, std::unique_ptr<SrvJob>> jobs;  // admitted, by ticket
@@ -329,7 +332,8 @@ using namespace gprt;
 
 namespace {
 
-constexpr int kNodes = 0, kTris = 1, kQuads = 2, kSpheres = 3, kMats = 4, kLights = 5;
+constexpr int kNodes = 0, kTris = 1, kQuads = 2, kSpheres = 3, kQuadrics = 4, kMats = 5, kLights = 6;
+constexpr int kPoolArrays = 7;
 
 void emit(gprt_server* sv, uint64_t ticket, uint32_t kind, uint32_t passes, uint32_t spp, int status,
           double submit_ms) {
@@ -358,19 +362,20 @@ size_t bytes_in_use(gprt_server* sv) {
 }
 
 // Element counts of a gprt_scene in the pool's arrays.
-void scene_counts(const gprt_scene* s, size_t cnt[6]) {
+void scene_counts(const gprt_scene* s, size_t cnt[kPoolArrays]) {
   const HostScene& h = s->host;
   cnt[kNodes] = h.nodes.size() / 8;
   cnt[kTris] = h.n_tris;
   cnt[kQuads] = h.n_quads;
   cnt[kSpheres] = h.n_spheres;
+  cnt[kQuadrics] = h.n_quadrics;
   cnt[kMats] = h.materials.size();
   cnt[kLights] = h.lights.size();
 }
 
-size_t scene_bytes(gprt_server* sv, const size_t cnt[6]) {
+size_t scene_bytes(gprt_server* sv, const size_t cnt[kPoolArrays]) {
   size_t b = 0;
-  for (int k = 0; k < 6; k++) b += cnt[k] * sv->pool[k].bytes_per();
+  for (int k = 0; k < kPoolArrays; k++) b += cnt[k] * sv->pool[k].bytes_per();
   return b;
 }
 
@@ -381,12 +386,14 @@ DevScene pool_view(gprt_server* sv) {
   d.tri_normals = static_cast<const float4*>(sv->pool[kTris].buf[1]);
   d.quads = static_cast<const float4*>(sv->pool[kQuads].buf[0]);
   d.spheres = static_cast<const float4*>(sv->pool[kSpheres].buf[0]);
+  d.quadrics = static_cast<const float4*>(sv->pool[kQuadrics].buf[0]);
   d.materials = static_cast<const DevMaterial*>(sv->pool[kMats].buf[0]);
   d.lights = static_cast<const DevLight*>(sv->pool[kLights].buf[0]);
   d.n_nodes = (int)sv->pool[kNodes].cap;
   d.root = -1;
   d.quad_base = kPoolQuadBase;
   d.sphere_base = kPoolSphereBase;
+  d.quadric_base = kPoolQuadricBase;
   d.n_prims = 0xFFFFFFFEu;
   return d;
 }
@@ -397,7 +404,8 @@ bool grow(gprt_server* sv, int k, size_t need_cap) {
   PoolArray& a = sv->pool[k];
   size_t new_cap = std::max(need_cap, a.cap + a.cap / 2);
   if (k == kTris || k == kQuads) new_cap = std::min<size_t>(new_cap, kPoolQuadBase);
-  if (k == kSpheres) new_cap = std::min<size_t>(new_cap, (size_t)0xFFFFFFFEu - kPoolSphereBase);
+  if (k == kSpheres) new_cap = std::min<size_t>(new_cap, kPoolQuadricBase - kPoolSphereBase);
+  if (k == kQuadrics) new_cap = std::min<size_t>(new_cap, (size_t)0xFFFFFFFEu - kPoolQuadricBase);
   if (k == kNodes || k == kMats || k == kLights) new_cap = std::min<size_t>(new_cap, 0x7FFFFFFF);
   if (new_cap < need_cap) return false;
   size_t used = bytes_in_use(sv);
@@ -447,7 +455,7 @@ void shrink_if_empty(gprt_server* sv) {
 }
 
 void evict(gprt_server* sv, PoolScene* ps) {
-  for (int k = 0; k < 6; k++) sv->pool[k].give(ps->off[k], ps->cnt[k]);
+  for (int k = 0; k < kPoolArrays; k++) sv->pool[k].give(ps->off[k], ps->cnt[k]);
   for (auto it = sv->scenes.begin(); it != sv->scenes.end(); ++it)
     if (it->get() == ps) {
       sv->scenes.erase(it);
@@ -457,12 +465,12 @@ void evict(gprt_server* sv, PoolScene* ps) {
 
 // Places the scene's arrays in the pool, evicting unreferenced scenes (least
 // recently used first) and growing arrays as the budget allows.
-bool place(gprt_server* sv, const size_t cnt[6], size_t off[6]) {
+bool place(gprt_server* sv, const size_t cnt[kPoolArrays], size_t off[kPoolArrays]) {
   for (;;) {
     bool ok = true;
-    size_t got[6] = {0, 0, 0, 0, 0, 0};
+    size_t got[kPoolArrays] = {0, 0, 0, 0, 0, 0, 0};
     int k = 0;
-    for (; k < 6; k++) {
+    for (; k < kPoolArrays; k++) {
       if (cnt[k] == 0) continue;
       if (!sv->pool[k].take(cnt[k], &got[k])) {
         ok = false;
@@ -470,7 +478,7 @@ bool place(gprt_server* sv, const size_t cnt[6], size_t off[6]) {
       }
     }
     if (ok) {
-      for (int i = 0; i < 6; i++) off[i] = got[i];
+      for (int i = 0; i < kPoolArrays; i++) off[i] = got[i];
       return true;
     }
     for (int i = 0; i < k; i++) sv->pool[i].give(got[i], cnt[i]);
@@ -491,12 +499,12 @@ bool place(gprt_server* sv, const size_t cnt[6], size_t off[6]) {
 PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   for (auto& ps : sv->scenes)
     if (ps->serial == s->serial) return ps.get();
-  size_t cnt[6], off[6];
+  size_t cnt[kPoolArrays], off[kPoolArrays];
   scene_counts(s, cnt);
   if (!place(sv, cnt, off)) return nullptr;
   auto ps = std::make_unique<PoolScene>();
   ps->serial = s->serial;
-  for (int k = 0; k < 6; k++) {
+  for (int k = 0; k < kPoolArrays; k++) {
     ps->off[k] = off[k];
     ps->cnt[k] = cnt[k];
   }
@@ -514,13 +522,15 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   copy(kTris, 1, d.tri_normals);
   copy(kQuads, 0, d.quads);
   copy(kSpheres, 0, d.spheres);
+  copy(kQuadrics, 0, d.quadrics);
   copy(kMats, 0, d.materials);
   copy(kLights, 0, d.lights);
   if (cnt[kNodes]) {
     float4* nodes = static_cast<float4*>(sv->pool[kNodes].buf[0]) + off[kNodes] * 8;
     uint32_t n = (uint32_t)cnt[kNodes];
     k_rebase_nodes<<<launch_grid(n * 4, 256, 4096), 256, 0, st>>>(nodes, n, (int)off[kNodes], (int)off[kTris],
-                                                                   (int)off[kQuads], (int)off[kSpheres]);
+                                                                   (int)off[kQuads], (int)off[kSpheres],
+                                                                   (int)off[kQuadrics]);
   }
   if (cnt[kLights]) {
     DevLight* L = static_cast<DevLight*>(sv->pool[kLights].buf[0]) + off[kLights];
@@ -596,7 +606,7 @@ void admit(gprt_server* sv) {
     if (sv->jobs.size() >= sv->desc.max_jobs) return;
     gprt_scene* s = r.scene;
     uint32_t npix = s->host.sampling.width * s->host.sampling.height;
-    size_t cnt[6];
+    size_t cnt[kPoolArrays];
     scene_counts(s, cnt);
     bool resident = false;
     for (auto& ps : sv->scenes) resident |= ps->serial == r.serial;
@@ -1049,6 +1059,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   sv->pool[kTris].elem[1] = sizeof(float4);
   sv->pool[kQuads].elem[0] = 5 * sizeof(float4);
   sv->pool[kSpheres].elem[0] = 2 * sizeof(float4);
+  sv->pool[kQuadrics].elem[0] = 5 * sizeof(float4);
   sv->pool[kMats].elem[0] = sizeof(DevMaterial);
   sv->pool[kLights].elem[0] = sizeof(DevLight);
   // path state of one step

@@ -20,7 +20,7 @@ GPRT_E_ADMISSION = -6
 GPRT_E_NOT_FOUND = -7
 
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_LAYERED = range(5)
-SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_MESH, SHAPE_TRIANGLE = range(5)
+SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_MESH, SHAPE_TRIANGLE, SHAPE_DISC, SHAPE_CYLINDER, SHAPE_CONE = range(8)
 LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE = range(4)
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
 CLOSEST, ANY = 0, 1
@@ -84,7 +84,7 @@ class SceneInfo(C.Structure):
                 ("n_triangles", C.c_uint64), ("n_quads", C.c_uint64), ("n_spheres", C.c_uint64),
                 ("n_nodes", C.c_uint64), ("device_bytes", C.c_uint64), ("image_width", C.c_uint32),
                 ("image_height", C.c_uint32), ("build_ms", C.c_double), ("flatten_ms", C.c_double),
-                ("bvh_ms", C.c_double), ("check_ms", C.c_double)]
+                ("bvh_ms", C.c_double), ("check_ms", C.c_double), ("n_quadrics", C.c_uint64)]
 
 
 class JobDesc(C.Structure):

@@ -75,6 +75,19 @@ def Triangle(v0, v1, v2, material):  # geometry.NewTriangle (triangle.go:20-33)
     return Shape(capi.SHAPE_TRIANGLE, material, tuple(v0) + tuple(v1) + tuple(v2))
 
 
+def Disc(center, normal, radius, material):  # geometry.NewDisc (disc.go:21-44)
+    return Shape(capi.SHAPE_DISC, material, tuple(center) + tuple(normal) + (radius,))
+
+
+def Cylinder(base, top, radius, capped, material):  # geometry.NewCylinder (cylinder.go:24-39)
+    return Shape(capi.SHAPE_CYLINDER, material, tuple(base) + tuple(top) + (radius, 1.0 if capped else 0.0))
+
+
+def Cone(base, base_radius, top, top_radius, capped, material):  # geometry.NewCone (cone.go:27-77)
+    return Shape(capi.SHAPE_CONE, material,
+                 tuple(base) + tuple(top) + (base_radius, top_radius, 1.0 if capped else 0.0))
+
+
 # numpy layout of gprt_material_desc (include/gprt.h)
 MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("outer", "<u4"), ("inner", "<u4"), ("reserved", "<u4"),
                            ("albedo", "<f8", 3), ("fuzz", "<f8"), ("ior", "<f8"), ("emission", "<f8", 3)])

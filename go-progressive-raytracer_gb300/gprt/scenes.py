@@ -13,6 +13,9 @@ synthetic workloads of this project from the same primitives:
 * ``default_style_scene``: the seeded many-sphere scenes of the batched
   workload (one ground sphere of radius 1000, three feature spheres and
   10-500 small spheres) under a gradient sky.
+* ``quadric_scene``: discs, capped and open cylinders, a pointed cone and
+  frustums (the reference's Disc / Cylinder / Cone shapes) with Lambertian,
+  metal and glass under a quad light and a gradient sky.
 * ``ray_batch``: seeded raw ray batches (coherent primaries and incoherent
   surface-to-sphere rays) for the intersection benchmark and parity tests.
 """
@@ -21,8 +24,8 @@ import math
 import numpy as np
 
 from . import _capi as capi
-from .scene import (MATERIAL_DTYPE, Box, CameraConfig, Dielectric, Emissive, Lambertian, Layered, MaterialTable,
-                    Mesh, Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, TriangleMesh)
+from .scene import (MATERIAL_DTYPE, Box, CameraConfig, Cone, Cylinder, Dielectric, Disc, Emissive, Lambertian, Layered,
+                    MaterialTable, Mesh, Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, TriangleMesh)
 
 CORNELL_SPHERES, CORNELL_BOXES, CORNELL_EMPTY = 0, 1, 2
 CORNELL_QUAD_LIGHT, CORNELL_SPHERE_LIGHT = 0, 2
@@ -117,6 +120,31 @@ def default_scene(camera=None):
           Sphere((0.5, 0.25, -0.5), 0.25, glass), Sphere((-0.5, 0.25, -0.5), 0.25, glass),
           Sphere((-0.5, 0.25, -0.5), -0.24, glass), Sphere((-0.5, 0.25, -0.5), 0.20, blue))
     s.add_gradient_infinite_light((0.5, 0.7, 1.0), (1.0, 1.0, 1.0))
+    return s.finalize_size()
+
+
+def quadric_scene(width=64, max_depth=8):
+    """Discs, cylinders and cones (geometry.NewDisc / NewCylinder / NewCone)
+    of every kind: a floor disc, capped and open cylinders, a pointed cone,
+    capped and open frustums, an axis-tilted cylinder; Lambertian, metal and
+    glass; a quad light and a gradient sky."""
+    cam = CameraConfig(center=(0.0, 2.5, 7.0), look_at=(0.0, 0.8, 0.0), up=(0.0, 1.0, 0.0), width=width,
+                       aspect_ratio=1.0, vfov=45.0)
+    s = Scene(camera=cam)
+    s.sampling = SamplingConfig(max_depth=max_depth, russian_roulette_min_bounces=16, adaptive_min_samples=1.0,
+                                adaptive_threshold=0.0)
+    white, red, blue = Lambertian((0.73, 0.73, 0.73)), Lambertian((0.65, 0.1, 0.1)), Lambertian((0.1, 0.2, 0.6))
+    steel, glass = Metal((0.8, 0.8, 0.85), 0.1), Dielectric(1.5)
+    s.add(Disc((0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 4.0, white),
+          Cylinder((-2.0, 0.0, -0.5), (-2.0, 1.6, -0.5), 0.5, True, red),
+          Cylinder((2.0, 0.0, -0.5), (2.0, 1.2, -0.5), 0.6, False, steel),
+          Cone((0.0, 0.0, -1.2), 0.8, (0.0, 2.0, -1.2), 0.0, True, blue),
+          Cone((-0.8, 0.0, 1.2), 0.5, (-0.8, 0.9, 1.2), 0.25, True, glass),
+          Cone((1.0, 0.0, 1.3), 0.45, (1.0, 0.7, 1.3), 0.2, False, white),
+          Cylinder((0.2, 0.4, 0.9), (1.0, 0.9, 0.3), 0.2, True, glass),
+          Disc((-1.2, 2.2, -2.0), (0.3, -0.2, 1.0), 0.7, steel))
+    s.add_quad_light((-1.0, 4.0, -1.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0), (6.0, 6.0, 6.0))
+    s.add_gradient_infinite_light((0.3, 0.4, 0.6), (0.7, 0.7, 0.7))
     return s.finalize_size()
 
 

@@ -78,7 +78,11 @@ enum gprt_shape_kind {
   GPRT_SHAPE_QUAD = 1,     /* p[0..2] corner, p[3..5] u, p[6..8] v */
   GPRT_SHAPE_BOX = 2,      /* p[0..2] center, p[3..5] half extents, p[6..8] rotation (rad, X->Y->Z) */
   GPRT_SHAPE_MESH = 3,     /* mesh = index into gprt_scene_desc.meshes */
-  GPRT_SHAPE_TRIANGLE = 4  /* p[0..2] v0, p[3..5] v1, p[6..8] v2 */
+  GPRT_SHAPE_TRIANGLE = 4, /* p[0..2] v0, p[3..5] v1, p[6..8] v2 */
+  GPRT_SHAPE_DISC = 5,     /* pkg/geometry/disc.go: p[0..2] centre, p[3..5] normal, p[6] radius */
+  GPRT_SHAPE_CYLINDER = 6, /* pkg/geometry/cylinder.go: p[0..2] base, p[3..5] top, p[6] radius, p[7] capped */
+  GPRT_SHAPE_CONE = 7      /* pkg/geometry/cone.go: p[0..2] base, p[3..5] top, p[6] base radius,
+                              p[7] top radius (< base radius; 0 = pointed), p[8] capped */
 };
 
 typedef struct gprt_shape_desc {
@@ -199,6 +203,7 @@ typedef struct gprt_scene_info {
   double flatten_ms;      /* of which: flattening the description into primitives */
   double bvh_ms;          /* of which: BVH build and primitive arrays (host SAH or device) */
   double check_ms;        /* of which: layout check of a device-built tree */
+  uint64_t n_quadrics;    /* discs, cylinders, cones */
 } gprt_scene_info;
 
 /* ---- progressive jobs ---------------------------------------------------- */

@@ -440,6 +440,98 @@ void geometryTests() {
 }
 
 // ---------------------------------------------------------------- materials and lights
+// Disc, cylinder and cone (pkg/geometry/disc_test.go, cylinder_test.go,
+// cone_test.go): the hit / miss cases, distances, points and normals.
+void quadricTests() {
+  Lambertian grey(Vec3(0.5, 0.5, 0.5));
+  SurfaceInteraction h;
+  {  // TestDiscHit (disc_test.go:12-89), TestDiscBoundingBox (:91-117)
+    Disc d(Vec3(0, 0, 0), Vec3(0, 1, 0), 1.0, &grey);
+    struct C { const char* n; Ray r; bool hit; };
+    C cs[] = {{"center", Ray(Vec3(0, 1, 0), Vec3(0, -1, 0)), true},
+              {"edge", Ray(Vec3(1, 1, 0), Vec3(0, -1, 0)), true},
+              {"outside radius", Ray(Vec3(1.1, 1, 0), Vec3(0, -1, 0)), false},
+              {"parallel", Ray(Vec3(0, 0, 0), Vec3(1, 0, 0)), false},
+              {"from below", Ray(Vec3(0, -1, 0), Vec3(0, 1, 0)), true}};
+    for (auto& c : cs) {
+      bool hit = d.hit(c.r, 0.001, 10.0, h);
+      bool ok = hit == c.hit;
+      if (!ok) g_detail = "hit mismatch";
+      if (ok && hit) ok = near(h.t, 1.0, 1e-6);
+      check(ok, std::string("disc_test.go:12 TestDiscHit/") + c.n);
+    }
+    AABB b = d.boundingBox();
+    check(nearV(b.min, Vec3(-1, 0, -1), 1e-9) && nearV(b.max, Vec3(1, 0, 1), 1e-9),
+          "disc_test.go:91 TestDiscBoundingBox");
+  }
+  {  // cylinder_test.go:98-560
+    Cylinder c(Vec3(0, 0, 0), Vec3(0, 2, 0), 1.0, false, &grey);
+    bool hit = c.hit(Ray(Vec3(2, 1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(1, 1, 0), 1e-6) && nearV(h.normal, Vec3(1, 0, 0), 1e-6) && h.frontFace,
+          "cylinder_test.go:98 TestCylinder_Hit_SimpleHit");
+    check(!c.hit(Ray(Vec3(2, 1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h), "cylinder_test.go:137 TestCylinder_Hit_Miss");
+    check(c.hit(Ray(Vec3(2, 1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h) &&
+              !c.hit(Ray(Vec3(2, 3, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h) &&
+              !c.hit(Ray(Vec3(2, -1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h),
+          "cylinder_test.go:156 TestCylinder_Hit_HeightBounds");
+    hit = c.hit(Ray(Vec3(0, 1, 0), Vec3(1, 0, 0)), 0.001, 1000.0, h);
+    check(hit && !h.frontFace && nearV(h.normal, Vec3(-1, 0, 0), 1e-6), "cylinder_test.go:205 TestCylinder_Hit_FromInside");
+    Cylinder cx(Vec3(0, 0, 0), Vec3(3, 0, 0), 1.0, false, &grey);
+    hit = cx.hit(Ray(Vec3(1.5, 2, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(1.5, 1, 0), 1e-6) && nearV(h.normal, Vec3(0, 1, 0), 1e-6),
+          "cylinder_test.go:238 TestCylinder_Hit_ArbitraryOrientation");
+    hit = c.hit(Ray(Vec3(-2, 1, 0), Vec3(1, 0, 0)), 0.001, 1000.0, h);
+    check(hit && near(h.t, 1.0, 1e-6) && nearV(h.point, Vec3(-1, 1, 0), 1e-6),
+          "cylinder_test.go:273 TestCylinder_Hit_TwoIntersections");
+    Ray r(Vec3(2, 1, 0), Vec3(-1, 0, 0));
+    check(!c.hit(r, 0.001, 0.5, h) && !c.hit(r, 3.5, 1000.0, h) && c.hit(r, 0.001, 1000.0, h) && near(h.t, 1.0, 1e-6),
+          "cylinder_test.go:304 TestCylinder_Hit_TBounds");
+    Cylinder cc(Vec3(0, 0, 0), Vec3(0, 2, 0), 1.0, true, &grey);
+    hit = cc.hit(Ray(Vec3(0.5, 3, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.5, 2, 0), 1e-6) && nearV(h.normal, Vec3(0, 1, 0), 1e-6),
+          "cylinder_test.go:339 TestCylinder_Capped_HitTopCap");
+    hit = cc.hit(Ray(Vec3(0.5, -1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.5, 0, 0), 1e-6) && nearV(h.normal, Vec3(0, -1, 0), 1e-6),
+          "cylinder_test.go:377 TestCylinder_Capped_HitBottomCap");
+    check(!cc.hit(Ray(Vec3(1.5, 3, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h),
+          "cylinder_test.go:415 TestCylinder_Capped_MissOutsideCapRadius");
+    check(!c.hit(Ray(Vec3(0.5, 3, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h),
+          "cylinder_test.go:521 TestCylinder_Uncapped_NoCapHits");
+  }
+  {  // cone_test.go:227-660
+    Cone c(Vec3(0, 0, 0), 1.0, Vec3(0, 2, 0), 0.0, false, &grey);
+    bool hit = c.hit(Ray(Vec3(2, 1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.5, 1, 0), 1e-6), "cone_test.go:227 TestCone_Hit_SimpleHit");
+    check(!c.hit(Ray(Vec3(2, 1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h), "cone_test.go:263 TestCone_Hit_Miss");
+    check(c.hit(Ray(Vec3(2, 1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h) &&
+              !c.hit(Ray(Vec3(2, 3, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h) &&
+              !c.hit(Ray(Vec3(2, -1, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h),
+          "cone_test.go:286 TestCone_Hit_HeightBounds");
+    Cone f(Vec3(0, 0, 0), 2.0, Vec3(0, 4, 0), 1.0, false, &grey);
+    hit = f.hit(Ray(Vec3(3, 2, 0), Vec3(-1, 0, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(1.5, 2, 0), 1e-6), "cone_test.go:339 TestCone_Hit_Frustum");
+    check(c.hit(Ray(Vec3(0, 1, 0), Vec3(1, 0, 0)), 0.001, 1000.0, h) && !h.frontFace,
+          "cone_test.go:371 TestCone_Hit_FromInside");
+    Ray r(Vec3(2, 1, 0), Vec3(-1, 0, 0));
+    check(!c.hit(r, 0.001, 1.0, h) && !c.hit(r, 10.0, 1000.0, h), "cone_test.go:399 TestCone_Hit_TBounds");
+    Cone cp(Vec3(0, 0, 0), 1.0, Vec3(0, 2, 0), 0.0, true, &grey);
+    hit = cp.hit(Ray(Vec3(0.5, -1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.5, 0, 0), 1e-6) && nearV(h.normal, Vec3(0, -1, 0), 1e-6),
+          "cone_test.go:428 TestCone_Capped_HitBaseCap_Pointed");
+    Cone fc(Vec3(0, 0, 0), 1.0, Vec3(0, 2, 0), 0.5, true, &grey);
+    hit = fc.hit(Ray(Vec3(0.3, -1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.3, 0, 0), 1e-6), "cone_test.go:467 TestCone_Capped_HitBaseCap_Frustum");
+    hit = fc.hit(Ray(Vec3(0.2, 3, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h);
+    check(hit && nearV(h.point, Vec3(0.2, 2, 0), 1e-6) && nearV(h.normal, Vec3(0, 1, 0), 1e-6),
+          "cone_test.go:497 TestCone_Capped_HitTopCap_Frustum");
+    Cone fu(Vec3(0, 0, 0), 1.0, Vec3(0, 2, 0), 0.3, false, &grey);
+    check(!c.hit(Ray(Vec3(2, -1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h) &&
+              !fu.hit(Ray(Vec3(2, -1, 0), Vec3(0, 1, 0)), 0.001, 1000.0, h) &&
+              !fu.hit(Ray(Vec3(0.2, 3, 0), Vec3(0, -1, 0)), 0.001, 1000.0, h),
+          "cone_test.go:609 TestCone_Uncapped_NoCapHits");
+  }
+}
+
 void materialLightTests() {
   {  // TestReflectanceFunction (pkg/material/dielectric_test.go:129-154)
     double r0 = reflectance(1.0, 1.0 / 1.5), r90 = reflectance(0.0, 1.0 / 1.5), r45 = reflectance(0.707, 1.0 / 1.5);
@@ -786,6 +878,7 @@ void rendererTests() {
 int main() {
   try {
     geometryTests();
+    quadricTests();
     materialLightTests();
     bdptTests();
     rendererTests();

@@ -52,6 +52,18 @@ Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
       case GPRT_SHAPE_SPHERE: shape = std::make_unique<Sphere>(v3(p), p[3], mat(sh.material)); break;
       case GPRT_SHAPE_QUAD: shape = std::make_unique<Quad>(v3(p), v3(p + 3), v3(p + 6), mat(sh.material)); break;
       case GPRT_SHAPE_TRIANGLE: shape = std::make_unique<Triangle>(v3(p), v3(p + 3), v3(p + 6), mat(sh.material)); break;
+      case GPRT_SHAPE_DISC: shape = std::make_unique<Disc>(v3(p), v3(p + 3), p[6], mat(sh.material)); break;
+      case GPRT_SHAPE_CYLINDER:
+        shape = std::make_unique<Cylinder>(v3(p), v3(p + 3), p[6], p[7] != 0, mat(sh.material));
+        break;
+      case GPRT_SHAPE_CONE:
+        // NewCone's checks (cone.go:28-50)
+        if (!(p[6] > 0) || p[7] < 0 || p[6] <= p[7] || !(v3(p + 3).sub(v3(p)).length() > 0)) {
+          err = "invalid cone";
+          return nullptr;
+        }
+        shape = std::make_unique<Cone>(v3(p), p[6], v3(p + 3), p[7], p[8] != 0, mat(sh.material));
+        break;
       case GPRT_SHAPE_BOX: {
         auto b = std::make_unique<Box>(v3(p), v3(p + 3), v3(p + 6), mat(sh.material));
         b->setId((int)i);

@@ -702,6 +702,243 @@ struct Quad : Shape {
   }
 };
 
+// Disc (disc.go:11-134): plane hit with |n.d| < 1e-6 rejected, inside when
+// |p - c|^2 <= r^2; UV from the right / up frame of NewDisc
+struct Disc : Shape {
+  Vec3 center, normal, right, up;
+  double radius;
+  const Material* material;
+  Disc(Vec3 c, Vec3 n, double r, const Material* m) : center(c), radius(r), material(m) {
+    normal = n.normalize();
+    Vec3 rv = std::fabs(normal.x) > 0.1 ? Vec3(0, 1, 0) : Vec3(1, 0, 0);
+    right = rv.cross(normal).normalize();
+    up = normal.cross(right).normalize();
+  }
+  bool hit(const Ray& ray, double tMin, double tMax, SurfaceInteraction& out) const override {
+    counters().prims++;
+    double den = normal.dot(ray.direction);
+    if (std::fabs(den) < 1e-6) return false;
+    double t = normal.dot(center.sub(ray.origin)) / den;
+    if (t < tMin || t > tMax) return false;
+    Vec3 p = ray.at(t);
+    Vec3 cp = p.sub(center);
+    if (cp.lengthSquared() > radius * radius) return false;
+    out = SurfaceInteraction();
+    out.t = t;
+    out.point = p;
+    out.material = material;
+    out.uv = Vec2((cp.dot(right) / radius + 1.0) / 2.0, (cp.dot(up) / radius + 1.0) / 2.0);
+    out.shape = id;
+    out.sub = 0;
+    out.setFaceNormal(ray, normal);
+    return true;
+  }
+  AABB boundingBox() const override {  // the four corners centre +- r right +- r up
+    Vec3 re = right.mul(radius), ue = up.mul(radius);
+    std::vector<Vec3> cs = {center.add(re).add(ue), center.add(re).sub(ue), center.sub(re).add(ue),
+                            center.sub(re).sub(ue)};
+    return AABB::fromPoints(cs);
+  }
+};
+
+// Circular cap shared by Cylinder and Cone (cylinder.go:224-266, cone.go:306-350)
+inline bool hit_cap(const Ray& ray, const Vec3& center, const Vec3& normal, double radius, double tMin, double tMax,
+                    double& t, Vec3& p) {
+  double den = ray.direction.dot(normal);
+  if (std::fabs(den) < 1e-8) return false;
+  t = center.sub(ray.origin).dot(normal) / den;
+  if (t < tMin || t > tMax) return false;
+  p = ray.at(t);
+  return p.sub(center).length() <= radius;
+}
+
+// Finite cylinder with optional caps (cylinder.go:24-266)
+struct Cylinder : Shape {
+  Vec3 base, top, axis;
+  double radius, height;
+  bool capped;
+  const Material* material;
+  Cylinder(Vec3 b, Vec3 tp, double r, bool cap, const Material* m)
+      : base(b), top(tp), radius(r), capped(cap), material(m) {
+    Vec3 av = top.sub(base);
+    height = av.length();
+    axis = av.normalize();
+  }
+  bool hit(const Ray& ray, double tMin, double tMax, SurfaceInteraction& out) const override {
+    counters().prims++;
+    double closest = tMax;
+    bool any = false;
+    Vec3 outward, point;
+    // body (hitBody, cylinder.go:125-221)
+    {
+      Vec3 delta = ray.origin.sub(base);
+      double DV = ray.direction.dot(axis), dV = delta.dot(axis);
+      double a = ray.direction.lengthSquared() - DV * DV;
+      double b = 2.0 * (delta.dot(ray.direction) - dV * DV);
+      double c = delta.lengthSquared() - dV * dV - radius * radius;
+      if (std::fabs(a) >= 1e-8) {
+        double disc = b * b - 4 * a * c;
+        if (disc >= 0) {
+          double sq = std::sqrt(disc);
+          double t1 = (-b - sq) / (2 * a), t2 = (-b + sq) / (2 * a);
+          double t = t1;
+          bool ok = true;
+          if (t < tMin || t > closest) {
+            t = t2;
+            if (t < tMin || t > closest) ok = false;
+          }
+          if (ok) {
+            Vec3 p = ray.at(t);
+            double h = p.sub(base).dot(axis);
+            if (h < 0 || h > height) {
+              ok = false;
+              if (t == t1) {
+                t = t2;
+                if (!(t < tMin || t > closest)) {
+                  p = ray.at(t);
+                  h = p.sub(base).dot(axis);
+                  ok = !(h < 0 || h > height);
+                }
+              }
+            }
+            if (ok) {
+              Vec3 onAxis = base.add(axis.mul(h));
+              outward = p.sub(onAxis).normalize();
+              point = p;
+              closest = t;
+              any = true;
+            }
+          }
+        }
+      }
+    }
+    if (capped) {
+      double t;
+      Vec3 p;
+      if (hit_cap(ray, base, axis.negate(), radius, tMin, closest, t, p)) {
+        closest = t;
+        point = p;
+        outward = axis.negate();
+        any = true;
+      }
+      if (hit_cap(ray, top, axis, radius, tMin, closest, t, p)) {
+        closest = t;
+        point = p;
+        outward = axis;
+        any = true;
+      }
+    }
+    if (!any) return false;
+    out = SurfaceInteraction();
+    out.t = closest;
+    out.point = point;
+    out.material = material;
+    out.shape = id;
+    out.sub = 0;
+    out.setFaceNormal(ray, outward);
+    return true;
+  }
+  AABB boundingBox() const override {  // segment box widened by r except along an axis-parallel direction
+    double e[3];
+    for (int k = 0; k < 3; k++) e[k] = std::fabs(axis.axis(k)) > 0.9999 ? 0.0 : radius;
+    Vec3 lo(std::min(base.x, top.x) - e[0], std::min(base.y, top.y) - e[1], std::min(base.z, top.z) - e[2]);
+    Vec3 hi(std::max(base.x, top.x) + e[0], std::max(base.y, top.y) + e[1], std::max(base.z, top.z) + e[2]);
+    return {lo, hi};
+  }
+};
+
+// Cone or frustum with optional caps (cone.go:27-350)
+struct Cone : Shape {
+  Vec3 base, top, axis, apex;
+  double r0, r1, height, tanAngle;
+  bool capped;
+  const Material* material;
+  Cone(Vec3 b, double br, Vec3 tp, double tr, bool cap, const Material* m)
+      : base(b), top(tp), r0(br), r1(tr), capped(cap), material(m) {
+    Vec3 av = top.sub(base);
+    height = av.length();
+    axis = av.normalize();
+    tanAngle = (r0 - r1) / height;
+    apex = r1 == 0 ? top : top.add(axis.mul(r1 * height / (r0 - r1)));
+  }
+  // validateIntersection (cone.go:279-303)
+  bool valid(const Ray& ray, double t, double tMin, double tMax) const {
+    if (t < tMin || t > tMax) return false;
+    Vec3 p = ray.at(t);
+    double h = p.sub(base).dot(axis);
+    if (h < -1e-8 || h > height + 1e-8) return false;
+    return p.sub(apex).dot(axis) <= 1e-8;
+  }
+  bool hit(const Ray& ray, double tMin, double tMax, SurfaceInteraction& out) const override {
+    counters().prims++;
+    double closest = tMax;
+    bool any = false;
+    Vec3 outward, point;
+    // body (hitBody, cone.go:180-276)
+    {
+      Vec3 CO = ray.origin.sub(apex);
+      double DV = ray.direction.dot(axis), COV = CO.dot(axis);
+      double k = tanAngle * tanAngle;
+      double a = ray.direction.lengthSquared() - (1 + k) * DV * DV;
+      double b = 2.0 * (ray.direction.dot(CO) - (1 + k) * DV * COV);
+      double c = CO.lengthSquared() - (1 + k) * COV * COV;
+      if (std::fabs(a) >= 1e-8) {
+        double disc = b * b - 4 * a * c;
+        if (disc >= 0) {
+          double sq = std::sqrt(disc);
+          double t = (-b - sq) / (2 * a);
+          bool ok = valid(ray, t, tMin, closest);
+          if (!ok) {
+            t = (-b + sq) / (2 * a);
+            ok = valid(ray, t, tMin, closest);
+          }
+          if (ok) {
+            Vec3 p = ray.at(t);
+            double h = p.sub(base).dot(axis);
+            Vec3 radial = p.sub(base.add(axis.mul(h)));
+            outward = radial.add(axis.mul((r0 - r1) / height)).normalize();
+            point = p;
+            closest = t;
+            any = true;
+          }
+        }
+      }
+    }
+    if (capped) {
+      double t;
+      Vec3 p;
+      if (hit_cap(ray, base, axis.negate(), r0, tMin, closest, t, p)) {
+        closest = t;
+        point = p;
+        outward = axis.negate();
+        any = true;
+      }
+      if (r1 > 0 && hit_cap(ray, top, axis, r1, tMin, closest, t, p)) {
+        closest = t;
+        point = p;
+        outward = axis;
+        any = true;
+      }
+    }
+    if (!any) return false;
+    out = SurfaceInteraction();
+    out.t = closest;
+    out.point = point;
+    out.material = material;
+    out.shape = id;
+    out.sub = 0;
+    out.setFaceNormal(ray, outward);
+    return true;
+  }
+  AABB boundingBox() const override {  // segment box widened by the base radius (cone.go:79-126)
+    double e[3];
+    for (int k = 0; k < 3; k++) e[k] = std::fabs(axis.axis(k)) > 0.9999 ? 0.0 : r0;
+    Vec3 lo(std::min(base.x, top.x) - e[0], std::min(base.y, top.y) - e[1], std::min(base.z, top.z) - e[2]);
+    Vec3 hi(std::max(base.x, top.x) + e[0], std::max(base.y, top.y) + e[1], std::max(base.z, top.z) + e[2]);
+    return {lo, hi};
+  }
+};
+
 // Triangle, Moller-Trumbore with epsilon 1e-8 (triangle.go:17-185)
 struct Triangle : Shape {
   Vec3 v0, v1, v2, normal;

@@ -17,13 +17,14 @@ def _both(ctx, scene):
     return gprt.GpuScene(ctx, flat), gprt.GpuScene(ctx, flat, device_bvh=True)
 
 
-@pytest.mark.parametrize("name", ["cornell", "spheres", "icosphere6"])
+@pytest.mark.parametrize("name", ["cornell", "spheres", "icosphere6", "quadrics"])
 def test_device_bvh_hits_match_host_bvh(ctx, name):
     import gprt
     from gprt import scenes
     from test_gpu_intersect import _camera_rays, _rays_in_bounds
     scene = {"cornell": lambda: scenes.cornell_baseline(64), "spheres": lambda: scenes.default_style_scene(17, 64, 64),
-             "icosphere6": lambda: scenes.icosphere_scene(level=6, width=64)}[name]()
+             "icosphere6": lambda: scenes.icosphere_scene(level=6, width=64),
+             "quadrics": lambda: scenes.quadric_scene(64)}[name]()
     host, dev = _both(ctx, scene)
     info = dev.info
     assert info.n_primitives == host.info.n_primitives and info.n_nodes > 0

@@ -76,6 +76,7 @@ SCENES = {
     "default_scene": lambda s: s.default_scene(),
     "icosphere6": lambda s: s.icosphere_scene(level=6, width=64),
     "spheres17": lambda s: s.default_style_scene(17, 64, 64),
+    "quadrics": lambda s: s.quadric_scene(64),
 }
 
 

@@ -58,6 +58,7 @@ SCENES = {
     "default_scene": lambda s: _fixed(s.default_scene(camera=_cam(64)), depth=8),
     "icosphere5": lambda s: s.icosphere_scene(level=5, width=48),
     "spheres17": lambda s: s.default_style_scene(17, 48, 48),
+    "quadrics": lambda s: s.quadric_scene(48),
 }
 
 
@@ -87,13 +88,14 @@ def test_pt_same_inputs_parity(ctx, oracle, name):
     assert frac <= 0.02, (med, frac)
 
 
-@pytest.mark.parametrize("name", ["cornell_boxes", "cornell_spheres", "default_scene"])
+@pytest.mark.parametrize("name", ["cornell_boxes", "cornell_spheres", "default_scene", "quadrics"])
 def test_bdpt_same_inputs_parity(ctx, oracle, name):
     import gprt
     from gprt import scenes
     scene = {"cornell_boxes": lambda: scenes.cornell_boxes_bdpt(width=32, max_depth=6),
              "cornell_spheres": lambda: _fixed(scenes.cornell_scene(scenes.CORNELL_SPHERES, camera=_cam(32)), 6),
-             "default_scene": lambda: _fixed(scenes.default_scene(camera=_cam(48)), depth=6)}[name]()
+             "default_scene": lambda: _fixed(scenes.default_scene(camera=_cam(48)), depth=6),
+             "quadrics": lambda: scenes.quadric_scene(32, max_depth=6)}[name]()
     gpu, stats, _ = gpu_render(ctx, scene, 8, seed=5, integrator=gprt.BDPTIntegrator())
     r, _ = oracle_render(oracle, scene, 8, seed=5, integrator=1)
     med, frac = same_input_stats(gpu, r.image())

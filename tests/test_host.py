@@ -38,7 +38,7 @@ def _validate(flat):
 
 
 @pytest.mark.parametrize("name", ["cornell_baseline", "cornell_spheres", "cornell_boxes", "default", "icosphere5",
-                                  "spheres17"])
+                                  "spheres17", "quadrics"])
 def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
     from gprt import scenes
     s = {"cornell_baseline": lambda: scenes.cornell_baseline(64),
@@ -46,7 +46,8 @@ def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
          "cornell_boxes": lambda: scenes.cornell_scene(scenes.CORNELL_BOXES),
          "default": lambda: scenes.default_scene(),
          "icosphere5": lambda: scenes.icosphere_scene(level=5, width=64),
-         "spheres17": lambda: scenes.default_style_scene(17, 64, 64)}[name]()
+         "spheres17": lambda: scenes.default_style_scene(17, 64, 64),
+         "quadrics": lambda: scenes.quadric_scene(64)}[name]()
     flat = s.to_desc()
     rc, info, err = _validate(flat)
     assert rc == 0, err
