@@ -18,7 +18,7 @@ def test_kat_all_pass(kat_results):
     assert rc == 0 and not fails, "\n".join(fails)
     summary = [l for l in lines if l.startswith("SUMMARY")][0]
     npass = int(summary.split("pass=")[1].split()[0])
-    assert npass >= 79
+    assert npass >= 106
 
 
 @pytest.mark.parametrize("family", [
@@ -26,6 +26,8 @@ def test_kat_all_pass(kat_results):
     "TestCameraPathBetaPropagation", "TestEvaluateDirectLightingStrategy", "TestVertexConvertSolidAngleToAreaPdf",
     "TestTriangle_Hit", "TestQuad_Hit", "TestSphere_Hit", "TestBox_Hit", "TestWorldRadius", "TestWeFunction",
     "TestMapRayToPixel", "TestPowerHeuristic", "TestDielectricEvaluateBRDF",
+    "TestDiscHit", "TestCylinder_Hit_SimpleHit", "TestCylinder_Capped_HitTopCap", "TestCylinder_Hit_ArbitraryOrientation",
+    "TestCone_Hit_Frustum", "TestCone_Capped_HitBaseCap_Pointed", "TestCone_Uncapped_NoCapHits",
 ])
 def test_kat_family_present_and_passing(kat_results, family):
     _, lines = kat_results
