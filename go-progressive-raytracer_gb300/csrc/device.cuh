@@ -112,6 +112,18 @@ __device__ __forceinline__ float3 sample_cosine_hemisphere(float3 n, float2 s) {
   float3 b = cross(n, t);
   return t * x + b * y + n * z;
 }
+// SampleCone (sampling.go:70-94): uniform direction within the cone of
+// cosine cos_total about the unit direction w
+__device__ __forceinline__ float3 sample_cone(float3 w, float cos_total, float2 s) {
+  float3 u = fabsf(w.x) > 0.1f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+  u = normalize(cross(u, w));
+  float3 v = cross(w, u);
+  float ct = 1.0f - s.x * (1.0f - cos_total);
+  float st = sqrtf(fmaxf(0.f, 1.0f - ct * ct));
+  float sp, cp;
+  sincosf(2.0f * kPi * s.y, &sp, &cp);
+  return u * (st * cp) + v * (st * sp) + w * ct;
+}
 // SampleOnUnitSphere (sampling.go:97-104)
 __device__ __forceinline__ float3 sample_on_unit_sphere(float2 s) {
   float z = 1.0f - 2.0f * s.x;
@@ -764,6 +776,8 @@ __device__ __forceinline__ bool scatter_basic(const DevMaterial& m, float3 din, 
 
 __device__ __forceinline__ bool scatter(const DevScene& sc, const DevMaterial& m, float3 din, const Surface& s,
                                         Rng& rng, Scatter& out) {
+  if (m.kind == kMatMix)  // Mix.Scatter (mix.go:30-37): material 2 below the ratio
+    return scatter_basic(load_material(sc, rng.next() < m.fuzz ? m.inner : m.outer), din, s, rng, out);
   if (m.kind != kMatLayered) return scatter_basic(m, din, s, rng, out);
   DevMaterial mo = load_material(sc, m.outer);
   Scatter o;
@@ -836,6 +850,9 @@ __device__ __forceinline__ bool is_reflection_path(float3 in, float3 out, float3
 
 __device__ __forceinline__ float3 brdf(const DevScene& sc, const DevMaterial& m, float3 in, float3 out,
                                        const Surface& s, bool radiance) {
+  if (m.kind == kMatMix)  // Mix.EvaluateBRDF (mix.go:40-46)
+    return brdf_basic(load_material(sc, m.outer), in, out, s, radiance) * (1.f - m.fuzz) +
+           brdf_basic(load_material(sc, m.inner), in, out, s, radiance) * m.fuzz;
   if (m.kind != kMatLayered) return brdf_basic(m, in, out, s, radiance);
   int sub = is_reflection_path(in, out, s.n) ? m.outer : m.inner;
   return brdf_basic(load_material(sc, sub), in, out, s, radiance);
@@ -861,6 +878,13 @@ __device__ __forceinline__ float pdf_basic(const DevMaterial& m, float3 out, flo
 }
 __device__ __forceinline__ float mat_pdf(const DevScene& sc, const DevMaterial& m, float3 in, float3 out, float3 n,
                                          bool& delta) {
+  if (m.kind == kMatMix) {  // Mix.PDF (mix.go:49-59): never delta
+    bool d;
+    float p1 = pdf_basic(load_material(sc, m.outer), out, n, d);
+    float p2 = pdf_basic(load_material(sc, m.inner), out, n, d);
+    delta = false;
+    return p1 * (1.f - m.fuzz) + p2 * m.fuzz;
+  }
   if (m.kind != kMatLayered) return pdf_basic(m, out, n, delta);
   int sub = is_reflection_path(in, out, n) ? m.outer : m.inner;
   bool d;
@@ -869,10 +893,15 @@ __device__ __forceinline__ float mat_pdf(const DevScene& sc, const DevMaterial& 
   return p;
 }
 
-// Emissive.Emit with a hit record (emissive.go:24-32): front face only
-__device__ __forceinline__ float3 emitted(const DevMaterial& m, bool front) {
-  if (m.kind != kMatEmissive || !front) return f3(0.f, 0.f, 0.f);
-  return m.emission;
+// Material Emit with a hit record, for a ray of direction d: Emissive
+// (emissive.go:24-32) emits from the front face; the disc spot light's
+// emitter (disc_spot_light.go:26-48) also needs d against its spot direction
+// (cosine at most -0.3, d as given).
+__device__ __forceinline__ float3 emitted(const DevMaterial& m, bool front, float3 d) {
+  if (!front) return f3(0.f, 0.f, 0.f);
+  if (m.kind == kMatEmissive) return m.emission;
+  if (m.kind == kMatSpotEmissive && dot(d, m.albedo) <= -0.3f) return m.emission;
+  return f3(0.f, 0.f, 0.f);
 }
 
 // ----------------------------------------------------------------- lights
@@ -888,8 +917,28 @@ __device__ __forceinline__ float3 gradient_emission(const DevLight& L, float3 dn
   return L.b * (1.0f - t) + L.a * t;
 }
 
+// Spot falloff (point_spot_light.go:140-158, disc_spot_light.go:150-168)
+__device__ __forceinline__ float spot_falloff(const DevLight& L, float c) {
+  if (c < L.cos_total) return 0.f;
+  if (c >= L.cos_falloff) return 1.f;
+  float x = (c - L.cos_total) / (L.cos_falloff - L.cos_total);
+  x = x * x;
+  return x * x;
+}
+
+// Disc.SampleUniform (disc.go:120-134) on a disc record (centre + radius,
+// normal, right, up)
+__device__ __forceinline__ float3 disc_point(const float4* Q, float2 u) {
+  float4 g0 = __ldg(Q);
+  float r = sqrtf(u.x) * g0.w;
+  float s_, c_;
+  sincosf(2.f * kPi * u.y, &s_, &c_);
+  return f3(g0) + f3(__ldg(Q + 2)) * (r * c_) + f3(__ldg(Q + 3)) * (r * s_);
+}
+
 // Light.Sample (quad_light.go:36-86, sphere_light.go:29-141,
-// uniform_infinite_light.go:66-80, gradient_infinite_light.go:77-91)
+// uniform_infinite_light.go:66-80, gradient_infinite_light.go:77-91,
+// disc_light.go, disc_spot_light.go, point_spot_light.go)
 __device__ __forceinline__ LightSample light_sample(const DevScene& sc, const DevLight& L, float3 p, float3 n,
                                                     float2 u) {
   LightSample ls;
@@ -964,6 +1013,54 @@ __device__ __forceinline__ LightSample light_sample(const DevScene& sc, const De
     ls.pdf = 1.0f / (4.f * kPi * r * r);
     return ls;
   }
+  if (L.kind == kLightDisc || L.kind == kLightDiscSpot) {
+    // DiscLight.Sample (disc_light.go:28-75); the spot variant scales the
+    // emission by the falloff seen from the sampled point (disc_spot_light.go:115-130)
+    const float4* Q = sc.quadrics + (size_t)L.prim * 5;
+    float3 N = f3(__ldg(Q + 1));
+    float3 sp = disc_point(Q, u);
+    float3 to = sp - p;
+    float dist = length(to);
+    ls.point = sp;
+    ls.normal = N;
+    if (dist == 0.f) {
+      ls.dir = f3(0.f, 1.f, 0.f);
+      ls.dist = 0.f;
+      ls.emission = f3(0.f, 0.f, 0.f);
+      ls.pdf = 1.f;
+      return ls;
+    }
+    float3 dir = to * (1.0f / dist);
+    float ct = fabsf(dot(N, -dir));
+    ls.pdf = ct < 1e-6f ? 0.f : (1.0f / L.area) * dist * dist / ct;
+    ls.dir = dir;
+    ls.dist = dist;
+    ls.emission = L.a;  // Emit(ray, nil) of the emissive material
+    if (L.kind == kLightDiscSpot) {
+      if (dot(dir, L.b) > -0.3f) ls.emission = f3(0.f, 0.f, 0.f);
+      ls.emission = ls.emission * spot_falloff(L, dot(L.b, normalize(p - sp)));
+    }
+    return ls;
+  }
+  if (L.kind == kLightPointSpot) {
+    // PointSpotLight.Sample (point_spot_light.go:46-97)
+    float3 to = L.pos - p;
+    float dist = length(to);
+    ls.point = L.pos;
+    ls.pdf = 1.f;
+    if (dist == 0.f) {
+      ls.normal = ls.dir = f3(0.f, 1.f, 0.f);
+      ls.dist = 0.f;
+      ls.emission = f3(0.f, 0.f, 0.f);
+      return ls;
+    }
+    float3 tl = to * (1.0f / dist);
+    ls.emission = L.a * (spot_falloff(L, dot(L.b, -tl)) / (dist * dist));
+    ls.normal = -tl;
+    ls.dir = tl;
+    ls.dist = dist;
+    return ls;
+  }
   // infinite lights: cosine-weighted hemisphere about the shading normal
   float3 dir = sample_cosine_hemisphere(n, u);
   ls.point = p + dir * 1e10f;
@@ -976,7 +1073,8 @@ __device__ __forceinline__ LightSample light_sample(const DevScene& sc, const De
 }
 
 // Light.PDF (quad_light.go:90-109, sphere_light.go:144-166,
-// uniform_infinite_light.go:83-91, gradient_infinite_light.go:94-102)
+// uniform_infinite_light.go:83-91, gradient_infinite_light.go:94-102,
+// disc_light.go:78-100 (also the disc spot light), point_spot_light.go:101-118)
 __device__ __forceinline__ float light_pdf(const DevScene& sc, const DevLight& L, float3 p, float3 n, float3 dir) {
   if (L.kind == kLightQuad) {
     const float4* Q = sc.quads + (size_t)L.prim * 5;
@@ -996,6 +1094,20 @@ __device__ __forceinline__ float light_pdf(const DevScene& sc, const DevLight& L
     float sinMax = S.w / dc;
     float cosMax = sqrtf(fmaxf(0.f, 1.f - sinMax * sinMax));
     return 1.0f / (2.f * kPi * (1.f - cosMax));
+  }
+  if (L.kind == kLightDisc || L.kind == kLightDiscSpot) {  // disc_light.go:78-100
+    const float4* Q = sc.quadrics + (size_t)L.prim * 5;
+    float t, part;
+    if (!hit_quadric(p, dir, Q, 0.001f, kInfF, t, part)) return 0.f;
+    float ct = fabsf(dot(f3(__ldg(Q + 1)), -dir));
+    if (ct < 1e-6f) return 0.f;
+    return (1.0f / L.area) * t * t / ct;
+  }
+  if (L.kind == kLightPointSpot) {  // point_spot_light.go:101-118
+    float3 to = L.pos - p;
+    float len = length(to);
+    if (len == 0.f) return 0.f;
+    return dot(dir, to * (1.0f / len)) > 0.999f ? 1.f : 0.f;
   }
   float c = dot(dir, n);
   return c <= 0.f ? 0.f : c / kPi;

@@ -43,7 +43,12 @@ struct BVert {  // bdpt.go:14-36
 
 __device__ __forceinline__ bool light_is_area(const DevScene& sc, int li) {
   int k = sc.lights[li].kind;
-  return k == kLightQuad || k == kLightSphere;
+  return k == kLightQuad || k == kLightSphere || k == kLightDisc || k == kLightDiscSpot;
+}
+
+// a vertex on a point light (LightTypePoint, bdpt_mis.go:130-137)
+__device__ __forceinline__ bool is_delta_light(const DevScene& sc, const BVert& v) {
+  return v.is(kFlagLight) && v.light >= 0 && sc.lights[v.light].kind == kLightPointSpot;
 }
 
 // Vertex.IsOnSurface (bdpt.go:42-49)
@@ -100,6 +105,7 @@ __device__ __forceinline__ float camera_importance(const DevCamera& c, float3 d)
 
 // ---------------------------------------------------------------- lights
 // SampleEmission (quad_light.go:113-145, sphere_light.go:169-184,
+// disc_light.go:103-110, disc_spot_light.go:210-240, point_spot_light.go:161-191,
 // light_sampling.go:58-115 for the infinite lights)
 __device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp, float2 sd, float3& p, float3& n,
                                 float3& dir, float3& Le, float& area_pdf, float& dir_pdf) {
@@ -129,6 +135,28 @@ __device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight&
     Le = L.a;
     return;
   }
+  if (L.kind == kLightDisc || L.kind == kLightDiscSpot || L.kind == kLightPointSpot) {
+    if (L.kind == kLightPointSpot) {
+      p = L.pos;
+      area_pdf = 1.f;
+    } else {
+      const float4* Q = sc.quadrics + (size_t)L.prim * 5;
+      p = disc_point(Q, sp);
+      n = f3(__ldg(Q + 1));
+      area_pdf = 1.0f / L.area;
+    }
+    if (L.kind == kLightDisc) {  // SampleEmissionDirection (light_sampling.go:58-80)
+      dir = sample_cosine_hemisphere(n, sd);
+      dir_pdf = dot(dir, n) / kPi;
+      Le = L.a;
+      return;
+    }
+    dir = sample_cone(L.b, L.cos_total, sd);
+    Le = L.a * spot_falloff(L, dot(dir, L.b));
+    dir_pdf = 1.0f / (2.f * kPi * (1.f - L.cos_total));  // UniformConePDF (light_sampling.go:83-85)
+    if (L.kind == kLightPointSpot) n = dir;
+    return;
+  }
   // SampleInfiniteLight (light_sampling.go:89-115)
   float3 d = sample_on_unit_sphere(sd);
   float3 up = fabsf(d.x) > 0.9f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
@@ -146,6 +174,7 @@ __device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight&
 }
 
 // PDF_Le direction pdf (quad_light.go:148-185, sphere_light.go:187-209,
+// disc_light.go:113-136, disc_spot_light.go:243-264, point_spot_light.go:194-214,
 // uniform_infinite_light.go:94-106); pos receives the position pdf
 __device__ __noinline__ float pdf_le(const DevScene& sc, const DevLight& L, float3 p, float3 dir, float& pos) {
   pos = 0.f;
@@ -174,6 +203,28 @@ __device__ __noinline__ float pdf_le(const DevScene& sc, const DevLight& L, floa
     if (dot(dir, n) <= 0.f) return 0.f;
     pos = 1.0f / (4.f * kPi * S.w * S.w);
     return dot(dir, n) / kPi;
+  }
+  if (L.kind == kLightDisc || L.kind == kLightDiscSpot) {
+    const float4* Q = sc.quadrics + (size_t)L.prim * 5;
+    float4 g0 = __ldg(Q);
+    float3 N = f3(__ldg(Q + 1));
+    // validatePointOnDisc (disc_light.go:153-165), tolerance 0.001
+    float3 tp = p - f3(g0);
+    float h = dot(tp, N);
+    if (fabsf(h) > 0.001f || length(tp - N * h) > g0.w) return 0.f;
+    float ct = dot(dir, N);
+    if (ct <= 0.f) return 0.f;
+    if (L.kind == kLightDiscSpot && dot(dir, L.b) < L.cos_total) {
+      pos = 1.0f / L.area;
+      return 0.f;
+    }
+    pos = 1.0f / L.area;
+    return ct / kPi;
+  }
+  if (L.kind == kLightPointSpot) {
+    if (length(p - L.pos) > 0.001f || dot(dir, L.b) < L.cos_total) return 0.f;
+    pos = 1.f;
+    return 1.0f / (2.f * kPi * (1.f - L.cos_total));
   }
   if (sc.world_radius <= 0.f) return 0.f;
   pos = 1.0f / (kPi * sc.world_radius * sc.world_radius);
@@ -357,7 +408,7 @@ __device__ __noinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, ui
     v.n = s.n;
     v.wi = -d;
     v.beta = beta;
-    v.Le = emitted(m, s.front);
+    v.Le = emitted(m, s.front, d);
     v.mat = s.mat;
     v.light = -1;
     v.prim = h.prim;
@@ -446,8 +497,8 @@ __device__ __noinline__ float mis_weight(const DevScene& sc, const SubpathRef& C
   for (int i = s - 1; i >= 0; i--) {
     BVert v = Lp[i];
     float fwd = v.fwd, rev = v.rev;
-    bool conn = !v.is(kFlagSpecular);  // no point lights on this path
-    if (i > 0) conn = conn && !Lp[i - 1].is(kFlagSpecular);
+    bool conn = !v.is(kFlagSpecular) && !is_delta_light(sc, v);
+    if (i > 0) conn = conn && !Lp[i - 1].is(kFlagSpecular) && !is_delta_light(sc, Lp[i - 1]);
     if (t == 1) {
       if (i == s - 1 && s > 1) {
         BVert a = Lp[s - 1];
@@ -682,8 +733,10 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
       lv.wi = f3(0.f, 0.f, 0.f);
       lv.light = li;
       lv.mat = -1;
-      lv.prim = L.kind == kLightQuad ? sc.quad_base + (uint32_t)L.prim
-                                     : (L.kind == kLightSphere ? sc.sphere_base + (uint32_t)L.prim : kNoHit);
+      lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
+                : L.kind == kLightSphere ? sc.sphere_base + (uint32_t)L.prim
+                : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
+                                                                     : kNoHit;
       lv.fwd = apdf * L.prob;
       lv.rev = 0.f;
       bool inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;

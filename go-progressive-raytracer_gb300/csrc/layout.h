@@ -13,7 +13,8 @@
 //   spheres    2 x float4 (32 B): (center, radius) (material, -, -, -)
 //   quadrics   5 x float4 (80 B): discs, cylinders and cones
 //              (p0, r0) (axis, height) (p1, r1) (apex, tan^2) (kind, material, capped, -)
-//              disc: p0 = centre, axis = unit normal, r0 = radius;
+//              disc: p0 = centre, axis = unit normal, r0 = radius, p1 = right,
+//              apex = up (the in-plane basis of Disc.SampleUniform);
 //              cylinder: p0 = base, p1 = top, r0 = r1 = radius;
 //              cone: p0 = base (radius r0), p1 = top (radius r1), apex of the extended cone
 // Primitive ids: triangles [0, quad_base), quads [quad_base, sphere_base),
@@ -39,8 +40,13 @@ constexpr int kTraceStack = 64;
 constexpr int kErrStackOverflow = 1;
 constexpr int kErrQueueOverflow = 2;
 
-enum : int { kMatLambertian = 0, kMatMetal = 1, kMatDielectric = 2, kMatEmissive = 3, kMatLayered = 4 };
-enum : int { kLightQuad = 0, kLightSphere = 1, kLightUniformInfinite = 2, kLightGradientInfinite = 3 };
+// kMatSpotEmissive: the disc spot light's directional emitter; albedo holds
+// the unit spot direction
+// kMatMix: outer / inner are materials 1 / 2, fuzz the ratio
+enum : int { kMatLambertian = 0, kMatMetal = 1, kMatDielectric = 2, kMatEmissive = 3, kMatLayered = 4,
+             kMatSpotEmissive = 5, kMatMix = 6 };
+enum : int { kLightQuad = 0, kLightSphere = 1, kLightUniformInfinite = 2, kLightGradientInfinite = 3, kLightDisc = 4,
+             kLightDiscSpot = 5, kLightPointSpot = 6 };
 
 struct DevMaterial {
   int kind, outer, inner, pad;
@@ -52,12 +58,17 @@ struct DevMaterial {
 
 struct DevLight {
   int kind;
-  int prim;   // index in the quad or sphere array (area lights)
+  int prim;   // index in the quad, sphere or quadric (disc) array (area lights)
   float prob; // light-sampler selection probability
-  float area; // quad area |u x v| (quad_light.go:19-27)
-  float3 a;   // emission (area, uniform) or top colour (gradient)
-  float3 b;   // bottom colour (gradient)
+  float area; // quad area |u x v| (quad_light.go:19-27); disc area pi r^2
+  float3 a;   // emission (area, uniform, spot) or top colour (gradient)
+  float cos_total;    // spot lights: cosine of the total cone angle
+  float3 b;   // bottom colour (gradient); unit spot direction (spot lights)
+  float cos_falloff;  // spot lights: cosine of the falloff start angle
+  float3 pos; // point spot light position
+  float pad;
 };
+static_assert(sizeof(DevLight) == 64, "DevLight is four 16-byte words");
 
 // Camera (pkg/geometry/camera.go:35-67), derived in float64 on the host
 struct DevCamera {

@@ -57,7 +57,7 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q,
       Surface s;
       surface_at(sc, f3(o4), d, h, s);
       DevMaterial m = load_material(sc, s.mat);
-      L += W * emitted(m, s.front);  // getEmittedLight (:108-113)
+      L += W * emitted(m, s.front, d);  // getEmittedLight (:108-113)
       Scatter sc_;
       if (scatter(sc, m, d, s, rng, sc_)) {
         if (sc_.pdf <= 0.f) {

@@ -138,11 +138,18 @@ struct Prim {
 // The reference BoundingBox of a disc, cylinder or cone (disc.go:95-118,
 // cylinder.go:42-94, cone.go:79-126): conservative, flat along an axis the
 // cylinder or cone is parallel to.
+float3 to_f3(const double* v) { return make_float3((float)v[0], (float)v[1], (float)v[2]); }
+
+// The in-plane basis of a disc (NewDisc, disc.go:21-43)
+void disc_basis(const D3& n, D3& right, D3& up) {
+  right = (std::fabs(n.x) > 0.1 ? D3(0, 1, 0) : D3(1, 0, 0)).cross(n).norm();
+  up = n.cross(right).norm();
+}
+
 DBox quadric_box(const Prim& p) {
   if (p.qkind == kQuadricDisc) {
-    D3 n = p.b.norm();
-    D3 right = (std::fabs(n.x) > 0.1 ? D3(0, 1, 0) : D3(1, 0, 0)).cross(n).norm();
-    D3 up = n.cross(right).norm();
+    D3 n = p.b.norm(), right, up;
+    disc_basis(n, right, up);
     D3 re = right * p.c.x, ue = up * p.c.x;
     D3 cs[4] = {p.a + re + ue, p.a + re - ue, p.a - re + ue, p.a - re - ue};
     return box_of(cs, 4);
@@ -161,8 +168,12 @@ void quadric_record(const Prim& p, float4 out[5]) {
   out[0] = out[1] = out[2] = out[3] = z;
   out[4] = make_float4(i2f((uint32_t)p.qkind), i2f(p.material), p.qkind == kQuadricDisc ? 0.f : (float)p.c.z, 0.f);
   if (p.qkind == kQuadricDisc) {
+    D3 n = p.b.norm(), right, up;
+    disc_basis(n, right, up);
     out[0] = mk4(p.a, (float)p.c.x);
-    out[1] = mk4(p.b.norm(), 0.f);
+    out[1] = mk4(n, 0.f);
+    out[2] = mk4(right, 0.f);
+    out[3] = mk4(up, 0.f);
     return;
   }
   D3 av = p.b - p.a;
@@ -499,22 +510,44 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     const gprt_material_desc& m = d->materials[i];
     DevMaterial dm{};
     dm.kind = (int)m.kind;
-    if (m.kind > GPRT_MAT_LAYERED) {
+    if (m.kind > GPRT_MAT_MIX) {
       err = "unknown material kind";
       return false;
     }
     dm.albedo = make_float3((float)m.albedo[0], (float)m.albedo[1], (float)m.albedo[2]);
+    if (m.kind == GPRT_MAT_SPOT_EMISSIVE) {  // albedo = the unit spot direction
+      D3 sd(m.albedo);
+      if (!(sd.len() > 0)) {
+        err = "spot emitter direction must be non-zero";
+        return false;
+      }
+      sd = sd.norm();
+      dm.albedo = make_float3((float)sd.x, (float)sd.y, (float)sd.z);
+    }
     dm.fuzz = (float)std::min(1.0, std::max(0.0, m.fuzz));
     dm.ior = (float)m.ior;
     dm.emission = make_float3((float)m.emission[0], (float)m.emission[1], (float)m.emission[2]);
     if (m.kind == GPRT_MAT_LAYERED) {
       if (m.outer >= d->n_materials || m.inner >= d->n_materials ||
-          d->materials[m.outer].kind == GPRT_MAT_LAYERED || d->materials[m.inner].kind == GPRT_MAT_LAYERED) {
-        err = "layered material must reference two non-layered materials";
+          d->materials[m.outer].kind == GPRT_MAT_LAYERED || d->materials[m.inner].kind == GPRT_MAT_LAYERED ||
+          d->materials[m.outer].kind == GPRT_MAT_MIX || d->materials[m.inner].kind == GPRT_MAT_MIX) {
+        err = "layered material must reference two non-layered, non-mix materials";
         return false;
       }
       dm.outer = (int)m.outer;
       dm.inner = (int)m.inner;
+    }
+    if (m.kind == GPRT_MAT_MIX) {  // NewMix clamps the ratio (mix.go:17-27)
+      auto basic = [&](uint32_t k) {
+        return k < d->n_materials && d->materials[k].kind != GPRT_MAT_LAYERED && d->materials[k].kind != GPRT_MAT_MIX;
+      };
+      if (!basic(m.outer) || !basic(m.inner)) {
+        err = "mix material must reference two non-layered, non-mix materials";
+        return false;
+      }
+      dm.outer = (int)m.outer;
+      dm.inner = (int)m.inner;
+      dm.fuzz = (float)std::min(1.0, std::max(0.0, m.fuzz));
     }
     out.materials[i] = dm;
   }
@@ -536,7 +569,8 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     }
     prims.reserve(total);
   }
-  std::vector<int> shape_quad_prim(d->n_shapes, -1), shape_sphere_prim(d->n_shapes, -1);
+  std::vector<int> shape_quad_prim(d->n_shapes, -1), shape_sphere_prim(d->n_shapes, -1),
+      shape_disc_prim(d->n_shapes, -1);
   DBox world{};
   bool have_world = false;
   auto add_world = [&](const DBox& b) {
@@ -583,6 +617,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
         if (!check_mat(s.material)) return false;
         Prim q{kPrimQuadric, i, 0, s.material, D3(p), D3(p + 3), D3(p[6], p[7], p[8]), 0};
         if (s.kind == GPRT_SHAPE_DISC) {
+          shape_disc_prim[i] = (int)prims.size();
           q.qkind = kQuadricDisc;
           q.c = D3(p[6], 0, 0);
           if (q.b.len() == 0) {
@@ -860,6 +895,41 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
         L.a = emission_of(prims[pid].material);
         break;
       }
+      case GPRT_LIGHT_DISC:
+      case GPRT_LIGHT_DISC_SPOT: {
+        if (l.shape >= d->n_shapes || shape_disc_prim[l.shape] < 0) {
+          err = "disc lights must reference a disc shape";
+          return false;
+        }
+        int pid = shape_disc_prim[l.shape];
+        uint32_t mk = d->materials[prims[pid].material].kind;
+        if ((l.kind == GPRT_LIGHT_DISC) == (mk == GPRT_MAT_SPOT_EMISSIVE)) {
+          err = "a disc spot light's disc (and only it) carries the spot emitter material";
+          return false;
+        }
+        L.prim = (int)final_index[pid];
+        L.area = (float)(M_PI * prims[pid].c.x * prims[pid].c.x);  // pi r^2 (disc_light.go:52)
+        L.a = l.kind == GPRT_LIGHT_DISC ? emission_of(prims[pid].material) : to_f3(l.color_a);
+        if (l.kind == GPRT_LIGHT_DISC) break;
+      }
+      // fall through: the spot parameters of the disc spot light
+      case GPRT_LIGHT_POINT_SPOT: {
+        // NewPointSpotLight / NewDiscSpotLight (point_spot_light.go:25-40, disc_spot_light.go:80-108)
+        D3 from(l.from), to(l.to);
+        if (!((to - from).len() > 0)) {
+          err = "spot light position and target must differ";
+          return false;
+        }
+        D3 dir = (to - from).norm();
+        L.b = make_float3((float)dir.x, (float)dir.y, (float)dir.z);
+        L.cos_total = (float)std::cos(l.cone_deg * M_PI / 180.0);
+        L.cos_falloff = (float)std::cos((l.cone_deg - l.cone_delta_deg) * M_PI / 180.0);
+        if (l.kind == GPRT_LIGHT_POINT_SPOT) {
+          L.a = to_f3(l.color_a);
+          L.pos = make_float3((float)from.x, (float)from.y, (float)from.z);
+        }
+        break;
+      }
       case GPRT_LIGHT_UNIFORM_INFINITE:
         L.a = make_float3((float)l.color_a[0], (float)l.color_a[1], (float)l.color_a[2]);
         out.has_infinite = 1;
@@ -877,7 +947,9 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     if (out.device_bvh)  // remapped to leaf order by the device builder
       out.pending.light_prim.push_back(l.kind == GPRT_LIGHT_QUAD     ? shape_quad_prim[l.shape]
                                        : l.kind == GPRT_LIGHT_SPHERE ? shape_sphere_prim[l.shape]
-                                                                     : -1);
+                                       : (l.kind == GPRT_LIGHT_DISC || l.kind == GPRT_LIGHT_DISC_SPOT)
+                                           ? shape_disc_prim[l.shape]
+                                           : -1);
   }
   // camera (NewCamera, pkg/geometry/camera.go:70-170) in float64
   const gprt_camera_desc& c = d->camera;
@@ -1052,6 +1124,20 @@ std::string validate_layout(const HostScene& s) {
       if (c == 0) return "primitive missing from the BVH";
       if (c > 1) return "primitive referenced twice";
     }
+  // area lights name a primitive of their kind (a disc for the disc lights)
+  for (const DevLight& L : s.lights) {
+    size_t n = L.kind == kLightQuad ? s.n_quads
+             : L.kind == kLightSphere ? s.n_spheres
+             : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? s.n_quadrics
+                                                                  : SIZE_MAX;
+    if (n == SIZE_MAX) continue;
+    if (L.prim < 0 || (size_t)L.prim >= n) return "light primitive out of range";
+    if (L.kind == kLightDisc || L.kind == kLightDiscSpot) {
+      int kind;
+      std::memcpy(&kind, &s.quadrics[(size_t)L.prim * 5 + 4].x, 4);
+      if (kind != kQuadricDisc) return "disc light does not name a disc";
+    }
+  }
   return "";
 }
 

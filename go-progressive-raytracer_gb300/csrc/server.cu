@@ -181,10 +181,11 @@ __global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_
   }
 }
 
-__global__ void k_rebase_lights(DevLight* L, uint32_t n, int quad_off, int sph_off) {
+__global__ void k_rebase_lights(DevLight* L, uint32_t n, int quad_off, int sph_off, int qdr_off) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (L[i].kind == kLightQuad) L[i].prim += quad_off;
     else if (L[i].kind == kLightSphere) L[i].prim += sph_off;
+    else if (L[i].kind == kLightDisc || L[i].kind == kLightDiscSpot) L[i].prim += qdr_off;
   }
 }
 
@@ -534,7 +535,8 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   }
   if (cnt[kLights]) {
     DevLight* L = static_cast<DevLight*>(sv->pool[kLights].buf[0]) + off[kLights];
-    k_rebase_lights<<<1, 128, 0, st>>>(L, (uint32_t)cnt[kLights], (int)off[kQuads], (int)off[kSpheres]);
+    k_rebase_lights<<<1, 128, 0, st>>>(L, (uint32_t)cnt[kLights], (int)off[kQuads], (int)off[kSpheres],
+                                       (int)off[kQuadrics]);
   }
   ps->root = cnt[kNodes] ? (int)off[kNodes] : -1;
   ps->has_infinite = d.has_infinite;

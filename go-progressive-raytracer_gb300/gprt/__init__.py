@@ -8,7 +8,7 @@ from . import _capi as capi  # noqa: F401
 from .renderer import (BDPTIntegrator, Context, GpuScene, PassResult, PathTracingIntegrator,  # noqa: F401
                        ProgressiveConfig, ProgressiveRaytracer, RenderStats, TileCompletionResult)
 from .scene import (Box, CameraConfig, Cone, Cylinder, Dielectric, Disc, Emissive, Lambertian, Layered,  # noqa: F401
-                    MaterialTable, Mesh, Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, Triangle,
-                    TriangleMesh)
+                    MaterialTable, Mesh, Metal, Mix, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, SpotEmissive,
+                    Triangle, TriangleMesh)
 from . import scenes  # noqa: F401
 from .server import RenderServer, ServerEvent, latency_summary  # noqa: F401

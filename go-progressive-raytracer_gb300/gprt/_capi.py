@@ -19,9 +19,10 @@ GPRT_E_CANCELLED = -5
 GPRT_E_ADMISSION = -6
 GPRT_E_NOT_FOUND = -7
 
-MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_LAYERED = range(5)
+MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_LAYERED, MAT_SPOT_EMISSIVE, MAT_MIX = range(7)
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_MESH, SHAPE_TRIANGLE, SHAPE_DISC, SHAPE_CYLINDER, SHAPE_CONE = range(8)
-LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE = range(4)
+(LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE, LIGHT_DISC, LIGHT_DISC_SPOT,
+ LIGHT_POINT_SPOT) = range(7)
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
 CLOSEST, ANY = 0, 1
 NO_HIT = 0xFFFFFFFF
@@ -47,7 +48,8 @@ class MeshDesc(C.Structure):
 
 class LightDesc(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("shape", C.c_uint32), ("color_a", C.c_double * 3),
-                ("color_b", C.c_double * 3), ("weight", C.c_double)]
+                ("color_b", C.c_double * 3), ("weight", C.c_double), ("from_", C.c_double * 3), ("to", C.c_double * 3),
+                ("cone_deg", C.c_double), ("cone_delta_deg", C.c_double)]
 
 
 class CameraDesc(C.Structure):

@@ -8,6 +8,7 @@ NewTriangleMesh, NewTriangle); lights follow pkg/lights and the Scene.Add*Light
 helpers.  ``Scene.to_desc()`` flattens it into the C ``gprt_scene_desc``.
 """
 import ctypes as C
+import math
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -48,6 +49,14 @@ def Emissive(emission):  # material.NewEmissive (emissive.go:12-14)
 
 def Layered(outer, inner):  # material.NewLayered (layered.go:16-21)
     return Material(capi.MAT_LAYERED, outer=outer, inner=inner)
+
+
+def Mix(material1, material2, ratio):  # material.NewMix (mix.go:17-27), ratio clamped to [0,1]
+    return Material(capi.MAT_MIX, outer=material1, inner=material2, fuzz=min(1.0, max(0.0, ratio)))
+
+
+def SpotEmissive(emission, direction):  # discSpotLightMaterial (disc_spot_light.go:13-51)
+    return Material(capi.MAT_SPOT_EMISSIVE, albedo=tuple(direction), emission=tuple(emission))
 
 
 # ---------------------------------------------------------------- shapes
@@ -129,16 +138,23 @@ class Light:
     color_a: Vec3 = (0.0, 0.0, 0.0)
     color_b: Vec3 = (0.0, 0.0, 0.0)
     weight: float = 1.0
+    from_: Vec3 = (0.0, 0.0, 0.0)  # spot lights: position and aim point
+    to: Vec3 = (0.0, 0.0, 0.0)
+    cone_deg: float = 0.0
+    cone_delta_deg: float = 0.0
 
 
 @dataclass
 class CameraConfig:  # geometry.CameraConfig (camera.go:18-32)
+    """Field defaults are Go's zero values, so that a partly filled config
+    (CameraConfig(width=96)) overrides only what it names when merged, as a
+    Go composite literal does; a camera used directly names every field."""
     center: Vec3 = (0.0, 0.0, 0.0)
-    look_at: Vec3 = (0.0, 0.0, -1.0)
-    up: Vec3 = (0.0, 1.0, 0.0)
-    width: int = 400
-    aspect_ratio: float = 1.0
-    vfov: float = 40.0
+    look_at: Vec3 = (0.0, 0.0, 0.0)
+    up: Vec3 = (0.0, 0.0, 0.0)
+    width: int = 0
+    aspect_ratio: float = 0.0
+    vfov: float = 0.0
     aperture: float = 0.0
     focus_distance: float = 0.0
 
@@ -206,6 +222,29 @@ class Scene:
         self.shapes.append(s)
         return s
 
+    def add_disc_light(self, center, normal, radius, emission):  # lights.NewDiscLight (disc_light.go:17-22)
+        d = Disc(center, normal, radius, Emissive(emission))
+        self.lights.append(Light(capi.LIGHT_DISC, shape=d))
+        self.shapes.append(d)
+        return d
+
+    def add_spot_light(self, from_, to, emission, cone_deg, cone_delta_deg, radius):
+        """scene.AddSpotLight (scene.go:117-123): a disc spot light whose disc
+        (facing `to`, directional emissive material) is also a shape."""
+        dv = [t - f for f, t in zip(from_, to)]
+        n = math.sqrt(sum(x * x for x in dv))
+        direction = tuple(x / n for x in dv)
+        d = Disc(from_, direction, radius, SpotEmissive(emission, direction))
+        self.lights.append(Light(capi.LIGHT_DISC_SPOT, shape=d, color_a=tuple(emission), from_=tuple(from_), to=tuple(to),
+                                 cone_deg=cone_deg, cone_delta_deg=cone_delta_deg))
+        self.shapes.append(d)
+        return d
+
+    def add_point_spot_light(self, from_, to, emission, cone_deg, cone_delta_deg, radius=0.0):
+        """scene.AddPointSpotLight (scene.go:125-129); `radius` is unused, as there."""
+        self.lights.append(Light(capi.LIGHT_POINT_SPOT, color_a=tuple(emission), from_=tuple(from_), to=tuple(to),
+                                 cone_deg=cone_deg, cone_delta_deg=cone_delta_deg))
+
     def add_uniform_infinite_light(self, emission):
         self.lights.append(Light(capi.LIGHT_UNIFORM_INFINITE, color_a=tuple(emission)))
 
@@ -239,7 +278,7 @@ class FlatScene:
                 m = Lambertian((0.0, 0.0, 0.0))
             k = id(m)
             if k not in index:
-                if m.kind == capi.MAT_LAYERED:
+                if m.kind in (capi.MAT_LAYERED, capi.MAT_MIX):
                     mat_id(m.outer)
                     mat_id(m.inner)
                 index[k] = n_mats()
@@ -292,7 +331,7 @@ class FlatScene:
             d["emission"] = m.emission
             d["fuzz"] = m.fuzz
             d["ior"] = m.ior
-            if m.kind == capi.MAT_LAYERED:
+            if m.kind in (capi.MAT_LAYERED, capi.MAT_MIX):
                 d["outer"] = index[id(m.outer)]
                 d["inner"] = index[id(m.inner)]
         for first, t in tables:
@@ -306,6 +345,10 @@ class FlatScene:
             for k in range(3):
                 d.color_a[k] = l.color_a[k]
                 d.color_b[k] = l.color_b[k]
+                d.from_[k] = l.from_[k]
+                d.to[k] = l.to[k]
+            d.cone_deg = l.cone_deg
+            d.cone_delta_deg = l.cone_delta_deg
             d.weight = scene.light_weights[i] if scene.light_weights else 1.0
         meshd = (capi.MeshDesc * max(1, len(meshes)))(*meshes) if meshes else (capi.MeshDesc * 1)()
         desc = capi.SceneDesc()

@@ -13,6 +13,9 @@ synthetic workloads of this project from the same primitives:
 * ``default_style_scene``: the seeded many-sphere scenes of the batched
   workload (one ground sphere of radius 1000, three feature spheres and
   10-500 small spheres) under a gradient sky.
+* ``cone_test_scene`` / ``cylinder_test_scene`` / ``sphere_grid_scene``
+  mirror scene.NewConeTestScene, scene.NewCylinderTestScene and
+  scene.NewSphereGridScene.
 * ``quadric_scene``: discs, capped and open cylinders, a pointed cone and
   frustums (the reference's Disc / Cylinder / Cone shapes) with Lambertian,
   metal and glass under a quad light and a gradient sky.
@@ -25,10 +28,10 @@ import numpy as np
 
 from . import _capi as capi
 from .scene import (MATERIAL_DTYPE, Box, CameraConfig, Cone, Cylinder, Dielectric, Disc, Emissive, Lambertian, Layered,
-                    MaterialTable, Mesh, Metal, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, TriangleMesh)
+                    MaterialTable, Mesh, Metal, Mix, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, TriangleMesh)
 
 CORNELL_SPHERES, CORNELL_BOXES, CORNELL_EMPTY = 0, 1, 2
-CORNELL_QUAD_LIGHT, CORNELL_SPHERE_LIGHT = 0, 2
+CORNELL_QUAD_LIGHT, CORNELL_POINT_LIGHT, CORNELL_SPHERE_LIGHT = 0, 1, 2
 
 
 def _cornell_camera(override=None):  # setupCornellCamera (cornell.go:59-77)
@@ -49,8 +52,8 @@ def _cornell_walls(s):  # addCornellWalls (cornell.go:91-147)
 
 
 def cornell_scene(geometry=CORNELL_SPHERES, light=CORNELL_QUAD_LIGHT, camera=None):
-    """scene.NewCornellScene (pkg/scene/cornell.go:32-257); the point-light
-    variant is not supported by the GPU path."""
+    """scene.NewCornellScene (pkg/scene/cornell.go:32-257) with its quad,
+    point and sphere light variants."""
     s = Scene(camera=_cornell_camera(camera))
     # createCornellSamplingConfig (cornell.go:80-88)
     s.sampling = SamplingConfig(samples_per_pixel=150, max_depth=5, russian_roulette_min_bounces=16,
@@ -62,6 +65,10 @@ def cornell_scene(geometry=CORNELL_SPHERES, light=CORNELL_QUAD_LIGHT, camera=Non
                          tuple(2.5 * e for e in emission))
     elif light == CORNELL_SPHERE_LIGHT:
         s.add_sphere_light((278.0, 556.0 - 0.001, 279.5), 52.5, tuple(2.05 * e for e in emission))
+    elif light == CORNELL_POINT_LIGHT:
+        # a 180-degree point spot light aimed at (0,-1,0) (cornell.go:170-182)
+        s.add_point_spot_light((278.0, 556.0 - 0.001, 279.5), (0.0, -1.0, 0.0), tuple(20000.0 * e for e in emission),
+                               180.0, 0.0)
     else:
         raise ValueError("unsupported Cornell light type")
     if geometry == CORNELL_SPHERES:  # addCornellSpheres (cornell.go:212-226)
@@ -123,11 +130,12 @@ def default_scene(camera=None):
     return s.finalize_size()
 
 
-def quadric_scene(width=64, max_depth=8):
+def quadric_scene(width=64, max_depth=8, disc_light=False):
     """Discs, cylinders and cones (geometry.NewDisc / NewCylinder / NewCone)
     of every kind: a floor disc, capped and open cylinders, a pointed cone,
     capped and open frustums, an axis-tilted cylinder; Lambertian, metal and
-    glass; a quad light and a gradient sky."""
+    glass; a quad light (or a downward disc light, lights.NewDiscLight) and a
+    gradient sky."""
     cam = CameraConfig(center=(0.0, 2.5, 7.0), look_at=(0.0, 0.8, 0.0), up=(0.0, 1.0, 0.0), width=width,
                        aspect_ratio=1.0, vfov=45.0)
     s = Scene(camera=cam)
@@ -143,8 +151,137 @@ def quadric_scene(width=64, max_depth=8):
           Cone((1.0, 0.0, 1.3), 0.45, (1.0, 0.7, 1.3), 0.2, False, white),
           Cylinder((0.2, 0.4, 0.9), (1.0, 0.9, 0.3), 0.2, True, glass),
           Disc((-1.2, 2.2, -2.0), (0.3, -0.2, 1.0), 0.7, steel))
-    s.add_quad_light((-1.0, 4.0, -1.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0), (6.0, 6.0, 6.0))
+    if disc_light:
+        s.add_disc_light((0.0, 4.0, 0.0), (0.0, -1.0, 0.0), 1.1, (8.0, 8.0, 8.0))
+    else:
+        s.add_quad_light((-1.0, 4.0, -1.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0), (6.0, 6.0, 6.0))
     s.add_gradient_infinite_light((0.3, 0.4, 0.6), (0.7, 0.7, 0.7))
+    return s.finalize_size()
+
+
+def _quadric_test_base(camera):
+    # the camera, sampling, ground and lighting shared by NewConeTestScene
+    # (cone_scene.go:10-179) and NewCylinderTestScene (cylinder_scene.go:10-119)
+    base = CameraConfig(center=(0.0, 1.5, 4.0), look_at=(0.0, 1.0, 0.0), up=(0.0, 1.0, 0.0), width=400,
+                        aspect_ratio=16.0 / 9.0, vfov=50.0, aperture=0.0, focus_distance=0.0)
+    s = Scene(camera=base.merged(camera))
+    s.sampling = SamplingConfig(samples_per_pixel=200, max_depth=50, russian_roulette_min_bounces=20,
+                                adaptive_min_samples=0.15, adaptive_threshold=0.01)
+    s.add(NewGroundQuad((0.0, 0.0, 0.0), 10000.0, Lambertian((0.5, 0.5, 0.5))))
+    return s
+
+
+def _quadric_test_lights(s):
+    s.add_sphere_light((3.0, 5.0, 3.0), 1.5, (10.0, 10.0, 10.0))
+    s.add_gradient_infinite_light((0.5, 0.7, 1.0), (1.0, 1.0, 1.0))
+    return s.finalize_size()
+
+
+def cone_test_scene(camera=None):
+    """scene.NewConeTestScene (pkg/scene/cone_scene.go:10-179)."""
+    s = _quadric_test_base(camera)
+    red, blue, green = Lambertian((0.8, 0.2, 0.2)), Lambertian((0.2, 0.2, 0.8)), Lambertian((0.2, 0.8, 0.2))
+    gold, glass = Metal((0.8, 0.6, 0.2), 0.1), Dielectric(1.5)
+    s.add(Cone((0.0, 0.0, 0.0), 0.5, (0.0, 2.0, 0.0), 0.0, True, red),
+          Cone((-2.0, 0.8, -0.8), 0.5, (-2.0, 0.2, 0.5), 0.2, True, gold),
+          Cone((2.0, 0.0, 0.0), 0.8, (2.0, 0.6, 0.0), 0.5, True, blue),
+          Cone((2.0, 0.6, 0.0), 0.5, (2.0, 1.8, 0.0), 0.0, True, glass),
+          Cone((-1.5, 0.0, -0.5), 0.4, (-1.2, 1.2, -0.3), 0.15, False, green),
+          Cone((-0.8, 0.0, 1.2), 0.3, (-0.8, 0.8, 1.2), 0.0, True, glass),
+          Cone((0.8, 0.2, 1.2), 0.3, (0.8, 1.0, 1.2), 0.0, True, glass))
+    return _quadric_test_lights(s)
+
+
+def cylinder_test_scene(camera=None):
+    """scene.NewCylinderTestScene (pkg/scene/cylinder_scene.go:10-119)."""
+    s = _quadric_test_base(camera)
+    red, blue = Lambertian((0.8, 0.2, 0.2)), Lambertian((0.2, 0.2, 0.8))
+    gold, glass = Metal((0.8, 0.6, 0.2), 0.1), Dielectric(1.5)
+    s.add(Cylinder((-0.3, 1.0, -1.5), (0.0, 1.2, 2.0), 0.35, False, gold),
+          Cylinder((-2.5, 0.3, 0.0), (-1.5, 0.3, 0.0), 0.3, True, blue),
+          Cylinder((1.8, 0.0, 0.0), (1.8, 2.0, 0.0), 0.5, True, red),
+          Cylinder((0.5, 0.0, 1.0), (0.5, 0.6, 1.0), 0.2, True, glass))
+    return _quadric_test_lights(s)
+
+
+def _oklch_to_rgb(l, c, h):
+    """OKLCH -> linear sRGB clamped to [0,1] (the OKLab transform published by
+    B. Ottosson, 2020), as spheregrid.go:14-40 colours its spheres."""
+    hr = h * math.pi / 180.0
+    a, b = c * math.cos(hr), c * math.sin(hr)
+    l_ = (l + 0.3963377774 * a + 0.2158037573 * b) ** 3
+    m_ = (l - 0.1055613458 * a - 0.0638541728 * b) ** 3
+    s_ = (l - 0.0894841775 * a - 1.2914855480 * b) ** 3
+    rgb = (4.0767416621 * l_ - 3.3077115913 * m_ + 0.2309699292 * s_,
+           -1.2684380046 * l_ + 2.6097574011 * m_ - 0.3413193965 * s_,
+           -0.0041960863 * l_ - 0.7034186147 * m_ + 1.7076147010 * s_)
+    return tuple(max(0.0, min(1.0, x)) for x in rgb)
+
+
+def sphere_grid_scene(grid_size=10, finish="metallic", camera=None):
+    """scene.NewSphereGridScene (pkg/scene/spheregrid.go:44-189): a
+    grid_size x grid_size grid of spheres over a 9 x 9 area, hue varying
+    along both axes; finish is one of matte, glossy (glass over Lambertian),
+    mirror, glass, mixed (Mix of Lambertian and metal, 50/50) or metallic."""
+    base = CameraConfig(center=(4.5, 6.0, 18.0), look_at=(4.5, 0.8, 4.5), up=(0.0, 1.0, 0.0), width=800,
+                        aspect_ratio=16.0 / 9.0, vfov=40.0, aperture=0.02, focus_distance=0.0)
+    s = Scene(camera=base.merged(camera))
+    s.sampling = SamplingConfig(samples_per_pixel=100, max_depth=40, russian_roulette_min_bounces=12,
+                                adaptive_min_samples=0.12, adaptive_threshold=0.015)
+    s.add_sphere_light((20.0, 25.0, 20.0), 8.0, (8.0, 7.5, 6.5))
+    s.add(NewGroundQuad((0.0, 0.0, 0.0), 10000.0, Lambertian((0.5, 0.5, 0.5))))
+    area = 9.0
+    spacing = area / float(grid_size - 1)
+    radius = max(0.02, min(0.35, spacing * 0.35))
+    lo_c, hi_c = 0.05, 0.25
+    for i in range(grid_size):
+        for j in range(grid_size):
+            pos = (i * spacing - area / 2.0 + 4.5, radius, j * spacing - area / 2.0 + 4.5)
+            fi, fj = i / float(grid_size - 1), j / float(grid_size - 1)
+            hue = math.fmod(fi * 330.0 + fj * 120.0, 360.0)
+            chroma = lo_c + 0.8 * (hi_c - lo_c) + 0.2 * (hi_c - lo_c) * fj
+            color = _oklch_to_rgb(0.65, chroma, hue)
+            if finish == "matte":
+                m = Lambertian(color)
+            elif finish == "glossy":
+                m = Layered(Dielectric(1.5), Lambertian(color))
+            elif finish == "mirror":
+                m = Metal((0.9, 0.9, 0.9), 0.0)
+            elif finish == "glass":
+                m = Dielectric(1.5)
+            elif finish == "mixed":
+                m = Mix(Lambertian(color), Metal(color, 0.1), 0.5)
+            else:
+                m = Metal(color, 0.05)
+            s.add(Sphere(pos, radius, m))
+    s.add_gradient_infinite_light((0.5, 0.7, 1.0), (1.0, 1.0, 1.0))
+    return s.finalize_size()
+
+
+def spot_scene(width=48, point=False, max_depth=8):
+    """The caustic-glass scene's lighting (scene.NewCausticGlassScene,
+    caustic_glass.go:36-95: a spot light from (0,5,9) at (-5,2.75,0) with a
+    30-degree cone, 5-degree falloff and (for the disc spot) radius 0.7, plus
+    a 0.1 uniform infinite light) and its camera, over procedural geometry in
+    place of the PLY meshes the reference loads: a floor, a glass sphere, a
+    Lambertian cylinder, a metal cone and a layered disc."""
+    cam = CameraConfig(center=(-5.5, 7.0, -5.5), look_at=(-4.75, 2.25, 0.0), up=(0.0, 1.0, 0.0), width=width,
+                       aspect_ratio=525.0 / 750.0, vfov=45.0)
+    s = Scene(camera=cam)
+    s.sampling = SamplingConfig(max_depth=max_depth, russian_roulette_min_bounces=16, adaptive_min_samples=1.0,
+                                adaptive_threshold=0.0)
+    intensity = (139.8113403320, 118.6366500854, 105.3887557983)
+    if point:
+        s.add_point_spot_light((0.0, 5.0, 9.0), (-5.0, 2.75, 0.0), intensity, 30.0, 5.0, 0.7)
+    else:
+        s.add_spot_light((0.0, 5.0, 9.0), (-5.0, 2.75, 0.0), intensity, 30.0, 5.0, 0.7)
+    s.add_uniform_infinite_light((0.1, 0.1, 0.1))
+    white = Lambertian((0.7, 0.7, 0.7))
+    s.add(Quad((-15.0, 0.0, -15.0), (30.0, 0.0, 0.0), (0.0, 0.0, 30.0), white),
+          Sphere((-5.0, 1.5, 0.0), 1.5, Dielectric(1.25)),
+          Cylinder((-2.5, 0.0, 1.5), (-2.5, 2.0, 1.5), 0.6, True, Lambertian((0.6, 0.3, 0.2))),
+          Cone((-7.5, 0.0, 1.0), 1.0, (-7.5, 2.5, 1.0), 0.0, True, Metal((0.8, 0.8, 0.8), 0.2)),
+          Disc((-4.0, 0.01, -2.5), (0.0, 1.0, 0.0), 1.2, Layered(Dielectric(1.5), Lambertian((0.2, 0.5, 0.3)))))
     return s.finalize_size()
 
 
@@ -290,7 +427,8 @@ def ray_batch(scene_vertices, scene_faces, n, seed=13, width=1024, camera=None):
     Returns an (n, 8) float32 array in gprt_ray layout."""
     rng = np.random.default_rng(seed)
     half = n // 2
-    cam = camera or CameraConfig(center=(0.0, 0.6, 3.4), look_at=(0.0, -0.15, 0.0), width=width)
+    cam = camera or CameraConfig(center=(0.0, 0.6, 3.4), look_at=(0.0, -0.15, 0.0), up=(0.0, 1.0, 0.0), width=width,
+                                 aspect_ratio=1.0, vfov=40.0)
     o = np.array(cam.center, dtype=np.float64)
     w = o - np.array(cam.look_at)
     w /= np.linalg.norm(w)

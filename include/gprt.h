@@ -59,18 +59,22 @@ enum gprt_material_kind {
   GPRT_MAT_METAL = 1,      /* pkg/material/metal.go (fuzz clamped to [0,1]) */
   GPRT_MAT_DIELECTRIC = 2, /* pkg/material/dielectric.go */
   GPRT_MAT_EMISSIVE = 3,   /* pkg/material/emissive.go */
-  GPRT_MAT_LAYERED = 4     /* pkg/material/layered.go (outer, inner) */
+  GPRT_MAT_LAYERED = 4,    /* pkg/material/layered.go (outer, inner) */
+  GPRT_MAT_SPOT_EMISSIVE = 5, /* the disc spot light's directional emitter (pkg/lights/disc_spot_light.go:13-51):
+                                 emission, albedo = spot direction (normalised by the library) */
+  GPRT_MAT_MIX = 6             /* pkg/material/mix.go: outer = material 1, inner = material 2 (neither layered nor
+                                  mix), fuzz = ratio (clamped to [0,1]; 0 = all material 1) */
 };
 
 typedef struct gprt_material_desc {
   uint32_t kind;     /* gprt_material_kind */
-  uint32_t outer;    /* LAYERED: material index of the outer layer */
-  uint32_t inner;    /* LAYERED: material index of the inner layer */
+  uint32_t outer;    /* LAYERED: material index of the outer layer; MIX: material 1 */
+  uint32_t inner;    /* LAYERED: material index of the inner layer; MIX: material 2 */
   uint32_t reserved;
   double albedo[3];  /* LAMBERTIAN, METAL */
-  double fuzz;       /* METAL */
+  double fuzz;       /* METAL; MIX: the ratio */
   double ior;        /* DIELECTRIC */
-  double emission[3];/* EMISSIVE */
+  double emission[3];/* EMISSIVE, SPOT_EMISSIVE */
 } gprt_material_desc;
 
 enum gprt_shape_kind {
@@ -108,15 +112,25 @@ enum gprt_light_kind {
   GPRT_LIGHT_QUAD = 0,              /* pkg/lights/quad_light.go; shape = a QUAD shape */
   GPRT_LIGHT_SPHERE = 1,            /* pkg/lights/sphere_light.go; shape = a SPHERE shape */
   GPRT_LIGHT_UNIFORM_INFINITE = 2,  /* pkg/lights/uniform_infinite_light.go; color_a = emission */
-  GPRT_LIGHT_GRADIENT_INFINITE = 3  /* pkg/lights/gradient_infinite_light.go; color_a = top, color_b = bottom */
+  GPRT_LIGHT_GRADIENT_INFINITE = 3, /* pkg/lights/gradient_infinite_light.go; color_a = top, color_b = bottom */
+  GPRT_LIGHT_DISC = 4,              /* pkg/lights/disc_light.go; shape = a DISC shape with an emissive material */
+  GPRT_LIGHT_DISC_SPOT = 5,         /* pkg/lights/disc_spot_light.go (scene.AddSpotLight); shape = the DISC at
+                                       `from` facing `to` whose material is SPOT_EMISSIVE; color_a = emission,
+                                       from, to, cone_deg, cone_delta_deg */
+  GPRT_LIGHT_POINT_SPOT = 6         /* pkg/lights/point_spot_light.go (scene.AddPointSpotLight); no shape;
+                                       color_a = emission, from, to, cone_deg, cone_delta_deg */
 };
 
 typedef struct gprt_light_desc {
   uint32_t kind;   /* gprt_light_kind */
-  uint32_t shape;  /* QUAD / SPHERE: index of the shape holding the geometry and emissive material */
+  uint32_t shape;  /* QUAD / SPHERE / DISC / DISC_SPOT: index of the shape holding the geometry and material */
   double color_a[3];
   double color_b[3];
   double weight;   /* light-sampler weight; used when gprt_scene_desc.weighted_sampler != 0 */
+  double from[3];  /* spot lights: position (disc centre) */
+  double to[3];    /* spot lights: the point aimed at */
+  double cone_deg;       /* spot lights: total cone angle, degrees */
+  double cone_delta_deg; /* spot lights: falloff transition angle, degrees */
 } gprt_light_desc;
 
 /* geometry.CameraConfig, pkg/geometry/camera.go:18-32 */

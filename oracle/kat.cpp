@@ -875,10 +875,182 @@ void rendererTests() {
 
 }  // namespace
 
+// Point spot, disc and disc spot lights (pkg/lights/point_spot_light_test.go,
+// disc_light_test.go, disc_spot_light_test.go).  Where the reference draws
+// its sample points from math/rand, a fixed grid of sample points stands in;
+// the checked properties are the reference's.
+void spotLightTests() {
+  const double pi = kPi;
+  std::vector<Vec2> grid;
+  for (int i = 0; i < 10; i++)
+    for (int j = 0; j < 10; j++) grid.push_back(Vec2((i + 0.37) / 10.0, (j + 0.61) / 10.0));
+  {  // TestPointSpotLight_NewPointSpotLight (point_spot_light_test.go:11-48)
+    PointSpotLight l(Vec3(0, 5, 0), Vec3(0, 0, 0), Vec3(1, 1, 1), 45.0, 5.0);
+    check(l.direction.sub(Vec3(0, -1, 0)).length() < 1e-6 && std::fabs(l.cosTotal - std::cos(45.0 * pi / 180)) < 1e-6 &&
+              std::fabs(l.cosStart - std::cos(40.0 * pi / 180)) < 1e-6,
+          "point_spot_light_test.go:11 TestPointSpotLight_NewPointSpotLight");
+  }
+  {  // TestPointSpotLight_Sample_WithinCone (:50-94)
+    PointSpotLight l(Vec3(0, 5, 0), Vec3(0, 0, 0), Vec3(100, 100, 100), 60.0, 5.0);
+    Vec3 tp(0, 1, 0);
+    LightSample s = l.sample(tp, Vec3(0, 1, 0), Vec2(0.3, 0.7));
+    double d = 4.0;
+    check(s.point.sub(Vec3(0, 5, 0)).length() < 1e-6 && s.direction.sub(Vec3(0, 1, 0)).length() < 1e-6 &&
+              std::fabs(s.distance - d) < 1e-6 &&
+              std::fabs(s.emission.length() - Vec3(100, 100, 100).length() / (d * d)) < 1e-6 && s.pdf == 1.0,
+          "point_spot_light_test.go:50 TestPointSpotLight_Sample_WithinCone");
+  }
+  {  // TestPointSpotLight_Sample_OutsideCone (:96-118)
+    PointSpotLight l(Vec3(0, 5, 0), Vec3(0, 0, 0), Vec3(100, 100, 100), 30.0, 5.0);
+    LightSample s = l.sample(Vec3(10, 1, 0), Vec3(0, 1, 0), Vec2(0.3, 0.7));
+    check(s.emission.length() <= 0.1, "point_spot_light_test.go:96 TestPointSpotLight_Sample_OutsideCone");
+  }
+  {  // TestPointSpotLight_PDF (:120-147)
+    PointSpotLight l(Vec3(0, 5, 0), Vec3(0, 0, 0), Vec3(100, 100, 100), 60.0, 5.0);
+    Vec3 tp(0, 1, 0), n(0, 1, 0), toL = Vec3(0, 5, 0).sub(tp).normalize();
+    check(l.pdf(tp, n, toL) == 1.0 && l.pdf(tp, n, toL.mul(-1)) == 0.0 && l.pdf(tp, n, Vec3(1, 0, 0)) == 0.0,
+          "point_spot_light_test.go:120 TestPointSpotLight_PDF");
+  }
+  Emissive e10(Vec3(10, 10, 10)), e5(Vec3(5, 5, 5)), e1(Vec3(1, 1, 1));
+  {  // TestDiscLightSample (disc_light_test.go:12-54)
+    Disc d(Vec3(0, 1, 0), Vec3(0, -1, 0), 1.0, &e10);
+    DiscLight l(&d);
+    bool ok = true;
+    for (Vec2 u : grid) {
+      LightSample s = l.sample(Vec3(0, 0, 0), Vec3(0, 1, 0), u);
+      ok = ok && s.point.sub(d.center).length() <= 1.0 + 1e-6 &&
+           s.direction.sub(s.point.normalize()).length() < 1e-12 && std::fabs(s.distance - s.point.length()) < 1e-6 &&
+           s.pdf > 0 && s.emission.length() > 0;
+    }
+    check(ok, "disc_light_test.go:12 TestDiscLightSample");
+  }
+  {  // TestDiscLightPDF (:56-108)
+    Disc d(Vec3(0, 1, 0), Vec3(0, -1, 0), 1.0, &e10);
+    DiscLight l(&d);
+    Vec3 o(0, 0, 0), n(0, 1, 0);
+    check(l.pdf(o, n, Vec3(0, 1, 0)) > 0, "disc_light_test.go:56 TestDiscLightPDF/Direction hits center of disc");
+    check(l.pdf(o, n, Vec3(1, 1, 0).normalize()) > 0, "disc_light_test.go:56 TestDiscLightPDF/Direction hits edge of disc");
+    check(l.pdf(o, n, Vec3(2, 1, 0).normalize()) == 0, "disc_light_test.go:56 TestDiscLightPDF/Direction misses disc");
+    check(l.pdf(o, n, Vec3(1, 0, 0)) == 0, "disc_light_test.go:56 TestDiscLightPDF/Direction parallel to disc");
+  }
+  {  // TestDiscLightSampleConsistency (:110-133)
+    Disc d(Vec3(0, 2, 0), Vec3(0, -1, 0), 0.5, &e5);
+    DiscLight l(&d);
+    bool ok = true;
+    for (Vec2 u : grid) {
+      LightSample s = l.sample(Vec3(0, 0, 0), Vec3(0, 1, 0), u);
+      ok = ok && std::fabs(s.pdf - l.pdf(Vec3(0, 0, 0), Vec3(0, 1, 0), s.direction)) <= 1e-10;
+    }
+    check(ok, "disc_light_test.go:110 TestDiscLightSampleConsistency");
+  }
+  {  // TestDiscLightEdgeCase (:175-204)
+    Disc d(Vec3(0, 1, 0), Vec3(0, -1, 0), 1.0, &e1);
+    DiscLight l(&d);
+    LightSample s = l.sample(Vec3(0, 0.99, 0), Vec3(0, 1, 0), Vec2(0.42, 0.17));
+    check(s.distance > 0 && s.pdf > 0 && s.point.sub(d.center).length() <= 1.0 + 1e-6,
+          "disc_light_test.go:175 TestDiscLightEdgeCase");
+  }
+  {  // TestDiscLight_SampleEmission (:206-273), TestDiscLight_EmissionSampling_Coverage (:351-410)
+    Disc d(Vec3(0, 0, 0), Vec3(0, 1, 0), 1.0, &e5);
+    DiscLight l(&d);
+    bool ok = true;
+    int centre = 0;
+    for (size_t k = 0; k < grid.size(); k++) {
+      EmissionSample s = l.sampleEmission(grid[k], grid[(k * 37 + 11) % grid.size()]);
+      double ct = s.direction.dot(s.normal);
+      double pp, pd;
+      l.pdfLe(s.point, s.direction, pp, pd);
+      ok = ok && s.point.length() <= 1.0 + 1e-9 && std::fabs(s.point.y) <= 1e-9 &&
+           s.normal.sub(Vec3(0, 1, 0)).length() <= 1e-9 && ct > 0 && std::fabs(s.direction.length() - 1) <= 1e-9 &&
+           std::fabs(s.areaPdf - 1.0 / pi) <= 1e-9 && std::fabs(s.directionPdf - ct / pi) <= 1e-9 &&
+           s.emission.x == 5.0 && s.emission.y == 5.0 && s.emission.z == 5.0 && std::fabs(s.areaPdf - pp) <= 1e-6;
+      centre += s.point.length() <= 0.5;
+    }
+    check(ok, "disc_light_test.go:206 TestDiscLight_SampleEmission");
+    check(std::fabs(centre / (double)grid.size() - 0.25) <= 0.1, "disc_light_test.go:351 TestDiscLight_EmissionSampling_Coverage");
+  }
+  {  // TestDiscLight_EmissionPDF (:275-349)
+    Disc d(Vec3(0, 0, 0), Vec3(0, 1, 0), 1.0, &e1);
+    DiscLight l(&d);
+    struct Cs { const char* n; Vec3 p, dir; bool expect; };
+    Cs cs[] = {{"Point on disc, direction in hemisphere", Vec3(0.5, 0, 0), Vec3(0, 1, 0), true},
+               {"Point on disc, direction below surface", Vec3(0.5, 0, 0), Vec3(0, -1, 0), false},
+               {"Point outside disc radius", Vec3(2, 0, 0), Vec3(0, 1, 0), false},
+               {"Point above disc plane", Vec3(0.5, 1, 0), Vec3(0, 1, 0), false},
+               {"Point at disc center", Vec3(0, 0, 0), Vec3(0, 1, 0), true}};
+    for (const Cs& c : cs) {
+      double pp, pd;
+      l.pdfLe(c.p, c.dir, pp, pd);
+      bool ok = c.expect ? std::fabs(pp - 1.0 / pi) <= 1e-9 : pp == 0;
+      check(ok, std::string("disc_light_test.go:275 TestDiscLight_EmissionPDF/") + c.n);
+    }
+  }
+  {  // TestDiscSpotLightFalloff (disc_spot_light_test.go:11-76)
+    double ct = std::cos(30 * pi / 180), cs = std::cos(25 * pi / 180);
+    double mid = std::cos(27.5 * pi / 180);
+    double dm = (mid - ct) / (cs - ct);
+    struct Fc { const char* n; double c, want; };
+    Fc fc[] = {{"Inside inner cone", std::cos(20 * pi / 180), 1.0},
+               {"At falloff start edge", std::cos(25 * pi / 180), 1.0},
+               {"In falloff region", mid, dm * dm * dm * dm},
+               {"At total width edge", std::cos(30 * pi / 180), 0.0},
+               {"Outside cone", std::cos(35 * pi / 180), 0.0}};
+    for (const Fc& f : fc)
+      check(std::fabs(spotFalloff(f.c, ct, cs) - f.want) <= 1e-6,
+            std::string("disc_spot_light_test.go:11 TestDiscSpotLightFalloff/") + f.n);
+  }
+  {  // TestDiscSpotLightSample (:78-144)
+    Vec3 from(0, 2, 0), to(0, 0, 0);
+    Vec3 dir = to.sub(from).normalize();
+    SpotEmissive m(Vec3(5, 5, 5), dir);
+    Disc d(from, dir, 0.2, &m);
+    DiscSpotLight l(&d, from, to, Vec3(5, 5, 5), 45.0, 10.0);
+    struct Sc { const char* n; Vec3 p; bool expect; };
+    Sc cs[] = {{"Point directly below", Vec3(0, 0, 0), true},
+               {"Point at edge of inner cone", Vec3(0.7, 0, 0), true},
+               {"Point in falloff region", Vec3(1.0, 0, 0), true},
+               {"Point outside cone", Vec3(3.0, 0, 0), false}};
+    for (const Sc& c : cs) {
+      bool ok = true;
+      for (Vec2 u : grid) {
+        LightSample s = l.sample(c.p, Vec3(0, 1, 0), u);
+        bool lit = s.emission.length() > 0;
+        ok = ok && s.point.sub(from).length() <= 0.2 + 1e-6 && (c.expect ? lit && s.pdf > 0 : !lit);
+      }
+      check(ok, std::string("disc_spot_light_test.go:78 TestDiscSpotLightSample/") + c.n);
+    }
+  }
+  {  // TestDiscSpotLightConsistentFalloff (:256-317): the falloff follows the sampled point
+    Vec3 from(0, 3, 0), to(0, 0, 0);
+    Vec3 dir = to.sub(from).normalize();
+    SpotEmissive m(Vec3(10, 10, 10), dir);
+    Disc d(from, dir, 1.5, &m);
+    DiscSpotLight l(&d, from, to, Vec3(10, 10, 10), 30.0, 5.0);
+    Vec3 tp(1.5, 0, 0);
+    Vec3 a = l.sample(tp, Vec3(0, 1, 0), Vec2(0.0, 0.0)).emission;
+    // the disc's `up` axis is +x here: theta = pi/2 is the edge nearest the point, 3pi/2 the farthest
+    Vec3 b = l.sample(tp, Vec3(0, 1, 0), Vec2(1.0, 0.25)).emission;
+    Vec3 c = l.sample(tp, Vec3(0, 1, 0), Vec2(1.0, 0.75)).emission;
+    check(!(a.sub(b).length() == 0 && a.sub(c).length() == 0) && c.length() < b.length(),
+          "disc_spot_light_test.go:256 TestDiscSpotLightConsistentFalloff");
+  }
+  {  // TestDiscSpotLightCreation (:319-366)
+    Vec3 from(1, 2, 3), to(4, 5, 6);
+    SpotEmissive m(Vec3(2, 3, 4), to.sub(from).normalize());
+    Disc d(from, to.sub(from), 0.3, &m);
+    DiscSpotLight l(&d, from, to, Vec3(2, 3, 4), 25.0, 8.0);
+    check(l.position.sub(from).length() == 0 && l.direction.sub(to.sub(from).normalize()).length() == 0 &&
+              std::fabs(l.cosTotal - std::cos(25 * pi / 180)) <= 1e-6 &&
+              std::fabs(l.cosStart - std::cos(17 * pi / 180)) <= 1e-6 && l.base.disc->radius == 0.3,
+          "disc_spot_light_test.go:319 TestDiscSpotLightCreation");
+  }
+}
+
 int main() {
   try {
     geometryTests();
     quadricTests();
+    spotLightTests();
     materialLightTests();
     bdptTests();
     rendererTests();

@@ -29,12 +29,27 @@ Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
       case GPRT_MAT_METAL: s->materials[i] = std::make_unique<Metal>(v3(m.albedo), m.fuzz); break;
       case GPRT_MAT_DIELECTRIC: s->materials[i] = std::make_unique<Dielectric>(m.ior); break;
       case GPRT_MAT_EMISSIVE: s->materials[i] = std::make_unique<Emissive>(v3(m.emission)); break;
+      case GPRT_MAT_SPOT_EMISSIVE:
+        s->materials[i] = std::make_unique<SpotEmissive>(v3(m.emission), v3(m.albedo).normalize());
+        break;
       case GPRT_MAT_LAYERED: break;
+      case GPRT_MAT_MIX: break;
       default: err = "unknown material kind"; return nullptr;
     }
   }
   for (uint32_t i = 0; i < d->n_materials; i++) {
     const gprt_material_desc& m = d->materials[i];
+    if (m.kind == GPRT_MAT_MIX) {
+      auto basic = [&](uint32_t k) {
+        return k < d->n_materials && d->materials[k].kind != GPRT_MAT_LAYERED && d->materials[k].kind != GPRT_MAT_MIX;
+      };
+      if (!basic(m.outer) || !basic(m.inner)) {
+        err = "mix material must reference two non-layered, non-mix materials";
+        return nullptr;
+      }
+      s->materials[i] = std::make_unique<Mix>(s->materials[m.outer].get(), s->materials[m.inner].get(), m.fuzz);
+      continue;
+    }
     if (m.kind != GPRT_MAT_LAYERED) continue;
     if (m.outer >= d->n_materials || m.inner >= d->n_materials || !s->materials[m.outer] ||
         !s->materials[m.inner]) {
@@ -114,6 +129,22 @@ Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
         light = std::make_unique<SphereLight>(static_cast<const Sphere*>(s->shapes[l.shape]));
         break;
       }
+      case GPRT_LIGHT_DISC:
+      case GPRT_LIGHT_DISC_SPOT: {
+        if (l.shape >= d->n_shapes || d->shapes[l.shape].kind != GPRT_SHAPE_DISC) {
+          err = "disc lights must reference a disc shape";
+          return nullptr;
+        }
+        const Disc* disc = static_cast<const Disc*>(s->shapes[l.shape]);
+        if (l.kind == GPRT_LIGHT_DISC)
+          light = std::make_unique<DiscLight>(disc);
+        else
+          light = std::make_unique<DiscSpotLight>(disc, v3(l.from), v3(l.to), v3(l.color_a), l.cone_deg, l.cone_delta_deg);
+        break;
+      }
+      case GPRT_LIGHT_POINT_SPOT:
+        light = std::make_unique<PointSpotLight>(v3(l.from), v3(l.to), v3(l.color_a), l.cone_deg, l.cone_delta_deg);
+        break;
       case GPRT_LIGHT_UNIFORM_INFINITE: light = std::make_unique<UniformInfiniteLight>(v3(l.color_a)); break;
       case GPRT_LIGHT_GRADIENT_INFINITE:
         light = std::make_unique<GradientInfiniteLight>(v3(l.color_a), v3(l.color_b));

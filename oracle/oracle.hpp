@@ -477,6 +477,26 @@ struct Emissive : Material {
   }
 };
 
+// discSpotLightMaterial (disc_spot_light.go:13-62): emits its base emission
+// from the front face, and only towards rays travelling against the spot
+// direction (cosine with it below -0.3, the ray direction as given)
+struct SpotEmissive : Material {
+  Vec3 emission, direction;
+  SpotEmissive(Vec3 e, Vec3 d) : emission(e), direction(d) {}
+  bool scatter(const Ray&, const SurfaceInteraction&, Sampler&, ScatterResult&) const override { return false; }
+  Vec3 evaluateBRDF(const Vec3&, const Vec3&, const SurfaceInteraction*, TransportMode) const override { return {}; }
+  double pdf(const Vec3&, const Vec3&, const Vec3&, bool& isDelta) const override {
+    isDelta = false;
+    return 0.0;
+  }
+  bool isEmitter() const override { return true; }
+  Vec3 emit(const Ray& r, const SurfaceInteraction* hit) const override {
+    if (hit != nullptr && !hit->frontFace) return {};
+    if (r.direction.dot(direction) > -0.3) return {};
+    return emission;
+  }
+};
+
 // isReflectionPath (layered.go:110-119)
 inline bool isReflectionPath(const Vec3& in, const Vec3& out, const Vec3& n) {
   Vec3 inc = in.negate();
@@ -524,6 +544,30 @@ struct Layered : Material {
     double p = isReflectionPath(in, out, n) ? outer->pdf(in, out, n, d) : inner->pdf(in, out, n, d);
     isDelta = false;
     return p;
+  }
+};
+
+// Mix (mix.go:9-59): one uniform number picks the material that scatters
+// (material 2 below the ratio); BRDF and pdf are the ratio-weighted blends,
+// never delta
+struct Mix : Material {
+  const Material* m1;
+  const Material* m2;
+  double ratio;
+  Mix(const Material* a, const Material* b, double r) : m1(a), m2(b), ratio(std::max(0.0, std::min(r, 1.0))) {}
+  bool scatter(const Ray& in, const SurfaceInteraction& hit, Sampler& s, ScatterResult& out) const override {
+    if (s.get1D() < ratio) return m2->scatter(in, hit, s, out);
+    return m1->scatter(in, hit, s, out);
+  }
+  Vec3 evaluateBRDF(const Vec3& in, const Vec3& out, const SurfaceInteraction* hit,
+                    TransportMode mode) const override {
+    return m1->evaluateBRDF(in, out, hit, mode).mul(1.0 - ratio).add(m2->evaluateBRDF(in, out, hit, mode).mul(ratio));
+  }
+  double pdf(const Vec3& in, const Vec3& out, const Vec3& n, bool& isDelta) const override {
+    bool d;
+    double p1 = m1->pdf(in, out, n, d), p2 = m2->pdf(in, out, n, d);
+    isDelta = false;
+    return p1 * (1.0 - ratio) + p2 * ratio;
   }
 };
 
@@ -1572,6 +1616,173 @@ struct GradientInfiniteLight : Light {
   void preprocess(const Vec3& c, double r) override {
     worldCenter = c;
     worldRadius = r;
+  }
+};
+
+// Spot falloff shared by the point and disc spot lights
+// (point_spot_light.go:140-158, disc_spot_light.go:150-168): 0 outside the
+// cone, 1 inside the inner cone, a quartic of the cosine ramp between
+inline double spotFalloff(double cosAngle, double cosTotal, double cosStart) {
+  if (cosAngle < cosTotal) return 0.0;
+  if (cosAngle >= cosStart) return 1.0;
+  double d = (cosAngle - cosTotal) / (cosStart - cosTotal);
+  return d * d * d * d;
+}
+
+// DiscLight (disc_light.go:12-165)
+struct DiscLight : Light {
+  const Disc* disc;
+  explicit DiscLight(const Disc* d) : disc(d) {}
+  LightType type() const override { return LightType::Area; }
+  double areaPdf() const { return 1.0 / (kPi * disc->radius * disc->radius); }
+  // Disc.SampleUniform (disc.go:120-134)
+  Vec3 samplePoint(Vec2 s) const {
+    double r = std::sqrt(s.x) * disc->radius;
+    double th = 2.0 * kPi * s.y;
+    return disc->center.add(disc->right.mul(r * std::cos(th))).add(disc->up.mul(r * std::sin(th)));
+  }
+  Vec3 emit(const Ray& r, const SurfaceInteraction* hit) const override {
+    if (disc->material && disc->material->isEmitter()) return disc->material->emit(r, hit);
+    return {};
+  }
+  LightSample sample(const Vec3& p, const Vec3&, Vec2 s) const override {
+    LightSample ls;
+    Vec3 sp = samplePoint(s);
+    Vec3 to = sp.sub(p);
+    double dist = to.length();
+    Vec3 dir = to.normalize();
+    ls.point = sp;
+    ls.normal = disc->normal;
+    if (dist == 0) {
+      ls.direction = Vec3(0, 1, 0);
+      ls.distance = 0;
+      ls.pdf = 1.0;
+      return ls;
+    }
+    double pdf = areaPdf();
+    double ct = std::fabs(disc->normal.dot(dir.mul(-1)));
+    ls.pdf = ct < 1e-6 ? 0.0 : pdf * dist * dist / ct;
+    ls.direction = dir;
+    ls.distance = dist;
+    ls.emission = emit(Ray(p, dir), nullptr);
+    return ls;
+  }
+  double pdf(const Vec3& p, const Vec3&, const Vec3& dir) const override {
+    SurfaceInteraction h;
+    if (!disc->hit(Ray(p, dir), 0.001, kInf, h)) return 0.0;
+    double ct = std::fabs(disc->normal.dot(dir.mul(-1)));
+    if (ct < 1e-6) return 0.0;
+    return areaPdf() * h.t * h.t / ct;
+  }
+  EmissionSample sampleEmission(Vec2 sp, Vec2 sd) const override {
+    return sampleEmissionDirection(samplePoint(sp), disc->normal, areaPdf(), disc->material, sd);
+  }
+  void pdfLe(const Vec3& p, const Vec3& dir, double& pdfPos, double& pdfDir) const override {
+    pdfPos = pdfDir = 0;
+    // validatePointOnDisc (disc_light.go:153-165), tolerance 0.001
+    Vec3 tp = p.sub(disc->center);
+    double h = tp.dot(disc->normal);
+    if (std::fabs(h) > 0.001) return;
+    if (tp.sub(disc->normal.mul(h)).length() > disc->radius) return;
+    if (dir.dot(disc->normal) <= 0) return;
+    pdfPos = areaPdf();
+    pdfDir = dir.dot(disc->normal) / kPi;
+  }
+};
+
+// DiscSpotLight (disc_spot_light.go:64-283): a DiscLight whose disc carries
+// the directional SpotEmissive material
+struct DiscSpotLight : Light {
+  Vec3 position, direction, emission;
+  double cosTotal, cosStart;
+  DiscLight base;
+  DiscSpotLight(const Disc* d, Vec3 from, Vec3 to, Vec3 e, double coneDeg, double deltaDeg)
+      : position(from), direction(to.sub(from).normalize()), emission(e), base(d) {
+    cosTotal = std::cos(coneDeg * kPi / 180.0);
+    cosStart = std::cos((coneDeg - deltaDeg) * kPi / 180.0);
+  }
+  LightType type() const override { return LightType::Area; }
+  Vec3 emit(const Ray& r, const SurfaceInteraction* hit) const override { return base.emit(r, hit); }
+  LightSample sample(const Vec3& p, const Vec3& n, Vec2 s) const override {
+    LightSample ls = base.sample(p, n, s);
+    Vec3 lightToPoint = p.sub(ls.point).normalize();
+    ls.emission = ls.emission.mul(spotFalloff(direction.dot(lightToPoint), cosTotal, cosStart));
+    return ls;
+  }
+  double pdf(const Vec3& p, const Vec3& n, const Vec3& dir) const override { return base.pdf(p, n, dir); }
+  EmissionSample sampleEmission(Vec2 sp, Vec2 sd) const override {
+    EmissionSample e;
+    e.point = base.samplePoint(sp);
+    e.normal = base.disc->normal;
+    e.direction = sampleCone(direction, cosTotal, sd);
+    e.emission = emission.mul(spotFalloff(e.direction.dot(direction), cosTotal, cosStart));
+    e.areaPdf = base.areaPdf();
+    e.directionPdf = 1.0 / (2.0 * kPi * (1.0 - cosTotal));  // UniformConePDF (light_sampling.go:83-85)
+    return e;
+  }
+  void pdfLe(const Vec3& p, const Vec3& dir, double& pdfPos, double& pdfDir) const override {
+    double bp, bd;
+    base.pdfLe(p, dir, bp, bd);
+    pdfPos = pdfDir = 0;
+    if (bp == 0.0 || bd == 0.0) return;
+    pdfPos = bp;
+    if (dir.dot(direction) < cosTotal) return;
+    pdfDir = bd;
+  }
+};
+
+// PointSpotLight (point_spot_light.go:10-222): a delta light
+struct PointSpotLight : Light {
+  Vec3 position, direction, emission;
+  double cosTotal, cosStart;
+  PointSpotLight(Vec3 from, Vec3 to, Vec3 e, double coneDeg, double deltaDeg)
+      : position(from), direction(to.sub(from).normalize()), emission(e) {
+    cosTotal = std::cos(coneDeg * kPi / 180.0);
+    cosStart = std::cos((coneDeg - deltaDeg) * kPi / 180.0);
+  }
+  LightType type() const override { return LightType::Point; }
+  Vec3 emit(const Ray&, const SurfaceInteraction*) const override { return emission; }
+  LightSample sample(const Vec3& p, const Vec3&, Vec2) const override {
+    LightSample ls;
+    ls.point = position;
+    Vec3 to = position.sub(p);
+    double dist = to.length();
+    ls.pdf = 1.0;
+    if (dist == 0) {
+      ls.normal = Vec3(0, 1, 0);
+      ls.direction = Vec3(0, 1, 0);
+      ls.distance = 0;
+      return ls;
+    }
+    Vec3 toLight = to.normalize();
+    double att = spotFalloff(direction.dot(toLight.mul(-1)), cosTotal, cosStart);
+    ls.emission = emission.mul(att / (dist * dist));
+    ls.normal = toLight.mul(-1);
+    ls.direction = toLight;
+    ls.distance = dist;
+    return ls;
+  }
+  double pdf(const Vec3& p, const Vec3&, const Vec3& dir) const override {
+    Vec3 to = position.sub(p);
+    if (to.length() == 0) return 0.0;
+    return dir.dot(to.normalize()) > 0.999 ? 1.0 : 0.0;
+  }
+  EmissionSample sampleEmission(Vec2, Vec2 sd) const override {
+    EmissionSample e;
+    e.point = position;
+    e.direction = sampleCone(direction, cosTotal, sd);
+    e.normal = e.direction;
+    e.emission = emission.mul(spotFalloff(e.direction.dot(direction), cosTotal, cosStart));
+    e.areaPdf = 1.0;
+    e.directionPdf = 1.0 / (2.0 * kPi * (1.0 - cosTotal));
+    return e;
+  }
+  void pdfLe(const Vec3& p, const Vec3& dir, double& pdfPos, double& pdfDir) const override {
+    pdfPos = pdfDir = 0;
+    if (p.sub(position).length() > 0.001) return;
+    if (dir.dot(direction) < cosTotal) return;
+    pdfPos = 1.0;
+    pdfDir = 1.0 / (2.0 * kPi * (1.0 - cosTotal));
   }
 };
 

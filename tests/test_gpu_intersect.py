@@ -77,7 +77,14 @@ SCENES = {
     "icosphere6": lambda s: s.icosphere_scene(level=6, width=64),
     "spheres17": lambda s: s.default_style_scene(17, 64, 64),
     "quadrics": lambda s: s.quadric_scene(64),
+    "cone_test": lambda s: s.cone_test_scene(_cam(64)),
+    "cylinder_test": lambda s: s.cylinder_test_scene(_cam(64)),
 }
+
+
+def _cam(w):
+    from gprt.scene import CameraConfig
+    return CameraConfig(width=w)
 
 
 @pytest.mark.parametrize("name", sorted(SCENES))

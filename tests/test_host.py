@@ -38,7 +38,8 @@ def _validate(flat):
 
 
 @pytest.mark.parametrize("name", ["cornell_baseline", "cornell_spheres", "cornell_boxes", "default", "icosphere5",
-                                  "spheres17", "quadrics"])
+                                  "spheres17", "quadrics", "spot_disc", "cornell_point",
+                                  "cone_test", "cylinder_test", "spheregrid"])
 def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
     from gprt import scenes
     s = {"cornell_baseline": lambda: scenes.cornell_baseline(64),
@@ -47,7 +48,12 @@ def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
          "default": lambda: scenes.default_scene(),
          "icosphere5": lambda: scenes.icosphere_scene(level=5, width=64),
          "spheres17": lambda: scenes.default_style_scene(17, 64, 64),
-         "quadrics": lambda: scenes.quadric_scene(64)}[name]()
+         "quadrics": lambda: scenes.quadric_scene(64),
+         "spot_disc": lambda: scenes.spot_scene(48),
+         "cornell_point": lambda: scenes.cornell_scene(scenes.CORNELL_BOXES, scenes.CORNELL_POINT_LIGHT),
+         "cone_test": lambda: scenes.cone_test_scene(),
+         "cylinder_test": lambda: scenes.cylinder_test_scene(),
+         "spheregrid": lambda: scenes.sphere_grid_scene(12, "mixed")}[name]()
     flat = s.to_desc()
     rc, info, err = _validate(flat)
     assert rc == 0, err
@@ -95,8 +101,12 @@ def test_camera_height_and_merge():
     from gprt.scene import CameraConfig
     c = CameraConfig(width=400, aspect_ratio=16 / 9)
     assert c.height == 225  # int(400 / (16/9)), camera.go:91
-    m = CameraConfig(width=400).merged(CameraConfig(width=512))
-    assert m.width == 512 and m.vfov == 40.0
+    base = CameraConfig(center=(278.0, 278.0, -800.0), look_at=(278.0, 278.0, 0.0), up=(0.0, 1.0, 0.0), width=400,
+                        aspect_ratio=1.0, vfov=40.0)
+    m = base.merged(CameraConfig(width=512))
+    # a partly filled override changes only the fields it names (camera.go:320-349)
+    assert m.width == 512 and m.vfov == 40.0 and m.look_at == (278.0, 278.0, 0.0) and m.up == (0.0, 1.0, 0.0)
+    assert base.merged(CameraConfig(look_at=(1.0, 2.0, 3.0))).look_at == (1.0, 2.0, 3.0)
 
 
 def test_flat_scene_material_dedup():
