@@ -138,6 +138,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def l2_absorption(traffic, alg_bytes, avg_ms, peak):
+    """How much of a traversal launch's algorithmic bytes reach DRAM (the
+    ncu traffic per launch scaled to the timed launch) and the DRAM-side
+    fraction of the HBM peak.  The upper BVH levels and, for scenes of a
+    few hundred spheres, whole trees stay in the 129 MB L2, so the
+    algorithmic fraction can exceed 1 while DRAM is far from busy: the
+    kernel is then bound by L2 and memory latency, not HBM bandwidth."""
+    if not traffic or not alg_bytes or not avg_ms:
+        return {}
+    dram_gbs = traffic / (avg_ms / 1e3) / 1e9
+    return {"dram_share_of_alg_bytes": traffic / alg_bytes, "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak}
+
+
 def committed_traffic(name, rays_per_launch):
     """DRAM bytes per launch of the extend kernel: the committed ncu capture's
     DRAM bytes per ray (a smaller case of the same kernel) x rays per launch."""
@@ -418,7 +431,8 @@ def bvh_stress(ctx, flat, torch):
            "msamples_per_s": npix * ICO_SPP * steps / (ms / 1e3) / 1e6, "ms_per_frame": ms / steps,
            "mrays_per_s": (cnt["extend_rays"] + cnt["shadow_rays"]) * steps / (ms / 1e3) / 1e6,
            "extend_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                               "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms},
+                               "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
+                               **l2_absorption(traffic, per_launch, avg_ms, peak)},
            "host_bvh_build_ms": g.info.build_ms,
            "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
     job.close()
@@ -547,6 +561,7 @@ def run_gprt(args):
             "rays_per_launch": cnt["extend_rays"] / max(1, launches_counted),
             "box_tests_per_ray": cnt["extend_boxes"] / max(1, cnt["extend_rays"]),
             "sphere_tests_per_ray": cnt["extend_prims"] / max(1, cnt["extend_rays"])}
+    roof.update(l2_absorption(traffic, per_launch, avg_ms, peak))
     kernel_ms = {k: kc[k + "_ms"] / args.steps for k in ("extend", "shade", "shadow", "other")}
 
     # the plain per-job path on the same batch (host clock around device-synchronised jobs)

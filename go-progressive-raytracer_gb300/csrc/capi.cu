@@ -26,6 +26,8 @@ int ensure_bdpt(gprt_job* j) {
   rc |= dev_alloc(ctx, b, &B.meta, ns);
   rc |= dev_alloc(ctx, b, &B.masks, ns);
   rc |= dev_alloc(ctx, b, &B.contrib, (size_t)ns * (B.maxv + 1) * B.maxv);
+  B.uv = nullptr;
+  if (j->scene->dev.has_textures) rc |= dev_alloc(ctx, b, &B.uv, (size_t)ns * 2 * B.maxv);
   if (rc) return GPRT_E_OOM;
   P.stats = nullptr;
   P.variant = 0;
@@ -293,6 +295,9 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   }
   rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
   rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tex_info, &d.tex_info, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.texels, &d.texels, &s->bytes);
+  d.has_textures = h.tex_info.empty() ? 0 : 1;
   if (rc) {
     free_all(s->buffers);
     return rc;

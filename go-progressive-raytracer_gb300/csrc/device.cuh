@@ -657,43 +657,82 @@ struct Surface {
   float3 p, n;
   bool front;
   int mat;
+  float2 uv;  // SurfaceInteraction.UV, set when the scene has textures
 };
+
+// UV of a point on a cylinder / cone body (cylinder.go:187-205, cone.go:234-253)
+__device__ __forceinline__ float2 axial_uv(float3 axis, float3 radial, float h, float height) {
+  float3 ref = fabsf(axis.y) < 0.9f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+  float3 tangent = normalize(cross(axis, ref));
+  float3 bitangent = cross(axis, tangent);
+  float a = atan2f(dot(radial, bitangent), dot(radial, tangent));
+  return make_float2((a + kPi) / (2.f * kPi), h / height);
+}
+// UV of a point on a cap of outward normal n (cylinder.go:241-255, cone.go:322-339)
+__device__ __forceinline__ float2 cap_uv(float3 n, float3 c, float r, float3 p) {
+  float3 ref = fabsf(n.y) < 0.9f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+  float3 tangent = normalize(cross(n, ref));
+  float3 bitangent = cross(n, tangent);
+  float3 l = p - c;
+  return make_float2((dot(l, tangent) / r + 1.f) * 0.5f, (dot(l, bitangent) / r + 1.f) * 0.5f);
+}
 
 __device__ __forceinline__ void surface_at(const DevScene& sc, float3 o, float3 d, const Hit& h, Surface& s) {
   s.p = o + d * h.t;  // Ray.At (pkg/core/vec3.go:216-218)
   float3 outward;
   uint32_t p = h.prim;
+  const bool uv = sc.has_textures;
   if (p < sc.quad_base) {
     const float4* T = sc.tris + (size_t)p * 3;
     float4 a = __ldg(T);
     float4 nn = __ldg(sc.tri_normals + p);
     outward = f3(nn);  // precomputed normalize(e1 x e2) (triangle.go:92-99)
     s.mat = __float_as_int(a.w);
+    if (uv) s.uv = make_float2(h.u, h.v);  // barycentrics (triangle.go:151-161)
   } else if (p < sc.sphere_base) {
     const float4* Q = sc.quads + (size_t)(p - sc.quad_base) * 5;
     outward = f3(__ldg(Q + 3));
     s.mat = __float_as_int(__ldg(Q + 1).w);
+    if (uv) s.uv = make_float2(h.u, h.v);  // (alpha, beta) (quad.go:165-166)
   } else if (p < sc.quadric_base) {
     const float4* S = sc.spheres + (size_t)(p - sc.sphere_base) * 2;
     float4 c = __ldg(S);
     outward = (s.p - f3(c)) * (1.0f / c.w);  // (p - c) / r (sphere.go:62)
     s.mat = __float_as_int(__ldg(S + 1).x);
+    if (uv) {  // spherical angles (sphere.go:64-68)
+      float theta = acosf(fminf(1.f, fmaxf(-1.f, -outward.y)));
+      float phi = atan2f(-outward.z, outward.x) + kPi;
+      s.uv = make_float2(phi / (2.f * kPi), theta / kPi);
+    }
   } else {
     const float4* Q = sc.quadrics + (size_t)(p - sc.quadric_base) * 5;
     float4 g0 = __ldg(Q), g1 = __ldg(Q + 1), g4 = __ldg(Q + 4);
     float3 axis = f3(g1);
     int kind = __float_as_int(g4.x);
     s.mat = __float_as_int(g4.y);
-    if (kind == kQuadricDisc || h.u == 2.f) {
-      outward = axis;  // disc normal, top cap
+    if (kind == kQuadricDisc) {
+      outward = axis;
+      if (uv) {  // disc.go:68-73
+        float3 l = s.p - f3(g0);
+        s.uv = make_float2((dot(l, f3(__ldg(Q + 2))) / g0.w + 1.f) * 0.5f,
+                           (dot(l, f3(__ldg(Q + 3))) / g0.w + 1.f) * 0.5f);
+      }
+    } else if (h.u == 2.f) {
+      outward = axis;  // top cap
+      if (uv) {
+        float4 g2 = __ldg(Q + 2);
+        s.uv = cap_uv(axis, f3(g2), g2.w, s.p);
+      }
     } else if (h.u == 1.f) {
       outward = -axis;  // base cap
+      if (uv) s.uv = cap_uv(-axis, f3(g0), g0.w, s.p);
     } else {
       // body: radial from the axis (cylinder.go:188-191), tilted by the
       // cone's slope (cone.go:240-248)
       float3 base = f3(g0);
       float hh = dot(s.p - base, axis);
       float3 radial = s.p - (base + axis * hh);
+      if (uv) s.uv = axial_uv(axis, radial, hh, g1.w);
       if (kind == kQuadricCone) radial = radial + axis * ((g0.w - __ldg(Q + 2).w) / g1.w);
       outward = normalize(radial);
     }
@@ -704,6 +743,23 @@ __device__ __forceinline__ void surface_at(const DevScene& sc, float3 o, float3 
 
 // ----------------------------------------------------------------- materials
 __device__ __forceinline__ DevMaterial load_material(const DevScene& sc, int m) { return sc.materials[m]; }
+
+// ImageTexture.Evaluate (image_texture.go:25-52): u, v wrapped into [0,1)
+// (Go's int() truncates toward zero), nearest texel, v = 0 at the last row
+__device__ __forceinline__ float3 tex_eval(const DevScene& sc, int t, float2 uv) {
+  uint4 ti = __ldg(sc.tex_info + t);
+  float u = uv.x - truncf(uv.x), v = uv.y - truncf(uv.y);
+  if (u < 0.f) u += 1.f;
+  if (v < 0.f) v += 1.f;
+  int x = (int)(u * (float)ti.y), y = (int)((1.f - v) * (float)ti.z);
+  x = min(max(x, 0), (int)ti.y - 1);
+  y = min(max(y, 0), (int)ti.z - 1);
+  return f3(__ldg(sc.texels + ti.x + (size_t)y * ti.y + (uint32_t)x));
+}
+// ColorSource.Evaluate of a Lambertian / Metal albedo (color_source.go)
+__device__ __forceinline__ float3 albedo_at(const DevScene& sc, const DevMaterial& m, const Surface& s) {
+  return m.tex >= 0 ? tex_eval(sc, m.tex, s.uv) : m.albedo;
+}
 
 __device__ __forceinline__ float3 reflect(float3 v, float3 n) { return v - n * (2.f * dot(v, n)); }
 // refractVector (pkg/material/dielectric.go:158-163)
@@ -731,15 +787,15 @@ struct Scatter {
 // Material.Scatter for Lambertian / Metal / Dielectric / Emissive / Layered
 // (lambertian.go:25-49, metal.go:38-62, dielectric.go:20-59,
 // emissive.go:17-21, layered.go:24-79).  Returns didScatter.
-__device__ __forceinline__ bool scatter_basic(const DevMaterial& m, float3 din, const Surface& s, Rng& rng,
-                                              Scatter& out) {
+__device__ __forceinline__ bool scatter_basic(const DevScene& sc, const DevMaterial& m, float3 din, const Surface& s,
+                                              Rng& rng, Scatter& out) {
   switch (m.kind) {
     case kMatLambertian: {
       float2 u = rng.next2();
       float3 dir = sample_cosine_hemisphere(s.n, u);
       float c = fmaxf(0.f, dot(normalize(dir), s.n));
       out.dir = dir;
-      out.att = m.albedo * (1.0f / kPi);
+      out.att = albedo_at(sc, m, s) * (1.0f / kPi);
       out.pdf = c / kPi;
       return true;
     }
@@ -750,7 +806,7 @@ __device__ __forceinline__ bool scatter_basic(const DevMaterial& m, float3 din, 
         r = r + sample_in_unit_sphere(f3(a, b, c)) * m.fuzz;
       }
       out.dir = r;
-      out.att = m.albedo;
+      out.att = albedo_at(sc, m, s);
       out.pdf = 0.f;
       return dot(r, s.n) > 0.f;
     }
@@ -777,11 +833,11 @@ __device__ __forceinline__ bool scatter_basic(const DevMaterial& m, float3 din, 
 __device__ __forceinline__ bool scatter(const DevScene& sc, const DevMaterial& m, float3 din, const Surface& s,
                                         Rng& rng, Scatter& out) {
   if (m.kind == kMatMix)  // Mix.Scatter (mix.go:30-37): material 2 below the ratio
-    return scatter_basic(load_material(sc, rng.next() < m.fuzz ? m.inner : m.outer), din, s, rng, out);
-  if (m.kind != kMatLayered) return scatter_basic(m, din, s, rng, out);
+    return scatter_basic(sc, load_material(sc, rng.next() < m.fuzz ? m.inner : m.outer), din, s, rng, out);
+  if (m.kind != kMatLayered) return scatter_basic(sc, m, din, s, rng, out);
   DevMaterial mo = load_material(sc, m.outer);
   Scatter o;
-  if (!scatter_basic(mo, din, s, rng, o)) return false;
+  if (!scatter_basic(sc, mo, din, s, rng, o)) return false;
   float3 sd = normalize(o.dir);
   if (!(dot(sd, s.n) < 0.f)) {
     out = o;
@@ -789,7 +845,7 @@ __device__ __forceinline__ bool scatter(const DevScene& sc, const DevMaterial& m
   }
   DevMaterial mi = load_material(sc, m.inner);
   Scatter in;
-  if (!scatter_basic(mi, sd, s, rng, in)) {
+  if (!scatter_basic(sc, mi, sd, s, rng, in)) {
     out = o;
     return true;
   }
@@ -801,15 +857,15 @@ __device__ __forceinline__ bool scatter(const DevScene& sc, const DevMaterial& m
 
 // EvaluateBRDF (lambertian.go:52-62, metal.go:65-77, dielectric.go:62-142,
 // emissive.go:35-38, layered.go:81-95)
-__device__ __forceinline__ float3 brdf_basic(const DevMaterial& m, float3 in, float3 out, const Surface& s,
-                                             bool radiance) {
+__device__ __forceinline__ float3 brdf_basic(const DevScene& sc, const DevMaterial& m, float3 in, float3 out,
+                                             const Surface& s, bool radiance) {
   switch (m.kind) {
     case kMatLambertian:
       if (dot(out, s.n) <= 0.f) return f3(0.f, 0.f, 0.f);
-      return m.albedo * (1.0f / kPi);
+      return albedo_at(sc, m, s) * (1.0f / kPi);
     case kMatMetal: {
       float3 r = reflect(-in, s.n);
-      if (length(out - r) < 0.001f) return m.albedo;
+      if (length(out - r) < 0.001f) return albedo_at(sc, m, s);
       return f3(0.f, 0.f, 0.f);
     }
     case kMatDielectric: {
@@ -851,11 +907,11 @@ __device__ __forceinline__ bool is_reflection_path(float3 in, float3 out, float3
 __device__ __forceinline__ float3 brdf(const DevScene& sc, const DevMaterial& m, float3 in, float3 out,
                                        const Surface& s, bool radiance) {
   if (m.kind == kMatMix)  // Mix.EvaluateBRDF (mix.go:40-46)
-    return brdf_basic(load_material(sc, m.outer), in, out, s, radiance) * (1.f - m.fuzz) +
-           brdf_basic(load_material(sc, m.inner), in, out, s, radiance) * m.fuzz;
-  if (m.kind != kMatLayered) return brdf_basic(m, in, out, s, radiance);
+    return brdf_basic(sc, load_material(sc, m.outer), in, out, s, radiance) * (1.f - m.fuzz) +
+           brdf_basic(sc, load_material(sc, m.inner), in, out, s, radiance) * m.fuzz;
+  if (m.kind != kMatLayered) return brdf_basic(sc, m, in, out, s, radiance);
   int sub = is_reflection_path(in, out, s.n) ? m.outer : m.inner;
-  return brdf_basic(load_material(sc, sub), in, out, s, radiance);
+  return brdf_basic(sc, load_material(sc, sub), in, out, s, radiance);
 }
 
 // Material.PDF (lambertian.go:65-72, metal.go:80-84, dielectric.go:145-149,

@@ -42,6 +42,7 @@ struct DevBdpt {
   uint4* meta;    // nc | nl << 8, sampler position after the subpaths, pixel, sample index
   uint2* masks;   // strategies that draw samples: light-tracing (bit s), direct-lighting (bit t)
   float4* contrib;
+  float2* uv;     // surface UV per vertex (scenes with textures only, else null)
   uint32_t ns;    // samples per chunk
   int maxv;       // vertices per subpath (10 or 18)
 };

@@ -33,6 +33,7 @@ constexpr int kFlagLight = 1, kFlagCamera = 2, kFlagSpecular = 4, kFlagInfinite 
 
 struct BVert {  // bdpt.go:14-36
   float3 p, n, beta, Le, wi;
+  float2 uv;  // surface UV (textured scenes)
   float fwd, rev;
   int mat;    // material index, -1 for none
   int light;  // index in the light table, -1 for none
@@ -255,6 +256,7 @@ __device__ __noinline__ float3 vertex_brdf(const DevScene& sc, const BVert& v, f
   s.n = v.n;
   s.front = v.is(kFlagFront);
   s.mat = v.mat;
+  s.uv = v.uv;
   return brdf(sc, load_material(sc, v.mat), v.wi, out, s, radiance);
 }
 
@@ -340,6 +342,7 @@ __device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, co
   B.v[3][k] = make_float4(x.Le.x, x.Le.y, x.Le.z, x.wi.y);
   B.v[4][k] = make_float4(x.wi.z, __int_as_float((x.mat + 1) | (x.flags << 24)), __int_as_float(x.light),
                           __uint_as_float(x.prim));
+  if (B.uv) B.uv[k] = x.mat >= 0 ? x.uv : make_float2(0.f, 0.f);
 }
 
 __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
@@ -358,6 +361,7 @@ __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
   x.flags = (mf >> 24) & 0xFF;
   x.light = __float_as_int(e.z);
   x.prim = __float_as_uint(e.w);
+  x.uv = B.uv ? B.uv[k] : make_float2(0.f, 0.f);
   return x;
 }
 
@@ -410,6 +414,7 @@ __device__ __noinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, ui
     v.beta = beta;
     v.Le = emitted(m, s.front, d);
     v.mat = s.mat;
+    v.uv = s.uv;
     v.light = -1;
     v.prim = h.prim;
     v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);

@@ -17,6 +17,8 @@
 //              apex = up (the in-plane basis of Disc.SampleUniform);
 //              cylinder: p0 = base, p1 = top, r0 = r1 = radius;
 //              cone: p0 = base (radius r0), p1 = top (radius r1), apex of the extended cone
+//   textures   tex_info uint4 per texture (first texel, width, height, -);
+//              texels float4 (r, g, b, -), row-major (ImageTexture.Pixels)
 // Primitive ids: triangles [0, quad_base), quads [quad_base, sphere_base),
 // spheres [sphere_base, quadric_base), quadrics [quadric_base, n_prims); each
 // type array is in BVH leaf order.
@@ -49,7 +51,8 @@ enum : int { kLightQuad = 0, kLightSphere = 1, kLightUniformInfinite = 2, kLight
              kLightDiscSpot = 5, kLightPointSpot = 6 };
 
 struct DevMaterial {
-  int kind, outer, inner, pad;
+  int kind, outer, inner;
+  int tex;  // Lambertian / Metal: texture index (albedo from the texture at the hit's UV), -1 for none
   float3 albedo;
   float fuzz;
   float3 emission;
@@ -88,6 +91,9 @@ struct DevScene {
   const float4* quadrics;
   const DevMaterial* materials;
   const DevLight* lights;
+  const uint4* tex_info;  // per texture: (first texel, width, height, -)
+  const float4* texels;   // RGB (+ pad), row-major per texture
+  int has_textures;       // surface UVs are computed only when set
   int n_nodes;
   int root;  // BVH root node of the scene (-1: empty)
   int n_lights;

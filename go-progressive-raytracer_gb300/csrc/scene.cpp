@@ -504,12 +504,39 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     err = "materials pointer is null";
     return false;
   }
+  // textures (NewImageTexture, image_texture.go:17-23)
+  out.tex_info.clear();
+  out.texels.clear();
+  if (d->n_textures && !d->textures) {
+    err = "textures missing";
+    return false;
+  }
+  for (uint32_t i = 0; i < d->n_textures; i++) {
+    const gprt_texture_desc& t = d->textures[i];
+    if (t.width == 0 || t.height == 0 || !t.pixels || (uint64_t)t.width * t.height > (1ull << 28) ||
+        out.texels.size() + (uint64_t)t.width * t.height > 0xFFFFFFFFull) {
+      err = "texture needs a size (at most 2^28 texels) and pixels";
+      return false;
+    }
+    out.tex_info.push_back(make_uint4((uint32_t)out.texels.size(), t.width, t.height, 0));
+    size_t n = (size_t)t.width * t.height;
+    for (size_t k = 0; k < n; k++)
+      out.texels.push_back(make_float4((float)t.pixels[3 * k], (float)t.pixels[3 * k + 1], (float)t.pixels[3 * k + 2], 0.f));
+  }
   // materials (NewMetal clamps fuzz, metal.go:18-30)
   out.materials.resize(d->n_materials);
   for (uint32_t i = 0; i < d->n_materials; i++) {
     const gprt_material_desc& m = d->materials[i];
     DevMaterial dm{};
     dm.kind = (int)m.kind;
+    dm.tex = -1;
+    if (m.kind == GPRT_MAT_LAMBERTIAN || m.kind == GPRT_MAT_METAL) {
+      if (m.texture > d->n_textures) {
+        err = "material texture index out of range";
+        return false;
+      }
+      dm.tex = (int)m.texture - 1;
+    }
     if (m.kind > GPRT_MAT_MIX) {
       err = "unknown material kind";
       return false;

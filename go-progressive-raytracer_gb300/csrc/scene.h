@@ -25,6 +25,8 @@ struct HostScene {
   std::vector<float4> nodes, tris, tri_normals, quads, spheres, quadrics;
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights;
+  std::vector<uint4> tex_info;  // per texture: first texel, width, height
+  std::vector<float4> texels;
   // primitive id -> (index in scene.Shapes, box face / mesh triangle)
   std::vector<uint32_t> prim_shape, prim_sub;
   uint32_t n_tris = 0, n_quads = 0, n_spheres = 0, n_quadrics = 0;

@@ -37,6 +37,11 @@
 namespace gprt {
 namespace {
 
+// the pool's arrays, one per kind of scene data
+constexpr int kNodes = 0, kTris = 1, kQuads = 2, kSpheres = 3, kQuadrics = 4, kMats = 5, kLights = 6, kTexInfo = 7,
+              kTexels = 8;
+constexpr int kPoolArrays = 9;
+
 constexpr uint32_t kPoolQuadBase = 1u << 30;
 constexpr uint32_t kPoolSphereBase = 2u << 30;
 constexpr uint32_t kPoolQuadricBase = 3u << 30;
@@ -48,6 +53,7 @@ struct StepHdr {
 struct DevItem {
   uint32_t path0, pix0, npix, layers;
   int root, mat_off, light_off, n_lights;
+  int tex_off, texel_off, has_textures, pad;
   int has_infinite, max_depth, rr_min_bounces, width;
   float3 world_center;
   float world_radius;
@@ -124,6 +130,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
       DevScene v = pool;
       v.materials = pool.materials + it.mat_off;
       v.lights = pool.lights + it.light_off;
+      v.tex_info = pool.tex_info + it.tex_off;
+      v.texels = pool.texels + it.texel_off;
+      v.has_textures = it.has_textures;
       v.n_lights = it.n_lights;
       v.has_infinite = it.has_infinite;
       v.world_center = it.world_center;
@@ -247,8 +256,8 @@ struct PoolArray {
 // A scene resident in the pool.
 struct PoolScene {
   uint64_t serial = 0;
-  size_t off[7] = {0, 0, 0, 0, 0, 0, 0};  // nodes, tris, quads, spheres, quadrics, materials, lights
-  size_t cnt[7] = {0, 0, 0, 0, 0, 0, 0};
+  size_t off[gprt::kPoolArrays] = {};  // element offsets in the pool arrays (kNodes ... kTexels)
+  size_t cnt[gprt::kPoolArrays] = {};
   int refs = 0;
   uint64_t last_use = 0;
   size_t bytes = 0;
@@ -291,7 +300,7 @@ struct gprt_server {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // state (smu)
   std::mutex smu;
-  gprt::PoolArray pool[7];
+  gprt::PoolArray pool[gprt::kPoolArrays];
   uint64_t pool_gen = 0;
   std::vector<std::unique_ptr<PoolScene>> scenes;
   std::map<uint64_t, std::unique_ptr<SrvJob>> jobs;  // admitted, by ticket
@@ -333,8 +342,7 @@ using namespace gprt;
 
 namespace {
 
-constexpr int kNodes = 0, kTris = 1, kQuads = 2, kSpheres = 3, kQuadrics = 4, kMats = 5, kLights = 6;
-constexpr int kPoolArrays = 7;
+
 
 void emit(gprt_server* sv, uint64_t ticket, uint32_t kind, uint32_t passes, uint32_t spp, int status,
           double submit_ms) {
@@ -372,6 +380,8 @@ void scene_counts(const gprt_scene* s, size_t cnt[kPoolArrays]) {
   cnt[kQuadrics] = h.n_quadrics;
   cnt[kMats] = h.materials.size();
   cnt[kLights] = h.lights.size();
+  cnt[kTexInfo] = h.tex_info.size();
+  cnt[kTexels] = h.texels.size();
 }
 
 size_t scene_bytes(gprt_server* sv, const size_t cnt[kPoolArrays]) {
@@ -390,6 +400,8 @@ DevScene pool_view(gprt_server* sv) {
   d.quadrics = static_cast<const float4*>(sv->pool[kQuadrics].buf[0]);
   d.materials = static_cast<const DevMaterial*>(sv->pool[kMats].buf[0]);
   d.lights = static_cast<const DevLight*>(sv->pool[kLights].buf[0]);
+  d.tex_info = static_cast<const uint4*>(sv->pool[kTexInfo].buf[0]);
+  d.texels = static_cast<const float4*>(sv->pool[kTexels].buf[0]);
   d.n_nodes = (int)sv->pool[kNodes].cap;
   d.root = -1;
   d.quad_base = kPoolQuadBase;
@@ -407,7 +419,8 @@ bool grow(gprt_server* sv, int k, size_t need_cap) {
   if (k == kTris || k == kQuads) new_cap = std::min<size_t>(new_cap, kPoolQuadBase);
   if (k == kSpheres) new_cap = std::min<size_t>(new_cap, kPoolQuadricBase - kPoolSphereBase);
   if (k == kQuadrics) new_cap = std::min<size_t>(new_cap, (size_t)0xFFFFFFFEu - kPoolQuadricBase);
-  if (k == kNodes || k == kMats || k == kLights) new_cap = std::min<size_t>(new_cap, 0x7FFFFFFF);
+  if (k == kNodes || k == kMats || k == kLights || k == kTexInfo || k == kTexels)
+    new_cap = std::min<size_t>(new_cap, 0x7FFFFFFF);
   if (new_cap < need_cap) return false;
   size_t used = bytes_in_use(sv);
   size_t extra = (new_cap - a.cap) * a.bytes_per();
@@ -469,7 +482,7 @@ void evict(gprt_server* sv, PoolScene* ps) {
 bool place(gprt_server* sv, const size_t cnt[kPoolArrays], size_t off[kPoolArrays]) {
   for (;;) {
     bool ok = true;
-    size_t got[kPoolArrays] = {0, 0, 0, 0, 0, 0, 0};
+    size_t got[kPoolArrays] = {};
     int k = 0;
     for (; k < kPoolArrays; k++) {
       if (cnt[k] == 0) continue;
@@ -526,6 +539,8 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   copy(kQuadrics, 0, d.quadrics);
   copy(kMats, 0, d.materials);
   copy(kLights, 0, d.lights);
+  copy(kTexInfo, 0, d.tex_info);  // texel indices stay scene-relative: jobs see offset views
+  copy(kTexels, 0, d.texels);
   if (cnt[kNodes]) {
     float4* nodes = static_cast<float4*>(sv->pool[kNodes].buf[0]) + off[kNodes] * 8;
     uint32_t n = (uint32_t)cnt[kNodes];
@@ -867,6 +882,9 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
     d.mat_off = (int)ps->off[kMats];
     d.light_off = (int)ps->off[kLights];
     d.n_lights = (int)ps->cnt[kLights];
+    d.tex_off = (int)ps->off[kTexInfo];
+    d.texel_off = (int)ps->off[kTexels];
+    d.has_textures = ps->cnt[kTexInfo] ? 1 : 0;
     d.has_infinite = ps->has_infinite;
     d.max_depth = ps->max_depth;
     d.rr_min_bounces = ps->rr_min;
@@ -1064,6 +1082,8 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   sv->pool[kQuadrics].elem[0] = 5 * sizeof(float4);
   sv->pool[kMats].elem[0] = sizeof(DevMaterial);
   sv->pool[kLights].elem[0] = sizeof(DevLight);
+  sv->pool[kTexInfo].elem[0] = sizeof(uint4);
+  sv->pool[kTexels].elem[0] = sizeof(float4);
   // path state of one step
   DevPaths& P = sv->P;
   auto& b = sv->path_bufs;

@@ -30,8 +30,12 @@ BUILD_DEVICE = 1
 NOALLOC_MAX_PATHS = 131072  # GPRT_NOALLOC_MAX_PATHS
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("pixels", C.POINTER(C.c_double))]
+
+
 class MaterialDesc(C.Structure):
-    _fields_ = [("kind", C.c_uint32), ("outer", C.c_uint32), ("inner", C.c_uint32), ("reserved", C.c_uint32),
+    _fields_ = [("kind", C.c_uint32), ("outer", C.c_uint32), ("inner", C.c_uint32), ("texture", C.c_uint32),
                 ("albedo", C.c_double * 3), ("fuzz", C.c_double), ("ior", C.c_double),
                 ("emission", C.c_double * 3)]
 
@@ -69,7 +73,8 @@ class SceneDesc(C.Structure):
                 ("meshes", C.POINTER(MeshDesc)), ("lights", C.POINTER(LightDesc)),
                 ("n_materials", C.c_uint32), ("n_shapes", C.c_uint32), ("n_meshes", C.c_uint32),
                 ("n_lights", C.c_uint32), ("weighted_sampler", C.c_uint32), ("build_flags", C.c_uint32),
-                ("camera", CameraDesc), ("sampling", SamplingDesc)]
+                ("camera", CameraDesc), ("sampling", SamplingDesc), ("textures", C.POINTER(TextureDesc)),
+                ("n_textures", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Ray(C.Structure):

@@ -19,6 +19,37 @@ from . import _capi as capi
 Vec3 = Sequence[float]
 
 
+# ---------------------------------------------------------------- textures
+@dataclass(eq=False)
+class ImageTexture:  # material.ImageTexture (image_texture.go:8-23)
+    pixels: np.ndarray  # (height, width, 3) float64, row y = 0 first
+
+    @property
+    def width(self):
+        return self.pixels.shape[1]
+
+    @property
+    def height(self):
+        return self.pixels.shape[0]
+
+
+def NewCheckerboardTexture(width, height, check_size, color1, color2):  # procedural_textures.go:8-30
+    y, x = np.mgrid[0:height, 0:width]
+    even = ((x // check_size + y // check_size) % 2) == 0
+    return ImageTexture(np.where(even[..., None], np.array(color1, dtype=np.float64), np.array(color2, dtype=np.float64)))
+
+
+def NewUVDebugTexture(width, height):  # procedural_textures.go:34-46: (u, v, 0) per texel
+    y, x = np.mgrid[0:height, 0:width]
+    return ImageTexture(np.stack([x / float(width - 1), y / float(height - 1), np.zeros((height, width))], axis=-1))
+
+
+def NewGradientTexture(width, height, color1, color2):  # procedural_textures.go:49-63: color1 at row 0
+    t = (np.arange(height, dtype=np.float64) / float(height - 1))[:, None, None]
+    row = np.array(color1, dtype=np.float64) * (1.0 - t) + np.array(color2, dtype=np.float64) * t
+    return ImageTexture(np.broadcast_to(row, (height, width, 3)).copy())
+
+
 # ---------------------------------------------------------------- materials
 @dataclass
 class Material:
@@ -29,6 +60,7 @@ class Material:
     emission: Vec3 = (0.0, 0.0, 0.0)
     outer: Optional["Material"] = None
     inner: Optional["Material"] = None
+    texture: Optional[ImageTexture] = None
 
 
 def Lambertian(albedo):  # material.NewLambertian (lambertian.go:15-18)
@@ -37,6 +69,14 @@ def Lambertian(albedo):  # material.NewLambertian (lambertian.go:15-18)
 
 def Metal(albedo, fuzz):  # material.NewMetal (metal.go:18-30), fuzz clamped to [0,1]
     return Material(capi.MAT_METAL, albedo=tuple(albedo), fuzz=min(1.0, max(0.0, fuzz)))
+
+
+def TexturedLambertian(texture):  # material.NewTexturedLambertian (lambertian.go:19-24)
+    return Material(capi.MAT_LAMBERTIAN, texture=texture)
+
+
+def TexturedMetal(texture, fuzz):  # material.NewTexturedMetal (metal.go:25-36)
+    return Material(capi.MAT_METAL, texture=texture, fuzz=min(1.0, max(0.0, fuzz)))
 
 
 def Dielectric(ior):  # material.NewDielectric (dielectric.go:15-17)
@@ -98,7 +138,7 @@ def Cone(base, base_radius, top, top_radius, capped, material):  # geometry.NewC
 
 
 # numpy layout of gprt_material_desc (include/gprt.h)
-MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("outer", "<u4"), ("inner", "<u4"), ("reserved", "<u4"),
+MATERIAL_DTYPE = np.dtype([("kind", "<u4"), ("outer", "<u4"), ("inner", "<u4"), ("texture", "<u4"),
                            ("albedo", "<f8", 3), ("fuzz", "<f8"), ("ior", "<f8"), ("emission", "<f8", 3)])
 assert MATERIAL_DTYPE.itemsize == C.sizeof(capi.MaterialDesc)
 
@@ -324,9 +364,15 @@ class FlatScene:
                     d.p[k] = float(x)
         total = n_mats()
         mdesc = np.zeros(max(1, total), dtype=MATERIAL_DTYPE)
+        textures, tex_index = [], {}
         for i, m in mats:
             d = mdesc[i]
             d["kind"] = m.kind
+            if m.texture is not None:
+                if id(m.texture) not in tex_index:
+                    tex_index[id(m.texture)] = len(textures)
+                    textures.append(m.texture)
+                d["texture"] = tex_index[id(m.texture)] + 1
             d["albedo"] = m.albedo
             d["emission"] = m.emission
             d["fuzz"] = m.fuzz
@@ -361,6 +407,14 @@ class FlatScene:
         desc.n_meshes = len(meshes)
         desc.n_lights = len(scene.lights)
         desc.weighted_sampler = 1 if scene.light_weights else 0
+        tdesc = (capi.TextureDesc * max(1, len(textures)))()
+        for k, t in enumerate(textures):
+            px = np.ascontiguousarray(t.pixels, dtype=np.float64)
+            self._keep.append(px)
+            tdesc[k].width, tdesc[k].height = t.width, t.height
+            tdesc[k].pixels = px.ctypes.data_as(C.POINTER(C.c_double))
+        desc.textures = C.cast(tdesc, C.POINTER(capi.TextureDesc))
+        desc.n_textures = len(textures)
         cam = scene.camera
         for k in range(3):
             desc.camera.center[k] = cam.center[k]

@@ -28,7 +28,9 @@ import numpy as np
 
 from . import _capi as capi
 from .scene import (MATERIAL_DTYPE, Box, CameraConfig, Cone, Cylinder, Dielectric, Disc, Emissive, Lambertian, Layered,
-                    MaterialTable, Mesh, Metal, Mix, NewGroundQuad, Quad, SamplingConfig, Scene, Sphere, TriangleMesh)
+                    MaterialTable, Mesh, Metal, Mix, NewCheckerboardTexture, NewGradientTexture, NewGroundQuad,
+                    NewUVDebugTexture, Quad, SamplingConfig, Scene, Sphere, TexturedLambertian, TexturedMetal, Triangle,
+                    TriangleMesh)
 
 CORNELL_SPHERES, CORNELL_BOXES, CORNELL_EMPTY = 0, 1, 2
 CORNELL_QUAD_LIGHT, CORNELL_POINT_LIGHT, CORNELL_SPHERE_LIGHT = 0, 1, 2
@@ -255,6 +257,32 @@ def sphere_grid_scene(grid_size=10, finish="metallic", camera=None):
                 m = Metal(color, 0.05)
             s.add(Sphere(pos, radius, m))
     s.add_gradient_infinite_light((0.5, 0.7, 1.0), (1.0, 1.0, 1.0))
+    return s.finalize_size()
+
+
+def texture_test_scene(camera=None):
+    """scene.NewTextureTestScene (pkg/scene/texture_test_scene.go:11-161):
+    one shape of each kind, textured with the procedural checkerboard,
+    gradient and UV-debug textures, on a checkered ground."""
+    base = CameraConfig(center=(0.0, 2.0, 10.0), look_at=(0.0, 1.0, 0.0), up=(0.0, 1.0, 0.0), width=800,
+                        aspect_ratio=16.0 / 9.0, vfov=50.0, aperture=0.0, focus_distance=0.0)
+    s = Scene(camera=base.merged(camera))
+    s.sampling = SamplingConfig(samples_per_pixel=100, max_depth=10, russian_roulette_min_bounces=5,
+                                adaptive_min_samples=0.15, adaptive_threshold=0.01)
+    checker = TexturedLambertian(NewCheckerboardTexture(256, 256, 32, (0.9, 0.9, 0.9), (0.2, 0.2, 0.8)))
+    gradient = TexturedLambertian(NewGradientTexture(256, 256, (1.0, 0.2, 0.2), (0.2, 1.0, 0.2)))
+    uv_debug = TexturedLambertian(NewUVDebugTexture(256, 256))
+    brick = TexturedLambertian(NewCheckerboardTexture(512, 512, 16, (0.7, 0.3, 0.1), (0.5, 0.2, 0.05)))
+    s.add(Sphere((-6.0, 1.0, 0.0), 1.0, checker),
+          Cylinder((-4.0, 0.0, 0.0), (-4.0, 2.0, 0.0), 0.6, True, gradient),
+          Cone((-2.0, 0.0, 0.0), 0.8, (-2.0, 2.0, 0.0), 0.2, True, uv_debug),
+          Box((0.0, 1.0, 0.0), (0.8, 0.8, 0.8), (0.0, 0.0, 0.0), brick),
+          Disc((2.0, 1.2, 0.0), (0.0, 0.0, 1.0), 0.9, checker),
+          Quad((3.5, 0.0, 0.2), (1.5, 0.0, -0.3), (0.0, 2.0, 0.0), gradient),
+          Triangle((5.5, 0.0, 0.0), (7.0, 0.0, 0.0), (6.25, 2.0, 0.0), uv_debug),
+          Quad((-10.0, 0.0, -5.0), (20.0, 0.0, 0.0), (0.0, 0.0, 15.0), brick))
+    s.add_sphere_light((0.0, 8.0, 5.0), 2.0, (20.0, 20.0, 20.0))
+    s.add_gradient_infinite_light((0.3, 0.4, 0.6), (0.2, 0.2, 0.2))
     return s.finalize_size()
 
 

@@ -66,11 +66,20 @@ enum gprt_material_kind {
                                   mix), fuzz = ratio (clamped to [0,1]; 0 = all material 1) */
 };
 
+/* material.ImageTexture (pkg/material/image_texture.go:8-52): a row-major
+ * RGB image, pixels[3 * (y * width + x) + c] (the memory of []core.Vec3) */
+typedef struct gprt_texture_desc {
+  uint32_t width;
+  uint32_t height;
+  const double* pixels;
+} gprt_texture_desc;
+
 typedef struct gprt_material_desc {
   uint32_t kind;     /* gprt_material_kind */
   uint32_t outer;    /* LAYERED: material index of the outer layer; MIX: material 1 */
   uint32_t inner;    /* LAYERED: material index of the inner layer; MIX: material 2 */
-  uint32_t reserved;
+  uint32_t texture;  /* LAMBERTIAN, METAL: 0 = the solid albedo; k = textures[k-1] (NewTexturedLambertian,
+                        NewTexturedMetal), evaluated at the hit's UV */
   double albedo[3];  /* LAMBERTIAN, METAL */
   double fuzz;       /* METAL; MIX: the ratio */
   double ior;        /* DIELECTRIC */
@@ -171,6 +180,9 @@ typedef struct gprt_scene_desc {
   uint32_t build_flags;      /* GPRT_BUILD_* */
   gprt_camera_desc camera;
   gprt_sampling_desc sampling;
+  const gprt_texture_desc* textures;
+  uint32_t n_textures;
+  uint32_t reserved;
 } gprt_scene_desc;
 
 /* ---- ray batches ----------------------------------------------------------

@@ -1046,8 +1046,40 @@ void spotLightTests() {
   }
 }
 
+// ImageTexture.Evaluate (pkg/material/image_texture_test.go)
+void textureTests() {
+  auto eq = [](Vec3 a, Vec3 b) { return a.sub(b).length() == 0; };
+  {  // TestImageTextureEvaluate (:10-53): 2x2 checker, row 0 at the top
+    ImageTexture t;
+    t.width = t.height = 2;
+    t.pixels = {Vec3(1, 1, 1), Vec3(0, 0, 0), Vec3(0, 0, 0), Vec3(1, 1, 1)};
+    Vec3 w(1, 1, 1), b(0, 0, 0);
+    check(eq(t.evaluate(Vec2(0.1, 0.1)), b) && eq(t.evaluate(Vec2(0.9, 0.1)), w) && eq(t.evaluate(Vec2(0.1, 0.9)), w) &&
+              eq(t.evaluate(Vec2(0.9, 0.9)), b),
+          "image_texture_test.go:10 TestImageTextureEvaluate");
+  }
+  {  // TestImageTextureWrapping (:55-78)
+    ImageTexture t;
+    t.width = t.height = 1;
+    t.pixels = {Vec3(1, 0, 0)};
+    bool ok = true;
+    for (Vec2 uv : {Vec2(0.5, 0.5), Vec2(1.5, 0.5), Vec2(0.5, 1.5), Vec2(-0.5, -0.5), Vec2(2.3, 3.7)})
+      ok = ok && eq(t.evaluate(uv), Vec3(1, 0, 0));
+    check(ok, "image_texture_test.go:55 TestImageTextureWrapping");
+  }
+  {  // TestImageTextureSampling (:80-112): 4x4 ramp
+    ImageTexture t;
+    t.width = t.height = 4;
+    for (int y = 0; y < 4; y++)
+      for (int x = 0; x < 4; x++) t.pixels.push_back(Vec3(1, 1, 1).mul((y * 4 + x) / 15.0));
+    check(eq(t.evaluate(Vec2(0.125, 0.875)), Vec3(0, 0, 0)) && eq(t.evaluate(Vec2(0.875, 0.125)), Vec3(1, 1, 1)),
+          "image_texture_test.go:80 TestImageTextureSampling");
+  }
+}
+
 int main() {
   try {
+    textureTests();
     geometryTests();
     quadricTests();
     spotLightTests();

@@ -20,13 +20,32 @@ namespace ref {
 Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
   auto s = std::make_unique<Scene>();
   auto v3 = [](const double* p) { return Vec3(p[0], p[1], p[2]); };
+  // textures (image_texture.go:17-23)
+  for (uint32_t i = 0; i < d->n_textures; i++) {
+    const gprt_texture_desc& t = d->textures[i];
+    if (t.width == 0 || t.height == 0 || !t.pixels) {
+      err = "texture needs a size and pixels";
+      return nullptr;
+    }
+    auto tex = std::make_unique<ImageTexture>();
+    tex->width = (int)t.width;
+    tex->height = (int)t.height;
+    tex->pixels.resize((size_t)t.width * t.height);
+    for (size_t k = 0; k < tex->pixels.size(); k++) tex->pixels[k] = v3(t.pixels + 3 * k);
+    s->textures.push_back(std::move(tex));
+  }
+  auto texture = [&](uint32_t k) -> const ImageTexture* { return k == 0 ? nullptr : s->textures[k - 1].get(); };
   // materials (two passes so Layered can reference later entries)
   s->materials.resize(d->n_materials);
   for (uint32_t i = 0; i < d->n_materials; i++) {
     const gprt_material_desc& m = d->materials[i];
+    if ((m.kind == GPRT_MAT_LAMBERTIAN || m.kind == GPRT_MAT_METAL) && m.texture > d->n_textures) {
+      err = "material texture index out of range";
+      return nullptr;
+    }
     switch (m.kind) {
-      case GPRT_MAT_LAMBERTIAN: s->materials[i] = std::make_unique<Lambertian>(v3(m.albedo)); break;
-      case GPRT_MAT_METAL: s->materials[i] = std::make_unique<Metal>(v3(m.albedo), m.fuzz); break;
+      case GPRT_MAT_LAMBERTIAN: s->materials[i] = std::make_unique<Lambertian>(v3(m.albedo), texture(m.texture)); break;
+      case GPRT_MAT_METAL: s->materials[i] = std::make_unique<Metal>(v3(m.albedo), m.fuzz, texture(m.texture)); break;
       case GPRT_MAT_DIELECTRIC: s->materials[i] = std::make_unique<Dielectric>(m.ior); break;
       case GPRT_MAT_EMISSIVE: s->materials[i] = std::make_unique<Emissive>(v3(m.emission)); break;
       case GPRT_MAT_SPOT_EMISSIVE:

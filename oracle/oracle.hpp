@@ -345,9 +345,31 @@ inline double reflectance(double cosine, double ratio) {
 }
 
 // Lambertian with SolidColor albedo (lambertian.go:25-72, color_source.go)
+// ImageTexture.Evaluate (image_texture.go:25-52): wrap u and v into [0,1),
+// nearest texel with v = 0 at the bottom row, clamped to the image
+struct ImageTexture {
+  int width = 0, height = 0;
+  std::vector<Vec3> pixels;  // row-major, pixels[y * width + x]
+  Vec3 evaluate(Vec2 uv) const {
+    double u = uv.x - (double)(long long)uv.x, v = uv.y - (double)(long long)uv.y;
+    if (u < 0) u += 1.0;
+    if (v < 0) v += 1.0;
+    long long x = (long long)(u * width), y = (long long)((1.0 - v) * height);
+    if (x >= width) x = width - 1;
+    if (y >= height) y = height - 1;
+    if (x < 0) x = 0;
+    if (y < 0) y = 0;
+    return pixels[(size_t)y * width + x];
+  }
+};
+
+// Lambertian (lambertian.go:10-72); the albedo may be a texture
+// (NewTexturedLambertian) evaluated at the hit's UV
 struct Lambertian : Material {
   Vec3 albedo;
-  explicit Lambertian(Vec3 a) : albedo(a) {}
+  const ImageTexture* tex = nullptr;
+  explicit Lambertian(Vec3 a, const ImageTexture* t = nullptr) : albedo(a), tex(t) {}
+  Vec3 albedoAt(const SurfaceInteraction& h) const { return tex ? tex->evaluate(h.uv) : albedo; }
   bool scatter(const Ray& in, const SurfaceInteraction& hit, Sampler& s,
                ScatterResult& out) const override {
     Vec3 dir = sampleCosineHemisphere(hit.normal, s.get2D());
@@ -355,14 +377,14 @@ struct Lambertian : Material {
     if (c < 0) c = 0;
     out.incoming = in;
     out.scattered = Ray(hit.point, dir);
-    out.attenuation = albedo.mul(1.0 / kPi);
+    out.attenuation = albedoAt(hit).mul(1.0 / kPi);
     out.pdf = c / kPi;
     return true;
   }
   Vec3 evaluateBRDF(const Vec3&, const Vec3& out, const SurfaceInteraction* hit,
                     TransportMode) const override {
     if (out.dot(hit->normal) <= 0) return {};
-    return albedo.mul(1.0 / kPi);
+    return albedoAt(*hit).mul(1.0 / kPi);
   }
   double pdf(const Vec3&, const Vec3& out, const Vec3& n, bool& isDelta) const override {
     isDelta = false;
@@ -376,21 +398,23 @@ struct Lambertian : Material {
 struct Metal : Material {
   Vec3 albedo;
   double fuzz;
-  Metal(Vec3 a, double f) : albedo(a), fuzz(std::min(1.0, std::max(0.0, f))) {}
+  const ImageTexture* tex = nullptr;  // NewTexturedMetal (metal.go:25-36)
+  Metal(Vec3 a, double f, const ImageTexture* t = nullptr) : albedo(a), fuzz(std::min(1.0, std::max(0.0, f))), tex(t) {}
+  Vec3 albedoAt(const SurfaceInteraction& h) const { return tex ? tex->evaluate(h.uv) : albedo; }
   bool scatter(const Ray& in, const SurfaceInteraction& hit, Sampler& s,
                ScatterResult& out) const override {
     Vec3 r = reflectVec(in.direction.normalize(), hit.normal);
     if (fuzz > 0) r = r.add(samplePointInUnitSphere(s.get3D()).mul(fuzz));
     out.incoming = in;
     out.scattered = Ray(hit.point, r);
-    out.attenuation = albedo;
+    out.attenuation = albedoAt(hit);
     out.pdf = 0;
     return out.scattered.direction.dot(hit.normal) > 0;
   }
   Vec3 evaluateBRDF(const Vec3& in, const Vec3& out, const SurfaceInteraction* hit,
                     TransportMode) const override {
     Vec3 r = reflectVec(in.negate(), hit->normal);
-    if (out.sub(r).length() < 0.001) return albedo;
+    if (out.sub(r).length() < 0.001) return albedoAt(*hit);
     return {};
   }
   double pdf(const Vec3&, const Vec3&, const Vec3&, bool& isDelta) const override {
@@ -785,6 +809,25 @@ struct Disc : Shape {
   }
 };
 
+// UV of a point on a cylinder or cone body (cylinder.go:187-205,
+// cone.go:234-253): v = height along the axis / length, u = the angle of the
+// radial vector in a basis built from the axis and a reference direction
+inline Vec2 axialUV(const Vec3& axis, const Vec3& radial, double h, double height) {
+  Vec3 ref = std::fabs(axis.y) < 0.9 ? Vec3(0, 1, 0) : Vec3(1, 0, 0);
+  Vec3 tangent = axis.cross(ref).normalize();
+  Vec3 bitangent = axis.cross(tangent);
+  double u = std::atan2(radial.dot(bitangent), radial.dot(tangent));
+  return Vec2((u + kPi) / (2.0 * kPi), h / height);
+}
+// UV of a point on a cap of outward normal n (cylinder.go:241-255, cone.go:322-339)
+inline Vec2 capUV(const Vec3& n, const Vec3& center, double radius, const Vec3& p) {
+  Vec3 ref = std::fabs(n.y) < 0.9 ? Vec3(0, 1, 0) : Vec3(1, 0, 0);
+  Vec3 tangent = n.cross(ref).normalize();
+  Vec3 bitangent = n.cross(tangent);
+  Vec3 l = p.sub(center);
+  return Vec2((l.dot(tangent) / radius + 1.0) / 2.0, (l.dot(bitangent) / radius + 1.0) / 2.0);
+}
+
 // Circular cap shared by Cylinder and Cone (cylinder.go:224-266, cone.go:306-350)
 inline bool hit_cap(const Ray& ray, const Vec3& center, const Vec3& normal, double radius, double tMin, double tMax,
                     double& t, Vec3& p) {
@@ -813,6 +856,7 @@ struct Cylinder : Shape {
     double closest = tMax;
     bool any = false;
     Vec3 outward, point;
+    Vec2 uv;
     // body (hitBody, cylinder.go:125-221)
     {
       Vec3 delta = ray.origin.sub(base);
@@ -848,6 +892,7 @@ struct Cylinder : Shape {
             if (ok) {
               Vec3 onAxis = base.add(axis.mul(h));
               outward = p.sub(onAxis).normalize();
+              uv = axialUV(axis, p.sub(onAxis), h, height);
               point = p;
               closest = t;
               any = true;
@@ -863,12 +908,14 @@ struct Cylinder : Shape {
         closest = t;
         point = p;
         outward = axis.negate();
+        uv = capUV(outward, base, radius, p);
         any = true;
       }
       if (hit_cap(ray, top, axis, radius, tMin, closest, t, p)) {
         closest = t;
         point = p;
         outward = axis;
+        uv = capUV(outward, top, radius, p);
         any = true;
       }
     }
@@ -876,6 +923,7 @@ struct Cylinder : Shape {
     out = SurfaceInteraction();
     out.t = closest;
     out.point = point;
+    out.uv = uv;
     out.material = material;
     out.shape = id;
     out.sub = 0;
@@ -918,6 +966,7 @@ struct Cone : Shape {
     double closest = tMax;
     bool any = false;
     Vec3 outward, point;
+    Vec2 uv;
     // body (hitBody, cone.go:180-276)
     {
       Vec3 CO = ray.origin.sub(apex);
@@ -941,6 +990,7 @@ struct Cone : Shape {
             double h = p.sub(base).dot(axis);
             Vec3 radial = p.sub(base.add(axis.mul(h)));
             outward = radial.add(axis.mul((r0 - r1) / height)).normalize();
+            uv = axialUV(axis, radial, h, height);
             point = p;
             closest = t;
             any = true;
@@ -955,12 +1005,14 @@ struct Cone : Shape {
         closest = t;
         point = p;
         outward = axis.negate();
+        uv = capUV(outward, base, r0, p);
         any = true;
       }
       if (r1 > 0 && hit_cap(ray, top, axis, r1, tMin, closest, t, p)) {
         closest = t;
         point = p;
         outward = axis;
+        uv = capUV(outward, top, r1, p);
         any = true;
       }
     }
@@ -968,6 +1020,7 @@ struct Cone : Shape {
     out = SurfaceInteraction();
     out.t = closest;
     out.point = point;
+    out.uv = uv;
     out.material = material;
     out.shape = id;
     out.sub = 0;
@@ -1870,6 +1923,7 @@ struct SamplingConfig {
 
 struct Scene {
   std::unique_ptr<Camera> camera;
+  std::vector<std::unique_ptr<ImageTexture>> textures;
   std::vector<std::unique_ptr<Material>> materials;
   std::vector<std::unique_ptr<Shape>> ownedShapes;
   std::vector<const Shape*> shapes;

@@ -39,7 +39,7 @@ def _validate(flat):
 
 @pytest.mark.parametrize("name", ["cornell_baseline", "cornell_spheres", "cornell_boxes", "default", "icosphere5",
                                   "spheres17", "quadrics", "spot_disc", "cornell_point",
-                                  "cone_test", "cylinder_test", "spheregrid"])
+                                  "cone_test", "cylinder_test", "spheregrid", "texture_test"])
 def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
     from gprt import scenes
     s = {"cornell_baseline": lambda: scenes.cornell_baseline(64),
@@ -53,7 +53,8 @@ def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
          "cornell_point": lambda: scenes.cornell_scene(scenes.CORNELL_BOXES, scenes.CORNELL_POINT_LIGHT),
          "cone_test": lambda: scenes.cone_test_scene(),
          "cylinder_test": lambda: scenes.cylinder_test_scene(),
-         "spheregrid": lambda: scenes.sphere_grid_scene(12, "mixed")}[name]()
+         "spheregrid": lambda: scenes.sphere_grid_scene(12, "mixed"),
+         "texture_test": lambda: scenes.texture_test_scene()}[name]()
     flat = s.to_desc()
     rc, info, err = _validate(flat)
     assert rc == 0, err

@@ -18,7 +18,7 @@ def test_kat_all_pass(kat_results):
     assert rc == 0 and not fails, "\n".join(fails)
     summary = [l for l in lines if l.startswith("SUMMARY")][0]
     npass = int(summary.split("pass=")[1].split()[0])
-    assert npass >= 106
+    assert npass >= 138
 
 
 @pytest.mark.parametrize("family", [
@@ -28,6 +28,8 @@ def test_kat_all_pass(kat_results):
     "TestMapRayToPixel", "TestPowerHeuristic", "TestDielectricEvaluateBRDF",
     "TestDiscHit", "TestCylinder_Hit_SimpleHit", "TestCylinder_Capped_HitTopCap", "TestCylinder_Hit_ArbitraryOrientation",
     "TestCone_Hit_Frustum", "TestCone_Capped_HitBaseCap_Pointed", "TestCone_Uncapped_NoCapHits",
+    "TestPointSpotLight_PDF", "TestDiscLightPDF", "TestDiscSpotLightFalloff", "TestImageTextureEvaluate",
+    "TestImageTextureWrapping",
 ])
 def test_kat_family_present_and_passing(kat_results, family):
     _, lines = kat_results
