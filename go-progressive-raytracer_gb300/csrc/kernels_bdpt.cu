@@ -8,15 +8,22 @@
 // splatted into the film's splat buffer with atomic adds and applied after
 // the pass (processSplats, pkg/renderer/progressive.go:371-391).
 //
-// Three kernels per chunk of samples:
+// Every helper is inlined: an out-of-line call takes its vertex and scene
+// arguments by reference, which puts them in each thread's local stack
+// (3 KB per thread for the strategy kernel, 245 MB at full occupancy, more
+// than L2), and that stack traffic went to DRAM.
+//
+// Four kernels per chunk of samples:
 //   k_bdpt_subpaths    one thread per sample builds both subpaths into a
 //                      global vertex store (fields indexed [vertex][sample]);
-//   k_bdpt_strategies  one thread per (strategy, sample), the samples of a
-//                      strategy in consecutive threads: each warp runs a
-//                      single (s,t) for 32 samples, so control flow is uniform
-//                      and vertex reads coalesce; its sampler position is the
-//                      sample's position after the subpaths plus the draws of
-//                      the strategies before it (draws_before);
+//   k_bdpt_list        lists, per strategy (s,t), the samples that have it;
+//   k_bdpt_strategies  one thread per listed (strategy, sample) item, the
+//                      items of a strategy in consecutive threads: each warp
+//                      runs a single (s,t) for 32 samples that have it, so
+//                      control flow is uniform and neighbouring warps share
+//                      code; its sampler position is the sample's position
+//                      after the subpaths plus the draws of the strategies
+//                      before it (draws_before);
 //   k_bdpt_sum         adds each sample's strategy contributions in the
 //                      reference's s-major order.
 #include <algorithm>
@@ -45,11 +52,6 @@ struct BVert {  // bdpt.go:14-36
 __device__ __forceinline__ bool light_is_area(const DevScene& sc, int li) {
   int k = sc.lights[li].kind;
   return k == kLightQuad || k == kLightSphere || k == kLightDisc || k == kLightDiscSpot;
-}
-
-// a vertex on a point light (LightTypePoint, bdpt_mis.go:130-137)
-__device__ __forceinline__ bool is_delta_light(const DevScene& sc, const BVert& v) {
-  return v.is(kFlagLight) && v.light >= 0 && sc.lights[v.light].kind == kLightPointSpot;
 }
 
 // Vertex.IsOnSurface (bdpt.go:42-49)
@@ -108,7 +110,7 @@ __device__ __forceinline__ float camera_importance(const DevCamera& c, float3 d)
 // SampleEmission (quad_light.go:113-145, sphere_light.go:169-184,
 // disc_light.go:103-110, disc_spot_light.go:210-240, point_spot_light.go:161-191,
 // light_sampling.go:58-115 for the infinite lights)
-__device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp, float2 sd, float3& p, float3& n,
+__device__ __forceinline__ void sample_emission(const DevScene& sc, const DevLight& L, float2 sp, float2 sd, float3& p, float3& n,
                                 float3& dir, float3& Le, float& area_pdf, float& dir_pdf) {
   if (L.kind == kLightQuad) {
     const float4* Q = sc.quads + (size_t)L.prim * 5;
@@ -177,7 +179,7 @@ __device__ __noinline__ void sample_emission(const DevScene& sc, const DevLight&
 // PDF_Le direction pdf (quad_light.go:148-185, sphere_light.go:187-209,
 // disc_light.go:113-136, disc_spot_light.go:243-264, point_spot_light.go:194-214,
 // uniform_infinite_light.go:94-106); pos receives the position pdf
-__device__ __noinline__ float pdf_le(const DevScene& sc, const DevLight& L, float3 p, float3 dir, float& pos) {
+__device__ __forceinline__ float pdf_le(const DevScene& sc, const DevLight& L, float3 p, float3 dir, float& pos) {
   pos = 0.f;
   if (L.kind == kLightQuad) {
     const float4* Q = sc.quads + (size_t)L.prim * 5;
@@ -247,7 +249,7 @@ __device__ float infinite_density(const DevScene& sc, float3 p, float3 n, float3
 
 // ---------------------------------------------------------------- BRDF at a vertex
 // evaluateBRDF (bdpt.go:564-583)
-__device__ __noinline__ float3 vertex_brdf(const DevScene& sc, const BVert& v, float3 out, bool radiance) {
+__device__ __forceinline__ float3 vertex_brdf(const DevScene& sc, const BVert& v, float3 out, bool radiance) {
   if (v.is(kFlagInfinite)) return f3(0.f, 0.f, 0.f);
   if (v.is(kFlagLight) && v.mat < 0) return f3(1.f, 1.f, 1.f);
   if (v.mat < 0) return f3(0.f, 0.f, 0.f);
@@ -261,7 +263,7 @@ __device__ __noinline__ float3 vertex_brdf(const DevScene& sc, const BVert& v, f
 }
 
 // calculateLightPdf (bdpt_mis.go:239-272)
-__device__ __noinline__ float vertex_light_pdf(const DevScene& sc, const BVert& cur, const BVert& to) {
+__device__ __forceinline__ float vertex_light_pdf(const DevScene& sc, const BVert& cur, const BVert& to) {
   float3 w = to.p - cur.p;
   float inv = 1.0f / dot(w, w);
   w = w * sqrtf(inv);
@@ -280,9 +282,7 @@ __device__ __noinline__ float vertex_light_pdf(const DevScene& sc, const BVert& 
 }
 
 // calculateVertexPdf (bdpt_mis.go:186-236)
-// (out of line: inlined into the weight walk it makes the strategy kernel
-// slower, instruction fetch dominating)
-__device__ __noinline__ float vertex_pdf(const DevScene& sc, const BVert& cur, const BVert* prev, const BVert& next) {
+__device__ __forceinline__ float vertex_pdf(const DevScene& sc, const BVert& cur, const BVert* prev, const BVert& next) {
   if (cur.is(kFlagLight)) return vertex_light_pdf(sc, cur, next);
   float3 wn = next.p - cur.p;
   if (dot(wn, wn) == 0.f) return 0.f;
@@ -310,7 +310,7 @@ __device__ __noinline__ float vertex_pdf(const DevScene& sc, const BVert& cur, c
 }
 
 // calculateLightOriginPdf (bdpt_mis.go:275-308)
-__device__ __noinline__ float light_origin_pdf(const DevScene& sc, const BVert& lv, const BVert& to) {
+__device__ __forceinline__ float light_origin_pdf(const DevScene& sc, const BVert& lv, const BVert& to) {
   float3 w = to.p - lv.p;
   if (dot(w, w) == 0.f) return 0.f;
   w = normalize(w);
@@ -325,7 +325,7 @@ __device__ __noinline__ float light_origin_pdf(const DevScene& sc, const BVert& 
 __device__ __forceinline__ float remap0(float f) { return f != 0.f ? f : 1.f; }
 
 // Any-hit test of a connection / shadow ray (one call site for all strategies).
-__device__ __noinline__ bool occluded(const DevScene& sc, float3 o, float3 d, float tmax, uint32_t skip, int* err) {
+__device__ __forceinline__ bool occluded(const DevScene& sc, float3 o, float3 d, float tmax, uint32_t skip, int* err) {
   Hit hh;
   return trace<true, false>(sc, o, d, 0.001f, tmax, skip, hh, err);
 }
@@ -365,18 +365,39 @@ __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
   return x;
 }
 
+// The pdfs and flags of a stored vertex (3 of its 5 fields), all the MIS
+// walk reads away from the connection.
+struct VPdf {
+  float fwd, rev;
+  int flags, light;
+};
+__device__ __forceinline__ VPdf get_vpdf(const DevBdpt& B, int v, uint32_t i) {
+  size_t k = (size_t)v * B.ns + i;
+  VPdf r;
+  r.fwd = B.v[0][k].w;
+  r.rev = B.v[1][k].w;
+  r.flags = (__float_as_int(B.v[4][k].y) >> 24) & 0xFF;
+  r.light = r.flags & kFlagLight ? __float_as_int(B.v[4][k].z) : -1;
+  return r;
+}
+// a vertex on a point light (LightTypePoint, bdpt_mis.go:130-137)
+__device__ __forceinline__ bool is_delta_light(const DevScene& sc, const VPdf& v) {
+  return (v.flags & kFlagLight) && v.light >= 0 && sc.lights[v.light].kind == kLightPointSpot;
+}
+
 // The vertices of one sample's subpath (camera: base 0, light: base maxv).
 struct SubpathRef {
   const DevBdpt* B;
   uint32_t i;
   int base;
   __device__ BVert operator[](int k) const { return get_vert(*B, base + k, i); }
+  __device__ VPdf pdfs(int k) const { return get_vpdf(*B, base + k, i); }
 };
 
 // extendPath (bdpt.go:206-291), writing vertex `len-1` once its reverse pdf
 // is final; `prev` enters as the subpath's first vertex.  Returns the length.
 template <int MAXV>
-__device__ __noinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, uint32_t i, int base, BVert prev,
+__device__ __forceinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, uint32_t i, int base, BVert prev,
                                         float3 o, float3 d, float3 beta, float pdf_fwd, int max_bounces, bool camera,
                                         Rng& rng, uint32_t skip, int* err) {
   int len = 1;
@@ -452,22 +473,23 @@ __device__ __noinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, ui
 }
 
 // calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
-__device__ __noinline__ float mis_weight(const DevScene& sc, const SubpathRef& C, const SubpathRef& Lp,
+__device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef& C, const SubpathRef& Lp,
                                          const BVert* sampled, int s, int t) {
   if (s + t == 2) return 1.f;
+  // vertices next to the connection are read in full where their pdfs are
+  // recomputed; the rest of the walk reads only pdfs and flags
   float sum = 0.f, ri = 1.f;
+  VPdf v = t >= 1 ? C.pdfs(t - 1) : VPdf{};
   for (int i = t - 1; i > 0; i--) {
-    BVert v = C[i];
+    VPdf pv = C.pdfs(i - 1);  // the predecessor: its flags here, the walk's next vertex
     float fwd = v.fwd, rev = v.rev;
-    bool conn = !v.is(kFlagSpecular);
+    bool conn = !(v.flags & kFlagSpecular);
     if (s == 0) {
       if (i == t - 1 && t > 1) {
-        BVert a = C[t - 1], b = C[t - 2];
-        rev = light_origin_pdf(sc, a, b);
+        rev = light_origin_pdf(sc, C[t - 1], C[t - 2]);
         conn = true;
       } else if (i == t - 2 && t > 2) {
-        BVert a = C[t - 1], b = C[t - 2];
-        rev = vertex_pdf(sc, a, nullptr, b);
+        rev = vertex_pdf(sc, C[t - 1], nullptr, C[t - 2]);
       }
     } else if (t == 1) {
       if (i == 0) {
@@ -477,61 +499,60 @@ __device__ __noinline__ float mis_weight(const DevScene& sc, const SubpathRef& C
       }
     } else if (s == 1) {
       if (i == t - 1 && t > 0) {
-        BVert a = C[t - 1];
-        rev = vertex_pdf(sc, *sampled, nullptr, a);
+        rev = vertex_pdf(sc, *sampled, nullptr, C[t - 1]);
         conn = true;
       } else if (i == t - 2 && t > 1) {
-        BVert a = C[t - 1], b = C[t - 2];
-        rev = vertex_pdf(sc, a, sampled, b);
+        rev = vertex_pdf(sc, C[t - 1], sampled, C[t - 2]);
       }
     } else {
       if (i == t - 1) {
-        BVert a = Lp[s - 1], b = Lp[s - 2], c = C[t - 1];
-        rev = vertex_pdf(sc, a, &b, c);
+        BVert b = Lp[s - 2];
+        rev = vertex_pdf(sc, Lp[s - 1], &b, C[t - 1]);
         conn = true;
       } else if (i == t - 2 && t > 1) {
-        BVert a = C[t - 1], b = Lp[s - 1], c = C[t - 2];
-        rev = vertex_pdf(sc, a, &b, c);
+        BVert b = Lp[s - 1];
+        rev = vertex_pdf(sc, C[t - 1], &b, C[t - 2]);
       }
     }
-    if (i > 0) conn = conn && !C[i - 1].is(kFlagSpecular);
+    conn = conn && !(pv.flags & kFlagSpecular);
     ri *= remap0(rev) / remap0(fwd);
     if (conn) sum += ri;
+    v = pv;
   }
   ri = 1.f;
+  v = s >= 1 ? Lp.pdfs(s - 1) : VPdf{};
   for (int i = s - 1; i >= 0; i--) {
-    BVert v = Lp[i];
+    VPdf pv = i > 0 ? Lp.pdfs(i - 1) : VPdf{};
     float fwd = v.fwd, rev = v.rev;
-    bool conn = !v.is(kFlagSpecular) && !is_delta_light(sc, v);
-    if (i > 0) conn = conn && !Lp[i - 1].is(kFlagSpecular) && !is_delta_light(sc, Lp[i - 1]);
+    bool conn = !(v.flags & kFlagSpecular) && !is_delta_light(sc, v);
+    if (i > 0) conn = conn && !(pv.flags & kFlagSpecular) && !is_delta_light(sc, pv);
     if (t == 1) {
       if (i == s - 1 && s > 1) {
-        BVert a = Lp[s - 1];
-        rev = vertex_pdf(sc, *sampled, nullptr, a);
+        rev = vertex_pdf(sc, *sampled, nullptr, Lp[s - 1]);
         conn = true;
       } else if (i == s - 2 && s > 1) {
-        BVert a = Lp[s - 1], b = Lp[s - 2];
-        rev = vertex_pdf(sc, a, sampled, b);
+        rev = vertex_pdf(sc, Lp[s - 1], sampled, Lp[s - 2]);
       }
     } else if (s == 1) {
       if (i == s - 1 && sampled) {
         fwd = sampled->fwd;
-        BVert a = C[t - 1], b = C[t - 2];
-        rev = vertex_pdf(sc, a, &b, *sampled);
+        BVert b = C[t - 2];
+        rev = vertex_pdf(sc, C[t - 1], &b, *sampled);
         conn = true;
       }
     } else {
       if (i == s - 1) {
-        BVert a = C[t - 1], b = C[t - 2], c = Lp[s - 1];
-        rev = vertex_pdf(sc, a, &b, c);
+        BVert b = C[t - 2];
+        rev = vertex_pdf(sc, C[t - 1], &b, Lp[s - 1]);
         conn = true;
       } else if (i == s - 2 && s > 1) {
-        BVert a = Lp[s - 1], b = C[t - 1], c = Lp[s - 2];
-        rev = vertex_pdf(sc, a, &b, c);
+        BVert b = C[t - 1];
+        rev = vertex_pdf(sc, Lp[s - 1], &b, Lp[s - 2]);
       }
     }
     ri *= remap0(rev) / remap0(fwd);
     if (conn) sum += ri;
+    v = pv;
   }
   return 1.f / (1.f + sum);
 }
@@ -551,7 +572,7 @@ __device__ __forceinline__ uint32_t draws_before(int s, int t, uint2 m) {
 
 // evaluateBDPTStrategy (bdpt.go:294-561) for strategy (s, t) of sample i;
 // returns the weighted contribution to the sample (t = 1 splats instead).
-__device__ __noinline__ float3 eval_strategy(const DevScene& sc, const DevFilm& film, const DevBdpt& B, uint32_t i,
+__device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFilm& film, const DevBdpt& B, uint32_t i,
                                              int s, int t, Rng& rs, int* err) {
   const float3 zero = f3(0.f, 0.f, 0.f);
   SubpathRef C{&B, i, 0}, Lp{&B, i, B.maxv};
@@ -776,35 +797,83 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
   }
 }
 
-// One thread per (strategy, sample): strategy k = s * MAXV + (t - 1); the
-// samples of one strategy are consecutive threads, so a warp evaluates one
-// (s, t) for 32 samples (uniform control flow and coalesced vertex reads).
+// Strategy k = s * MAXV + (t - 1) of a sample is evaluated when s <= nl and
+// t <= nc, except (1,1) (bdpt.go:300-301) and s = 0 with t != nc (the
+// path-tracing strategy contributes only at the full camera path).
+__device__ __forceinline__ bool has_strategy(int s, int t, int nc, int nl) {
+  return s <= nl && t <= nc && !(s == 1 && t == 1) && !(s == 0 && t != nc);
+}
+
+// Lists, per strategy, the samples that have it, so that the strategy kernel
+// gives each warp 32 real (s, t, sample) items: one warp-aggregated atomic per
+// strategy and warp.  The order within a list does not matter: every item
+// writes its own contribution slot.
 template <int MAXV>
-__global__ void __launch_bounds__(128) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+__global__ void k_bdpt_list(DevPaths PS, ChunkDesc ch) {
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
-  const uint64_t total = (uint64_t)(MAXV + 1) * MAXV * n;
-  int* err = reinterpret_cast<int*>(PS.counters + 3);
-  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < total;
-       g += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t k = (uint32_t)(g / n), i = (uint32_t)(g - (uint64_t)k * n);
-    int s = (int)(k / MAXV), t = (int)(k % MAXV) + 1;
-    uint4 m = B.meta[i];
-    int nc = (int)(m.x & 0xFF), nl = (int)(m.x >> 8);
-    if (s > nl || t > nc) continue;
-    float3 c = f3(0.f, 0.f, 0.f);
-    // (1,1) is skipped (bdpt.go:300-301); s = 0 contributes only at t = nc
-    if (!(s == 1 && t == 1) && !(s == 0 && t != nc)) {
-      Rng rs;
-      rs.init(ch.seed, m.z, m.w, m.y + draws_before(s, t, B.masks[i]));
-      c = eval_strategy(sc, film, B, i, s, t, rs, err);
+  const int lane = threadIdx.x & 31;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    uint32_t i = base + threadIdx.x;
+    int nc = 0, nl = -1;
+    if (i < n) {
+      uint32_t m = B.meta[i].x;
+      nc = (int)(m & 0xFF);
+      nl = (int)(m >> 8);
     }
+    for (int k = 0; k < (MAXV + 1) * MAXV; k++) {
+      int s = k / MAXV, t = k % MAXV + 1;
+      bool has = has_strategy(s, t, nc, nl);
+      unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
+      if (!mask) continue;
+      int leader = __ffs(mask) - 1;
+      uint32_t at = 0;
+      if (lane == leader) at = atomicAdd(B.scount + k, (uint32_t)__popc(mask));
+      at = __shfl_sync(0xFFFFFFFFu, at, leader);
+      if (has) B.slist[(size_t)k * B.ns + at + __popc(mask & ((1u << lane) - 1u))] = i;
+    }
+  }
+}
+
+// One thread per listed (strategy, sample) item, the items of a strategy
+// consecutive: a warp evaluates one (s, t) for 32 samples that have it
+// (uniform control flow, neighbouring warps on the same code).
+template <int MAXV>
+__global__ void __launch_bounds__(128) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+  constexpr int K = (MAXV + 1) * MAXV;
+  __shared__ uint32_t first[K + 1];  // prefix sums of the list lengths
+  const DevBdpt& B = PS.bd;
+  const uint32_t n = ch.npix * ch.layers;
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int k = 0; k < K; k++) {
+      first[k] = acc;
+      acc += B.scount[k];
+    }
+    first[K] = acc;
+  }
+  __syncthreads();
+  const uint32_t total = first[K];
+  int* err = reinterpret_cast<int*>(PS.counters + 3);
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int lo = 0, hi = K;  // the strategy k with first[k] <= g < first[k + 1]
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (first[mid] <= g) lo = mid;
+      else hi = mid;
+    }
+    const int k = lo;
+    const uint32_t i = B.slist[(size_t)k * B.ns + (g - first[k])];
+    const int s = k / MAXV, t = k % MAXV + 1;
+    uint4 m = B.meta[i];
+    Rng rs;
+    rs.init(ch.seed, m.z, m.w, m.y + draws_before(s, t, B.masks[i]));
+    float3 c = eval_strategy(sc, film, B, i, s, t, rs, err);
     B.contrib[(size_t)k * n + i] = make_float4(c.x, c.y, c.z, 0.f);
   }
 }
 
-// The sample's radiance: its strategies' contributions summed in the
-// reference's s-major order (the same additions as its RayColor loop).
 template <int MAXV>
 __global__ void k_bdpt_sum(DevPaths PS, ChunkDesc ch) {
   const DevBdpt& B = PS.bd;
@@ -815,7 +884,7 @@ __global__ void k_bdpt_sum(DevPaths PS, ChunkDesc ch) {
     float3 total = f3(0.f, 0.f, 0.f);
     for (int s = 0; s <= nl; s++)
       for (int t = 1; t <= nc; t++) {
-        if (s == 1 && t == 1) continue;
+        if (!has_strategy(s, t, nc, nl)) continue;  // (1,1) and (0, t < nc) contribute nothing
         float4 c = B.contrib[(size_t)(s * MAXV + t - 1) * n + i];
         total += f3(c);
       }
@@ -835,12 +904,15 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
   int g1 = launch_grid(n, 128, 0);
   int g2 = std::max(1, sms * 16);
   int g3 = launch_grid(n, 256, 0);
+  cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * (P.bd.maxv + 1) * P.bd.maxv, st);
   if (P.bd.maxv == 10) {
     k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_list<10><<<g3, 256, 0, st>>>(P, ch);
     k_bdpt_strategies<10><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_sum<10><<<g3, 256, 0, st>>>(P, ch);
   } else {
     k_bdpt_subpaths<18><<<g1, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_list<18><<<g3, 256, 0, st>>>(P, ch);
     k_bdpt_strategies<18><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_sum<18><<<g3, 256, 0, st>>>(P, ch);
   }
