@@ -473,6 +473,7 @@ __device__ __forceinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B,
 }
 
 // calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
+template <int CLS>
 __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef& C, const SubpathRef& Lp,
                                          const BVert* sampled, int s, int t) {
   if (s + t == 2) return 1.f;
@@ -484,20 +485,20 @@ __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef
     VPdf pv = C.pdfs(i - 1);  // the predecessor: its flags here, the walk's next vertex
     float fwd = v.fwd, rev = v.rev;
     bool conn = !(v.flags & kFlagSpecular);
-    if (s == 0) {
+    if (CLS == 0) {
       if (i == t - 1 && t > 1) {
         rev = light_origin_pdf(sc, C[t - 1], C[t - 2]);
         conn = true;
       } else if (i == t - 2 && t > 2) {
         rev = vertex_pdf(sc, C[t - 1], nullptr, C[t - 2]);
       }
-    } else if (t == 1) {
+    } else if (CLS == 1) {
       if (i == 0) {
         fwd = sampled->fwd;
         rev = sampled->rev;
         conn = true;
       }
-    } else if (s == 1) {
+    } else if (CLS == 2) {
       if (i == t - 1 && t > 0) {
         rev = vertex_pdf(sc, *sampled, nullptr, C[t - 1]);
         conn = true;
@@ -526,14 +527,14 @@ __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef
     float fwd = v.fwd, rev = v.rev;
     bool conn = !(v.flags & kFlagSpecular) && !is_delta_light(sc, v);
     if (i > 0) conn = conn && !(pv.flags & kFlagSpecular) && !is_delta_light(sc, pv);
-    if (t == 1) {
+    if (CLS == 1) {
       if (i == s - 1 && s > 1) {
         rev = vertex_pdf(sc, *sampled, nullptr, Lp[s - 1]);
         conn = true;
       } else if (i == s - 2 && s > 1) {
         rev = vertex_pdf(sc, Lp[s - 1], sampled, Lp[s - 2]);
       }
-    } else if (s == 1) {
+    } else if (CLS == 2) {
       if (i == s - 1 && sampled) {
         fwd = sampled->fwd;
         BVert b = C[t - 2];
@@ -572,6 +573,7 @@ __device__ __forceinline__ uint32_t draws_before(int s, int t, uint2 m) {
 
 // evaluateBDPTStrategy (bdpt.go:294-561) for strategy (s, t) of sample i;
 // returns the weighted contribution to the sample (t = 1 splats instead).
+template <int CLS>
 __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFilm& film, const DevBdpt& B, uint32_t i,
                                              int s, int t, Rng& rs, int* err) {
   const float3 zero = f3(0.f, 0.f, 0.f);
@@ -584,11 +586,11 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
   float3 ro = zero, rd = f3(0.f, 0.f, 1.f);
   float rt = 0.f;
   uint32_t rskip = kNoHit;
-  if (s == 0) {
+  if (CLS == 0) {
     // evaluatePathTracingStrategy (bdpt.go:317-332): the caller passes t == nc only
     BVert last = C[t - 1];
     Lc = last.Le * last.beta;
-  } else if (t == 1) {
+  } else if (CLS == 1) {
     // evaluateLightTracingStrategy (bdpt.go:398-486)
     BVert lv = Lp[s - 1];
     if (s <= 1 || lv.is(kFlagSpecular)) return zero;
@@ -628,7 +630,7 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
     has = true;
     splat = true;
     Lc = c;
-  } else if (s == 1) {
+  } else if (CLS == 2) {
     // evaluateDirectLightingStrategy (bdpt.go:334-394)
     BVert cv = C[t - 1];
     if (cv.is(kFlagSpecular) || cv.mat < 0) return zero;
@@ -695,7 +697,7 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
     sampled.rev = total_light_pdf(sc, sampled.p, sampled.n, normalize(Lp[s - 1].p - sampled.p));
   }
   if (is_zero(Lc) && !splat) return zero;
-  float w = mis_weight(sc, C, Lp, has ? &sampled : nullptr, s, t);
+  float w = mis_weight<CLS>(sc, C, Lp, has ? &sampled : nullptr, s, t);
   if (splat) {
     float3 c = Lc * w;
     float4* dst = film.splat + (size_t)spy * film.width + spx;
@@ -836,20 +838,31 @@ __global__ void k_bdpt_list(DevPaths PS, ChunkDesc ch) {
   }
 }
 
-// One thread per listed (strategy, sample) item, the items of a strategy
-// consecutive: a warp evaluates one (s, t) for 32 samples that have it
-// (uniform control flow, neighbouring warps on the same code).
-template <int MAXV>
-__global__ void __launch_bounds__(128) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+// The strategy classes, each evaluated by its own launch so that a launch
+// holds only its class's code: 0 the path-tracing strategy (s = 0, t = nc),
+// 1 light tracing (s >= 2, t = 1), 2 direct lighting (s = 1, t >= 2),
+// 3 connections (s, t >= 2).
+__host__ __device__ constexpr int strategy_class(int s, int t) {
+  return s == 0 ? 0 : t == 1 ? 1 : s == 1 ? 2 : 3;
+}
+
+// One thread per listed (strategy, sample) item of class CLS, the items of a
+// strategy consecutive: a warp evaluates one (s, t) for 32 samples that have
+// it (uniform control flow, neighbouring warps on the same code).  The work
+// is latency-bound; 8 blocks per SM (at most 64 registers, a few spilled)
+// measured fastest on the Cornell-boxes frame (558 ms vs 624 ms at 96
+// registers and 5 blocks).
+template <int MAXV, int CLS>
+__global__ void __launch_bounds__(128, 8) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
   constexpr int K = (MAXV + 1) * MAXV;
-  __shared__ uint32_t first[K + 1];  // prefix sums of the list lengths
+  __shared__ uint32_t first[K + 1];  // prefix sums of the list lengths of the class
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
   if (threadIdx.x == 0) {
     uint32_t acc = 0;
     for (int k = 0; k < K; k++) {
       first[k] = acc;
-      acc += B.scount[k];
+      if (strategy_class(k / MAXV, k % MAXV + 1) == CLS) acc += B.scount[k];
     }
     first[K] = acc;
   }
@@ -869,7 +882,7 @@ __global__ void __launch_bounds__(128) k_bdpt_strategies(DevScene sc, DevFilm fi
     uint4 m = B.meta[i];
     Rng rs;
     rs.init(ch.seed, m.z, m.w, m.y + draws_before(s, t, B.masks[i]));
-    float3 c = eval_strategy(sc, film, B, i, s, t, rs, err);
+    float3 c = eval_strategy<CLS>(sc, film, B, i, s, t, rs, err);
     B.contrib[(size_t)k * n + i] = make_float4(c.x, c.y, c.z, 0.f);
   }
 }
@@ -908,12 +921,18 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
   if (P.bd.maxv == 10) {
     k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_list<10><<<g3, 256, 0, st>>>(P, ch);
-    k_bdpt_strategies<10><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<10, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<10, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<10, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<10, 3><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_sum<10><<<g3, 256, 0, st>>>(P, ch);
   } else {
     k_bdpt_subpaths<18><<<g1, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_list<18><<<g3, 256, 0, st>>>(P, ch);
-    k_bdpt_strategies<18><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<18, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<18, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<18, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
+    k_bdpt_strategies<18, 3><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_sum<18><<<g3, 256, 0, st>>>(P, ch);
   }
 }
