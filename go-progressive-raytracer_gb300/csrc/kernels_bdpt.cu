@@ -742,48 +742,64 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
     c.prim = kNoHit;
     c.flags = kFlagCamera;
     float dir_pdf = camera_dir_pdf(sc.cam, o, d);
-    int nc = gen_subpath<MAXV>(sc, B, p, 0, c, o, d, f3(1.f, 1.f, 1.f), dir_pdf, sc.max_depth, true, rng, kNoHit, err);
-    // generateLightPath (bdpt.go:139-202)
-    int nl = 0;
-    if (sc.n_lights > 0) {
-      float ul = rng.next();
-      int li = pick_light(sc, ul);
-      DevLight L = sc.lights[li];
-      float2 sp = rng.next2();
-      float2 sd = rng.next2();
-      float3 ep, en, ed, Le;
-      float apdf, dpdf;
-      sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
-      float ct = fabsf(dot(ed, en));
-      BVert lv;
-      lv.p = ep;
-      lv.n = en;
-      lv.wi = f3(0.f, 0.f, 0.f);
-      lv.light = li;
-      lv.mat = -1;
-      lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
-                : L.kind == kLightSphere ? sc.sphere_base + (uint32_t)L.prim
-                : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
-                                                                     : kNoHit;
-      lv.fwd = apdf * L.prob;
-      lv.rev = 0.f;
-      bool inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
-      lv.flags = kFlagLight | (inf ? kFlagInfinite : 0);
-      lv.beta = Le;
-      lv.Le = Le;
-      float3 beta = Le * (ct / (L.prob * apdf * dpdf));
-      nl = gen_subpath<MAXV>(sc, B, p, MAXV, lv, ep, ed, beta, dpdf, sc.max_depth - 1, false, rng, lv.prim, err);
-      if (inf) {
-        if (nl > 1) {
-          BVert fb = get_vert(B, MAXV + 1, p);
-          fb.fwd = apdf * L.prob;
-          if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
-          put_vert(B, MAXV + 1, p, fb);
-        }
-        BVert l0 = get_vert(B, MAXV, p);
-        l0.fwd = infinite_density(sc, ep, en, ed);
-        put_vert(B, MAXV, p, l0);
+    // generateLightPath (bdpt.go:139-202) follows in the same sampler stream;
+    // both subpaths go through one inlined gen_subpath (half the code)
+    int nc = 0, nl = 0;
+    float3 beta = f3(1.f, 1.f, 1.f), ep = o, en = f3(0.f, 0.f, 0.f), ed = d;
+    float pdf = dir_pdf, apdf = 0.f, lprob = 1.f;
+    int maxb = sc.max_depth, base = 0;
+    uint32_t skip = kNoHit;
+    bool inf = false;
+    BVert start = c;
+    for (int phase = 0; phase < 2; phase++) {
+      if (phase == 1) {
+        if (sc.n_lights == 0) break;
+        float ul = rng.next();
+        int li = pick_light(sc, ul);
+        DevLight L = sc.lights[li];
+        float2 sp = rng.next2();
+        float2 sd = rng.next2();
+        float3 Le;
+        float dpdf;
+        sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
+        float ct = fabsf(dot(ed, en));
+        BVert& lv = start;
+        lv.p = ep;
+        lv.n = en;
+        lv.wi = f3(0.f, 0.f, 0.f);
+        lv.light = li;
+        lv.mat = -1;
+        lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
+                  : L.kind == kLightSphere ? sc.sphere_base + (uint32_t)L.prim
+                  : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
+                                                                       : kNoHit;
+        lv.fwd = apdf * L.prob;
+        lv.rev = 0.f;
+        inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
+        lv.flags = kFlagLight | (inf ? kFlagInfinite : 0);
+        lv.beta = Le;
+        lv.Le = Le;
+        lprob = L.prob;
+        beta = Le * (ct / (L.prob * apdf * dpdf));
+        pdf = dpdf;
+        maxb = sc.max_depth - 1;
+        base = MAXV;
+        skip = lv.prim;
       }
+      int len = gen_subpath<MAXV>(sc, B, p, base, start, ep, ed, beta, pdf, maxb, phase == 0, rng, skip, err);
+      if (phase == 0) nc = len;
+      else nl = len;
+    }
+    if (inf) {
+      if (nl > 1) {
+        BVert fb = get_vert(B, MAXV + 1, p);
+        fb.fwd = apdf * lprob;
+        if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
+        put_vert(B, MAXV + 1, p, fb);
+      }
+      BVert l0 = get_vert(B, MAXV, p);
+      l0.fwd = infinite_density(sc, ep, en, ed);
+      put_vert(B, MAXV, p, l0);
     }
     // which strategies draw uniform numbers (draws_before)
     uint32_t lm = 0, cm = 0;
