@@ -473,47 +473,74 @@ __device__ __forceinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B,
 }
 
 // calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
+// A vertex named by a pdf request: camera subpath vertex k (k >= 0), light
+// subpath vertex k (kLightV + k), the strategy's sampled vertex, or none.
+constexpr int kNoV = -1, kSampledV = -2, kLightV = 1024;
+
+__device__ __forceinline__ BVert fetch_vert(const SubpathRef& C, const SubpathRef& Lp, const BVert* sampled, int id) {
+  if (id == kSampledV) return *sampled;
+  return id >= kLightV ? Lp[id - kLightV] : C[id];
+}
+
 template <int CLS>
 __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef& C, const SubpathRef& Lp,
                                          const BVert* sampled, int s, int t) {
   if (s + t == 2) return 1.f;
-  // vertices next to the connection are read in full where their pdfs are
-  // recomputed; the rest of the walk reads only pdfs and flags
+  // The reverse pdfs the walk recomputes next to the connection
+  // (bdpt_mis.go:61-105 camera side, :140-178 light side): at most two per
+  // side, each calculateVertexPdf(cur, prev, next), or for s = 0 at t-1
+  // calculateLightOriginPdf(cur, next).  They are named by vertex ids and
+  // evaluated in one loop, so the pdf code is inlined once.
+  int rq[4][3];
+  int nq = 0;
+  int cam1 = -1, cam2 = -1, lit1 = -1, lit2 = -1;  // request of rev at t-1, t-2, s-1, s-2
+  const int c1 = t - 1, c2 = t - 2, l1 = kLightV + s - 1, l2 = kLightV + s - 2;
+  auto add = [&](int cur, int prev, int next) {
+    rq[nq][0] = cur;
+    rq[nq][1] = prev;
+    rq[nq][2] = next;
+    return nq++;
+  };
+  if (CLS == 0) {
+    if (t > 1) cam1 = add(c1, kNoV, c2);  // the light origin pdf
+    if (t > 2) cam2 = add(c1, kNoV, c2);
+  } else if (CLS == 1) {
+    lit1 = add(kSampledV, kNoV, l1);
+    lit2 = add(l1, kSampledV, l2);
+  } else if (CLS == 2) {
+    cam1 = add(kSampledV, kNoV, c1);
+    cam2 = add(c1, kSampledV, c2);
+    lit1 = add(c1, c2, kSampledV);
+  } else {
+    cam1 = add(l1, l2, c1);
+    cam2 = add(c1, l1, c2);
+    lit1 = add(c1, c2, l1);
+    lit2 = add(l1, c1, l2);
+  }
+  float rv[4];
+  for (int q = 0; q < nq; q++) {
+    BVert cur = fetch_vert(C, Lp, sampled, rq[q][0]);
+    BVert next = fetch_vert(C, Lp, sampled, rq[q][2]);
+    if (CLS == 0 && q == cam1) {
+      rv[q] = light_origin_pdf(sc, cur, next);
+    } else {
+      BVert prev;
+      bool hp = rq[q][1] != kNoV;
+      if (hp) prev = fetch_vert(C, Lp, sampled, rq[q][1]);
+      rv[q] = vertex_pdf(sc, cur, hp ? &prev : nullptr, next);
+    }
+  }
   float sum = 0.f, ri = 1.f;
   VPdf v = t >= 1 ? C.pdfs(t - 1) : VPdf{};
   for (int i = t - 1; i > 0; i--) {
     VPdf pv = C.pdfs(i - 1);  // the predecessor: its flags here, the walk's next vertex
     float fwd = v.fwd, rev = v.rev;
     bool conn = !(v.flags & kFlagSpecular);
-    if (CLS == 0) {
-      if (i == t - 1 && t > 1) {
-        rev = light_origin_pdf(sc, C[t - 1], C[t - 2]);
-        conn = true;
-      } else if (i == t - 2 && t > 2) {
-        rev = vertex_pdf(sc, C[t - 1], nullptr, C[t - 2]);
-      }
-    } else if (CLS == 1) {
-      if (i == 0) {
-        fwd = sampled->fwd;
-        rev = sampled->rev;
-        conn = true;
-      }
-    } else if (CLS == 2) {
-      if (i == t - 1 && t > 0) {
-        rev = vertex_pdf(sc, *sampled, nullptr, C[t - 1]);
-        conn = true;
-      } else if (i == t - 2 && t > 1) {
-        rev = vertex_pdf(sc, C[t - 1], sampled, C[t - 2]);
-      }
-    } else {
-      if (i == t - 1) {
-        BVert b = Lp[s - 2];
-        rev = vertex_pdf(sc, Lp[s - 1], &b, C[t - 1]);
-        conn = true;
-      } else if (i == t - 2 && t > 1) {
-        BVert b = Lp[s - 1];
-        rev = vertex_pdf(sc, C[t - 1], &b, C[t - 2]);
-      }
+    if (i == t - 1 && cam1 >= 0) {
+      rev = rv[cam1];
+      conn = true;
+    } else if (i == t - 2 && cam2 >= 0) {
+      rev = rv[cam2];
     }
     conn = conn && !(pv.flags & kFlagSpecular);
     ri *= remap0(rev) / remap0(fwd);
@@ -527,29 +554,12 @@ __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef
     float fwd = v.fwd, rev = v.rev;
     bool conn = !(v.flags & kFlagSpecular) && !is_delta_light(sc, v);
     if (i > 0) conn = conn && !(pv.flags & kFlagSpecular) && !is_delta_light(sc, pv);
-    if (CLS == 1) {
-      if (i == s - 1 && s > 1) {
-        rev = vertex_pdf(sc, *sampled, nullptr, Lp[s - 1]);
-        conn = true;
-      } else if (i == s - 2 && s > 1) {
-        rev = vertex_pdf(sc, Lp[s - 1], sampled, Lp[s - 2]);
-      }
-    } else if (CLS == 2) {
-      if (i == s - 1 && sampled) {
-        fwd = sampled->fwd;
-        BVert b = C[t - 2];
-        rev = vertex_pdf(sc, C[t - 1], &b, *sampled);
-        conn = true;
-      }
-    } else {
-      if (i == s - 1) {
-        BVert b = C[t - 2];
-        rev = vertex_pdf(sc, C[t - 1], &b, Lp[s - 1]);
-        conn = true;
-      } else if (i == s - 2 && s > 1) {
-        BVert b = C[t - 1];
-        rev = vertex_pdf(sc, Lp[s - 1], &b, Lp[s - 2]);
-      }
+    if (i == s - 1 && lit1 >= 0) {
+      if (CLS == 2) fwd = sampled->fwd;
+      rev = rv[lit1];
+      conn = true;
+    } else if (i == s - 2 && lit2 >= 0) {
+      rev = rv[lit2];
     }
     ri *= remap0(rev) / remap0(fwd);
     if (conn) sum += ri;
