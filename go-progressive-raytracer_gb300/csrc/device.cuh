@@ -1020,7 +1020,7 @@ __device__ __forceinline__ LightSample light_sample(const DevScene& sc, const De
     return ls;
   }
   if (L.kind == kLightSphere) {
-    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float4 S = make_float4(L.pos.x, L.pos.y, L.pos.z, L.radius);
     float3 c = f3(S);
     float r = S.w;
     float3 tc = c - p;
@@ -1142,7 +1142,7 @@ __device__ __forceinline__ float light_pdf(const DevScene& sc, const DevLight& L
     return (1.0f / L.area) * t * t / ct;
   }
   if (L.kind == kLightSphere) {
-    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float4 S = make_float4(L.pos.x, L.pos.y, L.pos.z, L.radius);
     float t;
     if (!hit_sphere(p, dir, S, 0.001f, kInfF, t)) return 0.f;
     float dc = length(f3(S) - p);

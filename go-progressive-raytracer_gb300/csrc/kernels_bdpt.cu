@@ -124,7 +124,7 @@ __device__ __forceinline__ void sample_emission(const DevScene& sc, const DevLig
     return;
   }
   if (L.kind == kLightSphere) {
-    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float4 S = make_float4(L.pos.x, L.pos.y, L.pos.z, L.radius);
     float z = 1.f - 2.f * sp.x;
     float r = sqrtf(fmaxf(0.f, 1.f - z * z));
     float s_, c_;
@@ -199,7 +199,7 @@ __device__ __forceinline__ float pdf_le(const DevScene& sc, const DevLight& L, f
     return ct <= 0.f ? 0.f : ct / kPi;
   }
   if (L.kind == kLightSphere) {
-    float4 S = __ldg(sc.spheres + (size_t)L.prim * 2);
+    float4 S = make_float4(L.pos.x, L.pos.y, L.pos.z, L.radius);
     float dc = length(p - f3(S));
     if (!(fabsf(dc - S.w) <= 0.001f * fmaxf(1.f, fabsf(S.w) * 1e-3f))) return 0.f;
     float3 n = normalize(p - f3(S));
@@ -780,7 +780,7 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
         lv.light = li;
         lv.mat = -1;
         lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
-                  : L.kind == kLightSphere ? sc.sphere_base + (uint32_t)L.prim
+                  : L.kind == kLightSphere ? (L.prim >= 0 ? sc.sphere_base + (uint32_t)L.prim : kNoHit)
                   : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
                                                                        : kNoHit;
         lv.fwd = apdf * L.prob;

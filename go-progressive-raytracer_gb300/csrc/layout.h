@@ -61,15 +61,16 @@ struct DevMaterial {
 
 struct DevLight {
   int kind;
-  int prim;   // index in the quad, sphere or quadric (disc) array (area lights)
+  int prim;   // index in the quad, sphere or quadric (disc) array (area lights);
+              // -1 for a sphere light that is not a scene shape
   float prob; // light-sampler selection probability
   float area; // quad area |u x v| (quad_light.go:19-27); disc area pi r^2
   float3 a;   // emission (area, uniform, spot) or top colour (gradient)
   float cos_total;    // spot lights: cosine of the total cone angle
   float3 b;   // bottom colour (gradient); unit spot direction (spot lights)
   float cos_falloff;  // spot lights: cosine of the falloff start angle
-  float3 pos; // point spot light position
-  float pad;
+  float3 pos; // point spot light position; sphere light centre
+  float radius;  // sphere light radius
 };
 static_assert(sizeof(DevLight) == 64, "DevLight is four 16-byte words");
 

@@ -913,12 +913,25 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
         break;
       }
       case GPRT_LIGHT_SPHERE: {
+        if (l.shape == GPRT_NO_SHAPE) {  // a sphere light that is not a scene shape (the PBRT point light)
+          if (!(l.radius > 0)) {
+            err = "a sphere light without a shape needs a positive radius";
+            return false;
+          }
+          L.prim = -1;
+          L.pos = to_f3(l.from);
+          L.radius = (float)l.radius;
+          L.a = to_f3(l.color_a);
+          break;
+        }
         if (l.shape >= d->n_shapes || shape_sphere_prim[l.shape] < 0) {
           err = "sphere light must reference a sphere shape";
           return false;
         }
         int pid = shape_sphere_prim[l.shape];
         L.prim = (int)final_index[pid];
+        L.pos = make_float3((float)prims[pid].a.x, (float)prims[pid].a.y, (float)prims[pid].a.z);
+        L.radius = (float)prims[pid].b.x;
         L.a = emission_of(prims[pid].material);
         break;
       }
@@ -973,7 +986,8 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
     out.lights.push_back(L);
     if (out.device_bvh)  // remapped to leaf order by the device builder
       out.pending.light_prim.push_back(l.kind == GPRT_LIGHT_QUAD     ? shape_quad_prim[l.shape]
-                                       : l.kind == GPRT_LIGHT_SPHERE ? shape_sphere_prim[l.shape]
+                                       : l.kind == GPRT_LIGHT_SPHERE
+                                           ? (l.shape == GPRT_NO_SHAPE ? -1 : shape_sphere_prim[l.shape])
                                        : (l.kind == GPRT_LIGHT_DISC || l.kind == GPRT_LIGHT_DISC_SPOT)
                                            ? shape_disc_prim[l.shape]
                                            : -1);
@@ -1157,7 +1171,7 @@ std::string validate_layout(const HostScene& s) {
              : L.kind == kLightSphere ? s.n_spheres
              : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? s.n_quadrics
                                                                   : SIZE_MAX;
-    if (n == SIZE_MAX) continue;
+    if (n == SIZE_MAX || (L.kind == kLightSphere && L.prim == -1)) continue;  // -1: a sphere light with no shape
     if (L.prim < 0 || (size_t)L.prim >= n) return "light primitive out of range";
     if (L.kind == kLightDisc || L.kind == kLightDiscSpot) {
       int kind;

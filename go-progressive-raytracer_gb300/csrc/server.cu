@@ -193,7 +193,7 @@ __global__ void k_rebase_nodes(float4* nodes, uint32_t n, int node_off, int tri_
 __global__ void k_rebase_lights(DevLight* L, uint32_t n, int quad_off, int sph_off, int qdr_off) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (L[i].kind == kLightQuad) L[i].prim += quad_off;
-    else if (L[i].kind == kLightSphere) L[i].prim += sph_off;
+    else if (L[i].kind == kLightSphere && L[i].prim >= 0) L[i].prim += sph_off;
     else if (L[i].kind == kLightDisc || L[i].kind == kLightDiscSpot) L[i].prim += qdr_off;
   }
 }

@@ -21,6 +21,7 @@ GPRT_E_NOT_FOUND = -7
 
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_LAYERED, MAT_SPOT_EMISSIVE, MAT_MIX = range(7)
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_MESH, SHAPE_TRIANGLE, SHAPE_DISC, SHAPE_CYLINDER, SHAPE_CONE = range(8)
+NO_SHAPE = 0xFFFFFFFF
 (LIGHT_QUAD, LIGHT_SPHERE, LIGHT_UNIFORM_INFINITE, LIGHT_GRADIENT_INFINITE, LIGHT_DISC, LIGHT_DISC_SPOT,
  LIGHT_POINT_SPOT) = range(7)
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
@@ -53,7 +54,7 @@ class MeshDesc(C.Structure):
 class LightDesc(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("shape", C.c_uint32), ("color_a", C.c_double * 3),
                 ("color_b", C.c_double * 3), ("weight", C.c_double), ("from_", C.c_double * 3), ("to", C.c_double * 3),
-                ("cone_deg", C.c_double), ("cone_delta_deg", C.c_double)]
+                ("cone_deg", C.c_double), ("cone_delta_deg", C.c_double), ("radius", C.c_double)]
 
 
 class CameraDesc(C.Structure):
@@ -158,6 +159,14 @@ F32P = C.POINTER(C.c_float)
 U32P = C.POINTER(C.c_uint32)
 U64P = C.POINTER(C.c_uint64)
 U8P = C.POINTER(C.c_uint8)
+F64PP = C.POINTER(C.POINTER(C.c_double))
+U32PP = C.POINTER(C.POINTER(C.c_uint32))
+
+
+class PlyInfo(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("n_vertices", "n_triangles", "has_normals", "has_colors", "has_texcoords",
+                                         "reserved")]
+
 
 # name -> (restype, argtypes); every symbol the header declares
 SIGNATURES = {
@@ -206,6 +215,13 @@ SIGNATURES = {
     "gprt_server_stream": (C.c_int, [P, PP]),
     "gprt_server_configure": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "gprt_server_autotune": (C.c_int, [P, C.c_double, C.POINTER(TuneResult)]),
+    "gprt_pbrt_parse": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(CameraDesc), PP, C.c_char_p, C.c_size_t]),
+    "gprt_pbrt_load": (C.c_int, [C.c_char_p, C.POINTER(CameraDesc), PP, C.c_char_p, C.c_size_t]),
+    "gprt_loaded_desc": (C.POINTER(SceneDesc), [P]),
+    "gprt_loaded_free": (None, [P]),
+    "gprt_ply_load": (C.c_int, [C.c_char_p, PP, C.c_char_p, C.c_size_t]),
+    "gprt_ply_get": (C.c_int, [P, C.POINTER(PlyInfo), F64PP, U32PP, F64PP, F64PP, F64PP]),
+    "gprt_ply_free": (None, [P]),
 }
 
 _lib = None

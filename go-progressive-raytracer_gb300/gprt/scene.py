@@ -182,6 +182,7 @@ class Light:
     to: Vec3 = (0.0, 0.0, 0.0)
     cone_deg: float = 0.0
     cone_delta_deg: float = 0.0
+    radius: float = 0.0  # a sphere light with no shape: its radius (centre in from_)
 
 
 @dataclass
@@ -388,6 +389,8 @@ class FlatScene:
             d.kind = l.kind
             if l.shape is not None:
                 d.shape = shape_index[id(l.shape)]
+            elif l.kind == capi.LIGHT_SPHERE:
+                d.shape = capi.NO_SHAPE
             for k in range(3):
                 d.color_a[k] = l.color_a[k]
                 d.color_b[k] = l.color_b[k]
@@ -395,6 +398,7 @@ class FlatScene:
                 d.to[k] = l.to[k]
             d.cone_deg = l.cone_deg
             d.cone_delta_deg = l.cone_delta_deg
+            d.radius = l.radius
             d.weight = scene.light_weights[i] if scene.light_weights else 1.0
         meshd = (capi.MeshDesc * max(1, len(meshes)))(*meshes) if meshes else (capi.MeshDesc * 1)()
         desc = capi.SceneDesc()

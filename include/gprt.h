@@ -119,7 +119,9 @@ typedef struct gprt_mesh_desc {
 
 enum gprt_light_kind {
   GPRT_LIGHT_QUAD = 0,              /* pkg/lights/quad_light.go; shape = a QUAD shape */
-  GPRT_LIGHT_SPHERE = 1,            /* pkg/lights/sphere_light.go; shape = a SPHERE shape */
+  GPRT_LIGHT_SPHERE = 1,            /* pkg/lights/sphere_light.go; shape = a SPHERE shape, or GPRT_NO_SHAPE for a
+                                       light whose sphere is not a scene shape (from = centre, radius, color_a =
+                                       emission; the PBRT point light, pkg/scene/pbrt_scene.go:340-349) */
   GPRT_LIGHT_UNIFORM_INFINITE = 2,  /* pkg/lights/uniform_infinite_light.go; color_a = emission */
   GPRT_LIGHT_GRADIENT_INFINITE = 3, /* pkg/lights/gradient_infinite_light.go; color_a = top, color_b = bottom */
   GPRT_LIGHT_DISC = 4,              /* pkg/lights/disc_light.go; shape = a DISC shape with an emissive material */
@@ -129,6 +131,8 @@ enum gprt_light_kind {
   GPRT_LIGHT_POINT_SPOT = 6         /* pkg/lights/point_spot_light.go (scene.AddPointSpotLight); no shape;
                                        color_a = emission, from, to, cone_deg, cone_delta_deg */
 };
+
+#define GPRT_NO_SHAPE 0xFFFFFFFFu
 
 typedef struct gprt_light_desc {
   uint32_t kind;   /* gprt_light_kind */
@@ -140,6 +144,7 @@ typedef struct gprt_light_desc {
   double to[3];    /* spot lights: the point aimed at */
   double cone_deg;       /* spot lights: total cone angle, degrees */
   double cone_delta_deg; /* spot lights: falloff transition angle, degrees */
+  double radius;         /* SPHERE with GPRT_NO_SHAPE: the sphere's radius */
 } gprt_light_desc;
 
 /* geometry.CameraConfig, pkg/geometry/camera.go:18-32 */
@@ -516,6 +521,44 @@ int gprt_server_configure(gprt_server* server, uint32_t step_paths, uint32_t blo
  * samples per second among those whose step takes at most max_step_ms
  * (0: no limit).  Needs admitted, unfinished jobs. */
 int gprt_server_autotune(gprt_server* server, double max_step_ms, gprt_tune_result* out);
+
+/* ---- loaders ------------------------------------------------------------
+ * PBRT-v4 subset scenes (loaders.LoadPBRT / ParsePBRT, pkg/loaders/pbrt.go)
+ * converted as scene.NewPBRTScene does (pkg/scene/pbrt_scene.go): the
+ * loaded handle owns a gprt_scene_desc (and its arrays) valid until
+ * gprt_loaded_free, ready for gprt_scene_create.  camera_override may be
+ * NULL (its non-zero fields win, MergeCameraConfig).  gprt_pbrt_load keeps
+ * the reference's path rules (validateFilePath, pbrt.go:391-433: under a
+ * scenes/ directory or the temporary directory, .pbrt, at most 512 bytes).
+ * Errors: GPRT_E_INVALID with the reference's message in errbuf.  Needs no
+ * GPU. */
+typedef struct gprt_loaded gprt_loaded;
+int gprt_pbrt_parse(const char* text, size_t len, const gprt_camera_desc* camera_override,
+                    gprt_loaded** out, char* errbuf, size_t err_len);
+int gprt_pbrt_load(const char* path, const gprt_camera_desc* camera_override, gprt_loaded** out,
+                   char* errbuf, size_t err_len);
+const gprt_scene_desc* gprt_loaded_desc(const gprt_loaded* loaded);
+void gprt_loaded_free(gprt_loaded* loaded);
+
+/* Binary little-endian PLY meshes (loaders.LoadPLY, pkg/loaders/ply.go):
+ * float x, y, z (and nx, ny, nz / u, v; uchar red, green, blue as [0,1]),
+ * triangular faces.  The arrays (3 doubles per vertex, 3 indices per
+ * triangle, 2 doubles per texture coordinate) feed gprt_mesh_desc directly
+ * and stay valid until gprt_ply_free; absent attributes return NULL. */
+typedef struct gprt_ply gprt_ply;
+typedef struct gprt_ply_info {
+  uint32_t n_vertices;
+  uint32_t n_triangles;
+  uint32_t has_normals;
+  uint32_t has_colors;
+  uint32_t has_texcoords;
+  uint32_t reserved;
+} gprt_ply_info;
+int gprt_ply_load(const char* path, gprt_ply** out, char* errbuf, size_t err_len);
+int gprt_ply_get(const gprt_ply* ply, gprt_ply_info* info, const double** vertices,
+                 const uint32_t** indices, const double** normals, const double** colors,
+                 const double** texcoords);
+void gprt_ply_free(gprt_ply* ply);
 
 #ifdef __cplusplus
 }

@@ -141,6 +141,15 @@ Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
         break;
       }
       case GPRT_LIGHT_SPHERE: {
+        if (l.shape == GPRT_NO_SHAPE) {  // its sphere is not a scene shape (not in the BVH)
+          auto sph = std::make_unique<Sphere>(v3(l.from), l.radius, nullptr);
+          auto em = std::make_unique<Emissive>(v3(l.color_a));
+          sph->material = em.get();
+          light = std::make_unique<SphereLight>(sph.get());
+          s->ownedShapes.push_back(std::move(sph));
+          s->materials.push_back(std::move(em));
+          break;
+        }
         if (l.shape >= d->n_shapes || d->shapes[l.shape].kind != GPRT_SHAPE_SPHERE) {
           err = "sphere light must reference a sphere shape";
           return nullptr;

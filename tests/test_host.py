@@ -14,7 +14,7 @@ from conftest import ROOT
 
 def header_symbols():
     txt = open(os.path.join(ROOT, "include", "gprt.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gprt_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|const \w+\s*\*)\s+(gprt_\w+)\s*\(", txt, re.M)))
 
 
 def test_library_exports_every_header_symbol(gprt_lib):
