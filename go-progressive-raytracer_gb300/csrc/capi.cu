@@ -29,7 +29,7 @@ int ensure_bdpt(gprt_job* j) {
   B.uv = nullptr;
   if (j->scene->dev.has_textures) rc |= dev_alloc(ctx, b, &B.uv, (size_t)ns * 2 * B.maxv);
   rc |= dev_alloc(ctx, b, &B.slist, (size_t)ns * (B.maxv + 1) * B.maxv);
-  rc |= dev_alloc(ctx, b, &B.scount, (size_t)(B.maxv + 1) * B.maxv);
+  rc |= dev_alloc(ctx, b, &B.scount, (size_t)(B.maxv + 1) * B.maxv + 1);  // + the subpath work counter
   if (rc) return GPRT_E_OOM;
   P.stats = nullptr;
   P.variant = 0;

@@ -44,7 +44,7 @@ struct DevBdpt {
   float4* contrib;
   float2* uv;     // surface UV per vertex (scenes with textures only, else null)
   uint32_t* slist;   // per strategy k: the samples that have it, ns slots from k * ns
-  uint32_t* scount;  // per strategy: entries in slist
+  uint32_t* scount;  // per strategy: entries in slist; then the subpath kernel's work counter
   uint32_t ns;    // samples per chunk
   int maxv;       // vertices per subpath (10 or 18)
 };

@@ -396,80 +396,90 @@ struct SubpathRef {
 
 // extendPath (bdpt.go:206-291), writing vertex `len-1` once its reverse pdf
 // is final; `prev` enters as the subpath's first vertex.  Returns the length.
+// The state of one subpath between bounces of extendPath.
+struct SubState {
+  BVert prev;  // the last vertex, written once its reverse pdf is final
+  float3 o, d, beta;
+  float pdf_fwd;
+  int len, b, max_bounces, base;
+  uint32_t skip;
+  bool camera;
+};
+
+// One bounce of extendPath (bdpt.go:206-291): returns true when the subpath
+// has ended (vertex len - 1, `prev`, is then still to be written).
 template <int MAXV>
-__device__ __forceinline__ int gen_subpath(const DevScene& sc, const DevBdpt& B, uint32_t i, int base, BVert prev,
-                                        float3 o, float3 d, float3 beta, float pdf_fwd, int max_bounces, bool camera,
-                                        Rng& rng, uint32_t skip, int* err) {
-  int len = 1;
-  for (int b = 0; b < max_bounces && len < MAXV; b++) {
-    Hit h;
-    if (!trace<false, false>(sc, o, d, 0.001f, kInfF, skip, h, err)) {
-      if (camera) {
-        // createBackgroundVertex (bdpt.go:585-601)
-        float3 bg = background(sc, d);
-        BVert v;
-        v.p = o + d * 1000.f;
-        v.n = -d;
-        v.wi = -d;
-        v.fwd = pdf_fwd;
-        v.rev = 0.f;
-        v.beta = beta;
-        v.Le = bg;
-        v.mat = -1;
-        v.light = -1;
-        v.prim = kNoHit;
-        v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
-        put_vert(B, base + len - 1, i, prev);
-        prev = v;
-        len++;
-      }
-      break;
+__device__ __forceinline__ bool subpath_step(const DevScene& sc, const DevBdpt& B, uint32_t i, SubState& st, Rng& rng,
+                                             int* err) {
+  if (!(st.b < st.max_bounces && st.len < MAXV)) return true;
+  Hit h;
+  if (!trace<false, false>(sc, st.o, st.d, 0.001f, kInfF, st.skip, h, err)) {
+    if (st.camera) {
+      // createBackgroundVertex (bdpt.go:585-601)
+      float3 bg = background(sc, st.d);
+      BVert v;
+      v.p = st.o + st.d * 1000.f;
+      v.n = -st.d;
+      v.wi = -st.d;
+      v.fwd = st.pdf_fwd;
+      v.rev = 0.f;
+      v.beta = st.beta;
+      v.Le = bg;
+      v.mat = -1;
+      v.light = -1;
+      v.prim = kNoHit;
+      v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
+      put_vert(B, st.base + st.len - 1, i, st.prev);
+      st.prev = v;
+      st.len++;
     }
-    Surface s;
-    surface_at(sc, o, d, h, s);
-    DevMaterial m = load_material(sc, s.mat);
-    BVert v;
-    v.p = s.p;
-    v.n = s.n;
-    v.wi = -d;
-    v.beta = beta;
-    v.Le = emitted(m, s.front, d);
-    v.mat = s.mat;
-    v.uv = s.uv;
-    v.light = -1;
-    v.prim = h.prim;
-    v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
-    v.rev = 0.f;
-    v.fwd = to_area(sc, prev, v, pdf_fwd);
-    Scatter scn;
-    if (!scatter(sc, m, d, s, rng, scn)) {
-      put_vert(B, base + len - 1, i, prev);
-      prev = v;
-      len++;
-      break;
-    }
-    pdf_fwd = scn.pdf;
-    if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
-    float ct = fabsf(dot(scn.dir, s.n));
-    if (scn.pdf <= 0.f) beta = beta * scn.att;
-    else beta = beta * scn.att * (ct / scn.pdf);
-    bool rdelta;
-    float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
-    if (rdelta) {
-      v.flags |= kFlagSpecular;
-      pdf_rev = 0.f;
-      pdf_fwd = 0.f;
-    }
-    prev.rev = to_area(sc, v, prev, pdf_rev);
-    put_vert(B, base + len - 1, i, prev);
-    prev = v;
-    len++;
-    o = s.p;
-    d = scn.dir;
-    skip = h.prim;
+    return true;
   }
-  put_vert(B, base + len - 1, i, prev);
-  return len;
+  Surface s;
+  const float3 d = st.d;
+  surface_at(sc, st.o, d, h, s);
+  DevMaterial m = load_material(sc, s.mat);
+  BVert v;
+  v.p = s.p;
+  v.n = s.n;
+  v.wi = -d;
+  v.beta = st.beta;
+  v.Le = emitted(m, s.front, d);
+  v.mat = s.mat;
+  v.uv = s.uv;
+  v.light = -1;
+  v.prim = h.prim;
+  v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
+  v.rev = 0.f;
+  v.fwd = to_area(sc, st.prev, v, st.pdf_fwd);
+  Scatter scn;
+  if (!scatter(sc, m, d, s, rng, scn)) {
+    put_vert(B, st.base + st.len - 1, i, st.prev);
+    st.prev = v;
+    st.len++;
+    return true;
+  }
+  st.pdf_fwd = scn.pdf;
+  if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
+  float ct = fabsf(dot(scn.dir, s.n));
+  if (scn.pdf <= 0.f) st.beta = st.beta * scn.att;
+  else st.beta = st.beta * scn.att * (ct / scn.pdf);
+  bool rdelta;
+  float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
+  if (rdelta) {
+    v.flags |= kFlagSpecular;
+    pdf_rev = 0.f;
+    st.pdf_fwd = 0.f;
+  }
+  st.prev.rev = to_area(sc, v, st.prev, pdf_rev);
+  put_vert(B, st.base + st.len - 1, i, st.prev);
+  st.prev = v;
+  st.len++;
+  st.o = s.p;
+  st.d = scn.dir;
+  st.skip = h.prim;
+  st.b++;
+  return false;
 }
 
 // calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
@@ -722,48 +732,75 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
 // generateCameraPath + generateLightPath (bdpt.go:106-202) for every sample
 // of the chunk, in the reference's draw order; records the subpath lengths,
 // the sampler position the strategies start from and the strategy draw masks.
+// Persistent: each lane advances its own sample one bounce at a time and,
+// when that sample's subpaths are done, takes the next sample from a
+// warp-aggregated counter, so a warp is not held by its longest path.
 template <int MAXV>
 __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
   const DevBdpt& B = PS.bd;
-  uint32_t n = ch.npix * ch.layers;
+  const uint32_t n = ch.npix * ch.layers;
+  uint32_t* next = B.scount + (MAXV + 1) * MAXV;  // the work counter, zeroed with the lists
   int* err = reinterpret_cast<int*>(PS.counters + 3);
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    uint32_t layer = p / ch.npix, i = p - layer * ch.npix;
-    uint32_t pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
-    uint32_t sample = film.count[pix] + layer;
-    int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
-    Rng rng;
-    rng.init(ch.seed, pix, sample);
-    float2 lens = rng.next2();
-    float2 jit = rng.next2();
-    float3 o, d;
-    camera_ray(sc.cam, x, y, lens, jit, o, d);
-    // generateCameraPath (bdpt.go:106-135)
-    BVert c;
-    c.p = o;
-    c.n = -d;
-    c.wi = f3(0.f, 0.f, 0.f);
-    c.beta = f3(1.f, 1.f, 1.f);
-    c.Le = f3(0.f, 0.f, 0.f);
-    c.fwd = 0.f;
-    c.rev = 0.f;
-    c.mat = -1;
-    c.light = -1;
-    c.prim = kNoHit;
-    c.flags = kFlagCamera;
-    float dir_pdf = camera_dir_pdf(sc.cam, o, d);
-    // generateLightPath (bdpt.go:139-202) follows in the same sampler stream;
-    // both subpaths go through one inlined gen_subpath (half the code)
-    int nc = 0, nl = 0;
-    float3 beta = f3(1.f, 1.f, 1.f), ep = o, en = f3(0.f, 0.f, 0.f), ed = d;
-    float pdf = dir_pdf, apdf = 0.f, lprob = 1.f;
-    int maxb = sc.max_depth, base = 0;
-    uint32_t skip = kNoHit;
-    bool inf = false;
-    BVert start = c;
-    for (int phase = 0; phase < 2; phase++) {
-      if (phase == 1) {
-        if (sc.n_lights == 0) break;
+  int phase = -1;  // -1: needs a sample, 0: camera subpath, 1: light subpath
+  uint32_t p = 0, pix = 0, sample = 0;
+  int nc = 0;
+  Rng rng;
+  SubState st;
+  // the light subpath's start, for the infinite-light corrections after it
+  float3 ep = f3(0.f, 0.f, 0.f), en = f3(0.f, 0.f, 0.f), ed = f3(0.f, 0.f, 0.f);
+  float apdf = 0.f, lprob = 1.f;
+  bool inf = false;
+  for (;;) {
+    if (phase < 0) {
+      unsigned act = __activemask();
+      int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+      uint32_t at = 0;
+      if (lane == leader) at = atomicAdd(next, (uint32_t)__popc(act));
+      at = __shfl_sync(act, at, leader);
+      p = at + (uint32_t)__popc(act & ((1u << lane) - 1u));
+      if (p >= n) break;
+      uint32_t layer = p / ch.npix, i = p - layer * ch.npix;
+      pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
+      sample = film.count[pix] + layer;
+      int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
+      rng.init(ch.seed, pix, sample);
+      float2 lens = rng.next2();
+      float2 jit = rng.next2();
+      float3 o, d;
+      camera_ray(sc.cam, x, y, lens, jit, o, d);
+      // generateCameraPath (bdpt.go:106-135)
+      BVert& c = st.prev;
+      c.p = o;
+      c.n = -d;
+      c.wi = f3(0.f, 0.f, 0.f);
+      c.beta = f3(1.f, 1.f, 1.f);
+      c.Le = f3(0.f, 0.f, 0.f);
+      c.fwd = 0.f;
+      c.rev = 0.f;
+      c.mat = -1;
+      c.light = -1;
+      c.prim = kNoHit;
+      c.flags = kFlagCamera;
+      st.o = o;
+      st.d = d;
+      st.beta = f3(1.f, 1.f, 1.f);
+      st.pdf_fwd = camera_dir_pdf(sc.cam, o, d);
+      st.len = 1;
+      st.b = 0;
+      st.max_bounces = sc.max_depth;
+      st.base = 0;
+      st.skip = kNoHit;
+      st.camera = true;
+      inf = false;
+      phase = 0;
+    }
+    if (!subpath_step<MAXV>(sc, B, p, st, rng, err)) continue;
+    put_vert(B, st.base + st.len - 1, p, st.prev);
+    int nl = 0;
+    if (phase == 0) {
+      nc = st.len;
+      if (sc.n_lights > 0) {
+        // generateLightPath (bdpt.go:139-202), in the same sampler stream
         float ul = rng.next();
         int li = pick_light(sc, ul);
         DevLight L = sc.lights[li];
@@ -773,7 +810,7 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
         float dpdf;
         sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
         float ct = fabsf(dot(ed, en));
-        BVert& lv = start;
+        BVert& lv = st.prev;
         lv.p = ep;
         lv.n = en;
         lv.wi = f3(0.f, 0.f, 0.f);
@@ -790,26 +827,32 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
         lv.beta = Le;
         lv.Le = Le;
         lprob = L.prob;
-        beta = Le * (ct / (L.prob * apdf * dpdf));
-        pdf = dpdf;
-        maxb = sc.max_depth - 1;
-        base = MAXV;
-        skip = lv.prim;
+        st.o = ep;
+        st.d = ed;
+        st.beta = Le * (ct / (L.prob * apdf * dpdf));
+        st.pdf_fwd = dpdf;
+        st.len = 1;
+        st.b = 0;
+        st.max_bounces = sc.max_depth - 1;
+        st.base = MAXV;
+        st.skip = lv.prim;
+        st.camera = false;
+        phase = 1;
+        continue;
       }
-      int len = gen_subpath<MAXV>(sc, B, p, base, start, ep, ed, beta, pdf, maxb, phase == 0, rng, skip, err);
-      if (phase == 0) nc = len;
-      else nl = len;
-    }
-    if (inf) {
-      if (nl > 1) {
-        BVert fb = get_vert(B, MAXV + 1, p);
-        fb.fwd = apdf * lprob;
-        if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
-        put_vert(B, MAXV + 1, p, fb);
+    } else {
+      nl = st.len;
+      if (inf) {
+        if (nl > 1) {
+          BVert fb = get_vert(B, MAXV + 1, p);
+          fb.fwd = apdf * lprob;
+          if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
+          put_vert(B, MAXV + 1, p, fb);
+        }
+        BVert l0 = get_vert(B, MAXV, p);
+        l0.fwd = infinite_density(sc, ep, en, ed);
+        put_vert(B, MAXV, p, l0);
       }
-      BVert l0 = get_vert(B, MAXV, p);
-      l0.fwd = infinite_density(sc, ep, en, ed);
-      put_vert(B, MAXV, p, l0);
     }
     // which strategies draw uniform numbers (draws_before)
     uint32_t lm = 0, cm = 0;
@@ -822,6 +865,7 @@ __global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film
       }
     B.meta[p] = make_uint4((uint32_t)nc | ((uint32_t)nl << 8), rng.pos, pix, sample);
     B.masks[p] = make_uint2(lm, cm);
+    phase = -1;
   }
 }
 
@@ -940,10 +984,10 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int g1 = launch_grid(n, 128, 0);
+  int g1 = std::min(launch_grid(n, 128, 0), std::max(1, sms * 8));  // persistent subpath kernel
   int g2 = std::max(1, sms * 16);
   int g3 = launch_grid(n, 256, 0);
-  cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * (P.bd.maxv + 1) * P.bd.maxv, st);
+  cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * ((P.bd.maxv + 1) * P.bd.maxv + 1), st);
   if (P.bd.maxv == 10) {
     k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_list<10><<<g3, 256, 0, st>>>(P, ch);
