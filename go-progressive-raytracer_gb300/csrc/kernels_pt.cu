@@ -236,7 +236,7 @@ void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch,
     int g = std::max(1, (int)((int64_t)grid * block / 128));
     k_pt_shade<128, 6><<<g, 128, 0, st>>>(sc, P, ch, cur, bounce);
   } else {
-    k_pt_shade<256, 1><<<grid, std::min(block, 256), 0, st>>>(sc, P, ch, cur, bounce);
+    k_pt_shade<256, 2><<<grid, std::min(block, 256), 0, st>>>(sc, P, ch, cur, bounce);
   }
 }
 

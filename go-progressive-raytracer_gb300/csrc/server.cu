@@ -750,7 +750,7 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
       k_srv_shade<128, 6><<<std::max(1, grid * block / 128), 128, 0, st>>>(pool, P, items, cur, b);
     else
-      k_srv_shade<256, 1><<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
+      k_srv_shade<256, 2><<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
     close();
     open();
     launch_pt_shadow(pool, P, cur, block, grid, st);
