@@ -278,6 +278,11 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
       free_all(s->buffers);
       return rc;
     }
+    // mesh normals / UVs by final triangle id, now that the builder has filled the primitive maps
+    apply_mesh_options(desc, h);
+    if (h.custom_normals && h.n_tris)
+      CK(ctx, cudaMemcpyAsync(const_cast<float4*>(d.tri_normals), h.tri_normals.data(), h.tri_normals.size() * 16,
+                              cudaMemcpyHostToDevice, ctx->stream));
     // the tree is checked on the host copy before any kernel walks it
     auto tc = std::chrono::steady_clock::now();
     std::string bad = validate_layout(h);
@@ -297,6 +302,7 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   }
   rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
   rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tri_uvs, &d.tri_uvs, &s->bytes);
   rc |= upload(ctx, s->buffers, h.tex_info, &d.tex_info, &s->bytes);
   rc |= upload(ctx, s->buffers, h.texels, &d.texels, &s->bytes);
   d.has_textures = h.tex_info.empty() ? 0 : 1;

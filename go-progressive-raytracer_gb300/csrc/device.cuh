@@ -688,7 +688,16 @@ __device__ __forceinline__ void surface_at(const DevScene& sc, float3 o, float3 
     float4 nn = __ldg(sc.tri_normals + p);
     outward = f3(nn);  // precomputed normalize(e1 x e2) (triangle.go:92-99)
     s.mat = __float_as_int(a.w);
-    if (uv) s.uv = make_float2(h.u, h.v);  // barycentrics (triangle.go:151-161)
+    if (uv) {  // per-vertex UVs interpolated with the barycentrics, else the barycentrics (triangle.go:151-161)
+      s.uv = make_float2(h.u, h.v);
+      if (sc.tri_uvs) {
+        float4 A = __ldg(sc.tri_uvs + 2 * (size_t)p), Bq = __ldg(sc.tri_uvs + 2 * (size_t)p + 1);
+        if (Bq.z != 0.f) {
+          float w = 1.f - h.u - h.v;
+          s.uv = make_float2(A.x * w + A.z * h.u + Bq.x * h.v, A.y * w + A.w * h.u + Bq.y * h.v);
+        }
+      }
+    }
   } else if (p < sc.sphere_base) {
     const float4* Q = sc.quads + (size_t)(p - sc.quad_base) * 5;
     outward = f3(__ldg(Q + 3));

@@ -8,7 +8,10 @@
 //              (meta = count | type << 8), or kEmptyChild.  Used slots come
 //              first, so a traversal stops at the first empty one.
 //   tris       3 x float4 (48 B): (v0, material) (e1 = v1 - v0, -) (e2 = v2 - v0, -)
-//   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64
+//   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64,
+//              or the mesh's custom normal (TriangleMeshOptions.Normals), normalised
+//   tri_uvs    2 x float4 per triangle when a mesh has VertexUVs:
+//              (uv0, uv1) (uv2, has, -), has = 0 for triangles without them
 //   quads      5 x float4 (80 B): (corner, D) (u, material) (v, -) (normal, -) (W, -)
 //   spheres    2 x float4 (32 B): (center, radius) (material, -, -, -)
 //   quadrics   5 x float4 (80 B): discs, cylinders and cones
@@ -92,6 +95,7 @@ struct DevScene {
   const float4* quadrics;
   const DevMaterial* materials;
   const DevLight* lights;
+  const float4* tri_uvs;  // per triangle (u0, v0, u1, v1) (u2, v2, has, -); null when no mesh has VertexUVs
   const uint4* tex_info;  // per texture: (first texel, width, height, -)
   const float4* texels;   // RGB (+ pad), row-major per texture
   int has_textures;       // surface UVs are computed only when set

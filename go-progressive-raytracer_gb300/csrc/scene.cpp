@@ -878,6 +878,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
       out.prim_shape[gid] = prims[k].shape;
       out.prim_sub[gid] = prims[k].sub;
     }
+    apply_mesh_options(d, out);
   }
   // lights (pkg/scene/scene.go:102-141) and the light sampler
   // (weighted_light_sampler.go:22-78)
@@ -1065,6 +1066,37 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
 // lies inside the parent's slot box; a leaf names a valid range of one
 // primitive array whose primitives lie inside its box.  Then every node but
 // the root must be referenced exactly once and every primitive exactly once.
+void apply_mesh_options(const gprt_scene_desc* d, HostScene& h) {
+  bool any_n = false, any_uv = false;
+  for (uint32_t k = 0; k < d->n_meshes; k++) {
+    any_n |= d->meshes[k].tri_normals != nullptr;
+    any_uv |= d->meshes[k].vertex_uvs != nullptr;
+  }
+  h.custom_normals = any_n;
+  h.tri_uvs.clear();
+  if ((!any_n && !any_uv) || h.n_tris == 0) return;
+  if (any_uv) h.tri_uvs.assign(2 * (size_t)h.n_tris, make_float4(0.f, 0.f, 0.f, 0.f));
+  parallel_for(h.n_tris, [&](size_t b0, size_t b1) {
+    for (size_t g = b0; g < b1; g++) {
+      const gprt_shape_desc& sh = d->shapes[h.prim_shape[g]];
+      if (sh.kind != GPRT_SHAPE_MESH) continue;
+      const gprt_mesh_desc& m = d->meshes[sh.mesh];
+      size_t t = h.prim_sub[g];
+      if (m.tri_normals) {  // NewTriangleWithNormal (triangle.go:35-49): normalised
+        D3 n = D3(m.tri_normals + 3 * t).norm();
+        h.tri_normals[g] = make_float4((float)n.x, (float)n.y, (float)n.z, 0.f);
+      }
+      if (m.vertex_uvs) {
+        const double* u0 = m.vertex_uvs + 2 * (size_t)m.indices[3 * t];
+        const double* u1 = m.vertex_uvs + 2 * (size_t)m.indices[3 * t + 1];
+        const double* u2 = m.vertex_uvs + 2 * (size_t)m.indices[3 * t + 2];
+        h.tri_uvs[2 * g] = make_float4((float)u0[0], (float)u0[1], (float)u1[0], (float)u1[1]);
+        h.tri_uvs[2 * g + 1] = make_float4((float)u2[0], (float)u2[1], 1.f, 0.f);
+      }
+    }
+  });
+}
+
 std::string validate_layout(const HostScene& s) {
   size_t nn = s.nodes.size() / 8;
   if (nn == 0) return (s.n_tris + s.n_quads + s.n_spheres + s.n_quadrics) ? "primitives without a BVH" : "";

@@ -25,6 +25,8 @@ struct HostScene {
   std::vector<float4> nodes, tris, tri_normals, quads, spheres, quadrics;
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights;
+  std::vector<float4> tri_uvs;  // per triangle when a mesh has VertexUVs (layout.h), else empty
+  bool custom_normals = false;  // a mesh gave TriangleMeshOptions.Normals (tri_normals patched)
   std::vector<uint4> tex_info;  // per texture: first texel, width, height
   std::vector<float4> texels;
   // primitive id -> (index in scene.Shapes, box face / mesh triangle)
@@ -47,6 +49,11 @@ struct HostScene {
 // holds the primitives, light indices refer to the flattened order, and the
 // primitive maps are filled by the builder.
 bool build_scene(const gprt_scene_desc* desc, HostScene& out, std::string& err, bool device_bvh = false);
+
+// TriangleMeshOptions.Normals / VertexUVs of the mesh triangles, applied by
+// final triangle id through the primitive maps (either builder): patches
+// tri_normals and fills tri_uvs.
+void apply_mesh_options(const gprt_scene_desc* desc, HostScene& h);
 
 // Checks the layout invariants of a built scene; returns "" when valid.
 std::string validate_layout(const HostScene& s);

@@ -53,7 +53,7 @@ struct StepHdr {
 struct DevItem {
   uint32_t path0, pix0, npix, layers;
   int root, mat_off, light_off, n_lights;
-  int tex_off, texel_off, has_textures, pad;
+  int tex_off, texel_off, has_textures, has_tri_uvs;
   int has_infinite, max_depth, rr_min_bounces, width;
   float3 world_center;
   float world_radius;
@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
       v.tex_info = pool.tex_info + it.tex_off;
       v.texels = pool.texels + it.texel_off;
       v.has_textures = it.has_textures;
+      v.tri_uvs = it.has_tri_uvs ? pool.tri_uvs : nullptr;
       v.n_lights = it.n_lights;
       v.has_infinite = it.has_infinite;
       v.world_center = it.world_center;
@@ -205,12 +206,13 @@ double now_ms(std::chrono::steady_clock::time_point t0) {
 // One growable device array (or two parallel ones) with a first-fit range
 // allocator over element indices.
 struct PoolArray {
-  size_t elem[2] = {0, 0};  // bytes per element of each parallel buffer (0: unused)
-  void* buf[2] = {nullptr, nullptr};
+  static constexpr int kBufs = 3;
+  size_t elem[kBufs] = {0, 0, 0};  // bytes per element of each parallel buffer (0: unused)
+  void* buf[kBufs] = {nullptr, nullptr, nullptr};
   size_t cap = 0;
   std::map<size_t, size_t> free_;  // offset -> length
 
-  size_t bytes_per() const { return elem[0] + elem[1]; }
+  size_t bytes_per() const { return elem[0] + elem[1] + elem[2]; }
   size_t bytes() const { return cap * bytes_per(); }
   bool take(size_t n, size_t* off) {
     for (auto it = free_.begin(); it != free_.end(); ++it) {
@@ -263,7 +265,7 @@ struct PoolScene {
   size_t bytes = 0;
   // per-job constants of the scene
   int root = -1;
-  int has_infinite = 0, max_depth = 0, rr_min = 0;
+  int has_infinite = 0, max_depth = 0, rr_min = 0, has_tri_uvs = 0;
   float3 world_center{};
   float world_radius = 0.f;
   DevCamera cam{};
@@ -395,6 +397,7 @@ DevScene pool_view(gprt_server* sv) {
   d.nodes = static_cast<const float4*>(sv->pool[kNodes].buf[0]);
   d.tris = static_cast<const float4*>(sv->pool[kTris].buf[0]);
   d.tri_normals = static_cast<const float4*>(sv->pool[kTris].buf[1]);
+  d.tri_uvs = static_cast<const float4*>(sv->pool[kTris].buf[2]);  // a job sees it only when its scene has UVs
   d.quads = static_cast<const float4*>(sv->pool[kQuads].buf[0]);
   d.spheres = static_cast<const float4*>(sv->pool[kSpheres].buf[0]);
   d.quadrics = static_cast<const float4*>(sv->pool[kQuadrics].buf[0]);
@@ -429,22 +432,22 @@ bool grow(gprt_server* sv, int k, size_t need_cap) {
     extra = (new_cap - a.cap) * a.bytes_per();
     if (used + extra > sv->desc.hbm_budget_bytes) return false;
   }
-  void* nb[2] = {nullptr, nullptr};
-  for (int b = 0; b < 2; b++) {
+  void* nb[PoolArray::kBufs] = {nullptr, nullptr, nullptr};
+  for (int b = 0; b < PoolArray::kBufs; b++) {
     if (!a.elem[b]) continue;
     if (cudaMalloc(&nb[b], new_cap * a.elem[b]) != cudaSuccess) {
       cudaGetLastError();
-      if (nb[0] && b == 1) cudaFree(nb[0]);
+      for (int q = 0; q < b; q++)
+        if (nb[q]) cudaFree(nb[q]);
       return false;
     }
     if (a.cap) cudaMemcpyAsync(nb[b], a.buf[b], a.cap * a.elem[b], cudaMemcpyDeviceToDevice, sv->stream);
   }
   cudaStreamSynchronize(sv->stream);
-  for (int b = 0; b < 2; b++)
+  for (int b = 0; b < PoolArray::kBufs; b++)
     if (a.buf[b]) cudaFree(a.buf[b]);
   size_t old = a.cap;
-  a.buf[0] = nb[0];
-  a.buf[1] = nb[1];
+  for (int b = 0; b < PoolArray::kBufs; b++) a.buf[b] = nb[b];
   a.cap = new_cap;
   a.give(old, new_cap - old);
   sv->pool_gen++;
@@ -456,7 +459,7 @@ void shrink_if_empty(gprt_server* sv) {
   if (!sv->scenes.empty()) return;
   bool any = false;
   for (auto& a : sv->pool) {
-    for (int b = 0; b < 2; b++)
+    for (int b = 0; b < PoolArray::kBufs; b++)
       if (a.buf[b]) {
         cudaFree(a.buf[b]);
         a.buf[b] = nullptr;
@@ -534,6 +537,7 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   copy(kNodes, 0, d.nodes);
   copy(kTris, 0, d.tris);
   copy(kTris, 1, d.tri_normals);
+  if (d.tri_uvs) copy(kTris, 2, d.tri_uvs);
   copy(kQuads, 0, d.quads);
   copy(kSpheres, 0, d.spheres);
   copy(kQuadrics, 0, d.quadrics);
@@ -555,6 +559,7 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   }
   ps->root = cnt[kNodes] ? (int)off[kNodes] : -1;
   ps->has_infinite = d.has_infinite;
+  ps->has_tri_uvs = d.tri_uvs ? 1 : 0;
   ps->max_depth = d.max_depth;
   ps->rr_min = d.rr_min_bounces;
   ps->world_center = d.world_center;
@@ -885,6 +890,7 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
     d.tex_off = (int)ps->off[kTexInfo];
     d.texel_off = (int)ps->off[kTexels];
     d.has_textures = ps->cnt[kTexInfo] ? 1 : 0;
+    d.has_tri_uvs = ps->has_tri_uvs;
     d.has_infinite = ps->has_infinite;
     d.max_depth = ps->max_depth;
     d.rr_min_bounces = ps->rr_min;
@@ -1077,6 +1083,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   sv->pool[kNodes].elem[0] = 8 * sizeof(float4);
   sv->pool[kTris].elem[0] = 3 * sizeof(float4);
   sv->pool[kTris].elem[1] = sizeof(float4);
+  sv->pool[kTris].elem[2] = 2 * sizeof(float4);  // TriangleMeshOptions.VertexUVs
   sv->pool[kQuads].elem[0] = 5 * sizeof(float4);
   sv->pool[kSpheres].elem[0] = 2 * sizeof(float4);
   sv->pool[kQuadrics].elem[0] = 5 * sizeof(float4);
@@ -1144,7 +1151,7 @@ int gprt_server_destroy(gprt_server* sv) {
     sv->jobs.clear();
     sv->scenes.clear();
     for (auto& a : sv->pool)
-      for (int b = 0; b < 2; b++)
+      for (int b = 0; b < gprt::PoolArray::kBufs; b++)
         if (a.buf[b]) cudaFree(a.buf[b]);
     drop_graphs(sv);
     for (auto& kv : sv->step_events)

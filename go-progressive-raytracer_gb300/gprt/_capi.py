@@ -48,7 +48,8 @@ class ShapeDesc(C.Structure):
 
 class MeshDesc(C.Structure):
     _fields_ = [("vertices", C.POINTER(C.c_double)), ("indices", C.POINTER(C.c_uint32)),
-                ("tri_materials", C.POINTER(C.c_uint32)), ("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32)]
+                ("tri_materials", C.POINTER(C.c_uint32)), ("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32),
+                ("tri_normals", C.POINTER(C.c_double)), ("vertex_uvs", C.POINTER(C.c_double))]
 
 
 class LightDesc(C.Structure):

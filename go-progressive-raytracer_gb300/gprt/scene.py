@@ -152,13 +152,42 @@ class MaterialTable:
 
 @dataclass
 class TriangleMesh:
-    """geometry.NewTriangleMesh(vertices, faces, material, &TriangleMeshOptions{Materials})
-    (pkg/geometry/triangle_mesh.go:33-146)."""
+    """geometry.NewTriangleMesh(vertices, faces, material, &TriangleMeshOptions{...})
+    (pkg/geometry/triangle_mesh.go:33-146).  TriangleMeshOptions: Materials
+    (``materials`` + ``material_index``), Normals (``normals``, one per
+    triangle), VertexUVs (``vertex_uvs``, one per vertex) and Rotation /
+    Center (applied to the vertices here, as rotateVertex does)."""
     vertices: np.ndarray  # (n, 3) float64
     faces: np.ndarray  # (m, 3) uint32
     material: Optional[Material] = None
     materials: Optional[object] = None  # list of Material, or a MaterialTable
     material_index: Optional[np.ndarray] = None  # (m,) index into `materials`
+    normals: Optional[np.ndarray] = None  # (m, 3) custom triangle normals
+    vertex_uvs: Optional[np.ndarray] = None  # (n, 2) texture coordinates
+    rotation: Optional[Vec3] = None  # radians about X, then Y, then Z
+    center: Optional[Vec3] = None  # the point rotated about
+
+    def placed_vertices(self) -> np.ndarray:
+        """The vertices after Rotation / Center (triangle_mesh.go:53-67, 170-199)."""
+        v = np.asarray(self.vertices, dtype=np.float64).reshape(-1, 3)
+        if self.rotation is None:
+            return v
+        v = v.copy()
+        if self.center is not None:
+            v -= np.asarray(self.center, dtype=np.float64)
+        rx, ry, rz = self.rotation
+        if rx != 0:
+            c, s = math.cos(rx), math.sin(rx)
+            v[:, 1], v[:, 2] = v[:, 1] * c - v[:, 2] * s, v[:, 1] * s + v[:, 2] * c
+        if ry != 0:
+            c, s = math.cos(ry), math.sin(ry)
+            v[:, 0], v[:, 2] = v[:, 0] * c + v[:, 2] * s, -v[:, 0] * s + v[:, 2] * c
+        if rz != 0:
+            c, s = math.cos(rz), math.sin(rz)
+            v[:, 0], v[:, 1] = v[:, 0] * c - v[:, 1] * s, v[:, 0] * s + v[:, 1] * c
+        if self.center is not None:
+            v += np.asarray(self.center, dtype=np.float64)
+        return v
 
 
 def Mesh(mesh: TriangleMesh):
@@ -336,7 +365,7 @@ class FlatScene:
             d.kind = s.kind
             if s.kind == capi.SHAPE_MESH:
                 m = s.mesh
-                v = np.ascontiguousarray(m.vertices, dtype=np.float64).reshape(-1, 3)
+                v = np.ascontiguousarray(m.placed_vertices(), dtype=np.float64).reshape(-1, 3)
                 f = np.ascontiguousarray(m.faces, dtype=np.uint32).reshape(-1, 3)
                 md = capi.MeshDesc()
                 md.vertices = v.ctypes.data_as(C.POINTER(C.c_double))
@@ -344,6 +373,18 @@ class FlatScene:
                 md.n_vertices = v.shape[0]
                 md.n_triangles = f.shape[0]
                 self._keep += [v, f]
+                if m.normals is not None:
+                    nrm = np.ascontiguousarray(m.normals, dtype=np.float64).reshape(-1, 3)
+                    if nrm.shape[0] != f.shape[0]:  # NewTriangleMesh panics (triangle_mesh.go:41-44)
+                        raise ValueError("number of normals must match number of triangles")
+                    md.tri_normals = nrm.ctypes.data_as(C.POINTER(C.c_double))
+                    self._keep.append(nrm)
+                if m.vertex_uvs is not None:
+                    uvs = np.ascontiguousarray(m.vertex_uvs, dtype=np.float64).reshape(-1, 2)
+                    if uvs.shape[0] != v.shape[0]:  # triangle_mesh.go:47-50
+                        raise ValueError("number of vertex UVs must match number of vertices")
+                    md.vertex_uvs = uvs.ctypes.data_as(C.POINTER(C.c_double))
+                    self._keep.append(uvs)
                 if isinstance(m.materials, MaterialTable):
                     first = n_mats()
                     tables.append((first, m.materials))

@@ -286,6 +286,41 @@ def texture_test_scene(camera=None):
     return s.finalize_size()
 
 
+def textured_mesh_scene(width=48, max_depth=8, n=12):
+    """A triangle mesh with every TriangleMeshOptions field: an n x n grid
+    with per-vertex UVs on a UV-debug texture (VertexUVs), per-triangle
+    normals tilted away from the geometric ones (Normals), a rotation about
+    its centre (Rotation / Center), and a checkerboard ground, under a sphere
+    light and a gradient sky."""
+    cam = CameraConfig(center=(0.0, 2.0, 4.5), look_at=(0.0, 0.6, 0.0), up=(0.0, 1.0, 0.0), width=width,
+                       aspect_ratio=1.0, vfov=45.0)
+    s = Scene(camera=cam)
+    s.sampling = SamplingConfig(max_depth=max_depth, russian_roulette_min_bounces=16, adaptive_min_samples=1.0,
+                                adaptive_threshold=0.0)
+    ys, xs = np.mgrid[0:n + 1, 0:n + 1] / float(n)
+    verts = np.stack([xs * 2.0 - 1.0, ys * 1.6 + 0.1, 0.15 * np.sin(6.0 * xs)], axis=-1).reshape(-1, 3)
+    uvs = np.stack([xs, ys], axis=-1).reshape(-1, 2)
+    faces = []
+    for j in range(n):
+        for i in range(n):
+            a, b, c, d = j * (n + 1) + i, j * (n + 1) + i + 1, (j + 1) * (n + 1) + i, (j + 1) * (n + 1) + i + 1
+            faces += [(a, b, d), (a, d, c)]
+    faces = np.array(faces, dtype=np.uint32)
+    e1 = verts[faces[:, 1]] - verts[faces[:, 0]]
+    e2 = verts[faces[:, 2]] - verts[faces[:, 0]]
+    geo = np.cross(e1, e2)
+    tilt = np.stack([0.4 * np.cos(np.arange(len(faces))), 0.3 * np.ones(len(faces)), np.zeros(len(faces))], axis=-1)
+    normals = geo / np.linalg.norm(geo, axis=1, keepdims=True) + tilt  # not unit: normalised as NewTriangleWithNormal does
+    mesh = TriangleMesh(vertices=verts, faces=faces, material=TexturedLambertian(NewUVDebugTexture(64, 64)),
+                        normals=normals, vertex_uvs=uvs, rotation=(0.0, 0.35, 0.1), center=(0.0, 0.9, 0.0))
+    s.add(Mesh(mesh),
+          Quad((-4.0, 0.0, -4.0), (8.0, 0.0, 0.0), (0.0, 0.0, 8.0),
+               TexturedLambertian(NewCheckerboardTexture(128, 128, 16, (0.8, 0.8, 0.8), (0.3, 0.3, 0.3)))))
+    s.add_sphere_light((1.5, 3.0, 2.0), 0.5, (12.0, 12.0, 12.0))
+    s.add_gradient_infinite_light((0.3, 0.4, 0.6), (0.6, 0.6, 0.6))
+    return s.finalize_size()
+
+
 def spot_scene(width=48, point=False, max_depth=8):
     """The caustic-glass scene's lighting (scene.NewCausticGlassScene,
     caustic_glass.go:36-95: a spot light from (0,5,9) at (-5,2.75,0) with a

@@ -106,15 +106,17 @@ typedef struct gprt_shape_desc {
   double p[9];
 } gprt_shape_desc;
 
-/* geometry.NewTriangleMesh(vertices, faces, material, &TriangleMeshOptions{Materials})
- * pkg/geometry/triangle_mesh.go:33-146.  Rotation/normals/UV options are
- * applied by the caller (they only transform inputs). */
+/* geometry.NewTriangleMesh(vertices, faces, material, &TriangleMeshOptions{...})
+ * pkg/geometry/triangle_mesh.go:33-146.  Rotation / Center only transform
+ * the vertices and are applied by the caller. */
 typedef struct gprt_mesh_desc {
   const double* vertices;      /* 3 * n_vertices */
   const uint32_t* indices;     /* 3 * n_triangles */
-  const uint32_t* tri_materials; /* n_triangles material indices, or NULL */
+  const uint32_t* tri_materials; /* n_triangles material indices, or NULL (Materials) */
   uint32_t n_vertices;
   uint32_t n_triangles;
+  const double* tri_normals;   /* 3 * n_triangles custom normals (normalised here), or NULL (Normals) */
+  const double* vertex_uvs;    /* 2 * n_vertices texture coordinates, or NULL (VertexUVs) */
 } gprt_mesh_desc;
 
 enum gprt_light_kind {

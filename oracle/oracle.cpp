@@ -116,7 +116,7 @@ Scene* buildScene(const gprt_scene_desc* d, std::string& err) {
         std::vector<const Material*> mats(m.n_triangles);
         for (uint32_t k = 0; k < m.n_triangles; k++)
           mats[k] = mat(m.tri_materials ? m.tri_materials[k] : sh.material);
-        auto tm = std::make_unique<TriangleMesh>(verts, idx, mats);
+        auto tm = std::make_unique<TriangleMesh>(verts, idx, mats, m.tri_normals, m.vertex_uvs);
         tm->setId((int)i);
         shape = std::move(tm);
         break;

@@ -1042,10 +1042,14 @@ struct Triangle : Shape {
   const Material* material;
   AABB bbox;
   int subIndex = 0;
+  bool hasUVs = false;
+  Vec2 uv0, uv1, uv2;  // NewTriangleWithUVs (triangle.go:51-68)
   Triangle(Vec3 a, Vec3 b, Vec3 c, const Material* m) : v0(a), v1(b), v2(c), material(m) {
     normal = v1.sub(v0).cross(v2.sub(v0)).normalize();  // computeNormal (triangle.go:92-99)
     bbox = AABB::fromPoints({v0, v1, v2});
   }
+  // NewTriangleWithNormal (triangle.go:35-49): the given normal, normalised
+  void setNormal(const Vec3& n) { normal = n.normalize(); }
   bool hit(const Ray& ray, double tMin, double tMax, SurfaceInteraction& out) const override {
     counters().prims++;
     const double eps = 1e-8;
@@ -1066,7 +1070,8 @@ struct Triangle : Shape {
     out.t = t;
     out.point = ray.at(t);
     out.material = material;
-    out.uv = Vec2(uu, vv);
+    // per-vertex UVs interpolated with the barycentrics, else the barycentrics (triangle.go:151-161)
+    out.uv = hasUVs ? uv0.mul(1.0 - uu - vv).add(uv1.mul(uu)).add(uv2.mul(vv)) : Vec2(uu, vv);
     out.shape = id;
     out.sub = subIndex;
     out.setFaceNormal(ray, normal);
@@ -1220,8 +1225,11 @@ struct TriangleMesh : Shape {
   std::vector<std::unique_ptr<Triangle>> tris;
   std::unique_ptr<BVH> bvh;
   AABB bbox;
+  // TriangleMeshOptions.Normals (one per triangle) and VertexUVs (one per
+  // vertex) are optional (triangle_mesh.go:20-26, 95-120)
   TriangleMesh(const std::vector<Vec3>& verts, const std::vector<uint32_t>& idx,
-               const std::vector<const Material*>& mats) {
+               const std::vector<const Material*>& mats, const double* tri_normals = nullptr,
+               const double* vertex_uvs = nullptr) {
     size_t n = idx.size() / 3;
     tris.reserve(n);
     std::vector<const Shape*> shapes;
@@ -1232,6 +1240,14 @@ struct TriangleMesh : Shape {
         throw std::runtime_error("Face index out of bounds");
       tris.push_back(std::make_unique<Triangle>(verts[a], verts[b], verts[c], mats[i]));
       tris.back()->subIndex = (int)i;
+      if (tri_normals) tris.back()->setNormal(Vec3(tri_normals[3 * i], tri_normals[3 * i + 1], tri_normals[3 * i + 2]));
+      if (vertex_uvs) {
+        Triangle& T = *tris.back();
+        T.hasUVs = true;
+        T.uv0 = Vec2(vertex_uvs[2 * a], vertex_uvs[2 * a + 1]);
+        T.uv1 = Vec2(vertex_uvs[2 * b], vertex_uvs[2 * b + 1]);
+        T.uv2 = Vec2(vertex_uvs[2 * c], vertex_uvs[2 * c + 1]);
+      }
       shapes.push_back(tris.back().get());
     }
     bvh = std::make_unique<BVH>(shapes);

@@ -17,14 +17,15 @@ def _both(ctx, scene):
     return gprt.GpuScene(ctx, flat), gprt.GpuScene(ctx, flat, device_bvh=True)
 
 
-@pytest.mark.parametrize("name", ["cornell", "spheres", "icosphere6", "quadrics"])
+@pytest.mark.parametrize("name", ["cornell", "spheres", "icosphere6", "quadrics", "textured_mesh"])
 def test_device_bvh_hits_match_host_bvh(ctx, name):
     import gprt
     from gprt import scenes
     from test_gpu_intersect import _camera_rays, _rays_in_bounds
     scene = {"cornell": lambda: scenes.cornell_baseline(64), "spheres": lambda: scenes.default_style_scene(17, 64, 64),
              "icosphere6": lambda: scenes.icosphere_scene(level=6, width=64),
-             "quadrics": lambda: scenes.quadric_scene(64)}[name]()
+             "quadrics": lambda: scenes.quadric_scene(64),
+             "textured_mesh": lambda: scenes.textured_mesh_scene(64)}[name]()
     host, dev = _both(ctx, scene)
     info = dev.info
     assert info.n_primitives == host.info.n_primitives and info.n_nodes > 0
@@ -45,10 +46,13 @@ def test_device_bvh_hits_match_host_bvh(ctx, name):
     dev.close()
 
 
-def test_device_bvh_render_equals_host_bvh_render(ctx):
+@pytest.mark.parametrize("name", ["icosphere5", "textured_mesh"])
+def test_device_bvh_render_equals_host_bvh_render(ctx, name):
+    """Also covers the mesh normals / UVs each builder applies by final triangle id."""
     import gprt
     from gprt import scenes
-    host, dev = _both(ctx, scenes.icosphere_scene(level=5, width=48))
+    scene = scenes.icosphere_scene(level=5, width=48) if name == "icosphere5" else scenes.textured_mesh_scene(48)
+    host, dev = _both(ctx, scene)
     films = []
     for g in (host, dev):
         r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=8, max_passes=1, seed=4))

@@ -68,6 +68,7 @@ SCENES = {
     "spheregrid_mixed": lambda s: _fixed(s.sphere_grid_scene(6, "mixed", _cam(64)), depth=8),
     "spheregrid_glossy": lambda s: _fixed(s.sphere_grid_scene(6, "glossy", _cam(64)), depth=8),
     "texture_test": lambda s: _fixed(s.texture_test_scene(_cam(96)), depth=8),
+    "textured_mesh": lambda s: s.textured_mesh_scene(48),
 }
 
 
@@ -124,7 +125,7 @@ def test_pt_same_inputs_parity(ctx, oracle, name):
 
 @pytest.mark.parametrize("name", ["cornell_boxes", "cornell_spheres", "default_scene", "quadrics",
                                   "quadrics_disc_light", "spot_disc", "spot_point", "cornell_point", "cone_test",
-                                  "spheregrid_mixed", "texture_test"])
+                                  "spheregrid_mixed", "texture_test", "textured_mesh"])
 def test_bdpt_same_inputs_parity(ctx, oracle, name):
     import gprt
     from gprt import scenes
@@ -139,7 +140,8 @@ def test_bdpt_same_inputs_parity(ctx, oracle, name):
                  scenes.CORNELL_BOXES, scenes.CORNELL_POINT_LIGHT, camera=_cam(32)), 6)),
              "cone_test": lambda: _untied(_fixed(scenes.cone_test_scene(_cam(48)), 6)),
              "spheregrid_mixed": lambda: _fixed(scenes.sphere_grid_scene(5, "mixed", _cam(48)), 6),
-             "texture_test": lambda: _fixed(scenes.texture_test_scene(_cam(64)), 6)}[name]()
+             "texture_test": lambda: _fixed(scenes.texture_test_scene(_cam(64)), 6),
+             "textured_mesh": lambda: scenes.textured_mesh_scene(32, max_depth=6)}[name]()
     gpu, stats, _ = gpu_render(ctx, scene, 8, seed=5, integrator=gprt.BDPTIntegrator())
     r, _ = oracle_render(oracle, scene, 8, seed=5, integrator=1)
     med, frac = same_input_stats(gpu, r.image())

@@ -42,6 +42,7 @@ def scenes(ctx):
         "spheres_b": gprt.GpuScene(ctx, S.default_style_scene(9, width=32, height=32).to_desc()),
         "textured": gprt.GpuScene(ctx, S.texture_test_scene(gprt.CameraConfig(width=48)).to_desc()),
         "spot": gprt.GpuScene(ctx, S.spot_scene(32).to_desc()),
+        "uvmesh": gprt.GpuScene(ctx, S.textured_mesh_scene(40).to_desc()),
     }
     yield out
     for g in out.values():
@@ -64,7 +65,7 @@ def test_job_alone_in_server_equals_plain_job(ctx, scenes):
 def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
     import gprt
     jobs = [("cornell", 3, 8, 4), ("ico", 5, 6, 2), ("spheres_a", 7, 12, 4), ("spheres_b", 11, 4, 1),
-            ("cornell", 13, 4, 4), ("textured", 17, 4, 2), ("spot", 19, 4, 4)]
+            ("cornell", 13, 4, 4), ("textured", 17, 4, 2), ("spot", 19, 4, 4), ("uvmesh", 23, 4, 2)]
     plain = [_plain_film(scenes[n], seed, spp) for n, seed, spp, _ in jobs]
     # a small step capacity forces jobs to share steps and to be split across them
     sv = gprt.RenderServer(ctx, step_paths=3 * 64 * 48)
@@ -75,7 +76,7 @@ def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
     for t, p in zip(tickets, plain):
         _same(sv.film(t), p)
     st = sv.stats()
-    assert st["resident_scenes"] == 6  # the two cornell requests share one pooled copy
+    assert st["resident_scenes"] == 7  # the two cornell requests share one pooled copy
     assert st["samples"] == sum(scenes[n].width * scenes[n].height * spp for n, _, spp, _ in jobs)
     sv.close()
 

@@ -39,7 +39,7 @@ def _validate(flat):
 
 @pytest.mark.parametrize("name", ["cornell_baseline", "cornell_spheres", "cornell_boxes", "default", "icosphere5",
                                   "spheres17", "quadrics", "spot_disc", "cornell_point",
-                                  "cone_test", "cylinder_test", "spheregrid", "texture_test"])
+                                  "cone_test", "cylinder_test", "spheregrid", "texture_test", "textured_mesh"])
 def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
     from gprt import scenes
     s = {"cornell_baseline": lambda: scenes.cornell_baseline(64),
@@ -54,7 +54,8 @@ def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
          "cone_test": lambda: scenes.cone_test_scene(),
          "cylinder_test": lambda: scenes.cylinder_test_scene(),
          "spheregrid": lambda: scenes.sphere_grid_scene(12, "mixed"),
-         "texture_test": lambda: scenes.texture_test_scene()}[name]()
+         "texture_test": lambda: scenes.texture_test_scene(),
+         "textured_mesh": lambda: scenes.textured_mesh_scene(64)}[name]()
     flat = s.to_desc()
     rc, info, err = _validate(flat)
     assert rc == 0, err
@@ -131,3 +132,18 @@ def test_oracle_renderer_schedule_and_determinism(oracle):
     assert np.array_equal(a, r2.image())
     _, lum, lum2, cnt = r.film()
     assert (cnt == 1).all()
+
+
+def test_mesh_rotation_and_option_counts():
+    # rotateVertex (triangle_mesh.go:170-199): X, then Y, then Z, about Center
+    import math
+    from gprt.scene import Lambertian, Mesh, Scene, TriangleMesh
+    m = TriangleMesh(vertices=np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [2.0, 0.0, 1.0]]),
+                     faces=np.array([[0, 1, 2]]), material=Lambertian((0.5, 0.5, 0.5)),
+                     rotation=(0.0, math.pi / 2, 0.0), center=(1.0, 0.0, 0.0))
+    v = m.placed_vertices()
+    assert np.allclose(v[0], [1.0, 0.0, 0.0]) and np.allclose(v[2], [2.0, 0.0, -1.0])
+    s = Scene()
+    s.add(Mesh(TriangleMesh(vertices=m.vertices, faces=m.faces, material=m.material, normals=np.zeros((2, 3)))))
+    with pytest.raises(ValueError, match="normals must match"):
+        s.to_desc()
