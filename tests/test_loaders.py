@@ -321,3 +321,63 @@ def test_ply_errors(loaders, tmp_path):
     write_ply(p, [(0, 0, 0)] * 3, [(0, 1, 7)])
     with pytest.raises(Exception, match="index out of range"):
         loaders.load_ply(p)
+
+
+def _png(path, pixels, ctype, depth=8, palette=None, trns=None, filters=(0,)):
+    import struct
+    import zlib
+    h, w = pixels.shape[:2]
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    raw = b""
+    for y in range(h):
+        f = filters[y % len(filters)]
+        row = pixels[y].reshape(-1)
+        data = row.astype(">u2").tobytes() if depth == 16 else row.astype(np.uint8).tobytes()
+        line = np.frombuffer(data, dtype=np.uint8).astype(np.int64)
+        bpp = ch * depth // 8
+        if f == 1:  # Sub
+            enc = line.copy()
+            enc[bpp:] = (line[bpp:] - line[:-bpp]) & 0xFF
+        else:
+            enc = line
+        raw += bytes([f]) + enc.astype(np.uint8).tobytes()
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+    blob = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    if palette is not None:
+        blob += chunk(b"PLTE", np.asarray(palette, dtype=np.uint8).tobytes())
+    if trns is not None:
+        blob += chunk(b"tRNS", bytes(trns))
+    blob += chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b"")
+    open(path, "wb").write(blob)
+
+
+def test_load_image_png(loaders, tmp_path):
+    # LoadImage (pkg/loaders/image.go:21-61, image_test.go): colour / 65535 of
+    # the alpha-premultiplied 16-bit RGBA of each pixel, row 0 at the top
+    p = str(tmp_path / "a.png")
+    rgb = np.array([[[255, 0, 0], [0, 255, 0]], [[0, 0, 255], [128, 64, 32]]], dtype=np.int64)
+    _png(p, rgb, 2, filters=(0, 1))
+    t = loaders.load_image(p)
+    assert t.width == 2 and t.height == 2
+    assert np.allclose(t.pixels, rgb / 255.0)
+    rgba = np.array([[[255, 255, 255, 128], [10, 20, 30, 255]]], dtype=np.int64)
+    _png(p, rgba, 6)
+    t = loaders.load_image(p)
+    a = 128 * 257
+    assert np.allclose(t.pixels[0, 0], np.floor(255 * 257 * a / 65535) / 65535)
+    assert np.allclose(t.pixels[0, 1], np.array([10, 20, 30]) / 255.0)
+    g16 = np.array([[[0], [65535], [4660]]], dtype=np.int64)
+    _png(p, g16, 0, depth=16)
+    t = loaders.load_image(p)
+    assert np.allclose(t.pixels[0, :, 0], [0.0, 1.0, 4660 / 65535])
+    _png(p, np.array([[[1], [0]]], dtype=np.int64), 3, palette=[[0, 0, 0], [200, 100, 50]], trns=[0, 255])
+    t = loaders.load_image(p)
+    assert np.allclose(t.pixels[0, 0], [200 / 255, 100 / 255, 50 / 255]) and np.allclose(t.pixels[0, 1], 0)
+    open(p, "wb").write(b"\xff\xd8\xff not a png")
+    with pytest.raises(ValueError, match="only PNG"):
+        loaders.load_image(p)
+    with pytest.raises(ValueError, match="failed to open image file"):
+        loaders.load_image(str(tmp_path / "missing.png"))
