@@ -151,13 +151,99 @@ def l2_absorption(traffic, alg_bytes, avg_ms, peak):
     return {"dram_share_of_alg_bytes": traffic / alg_bytes, "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak}
 
 
-def committed_traffic(name, rays_per_launch):
+_L2_PEAK = {}
+
+
+def l2_copy_gbs(torch):
+    """L2-resident copy bandwidth of this GPU, measured like the HBM peak (a
+    torch copy, read + write bytes) but over a 2 x 40 MB working set that the
+    129 MB L2 holds: 64 copies captured in one CUDA graph (no launch gaps),
+    best of 5 replays after a warm-up.  The denominator for traversal
+    kernels whose upper tree levels stay in L2."""
+    if "gbs" in _L2_PEAK:
+        return _L2_PEAK["gbs"]
+    n = 20 * 1024 * 1024  # bf16 elements: 40 MB per buffer
+    a = torch.ones(n, dtype=torch.bfloat16, device="cuda")
+    b = torch.empty_like(a)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            b.copy_(a)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    reps = 64
+    with torch.cuda.graph(g):
+        for _ in range(reps):
+            b.copy_(a)
+    best = None
+    for k in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        e1.synchronize()
+        if k:
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+    gbs = 2 * a.numel() * a.element_size() * reps / (best / 1e3) / 1e9
+    del g, a, b
+    _L2_PEAK["gbs"] = gbs
+    return gbs
+
+
+def l2_fraction(achieved, torch):
+    """The traversal kernel's algorithmic bandwidth against the L2 copy
+    bandwidth (the node and primitive fetches that L2 and L1 serve)."""
+    try:
+        gbs = l2_copy_gbs(torch)
+    except Exception as e:  # reported, not fatal: the HBM roofline stands
+        return {"l2_peak_error": str(e)}
+    return {"l2_copy_gbs": gbs, "frac_of_l2": (achieved / gbs) if achieved else None,
+            "l2_peak_how": "torch bf16 copy over 2 x 40 MB (L2-resident), 64 copies per CUDA graph, best of 5"}
+
+
+# Path-state bytes of one shading step (the SoA queues of the wavefront):
+# a shaded path reads ray origin, direction, hit, weight, roulette
+# throughput, radiance and ids (7 x 16 B); a continuing path writes all but
+# the hit to the next queue (6 x 16 B); a finished path writes its radiance
+# (16 B); a shadow ray writes origin, direction, contribution (3 x 16 B) and
+# its BVH root (4 B).
+SHADE_READ_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 96, 16, 52
+
+
+def shade_roofline(cnt, kc, samples, peak, peak_kind, timing_source):
+    """Roofline of the multi-job shading kernel.  Paths shaded = extend rays
+    (every queued path is traced, then shaded); each sample's path finishes
+    exactly once, so continuing paths = shaded - samples.  Material, light
+    and item tables (a few KB per job, L1-resident) are not counted."""
+    shaded, shadow = cnt["extend_rays"], cnt["shadow_rays"]
+    alg = (SHADE_READ_B * shaded + SHADE_CONT_B * (shaded - samples) + SHADE_DONE_B * samples +
+           SHADE_SHADOW_B * shadow)
+    launches = max(1, cnt["shade_launches"])
+    per_launch = alg / launches
+    avg_ms = kc["shade_ms"] / max(1, kc["shade_launches"])
+    achieved = per_launch / (avg_ms / 1e3) / 1e9 if kc["shade_launches"] else None
+    traffic, _ = committed_traffic("shade_batch_traffic.json", shaded / launches, key="dram_bytes_per_path")
+    r = {"bound": "hbm", "kernel": "k_srv_shade (one bounce of every path of a step, all jobs)",
+         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "traffic": traffic,
+         "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launch_timing": timing_source,
+         "paths_per_launch": shaded / launches, "shadow_rays_per_path": shadow / max(1, shaded),
+         "alg_bytes_per_path": alg / max(1, shaded)}
+    if traffic and avg_ms:
+        r["dram_gbs"] = traffic / (avg_ms / 1e3) / 1e9
+        r["dram_frac"] = r["dram_gbs"] / peak
+    return r
+
+
+def committed_traffic(name, rays_per_launch, key="dram_bytes_per_ray"):
     """DRAM bytes per launch of the extend kernel: the committed ncu capture's
     DRAM bytes per ray (a smaller case of the same kernel) x rays per launch."""
     p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
         d = json.load(open(p))
-        return d["dram_bytes_per_ray"] * rays_per_launch, d
+        return d[key] * rays_per_launch, d
     return None, None
 
 
@@ -432,7 +518,7 @@ def bvh_stress(ctx, flat, torch):
            "mrays_per_s": (cnt["extend_rays"] + cnt["shadow_rays"]) * steps / (ms / 1e3) / 1e6,
            "extend_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                                "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
-                               **l2_absorption(traffic, per_launch, avg_ms, peak)},
+                               **l2_absorption(traffic, per_launch, avg_ms, peak), **l2_fraction(achieved, torch)},
            "host_bvh_build_ms": g.info.build_ms,
            "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
     job.close()
@@ -545,9 +631,10 @@ def run_gprt(args):
     sv.close()
     del flush
 
-    # roofline of the dominant kernel: closest-hit traversal ("extend") over
-    # the pooled sphere BVHs.  Algorithmic bytes per ray: ray in (32 B) + hit
-    # out (16 B) + 24 B per child-box test + 16 B (center, radius) per sphere test.
+    # rooflines of the two largest kernels; `roofline` is the one with the
+    # larger measured time.  Closest-hit traversal ("extend") over the pooled
+    # sphere BVHs: algorithmic bytes per ray = ray in (32 B) + hit out (16 B)
+    # + 24 B per child-box test + 16 B (center, radius) per sphere test.
     peak, peak_kind = measured_peaks()
     alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 16 * cnt["extend_prims"]
     per_launch = alg / max(1, launches_counted)
@@ -562,7 +649,12 @@ def run_gprt(args):
             "box_tests_per_ray": cnt["extend_boxes"] / max(1, cnt["extend_rays"]),
             "sphere_tests_per_ray": cnt["extend_prims"] / max(1, cnt["extend_rays"])}
     roof.update(l2_absorption(traffic, per_launch, avg_ms, peak))
+    roof.update(l2_fraction(achieved, torch))
+    roof_shade = shade_roofline(cnt, kc, samples_per_step, peak, peak_kind, timing_source)
     kernel_ms = {k: kc[k + "_ms"] / args.steps for k in ("extend", "shade", "shadow", "other")}
+    rooflines = {"extend": roof, "shade": roof_shade}
+    if kc["shade_ms"] > kc["extend_ms"]:
+        roof = roof_shade
 
     # the plain per-job path on the same batch (host clock around device-synchronised jobs)
     plain = None
@@ -645,7 +737,7 @@ def run_gprt(args):
                                          "candidates": tune["candidates"]},
                            "server_steps_per_batch": (st1["steps"] - st0["steps"]) / args.steps},
                 "plain": plain, "serving": serving, "bvh_stress": stress,
-                "roofline": roof, "kernel_ms_per_step": kernel_ms, "cpu_baseline": cpu, "e2e": e2e,
+                "roofline": roof, "rooflines": rooflines, "kernel_ms_per_step": kernel_ms, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(timed_kernels), "clocks": clk}
         print(json.dumps(line))
     for g in gscenes:
