@@ -376,9 +376,9 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   uint2 *qin = qa, *qout = qb;
   int in_slot = 0, levels = 0;
   for (;;) {
-    uint32_t cnt = 0;
-    CK(ctx, cudaMemcpyAsync(&cnt, qn + in_slot, 4, cudaMemcpyDeviceToHost, st));
+    CK(ctx, cudaMemcpyAsync(ctx->h_words, qn + in_slot, 4, cudaMemcpyDeviceToHost, st));
     CK(ctx, cudaStreamSynchronize(st));
+    uint32_t cnt = ctx->h_words[0];
     if (cnt == 0) break;
     levels++;
     CK(ctx, cudaMemsetAsync(qn + (in_slot ^ 1), 0, 4, st));
@@ -387,11 +387,11 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
     std::swap(qin, qout);
     in_slot ^= 1;
   }
-  uint32_t n4 = 0;
-  int e = 0;
-  CK(ctx, cudaMemcpyAsync(&n4, qn + 2, 4, cudaMemcpyDeviceToHost, st));
-  CK(ctx, cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, st));
+  CK(ctx, cudaMemcpyAsync(ctx->h_words, qn + 2, 4, cudaMemcpyDeviceToHost, st));
+  CK(ctx, cudaMemcpyAsync(ctx->h_words + 1, err, 4, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaStreamSynchronize(st));
+  uint32_t n4 = ctx->h_words[0];
+  int e = (int)ctx->h_words[1];
   if (e) return cleanup(fail(ctx, GPRT_E_BOUND, "device BVH build exceeded its node capacity"));
   // 6. primitive arrays in leaf order, and the node array at its final size
   float4 *nodes = nullptr, *tris = nullptr, *normals = nullptr, *quads = nullptr, *spheres = nullptr,

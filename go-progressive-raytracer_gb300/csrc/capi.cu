@@ -195,11 +195,12 @@ int add_samples(gprt_job* j, uint32_t spp, uint32_t npix, const uint32_t* list) 
 
 int check_device_errors(gprt_job* j) {
   gprt_ctx* ctx = j->scene->ctx;
-  uint32_t err = 0;
+  j->h_words[0] = 0;
   if (j->paths.counters) {
-    CK(ctx, cudaMemcpyAsync(&err, j->paths.counters + 3, 4, cudaMemcpyDeviceToHost, j->stream));
+    CK(ctx, cudaMemcpyAsync(j->h_words, j->paths.counters + 3, 4, cudaMemcpyDeviceToHost, j->stream));
   }
   CK(ctx, cudaStreamSynchronize(j->stream));
+  uint32_t err = j->h_words[0];
   if (err) {
     return fail(ctx, GPRT_E_BOUND,
                 std::string("device bound exceeded:") + ((err & kErrStackOverflow) ? " traversal stack" : "") +
@@ -227,6 +228,11 @@ int gprt_ctx_create(int device, gprt_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess) return GPRT_E_DEVICE;
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return GPRT_E_DEVICE;
+  if (cudaMallocHost(reinterpret_cast<void**>(&c->h_words), 64) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(c->stream);
+    return GPRT_E_OOM;
+  }
   *out = c.release();
   return GPRT_OK;
 }
@@ -249,6 +255,7 @@ int gprt_ctx_destroy(gprt_ctx* ctx) {
     while (!ctx->scenes.empty()) gprt_scene_destroy(*ctx->scenes.begin());
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    cudaFreeHost(ctx->h_words);
   }
   delete ctx;
   return GPRT_OK;
@@ -444,9 +451,10 @@ int gprt_intersect_host(gprt_scene* s, const gprt_ray* rays, uint32_t n, uint32_
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   free_all(tmp);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "intersect_host");
-  int err = 0;
-  cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (err) return fail(ctx, GPRT_E_BOUND, "device bound exceeded: traversal stack");
+  if (cudaMemcpyAsync(ctx->h_words, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return cuda_fail(ctx, cudaGetLastError(), "intersect_host error word");
+  if (ctx->h_words[0]) return fail(ctx, GPRT_E_BOUND, "device bound exceeded: traversal stack");
   return GPRT_OK;
 }
 
@@ -505,8 +513,14 @@ int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
     free_all(j->buffers);
     return GPRT_E_OOM;
   }
+  if (cudaMallocHost(reinterpret_cast<void**>(&j->h_words), 16) != cudaSuccess) {
+    cudaGetLastError();
+    free_all(j->buffers);
+    return fail(ctx, GPRT_E_OOM, "pinned job words");
+  }
   if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_all(j->buffers);
+    cudaFreeHost(j->h_words);
     return fail(ctx, GPRT_E_DEVICE, "stream creation failed");
   }
   cudaEventCreate(&j->ev0);
@@ -518,6 +532,8 @@ int gprt_job_create(gprt_scene* s, const gprt_job_desc* desc, gprt_job** out) {
   cudaError_t e = cudaStreamSynchronize(j->stream);
   if (e != cudaSuccess) {
     free_all(j->buffers);
+    cudaFreeHost(j->h_words);
+    cudaStreamDestroy(j->stream);
     return cuda_fail(ctx, e, "job init");
   }
   j->uniform_count = 0;
@@ -533,6 +549,7 @@ int gprt_job_destroy(gprt_job* j) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(j->stream);
   free_all(j->buffers);
+  cudaFreeHost(j->h_words);
   cudaStreamDestroy(j->stream);
   cudaEventDestroy(j->ev0);
   cudaEventDestroy(j->ev1);
@@ -591,9 +608,9 @@ int gprt_job_render_pass(gprt_job* j, uint32_t pass, gprt_render_stats* stats) {
       launch_active_pixels(j->film, target, min_s, (float)sd.adaptive_threshold, j->d_pix_list, j->d_active,
                            j->stream);
       j->launches++;
-      uint32_t active = 0;
-      CK(ctx, cudaMemcpyAsync(&active, j->d_active, 4, cudaMemcpyDeviceToHost, j->stream));
+      CK(ctx, cudaMemcpyAsync(j->h_words + 1, j->d_active, 4, cudaMemcpyDeviceToHost, j->stream));
       CK(ctx, cudaStreamSynchronize(j->stream));
+      uint32_t active = j->h_words[1];
       if (active == 0) break;
       if (active != npix) j->uniform_count = -1;
       rc = add_samples(j, 1, active, j->d_pix_list);

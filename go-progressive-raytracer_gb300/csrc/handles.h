@@ -22,6 +22,10 @@ struct gprt_ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  // pinned words for small read-backs (counts, error flags): a copy into
+  // pageable memory blocks inside the runtime until the stream drains and
+  // stalls other threads' CUDA calls meanwhile
+  uint32_t* h_words = nullptr;
   std::recursive_mutex mu;
   std::string err;
   std::set<gprt_scene*> scenes;
@@ -41,6 +45,7 @@ struct gprt_scene {
 
 struct gprt_job {
   gprt_scene* scene = nullptr;
+  uint32_t* h_words = nullptr;  // pinned: [0] error bits, [1] active pixels
   gprt_job_desc desc{};
   DevFilm film{};
   DevPaths paths{};

@@ -309,6 +309,16 @@ struct gprt_server {
   DevPaths P{};
   std::vector<void*> path_bufs;
   size_t path_bytes = 0;
+  // read-back staging (resolved image before the copy to the host), grown
+  // on demand under smu and kept: a cudaFree per read would synchronise the
+  // device while steps run
+  std::vector<void*> rb_bufs;
+  size_t rb_bytes = 0;
+  unsigned char* rb = nullptr;
+  // pinned host staging of read-backs: the device-to-host copy runs at the
+  // link's rate, then one host memcpy into the caller's (pageable) buffer
+  unsigned char* rb_host = nullptr;
+  size_t rb_host_bytes = 0;
   size_t reserve = 0;      // bytes promised to the film being admitted
   uint32_t capacity = 0;   // path capacity allocated
   uint32_t step_paths = 0; // paths per step (<= capacity)
@@ -316,7 +326,9 @@ struct gprt_server {
   uint32_t flags = 0;
   // item table: [hdr | path0[max+1] | pix0[max+1]] then items[max]
   unsigned char* d_table = nullptr;
-  unsigned char* h_table = nullptr;  // pinned
+  unsigned char* h_table = nullptr;  // pinned (table_bytes, then the step's error word)
+  uint32_t* h_err = nullptr;         // pinned: a pageable read-back would block inside the runtime
+                                     // until the step ends, stalling other threads' CUDA calls
   size_t table_bytes = 0, prefix_bytes = 0;
   std::map<int, cudaGraphExec_t> graphs;  // by depth
   uint64_t graph_gen = ~0ull;
@@ -933,9 +945,9 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
   int rc = run_step(sv, D);
   if (rc) return rc;
   CK(ctx, cudaEventRecord(sv->ev1, sv->stream));
-  uint32_t err = 0;
-  CK(ctx, cudaMemcpyAsync(&err, sv->P.counters + 3, 4, cudaMemcpyDeviceToHost, sv->stream));
+  CK(ctx, cudaMemcpyAsync(sv->h_err, sv->P.counters + 3, 4, cudaMemcpyDeviceToHost, sv->stream));
   CK(ctx, cudaStreamSynchronize(sv->stream));
+  uint32_t err = *sv->h_err;
   float ms = 0;
   cudaEventElapsedTime(&ms, sv->ev0, sv->ev1);
   if (ms_out) *ms_out = ms;
@@ -1023,15 +1035,33 @@ int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out) {
   if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
   size_t npix = j->npix;
   size_t bytes = kind == 0 ? npix * 4 : npix * 3 * sizeof(float);
-  std::vector<void*> tmp;
-  uint8_t* d = nullptr;
-  if (dev_alloc(ctx, tmp, &d, bytes)) return GPRT_E_OOM;
+  if (bytes > sv->rb_bytes) {
+    cudaStreamSynchronize(sv->stream);  // the old staging buffer may still be read
+    free_all(sv->rb_bufs);
+    sv->rb = nullptr;
+    sv->rb_bytes = 0;
+    if (dev_alloc(ctx, sv->rb_bufs, &sv->rb, bytes)) return GPRT_E_OOM;
+    sv->rb_bytes = bytes;
+  }
+  if (bytes > sv->rb_host_bytes) {
+    if (sv->rb_host) cudaFreeHost(sv->rb_host);
+    sv->rb_host = nullptr;
+    sv->rb_host_bytes = 0;
+    void* h = nullptr;
+    if (cudaHostAlloc(&h, bytes, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, GPRT_E_OOM, "pinned read-back buffer");
+    }
+    sv->rb_host = static_cast<unsigned char*>(h);
+    sv->rb_host_bytes = bytes;
+  }
+  uint8_t* d = sv->rb;
   if (kind == 0) launch_resolve_rgba8(j->film, d, sv->stream);
   else launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->stream);
-  cudaError_t e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, sv->stream);
+  cudaError_t e = cudaMemcpyAsync(sv->rb_host, d, bytes, cudaMemcpyDeviceToHost, sv->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
-  free_all(tmp);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server read-back");
+  std::memcpy(out, sv->rb_host, bytes);
   return GPRT_OK;
 }
 
@@ -1114,11 +1144,12 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
     return fail(ctx, GPRT_E_ADMISSION, "the budget does not cover the path state of one step");
   }
   if (dev_alloc(ctx, b, &sv->d_table, sv->table_bytes) ||
-      cudaMallocHost(reinterpret_cast<void**>(&sv->h_table), sv->table_bytes) != cudaSuccess) {
+      cudaMallocHost(reinterpret_cast<void**>(&sv->h_table), sv->table_bytes + 256) != cudaSuccess) {
     cudaGetLastError();
     free_all(b);
     return fail(ctx, GPRT_E_OOM, "item table allocation failed");
   }
+  sv->h_err = reinterpret_cast<uint32_t*>(sv->h_table + sv->table_bytes);
   if (cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_all(b);
     cudaFreeHost(sv->h_table);
@@ -1157,6 +1188,8 @@ int gprt_server_destroy(gprt_server* sv) {
     for (auto& kv : sv->step_events)
       for (auto e : kv.second) cudaEventDestroy(e);
     free_all(sv->path_bufs);
+    free_all(sv->rb_bufs);
+    if (sv->rb_host) cudaFreeHost(sv->rb_host);
     if (sv->h_table) cudaFreeHost(sv->h_table);
     cudaEventDestroy(sv->ev0);
     cudaEventDestroy(sv->ev1);
