@@ -736,7 +736,7 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
 // when that sample's subpaths are done, takes the next sample from a
 // warp-aggregated counter, so a warp is not held by its longest path.
 template <int MAXV>
-__global__ void __launch_bounds__(128) k_bdpt_subpaths(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+__global__ void __launch_bounds__(128, 4) k_bdpt_subpaths(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
   uint32_t* next = B.scount + (MAXV + 1) * MAXV;  // the work counter, zeroed with the lists
