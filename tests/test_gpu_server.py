@@ -205,3 +205,43 @@ def test_server_autotune_keeps_films_and_picks_a_valid_config(ctx, scenes):
     _same(sv.film(ts[0]), _plain_film(scenes["spheres_a"], 1, 4))
     _same(sv.film(ts[1]), _plain_film(scenes["ico"], 2, 4))
     sv.close()
+
+
+def test_scenes_built_while_the_loop_thread_renders(ctx, scenes):
+    # a serving front door: the loop thread renders the jobs already
+    # submitted while the host creates the next scenes and submits each as
+    # soon as it exists; every film equals the same job rendered alone, and
+    # the RGBA8 read-backs (through the server's staging buffers) equal the
+    # resolve of that film
+    import time
+    import gprt
+    from gprt import scenes as S
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    sv.start()
+    keep = sv.submit(scenes["ico"], _cfg(64, 4, 5))  # keeps the loop busy meanwhile
+    made, tickets = [], []
+    for k in range(6):
+        g = gprt.GpuScene(ctx, S.default_style_scene(20 + k, width=32 + 8 * k, height=24 + 8 * k).to_desc())
+        made.append(g)
+        tickets.append(sv.submit(g, _cfg(4, 2, 11 + k)))
+    want = set(tickets + [keep])
+    done, deadline = set(), time.perf_counter() + 120
+    while done != want:
+        assert time.perf_counter() < deadline
+        for e in sv.poll(256, timeout_ms=10):
+            assert e.kind not in ("failed", "refused", "cancelled")
+            if e.kind == "done":
+                done.add(e.ticket)
+    sv.stop()
+    for k, (g, t) in enumerate(zip(made, tickets)):
+        _same(sv.film(t), _plain_film(g, 11 + k, 4))
+        rgba = sv.rgba8(t)
+        r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=4, max_passes=1, seed=11 + k))
+        r.add_samples(4)
+        assert np.array_equal(rgba, r.rgba8())
+        r.close()
+        sv.release(t)
+    sv.release(keep)
+    sv.close()
+    for g in made:
+        g.close()
