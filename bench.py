@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--impl", default="gprt", choices=["gprt", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--stream-requests", type=int, default=48)
-    ap.add_argument("--rates", default="20,100,200")
+    ap.add_argument("--rates", default="20,50,100,200")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bvh-stress", action="store_true")
     ap.add_argument("--no-stream", action="store_true")
