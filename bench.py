@@ -389,6 +389,11 @@ def run_plain_batch(gscenes, spps, seed=1):
     return n
 
 
+# request kinds of the serving stream rendered with BDPT (the Cornell-boxes
+# scene, kind 2 of scenes.serving_requests)
+BDPT_KINDS = (2,)
+
+
 def stream_batched(ctx, server_kw, tune, reqs, arrivals, gs):
     """Serves a request stream with the batched server's loop thread."""
     import gprt
@@ -401,7 +406,7 @@ def stream_batched(ctx, server_kw, tune, reqs, arrivals, gs):
         while time.perf_counter() - t0 < at:
             time.sleep(0.0002)
         cfg = gprt.ProgressiveConfig(initial_samples=4, max_samples_per_pixel=spp, max_passes=spp // 4, seed=5)
-        tickets.append(sv.submit(gs[kind], cfg))
+        tickets.append(sv.submit(gs[kind], cfg, integrator=gprt.BDPTIntegrator() if kind in BDPT_KINDS else None))
     ev = []
     deadline = time.perf_counter() + 600
     while len({e.ticket for e in ev if e.kind == "done"}) < len(tickets) and time.perf_counter() < deadline:
@@ -427,7 +432,8 @@ def stream_plain(reqs, arrivals, gs):
         if now < at:
             time.sleep(at - now)
         r = gprt.ProgressiveRaytracer(gs[kind], gprt.ProgressiveConfig(max_samples_per_pixel=spp, max_passes=spp // 4,
-                                                                       seed=5))
+                                                                       seed=5),
+                                      integrator=gprt.BDPTIntegrator() if kind in BDPT_KINDS else None)
         for p in range(spp // 4):
             r.add_samples(4)
             r.sync()
@@ -446,18 +452,25 @@ def serving_section(ctx, args, server_kw, tune, flats):
     sizes = [g.width * g.height for g in gs]
     reqs = scenes.serving_requests(args.stream_requests)
     samples = sum(sizes[k] * spp for k, spp in reqs)
-    out = {"requests": len(reqs), "mix": "Cornell 400^2 / icosphere 1024^2 / Cornell boxes 512^2 / default-style "
-                                         "scene, target spp U{16..256} in passes of 4 spp",
+    out = {"requests": len(reqs), "mix": "Cornell 400^2 PT / icosphere 1024^2 PT / Cornell boxes 512^2 BDPT / "
+                                         "default-style 512^2 scene PT, target spp U{16..256} in passes of 4 spp",
+           "bdpt_requests": sum(1 for k, _ in reqs if k in BDPT_KINDS),
+           "requests_512sq_pt": sum(1 for k, _ in reqs if sizes[k] == 512 * 512 and k not in BDPT_KINDS),
            "samples_per_stream": samples, "rates": {}}
     rates = [float(x) for x in args.rates.split(",") if x]
     for rate in rates:
         arr = scenes.poisson_arrivals(len(reqs), rate)
         ev, tickets, span, st = stream_batched(ctx, server_kw, tune, reqs, arr, gs)
         t512 = [t for t, (k, _) in zip(tickets, reqs) if gs[k].width == 512 and gs[k].height == 512]
+        pt512 = [t for t, (k, _) in zip(tickets, reqs) if t in t512 and k not in BDPT_KINDS]
+        bd512 = [t for t, (k, _) in zip(tickets, reqs) if t in t512 and k in BDPT_KINDS]
         out["rates"][str(int(rate))] = {
             "batched": {"msamples_per_s": samples / span / 1e6, "makespan_s": span,
                         **gprt.latency_summary(ev),
                         "ttfp_p99_ms_512sq": gprt.latency_summary(ev, t512)["ttfp_p99_ms"],
+                        "ttfp_p99_ms_512sq_pt": gprt.latency_summary(ev, pt512)["ttfp_p99_ms"] if pt512 else None,
+                        "ttfp_p99_ms_512sq_bdpt": gprt.latency_summary(ev, bd512)["ttfp_p99_ms"] if bd512 else None,
+                        "ttfp_p50_ms_512sq_bdpt": gprt.latency_summary(ev, bd512)["ttfp_p50_ms"] if bd512 else None,
                         "steps": st["steps"], "graph_launches": st["graph_launches"]}}
     mid = rates[len(rates) // 2] if rates else None
     if mid is not None:
@@ -735,7 +748,9 @@ def run_gprt(args):
     if rank == 0 and not args.no_stream:
         from gprt import scenes
         ico_flat = scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH).to_desc()
-        flats = [scenes.cornell_baseline(400).to_desc(), ico_flat, scenes.cornell_boxes_bdpt(512).to_desc(), jobs[0][0]]
+        # C3's kind: the batch's first 512^2 job, so that 512^2 requests of both integrators arrive
+        c3 = next(f for (f, _), g in zip(jobs, gscenes) if g.width == 512 and g.height == 512)
+        flats = [scenes.cornell_baseline(400).to_desc(), ico_flat, scenes.cornell_boxes_bdpt(512).to_desc(), c3]
         serving = serving_section(ctx, args, server_kw, tune, flats)
 
     stress = None

@@ -209,6 +209,63 @@ int check_device_errors(gprt_job* j) {
   return GPRT_OK;
 }
 
+// Uploads the primitive and node arrays of s->host (host-built BVH, and the
+// server's private copies).
+int upload_geometry(gprt_ctx* ctx, gprt_scene* s) {
+  HostScene& h = s->host;
+  DevScene& d = s->dev;
+  int rc = 0;
+  rc |= upload(ctx, s->buffers, h.nodes, &d.nodes, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tris, &d.tris, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.quadrics, &d.quadrics, &s->bytes);
+  return rc;
+}
+
+// Uploads materials, lights and textures, sets the scalar fields of s->dev
+// and waits for the copies; frees the scene's buffers on failure.
+int upload_rest(gprt_ctx* ctx, gprt_scene* s) {
+  HostScene& h = s->host;
+  DevScene& d = s->dev;
+  int rc = 0;
+  rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tri_uvs, &d.tri_uvs, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.tex_info, &d.tex_info, &s->bytes);
+  rc |= upload(ctx, s->buffers, h.texels, &d.texels, &s->bytes);
+  d.has_textures = h.tex_info.empty() ? 0 : 1;
+  if (rc) {
+    free_all(s->buffers);
+    return rc;
+  }
+  if (dev_alloc(ctx, s->buffers, &s->d_err, 1)) {
+    free_all(s->buffers);
+    return GPRT_E_OOM;
+  }
+  cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
+  d.n_nodes = (int)(h.nodes.size() / 8);
+  d.root = d.n_nodes > 0 ? 0 : -1;
+  d.n_lights = (int)h.lights.size();
+  d.quad_base = h.n_tris;
+  d.sphere_base = h.n_tris + h.n_quads;
+  d.quadric_base = h.n_tris + h.n_quads + h.n_spheres;
+  d.n_prims = h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
+  d.has_infinite = h.has_infinite;
+  d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
+  d.world_radius = (float)h.world_radius;
+  d.cam = h.cam;
+  d.max_depth = (int)h.sampling.max_depth;
+  d.rr_min_bounces = (int)h.sampling.rr_min_bounces;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    free_all(s->buffers);
+    return cuda_fail(ctx, e, "scene upload");
+  }
+  return GPRT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -300,46 +357,14 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
       return fail(ctx, GPRT_E_DEVICE, "device BVH build produced an invalid tree: " + bad);
     }
   } else {
-    rc |= upload(ctx, s->buffers, h.nodes, &d.nodes, &s->bytes);
-    rc |= upload(ctx, s->buffers, h.tris, &d.tris, &s->bytes);
-    rc |= upload(ctx, s->buffers, h.tri_normals, &d.tri_normals, &s->bytes);
-    rc |= upload(ctx, s->buffers, h.quads, &d.quads, &s->bytes);
-    rc |= upload(ctx, s->buffers, h.spheres, &d.spheres, &s->bytes);
-    rc |= upload(ctx, s->buffers, h.quadrics, &d.quadrics, &s->bytes);
+    rc = upload_geometry(ctx, s.get());
+    if (rc) {
+      free_all(s->buffers);
+      return rc;
+    }
   }
-  rc |= upload(ctx, s->buffers, h.materials, &d.materials, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.lights, &d.lights, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.tri_uvs, &d.tri_uvs, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.tex_info, &d.tex_info, &s->bytes);
-  rc |= upload(ctx, s->buffers, h.texels, &d.texels, &s->bytes);
-  d.has_textures = h.tex_info.empty() ? 0 : 1;
-  if (rc) {
-    free_all(s->buffers);
-    return rc;
-  }
-  if (dev_alloc(ctx, s->buffers, &s->d_err, 1)) {
-    free_all(s->buffers);
-    return GPRT_E_OOM;
-  }
-  cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
-  d.n_nodes = (int)(h.nodes.size() / 8);
-  d.root = d.n_nodes > 0 ? 0 : -1;
-  d.n_lights = (int)h.lights.size();
-  d.quad_base = h.n_tris;
-  d.sphere_base = h.n_tris + h.n_quads;
-  d.quadric_base = h.n_tris + h.n_quads + h.n_spheres;
-  d.n_prims = h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
-  d.has_infinite = h.has_infinite;
-  d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
-  d.world_radius = (float)h.world_radius;
-  d.cam = h.cam;
-  d.max_depth = (int)h.sampling.max_depth;
-  d.rr_min_bounces = (int)h.sampling.rr_min_bounces;
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess) {
-    free_all(s->buffers);
-    return cuda_fail(ctx, e, "scene upload");
-  }
+  rc = upload_rest(ctx, s.get());
+  if (rc) return rc;
   ctx->scenes.insert(s.get());
   *out = s.release();
   return GPRT_OK;
@@ -975,3 +1000,41 @@ extern "C" int gprt_autotune(gprt_scene* s, const gprt_job_desc* base, uint32_t 
   out->best_ms = best;
   return GPRT_OK;
 }
+
+namespace gprt {
+
+int clone_scene(gprt_scene* src, gprt_scene** out) {
+  gprt_ctx* ctx = src->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  *out = nullptr;
+  auto s = std::make_unique<gprt_scene>();
+  s->ctx = ctx;
+  s->serial = src->serial;
+  s->host = src->host;
+  s->dev = DevScene{};
+  int rc = upload_geometry(ctx, s.get());
+  if (rc) {
+    free_all(s->buffers);
+    return rc;
+  }
+  rc = upload_rest(ctx, s.get());
+  if (rc) return rc;
+  *out = s.release();
+  return GPRT_OK;
+}
+
+size_t bdpt_job_bytes(const gprt_scene* s, const gprt_job_desc& d) {
+  const HostScene& h = s->host;
+  uint64_t npix = (uint64_t)h.sampling.width * h.sampling.height;
+  uint64_t ns = d.chunk_paths ? d.chunk_paths : npix * std::max(1u, d.max_samples_per_pixel);
+  ns = std::min<uint64_t>(ns, 1u << 20);
+  int maxv = bdpt_maxv((int)h.sampling.max_depth);
+  size_t film = (size_t)npix * (sizeof(float4) * 2 + 3 * sizeof(uint32_t)) + 256;
+  size_t work = bdpt_bytes((uint32_t)ns, maxv) + (size_t)ns * sizeof(float4) +               // vertices, Lout
+                (size_t)ns * (maxv + 1) * maxv * sizeof(uint32_t) + 64 * sizeof(uint32_t);  // strategy lists
+  if (!h.tex_info.empty()) work += (size_t)ns * 2 * maxv * sizeof(float2);
+  return film + work;
+}
+
+}  // namespace gprt

@@ -126,6 +126,13 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
 // Cancels the server's pending requests for a scene that is being destroyed
 // (server.cu).  Called with the scene's context locked.
 void server_forget_scene(gprt_server* sv, gprt_scene* s);
+// A private copy of scene `src` (the same host description, its own device
+// arrays), not listed among the context's scenes; gprt_scene_destroy
+// releases it with the jobs on it.  The server renders BDPT requests on one.
+int clone_scene(gprt_scene* src, gprt_scene** out);
+// Device bytes of a BDPT job on scene `s`: film, and the subpath vertices and
+// strategy buffers of one chunk as gprt_job_create and its first pass allocate them.
+size_t bdpt_job_bytes(const gprt_scene* s, const gprt_job_desc& d);
 
 inline uint32_t samples_for_pass(const gprt_job_desc& d, uint32_t pass) {
   if (d.max_passes == 1) return d.max_samples_per_pixel;

@@ -292,6 +292,10 @@ struct SrvJob {
   bool running = true;
   double submit_ms = 0, admit_ms = 0;
   uint64_t last_served = 0;
+  // BDPT requests: a per-job render on a private copy of the scene (which
+  // the caller may destroy meanwhile), one pass between batched steps
+  gprt_scene* bd_scene = nullptr;
+  gprt_job* bd = nullptr;
 };
 
 struct gprt_server {
@@ -309,6 +313,7 @@ struct gprt_server {
   DevPaths P{};
   std::vector<void*> path_bufs;
   size_t path_bytes = 0;
+  uint64_t bd_rounds = 0;  // BDPT passes run (their least-recently-served order)
   // read-back staging (resolved image before the copy to the host), grown
   // on demand under smu and kept: a cudaFree per read would synchronise the
   // device while steps run
@@ -594,6 +599,11 @@ void release_job(gprt_server* sv, SrvJob* j) {
     j->ps = nullptr;
   }
   free_all(j->bufs);
+  if (j->bd_scene) {
+    gprt_scene_destroy(j->bd_scene);  // and the job on it
+    j->bd_scene = nullptr;
+    j->bd = nullptr;
+  }
 }
 
 // Moves the job past passes that need no new samples; finishes it after its
@@ -650,6 +660,59 @@ void admit(gprt_server* sv) {
       std::lock_guard<std::mutex> q(sv->qmu);
       sv->pending.pop_front();
     };
+    if (r.desc.integrator == GPRT_INTEGRATOR_BDPT) {
+      // film + subpath working set + the private scene copy
+      size_t need_b = bdpt_job_bytes(s, r.desc) + s->bytes;
+      if (fixed + need_b > sv->desc.hbm_budget_bytes) {
+        pop();
+        sv->st.refused++;
+        emit(sv, r.ticket, GPRT_EV_REFUSED, 0, 0, GPRT_E_ADMISSION, r.submit_ms);
+        continue;
+      }
+      if (bytes_in_use(sv) + need_b > sv->desc.hbm_budget_bytes) {
+        bool freed = false;  // unreferenced cached scenes go first
+        for (auto& ps : sv->scenes)
+          if (ps->refs == 0) {
+            evict(sv, ps.get());
+            freed = true;
+            break;
+          }
+        if (freed) {
+          shrink_if_empty(sv);
+          continue;
+        }
+        return;  // waits for running jobs to finish
+      }
+      gprt_scene* copy = nullptr;
+      gprt_job* bj = nullptr;
+      int rc = clone_scene(s, &copy);
+      if (rc == GPRT_OK) rc = gprt_job_create(copy, &r.desc, &bj);
+      if (rc != GPRT_OK) {
+        if (copy) gprt_scene_destroy(copy);
+        if (rc == GPRT_E_OOM) return;  // device full: retry next step
+        pop();
+        sv->st.refused++;
+        emit(sv, r.ticket, GPRT_EV_REFUSED, 0, 0, rc, r.submit_ms);
+        continue;
+      }
+      auto j = std::make_unique<SrvJob>();
+      j->ticket = r.ticket;
+      j->desc = r.desc;
+      j->npix = npix;
+      j->submit_ms = r.submit_ms;
+      j->bd_scene = copy;
+      j->bd = bj;
+      j->film_bytes = need_b;
+      j->admit_ms = now_ms(sv->t0);
+      pop();
+      sv->st.admitted++;
+      sv->n_running++;
+      emit(sv, r.ticket, GPRT_EV_ADMITTED, 0, 0, GPRT_OK, r.submit_ms);
+      SrvJob* raw = j.get();
+      sv->jobs[r.ticket] = std::move(j);
+      advance(sv, raw, false);
+      continue;
+    }
     if (npix > sv->capacity || fixed + need > sv->desc.hbm_budget_bytes) {
       pop();
       sv->st.refused++;
@@ -858,7 +921,7 @@ struct Item {
 std::vector<Item> pack(gprt_server* sv) {
   std::vector<SrvJob*> order;
   for (auto& kv : sv->jobs)
-    if (kv.second->running) order.push_back(kv.second.get());
+    if (kv.second->running && !kv.second->bd) order.push_back(kv.second.get());
   std::stable_sort(order.begin(), order.end(),
                    [](const SrvJob* a, const SrvJob* b) { return a->last_served < b->last_served; });
   std::vector<Item> items;
@@ -932,13 +995,18 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
   return D;
 }
 
-// One step: admission, one batched wavefront, events.  Returns the number of
-// items run (0: nothing to do) or a negative status.
-int step_impl(gprt_server* sv, bool dry, double* ms_out) {
+// One batched path-tracing wavefront over the running path-tracing jobs, and
+// its events; `overlap` runs once the wavefront is queued, before waiting for
+// it (work on other streams then shares the GPU with it).  Returns the number
+// of items run (0: none) or a negative status.
+template <class F>
+int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
   gprt_ctx* ctx = sv->ctx;
-  if (!dry) admit(sv);
   std::vector<Item> items = pack(sv);
-  if (items.empty()) return 0;
+  if (items.empty()) {
+    overlap();
+    return 0;
+  }
   uint64_t paths = 0;
   int D = upload_items(sv, items, dry, &paths);
   CK(ctx, cudaEventRecord(sv->ev0, sv->stream));
@@ -946,6 +1014,7 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
   if (rc) return rc;
   CK(ctx, cudaEventRecord(sv->ev1, sv->stream));
   CK(ctx, cudaMemcpyAsync(sv->h_err, sv->P.counters + 3, 4, cudaMemcpyDeviceToHost, sv->stream));
+  overlap();
   CK(ctx, cudaStreamSynchronize(sv->stream));
   uint32_t err = *sv->h_err;
   float ms = 0;
@@ -974,6 +1043,70 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
     if (j->spp_done >= j->pass_target) advance(sv, j, true);
   }
   return (int)items.size();
+}
+
+// BDPT samples rendered per step at most (whole samples per pixel, at least
+// one): about 5 ms of Cornell-boxes BDPT, so a step that carries BDPT work
+// stays short and every job's next pass (time to first pass above all)
+// waits for little.
+constexpr uint64_t kBdptStepSamples = 1u << 18;
+
+// The BDPT job served next: jobs still before their first pass first, the
+// oldest request of those first (a burst then finishes its first passes one
+// after another instead of all at the end), then the least recently served;
+// null when none runs.
+SrvJob* next_bdpt(gprt_server* sv) {
+  SrvJob* pick = nullptr;
+  auto before = [](const SrvJob* a, const SrvJob* b) {
+    bool fa = a->passes == 0, fb = b->passes == 0;
+    if (fa != fb) return fa;
+    if (fa) return a->submit_ms < b->submit_ms || (a->submit_ms == b->submit_ms && a->ticket < b->ticket);
+    return a->last_served < b->last_served;
+  };
+  for (auto& kv : sv->jobs) {
+    SrvJob* j = kv.second.get();
+    if (j->bd && j->running && (!pick || before(j, pick))) pick = j;
+  }
+  return pick;
+}
+
+// Completes the pass of `n` samples queued for BDPT job j (status rc of the
+// launch): waits for it and emits its events.
+void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc) {
+  if (rc == GPRT_OK) rc = gprt_job_sync(j->bd);
+  if (rc != GPRT_OK) {
+    emit(sv, j->ticket, GPRT_EV_FAILED, j->passes, j->spp_done, rc, j->submit_ms);
+    release_job(sv, j);
+    return;
+  }
+  j->spp_done += n;
+  j->last_served = ++sv->bd_rounds;
+  sv->st.samples += (uint64_t)n * j->npix;
+  if (j->spp_done >= j->pass_target) advance(sv, j, true);
+}
+
+// One step: admission, one batched path-tracing wavefront and, on the BDPT
+// job's own stream at the same time, the next samples of one BDPT job's pass
+// (RenderPass of one job, progressive.go:126-223: all pixels take the pass's
+// new samples, here in slices of at most kBdptStepSamples; splats are applied
+// after each slice); then the events of both.  Returns the number of items
+// run (0: nothing to do) or a negative status.
+int step_impl(gprt_server* sv, bool dry, double* ms_out) {
+  if (!dry) admit(sv);
+  SrvJob* bj = dry ? nullptr : next_bdpt(sv);
+  uint32_t bn = 0;
+  int brc = GPRT_OK;
+  bool launched = false;
+  int n = pt_step(sv, dry, ms_out, [&]() {
+    if (!bj) return;
+    uint64_t per = std::max<uint64_t>(1, kBdptStepSamples / std::max<uint32_t>(1, bj->npix));
+    bn = (uint32_t)std::min<uint64_t>(bj->pass_target - bj->spp_done, per);
+    brc = gprt_job_add_samples(bj->bd, bn);  // queued on the job's stream
+    launched = true;
+  });
+  if (launched) finish_bdpt(sv, bj, bn, brc);
+  if (n < 0) return n;
+  return n + (launched ? 1 : 0);
 }
 
 SrvJob* find_job(gprt_server* sv, uint64_t ticket) {
@@ -1032,6 +1165,9 @@ int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out) {
   cudaSetDevice(ctx->device);
   SrvJob* j = find_job(sv, ticket);
   if (!j) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
+  if (j->bd)  // BDPT: the per-job film (splats included)
+    return kind == 0 ? gprt_job_read_rgba8(j->bd, static_cast<uint8_t*>(out))
+                     : gprt_job_read_image(j->bd, static_cast<float*>(out));
   if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
   size_t npix = j->npix;
   size_t bytes = kind == 0 ? npix * 4 : npix * 3 * sizeof(float);
@@ -1178,7 +1314,10 @@ int gprt_server_destroy(gprt_server* sv) {
     std::lock_guard<std::mutex> g(sv->smu);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(sv->stream);
-    for (auto& kv : sv->jobs) free_all(kv.second->bufs);
+    for (auto& kv : sv->jobs) {
+      kv.second->running = false;  // the server is going: no counters to keep
+      release_job(sv, kv.second.get());
+    }
     sv->jobs.clear();
     sv->scenes.clear();
     for (auto& a : sv->pool)
@@ -1206,8 +1345,8 @@ int gprt_server_destroy(gprt_server* sv) {
 int gprt_server_submit(gprt_server* sv, gprt_scene* s, const gprt_job_desc* desc, uint64_t* ticket) {
   if (!sv || !s || !desc || s->ctx != sv->ctx) return GPRT_E_INVALID;
   gprt_ctx* ctx = sv->ctx;
-  if (desc->integrator != GPRT_INTEGRATOR_PATH_TRACING)
-    return fail(ctx, GPRT_E_INVALID, "the batched server runs path tracing only");
+  if (desc->integrator != GPRT_INTEGRATOR_PATH_TRACING && desc->integrator != GPRT_INTEGRATOR_BDPT)
+    return fail(ctx, GPRT_E_INVALID, "unknown integrator");
   gprt_job_desc d = *desc;
   if (d.initial_samples == 0) d.initial_samples = 1;
   if (d.max_samples_per_pixel == 0) d.max_samples_per_pixel = 50;
@@ -1316,6 +1455,7 @@ int gprt_server_read_film(gprt_server* sv, uint64_t ticket, float* rgb_sum, floa
   gprt_ctx* ctx = sv->ctx;
   cudaSetDevice(ctx->device);
   SrvJob* j = find_job(sv, ticket);
+  if (j && j->bd) return gprt_job_read_film(j->bd, rgb_sum, lum_sum, lum2_sum, count);
   if (!j || j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
   uint32_t npix = j->npix;
   CK(ctx, cudaStreamSynchronize(sv->stream));

@@ -42,9 +42,12 @@ class RenderServer:
         self.h = h
         self.sizes: Dict[int, tuple] = {}
 
-    def submit(self, gscene: GpuScene, config: ProgressiveConfig) -> int:
+    def submit(self, gscene: GpuScene, config: ProgressiveConfig, integrator=None) -> int:
+        """Queues a render of `gscene` (path tracing unless `integrator` is a
+        BDPTIntegrator; BDPT requests render pass by pass between the batched
+        path-tracing steps, on the server's own copy of the scene)."""
         d = capi.JobDesc()
-        d.integrator = capi.INTEGRATOR_PATH_TRACING
+        d.integrator = integrator.kind if integrator is not None else capi.INTEGRATOR_PATH_TRACING
         d.initial_samples = config.initial_samples
         d.max_samples_per_pixel = config.max_samples_per_pixel
         d.max_passes = config.max_passes

@@ -445,8 +445,16 @@ int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* r
  * stopping is not applied).  A job's film equals, bit for bit, the film of a
  * gprt_job with the same scene, seed and sample count: each sample is keyed
  * by (seed, pixel, sample index) and each pixel accumulates its samples in
- * order, whatever else shares the wavefront.  Path tracing only
- * (integrator = GPRT_INTEGRATOR_PATH_TRACING). */
+ * order, whatever else shares the wavefront.  BDPT requests
+ * (integrator = GPRT_INTEGRATOR_BDPT) are admitted with a private copy of
+ * the scene and the BDPT working set of one chunk (both counted against the
+ * budget, held until release); each step renders, beside the batched
+ * path-tracing wavefront and on the job's own stream, up to 2^18 samples
+ * (whole samples per pixel) of one BDPT job's pass: jobs before their first
+ * pass first, then the least recently served.  Their film equals that of a
+ * gprt_job on the same scene given the same samples, up to the summation
+ * order of the light-tracing splats (float atomics; applied after each
+ * slice). */
 typedef struct gprt_server_desc {
   uint64_t hbm_budget_bytes; /* device bytes held at most: path state + scene pool + films (0: 60 GiB) */
   uint32_t max_jobs;         /* admitted (unreleased) jobs at most (0: 1024) */

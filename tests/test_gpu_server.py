@@ -245,3 +245,85 @@ def test_scenes_built_while_the_loop_thread_renders(ctx, scenes):
     sv.close()
     for g in made:
         g.close()
+
+
+def _bdpt_passes_film(g, seed, pass_spp):
+    # the per-job BDPT film after the same passes (splats applied after each)
+    import gprt
+    r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=sum(pass_spp), max_passes=1,
+                                                            seed=seed), integrator=gprt.BDPTIntegrator())
+    for n in pass_spp:
+        r.add_samples(n)
+    f = r.film()
+    r.close()
+    return f
+
+
+def _close_bdpt(a, b):
+    # BDPT t = 1 splats land through float atomics, so their summation order
+    # (the last bits of splat-receiving pixels) varies from run to run even
+    # for the same job: sums agree to 1e-4 relative, sample counts exactly
+    rgb_a, lum_a, lum2_a, cnt_a = a
+    rgb_b, lum_b, lum2_b, cnt_b = b
+    assert np.array_equal(cnt_a, cnt_b)
+    for x, y in ((rgb_a, rgb_b), (lum_a, lum_b), (lum2_a, lum2_b)):
+        assert np.allclose(x, y, rtol=1e-4, atol=1e-6 * max(1.0, float(np.abs(y).max())))
+
+
+def _pass_spp(events, ticket):
+    spp = [e.samples_per_pixel for e in events if e.ticket == ticket and e.kind == "pass"]
+    return [b - a for a, b in zip([0] + spp[:-1], spp)]
+
+
+def test_bdpt_served_beside_path_tracing(ctx, scenes):
+    # BDPT requests render pass by pass on the server's copy of the scene;
+    # the BDPT film equals the per-job render given the same passes, and the
+    # path-tracing jobs sharing the server are unchanged
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    tb = sv.submit(scenes["cornell"], _cfg(8, 2, 21), integrator=gprt.BDPTIntegrator())
+    tp = sv.submit(scenes["spheres_a"], _cfg(4, 2, 22))
+    tq = sv.submit(scenes["uvmesh"], _cfg(4, 4, 23))
+    ev = sv.run_until_idle()
+    kinds = [e.kind for e in ev if e.ticket == tb]
+    assert kinds[0] == "admitted" and kinds[-1] == "done" and set(kinds[1:-1]) == {"pass"}
+    passes = _pass_spp(ev, tb)
+    assert sum(passes) == 8
+    _close_bdpt(sv.film(tb), _bdpt_passes_film(scenes["cornell"], 21, passes))
+    _same(sv.film(tp), _plain_film(scenes["spheres_a"], 22, 4))
+    _same(sv.film(tq), _plain_film(scenes["uvmesh"], 23, 4))
+    img = sv.rgba8(tb)
+    assert img.shape == (48, 48, 4) and img[..., :3].max() > 0
+    for t in (tb, tp, tq):
+        sv.release(t)
+    sv.close()
+
+
+def test_bdpt_job_outlives_its_scene_and_can_be_cancelled(ctx):
+    import gprt
+    from gprt import scenes as S
+    desc = S.cornell_baseline(32).to_desc()
+    g = gprt.GpuScene(ctx, desc)
+    ref = gprt.GpuScene(ctx, desc)
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    t = sv.submit(g, _cfg(6, 2, 31), integrator=gprt.BDPTIntegrator())
+    t2 = sv.submit(g, _cfg(400, 2, 32), integrator=gprt.BDPTIntegrator())
+    ev = []
+    for _ in range(2):
+        sv.step()
+        ev += sv.poll()
+    g.close()  # the server renders on its own copy
+    for _ in range(3):
+        sv.step()
+        ev += sv.poll()
+    sv.cancel(t2)
+    ev += sv.run_until_idle()
+    kinds = [e.kind for e in ev if e.ticket == t]
+    assert kinds[0] == "admitted" and kinds[-1] == "done"
+    assert [e.kind for e in ev if e.ticket == t2][-1] == "cancelled"
+    _close_bdpt(sv.film(t), _bdpt_passes_film(ref, 31, _pass_spp(ev, t)))
+    sv.release(t)
+    st = sv.stats()
+    assert st["active_jobs"] == 0
+    sv.close()
+    ref.close()
