@@ -327,3 +327,30 @@ def test_bdpt_job_outlives_its_scene_and_can_be_cancelled(ctx):
     assert st["active_jobs"] == 0
     sv.close()
     ref.close()
+
+
+def test_bdpt_admission_by_budget(ctx, scenes):
+    # a BDPT request holds its film, one chunk's subpath working set and a
+    # copy of its scene: refused when that never fits the budget, admitted
+    # (and its bytes held until release) when it does
+    import gprt
+    g = scenes["cornell"]
+    sv0 = gprt.RenderServer(ctx, step_paths=1 << 12)
+    t = sv0.submit(g, _cfg(4, 2, 1), integrator=gprt.BDPTIntegrator())
+    sv0.step()
+    st0 = sv0.stats()
+    assert st0["active_jobs"] == 1
+    with_bdpt = st0["bytes_in_use"]
+    sv0.cancel(t)
+    bare = sv0.stats()["bytes_in_use"]  # path state and table only
+    sv0.close()
+    assert with_bdpt > bare
+    sv = gprt.RenderServer(ctx, hbm_budget_bytes=bare + (with_bdpt - bare) // 2, step_paths=1 << 12)
+    tb = sv.submit(g, _cfg(4, 2, 1), integrator=gprt.BDPTIntegrator())
+    tp = sv.submit(scenes["spheres_b"], _cfg(2, 2, 3))
+    ev = sv.run_until_idle()
+    refused = [e for e in ev if e.ticket == tb and e.kind == "refused"]
+    assert refused and refused[0].status == gprt.capi.GPRT_E_ADMISSION
+    assert any(e.ticket == tp and e.kind == "done" for e in ev)
+    _same(sv.film(tp), _plain_film(scenes["spheres_b"], 3, 2))
+    sv.close()
