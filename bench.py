@@ -394,11 +394,17 @@ def run_plain_batch(gscenes, spps, seed=1):
 BDPT_KINDS = (2,)
 
 
+# Path capacity of a serving step at most: the offline batch may tune larger
+# steps (fewer, longer launches), but a step is what a new request waits for
+# before its first pass, so serving keeps them at 2^23 paths (about 5-10 ms).
+SERVING_STEP_PATHS = 1 << 23
+
+
 def stream_batched(ctx, server_kw, tune, reqs, arrivals, gs):
     """Serves a request stream with the batched server's loop thread."""
     import gprt
     sv = gprt.RenderServer(ctx, **server_kw)
-    sv.configure(tune["chunk_paths"], tune["block_size"], tune["flags"])
+    sv.configure(min(tune["chunk_paths"], SERVING_STEP_PATHS), tune["block_size"], tune["flags"])
     sv.start()
     t0 = time.perf_counter()
     tickets = []

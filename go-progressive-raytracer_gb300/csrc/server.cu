@@ -922,8 +922,19 @@ std::vector<Item> pack(gprt_server* sv) {
   std::vector<SrvJob*> order;
   for (auto& kv : sv->jobs)
     if (kv.second->running && !kv.second->bd) order.push_back(kv.second.get());
-  std::stable_sort(order.begin(), order.end(),
-                   [](const SrvJob* a, const SrvJob* b) { return a->last_served < b->last_served; });
+  // jobs before their first pass first, the smallest first pass first (a
+  // burst of arrivals then shows small images at once and does not wait
+  // behind the first pass of a 1024^2 job), then the least recently served
+  std::stable_sort(order.begin(), order.end(), [](const SrvJob* a, const SrvJob* b) {
+    bool fa = a->passes == 0, fb = b->passes == 0;
+    if (fa != fb) return fa;
+    if (fa) {
+      uint64_t wa = (uint64_t)(a->pass_target - a->spp_done) * a->npix;
+      uint64_t wb = (uint64_t)(b->pass_target - b->spp_done) * b->npix;
+      if (wa != wb) return wa < wb;
+    }
+    return a->last_served < b->last_served;
+  });
   std::vector<Item> items;
   uint64_t used = 0;
   for (SrvJob* j : order) {
