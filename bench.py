@@ -212,7 +212,7 @@ def l2_fraction(achieved, torch):
 SHADE_READ_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 96, 16, 52
 
 
-def shade_roofline(cnt, kc, samples, peak, peak_kind, timing_source):
+def shade_roofline(cnt, kc, kc_batches, samples, peak, peak_kind, timing_source):
     """Roofline of the multi-job shading kernel.  Paths shaded = extend rays
     (every queued path is traced, then shaded); each sample's path finishes
     exactly once, so continuing paths = shaded - samples.  Material, light
@@ -220,7 +220,9 @@ def shade_roofline(cnt, kc, samples, peak, peak_kind, timing_source):
     shaded, shadow = cnt["extend_rays"], cnt["shadow_rays"]
     alg = (SHADE_READ_B * shaded + SHADE_CONT_B * (shaded - samples) + SHADE_DONE_B * samples +
            SHADE_SHADOW_B * shadow)
-    launches = max(1, cnt["shade_launches"])
+    # per launch of the timed configuration: the counting run may split the
+    # batch into steps of another size
+    launches = max(1.0, kc["shade_launches"] / kc_batches)
     per_launch = alg / launches
     avg_ms = kc["shade_ms"] / max(1, kc["shade_launches"])
     achieved = per_launch / (avg_ms / 1e3) / 1e9 if kc["shade_launches"] else None
@@ -527,10 +529,11 @@ def bvh_stress(ctx, flat, torch):
     kc = job.counters()
     peak, _ = measured_peaks()
     alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 36 * cnt["extend_prims"]
-    per_launch = alg / max(1, cnt["extend_launches"])
+    launches_timed = max(1.0, kc["extend_launches"] / steps)  # per frame, as timed (tuned chunk size)
+    per_launch = alg / launches_timed
     avg_ms = kc["extend_ms"] / max(1, kc["extend_launches"])
     achieved = per_launch / (avg_ms / 1e3) / 1e9
-    traffic, _ = committed_traffic("extend_traffic.json", cnt["extend_rays"] / max(1, cnt["extend_launches"]))
+    traffic, _ = committed_traffic("extend_traffic.json", cnt["extend_rays"] / launches_timed)
     npix = g.width * g.height
     out = {"workload": "icosphere-L8 displaced (1,310,720 tris), ground quad, uniform sky; 1024x1024, 16 spp, depth 8",
            "msamples_per_s": npix * ICO_SPP * steps / (ms / 1e3) / 1e6, "ms_per_frame": ms / steps,
@@ -594,7 +597,6 @@ def run_gprt(args):
     run_batch(sv, gscenes, spps)
     cnt = sv.counters()
     sv.close()
-    launches_counted = cnt["extend_launches"]
 
     # the batched server, autotuned on the admitted batch (tuning steps change no film)
     sv = gprt.RenderServer(ctx, step_paths=cap)
@@ -630,6 +632,7 @@ def run_gprt(args):
     clk = clocks.stop()
     st1 = sv.stats()
     kc = sv.counters()
+    kc_batches = args.steps  # the launch counts cover the timed batches
     timed_kernels = st1["kernels"] - st0["kernels"] + args.steps  # + the flush kernels
     ms, value = aggregate_over_ranks(ms, samples_per_step, args.steps, dist, "cuda")
     if dist:
@@ -646,6 +649,7 @@ def run_gprt(args):
         run_batch(sv, gscenes, spps)
         kc = sv.counters()
         kc = {k: (v * args.steps if k.endswith("_ms") else v) for k, v in kc.items()}
+        kc_batches = 1  # launch counts of the one extra batch
         timing_source = "CUDA events around direct launches, one batch after the timed region"
     sv.close()
     del flush
@@ -656,20 +660,23 @@ def run_gprt(args):
     # + 24 B per child-box test + 16 B (center, radius) per sphere test.
     peak, peak_kind = measured_peaks()
     alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 16 * cnt["extend_prims"]
-    per_launch = alg / max(1, launches_counted)
+    # launches of the timed configuration per batch (the counting run above may
+    # use another step size; the per-batch counts do not depend on it)
+    launches_timed = max(1.0, kc["extend_launches"] / kc_batches)
+    per_launch = alg / launches_timed
     avg_ms = kc["extend_ms"] / max(1, kc["extend_launches"])
     achieved = per_launch / (avg_ms / 1e3) / 1e9 if kc["extend_launches"] else None
-    traffic, _ = committed_traffic("extend_batch_traffic.json", cnt["extend_rays"] / max(1, launches_counted))
+    traffic, _ = committed_traffic("extend_batch_traffic.json", cnt["extend_rays"] / launches_timed)
     roof = {"bound": "hbm", "kernel": "k_pt_extend (closest-hit BVH4 traversal, all jobs of a step)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "traffic": traffic,
             "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launch_timing": timing_source,
-            "rays_per_launch": cnt["extend_rays"] / max(1, launches_counted),
+            "rays_per_launch": cnt["extend_rays"] / launches_timed,
             "box_tests_per_ray": cnt["extend_boxes"] / max(1, cnt["extend_rays"]),
             "sphere_tests_per_ray": cnt["extend_prims"] / max(1, cnt["extend_rays"])}
     roof.update(l2_absorption(traffic, per_launch, avg_ms, peak))
     roof.update(l2_fraction(achieved, torch))
-    roof_shade = shade_roofline(cnt, kc, samples_per_step, peak, peak_kind, timing_source)
+    roof_shade = shade_roofline(cnt, kc, kc_batches, samples_per_step, peak, peak_kind, timing_source)
     kernel_ms = {k: kc[k + "_ms"] / args.steps for k in ("extend", "shade", "shadow", "other")}
     rooflines = {"extend": roof, "shade": roof_shade}
     if kc["shade_ms"] > kc["extend_ms"]:
