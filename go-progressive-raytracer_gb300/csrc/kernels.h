@@ -57,7 +57,8 @@ struct DevPaths {
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
   float4* sh_c;    // contribution rgb, target: slot of the next queue, or origin index | kShadowToOrigin
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
-  uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch
+  uint32_t* order; // multi-scene wavefronts: queue slots with hits first, misses last (null: queue order)
+  uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch, [6],[7] order
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
   uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY
@@ -78,10 +79,10 @@ constexpr uint32_t kShadowToOrigin = 0x80000000u;
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Device bytes of the path state of `cap` paths (one region: counters, two
-// queues, hits, origin radiance, shadow rays; sh_root when multi-scene).
+// queues, hits, origin radiance, shadow rays; sh_root and order when multi-scene).
 constexpr size_t path_region_bytes(uint32_t cap, bool multi) {
   return 256 + 2 * (5 * align256((size_t)cap * sizeof(float4)) + align256((size_t)cap * sizeof(uint4))) +
-         5 * align256((size_t)cap * sizeof(float4)) + (multi ? align256((size_t)cap * sizeof(int)) : 0);
+         5 * align256((size_t)cap * sizeof(float4)) + (multi ? 2 * align256((size_t)cap * sizeof(int)) : 0);
 }
 
 // Points the arrays of P at consecutive 256-byte-aligned ranges of `base`

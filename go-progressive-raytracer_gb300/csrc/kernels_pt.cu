@@ -152,6 +152,8 @@ __global__ void __launch_bounds__(128, 8)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     counters[cur ^ 1] = 0;  // next queue and shadow queue start empty
     counters[2] = 0;
+    counters[6] = 0;  // hit / miss counts of the slot order built after this launch
+    counters[7] = 0;
   }
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
@@ -167,6 +169,8 @@ __global__ void __launch_bounds__(256)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     counters[cur ^ 1] = 0;
     counters[2] = 0;
+    counters[6] = 0;
+    counters[7] = 0;
   }
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
@@ -372,6 +376,7 @@ void carve_paths(unsigned char* base, uint32_t cap, bool multi, DevPaths& P) {
   P.sh_d = reinterpret_cast<float4*>(take(f4));
   P.sh_c = reinterpret_cast<float4*>(take(f4));
   P.sh_root = multi ? reinterpret_cast<int*>(take(align256((size_t)cap * sizeof(int)))) : nullptr;
+  P.order = multi ? reinterpret_cast<uint32_t*>(take(align256((size_t)cap * sizeof(uint32_t)))) : nullptr;
   P.capacity = cap;
 }
 

@@ -108,6 +108,46 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
   }
 }
 
+// The slots of queue `cur` reordered: paths whose ray hit a surface first,
+// missed rays (a background lookup) last, each group in blocks of 1,024
+// slots (one atomic per block and group).  The shading kernel then runs warps
+// of hits and warps of misses instead of mixing both lane by lane; every
+// path is shaded exactly as in queue order.
+__global__ void __launch_bounds__(1024) k_hit_order(DevPaths P, int cur) {
+  __shared__ uint32_t wh[32], wm[32];
+  __shared__ uint32_t bh, bm;
+  const uint32_t n = P.counters[cur];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
+    uint32_t i = base + threadIdx.x;
+    bool live = i < n;
+    bool hit = live && __float_as_uint(P.hit[i].y) != kNoHit;
+    unsigned mh = __ballot_sync(0xffffffffu, hit), ml = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) {
+      wh[w] = __popc(mh);
+      wm[w] = __popc(ml & ~mh);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t th = 0, tm = 0;
+      for (int k = 0; k < 32; k++) {
+        uint32_t a = wh[k], b = wm[k];
+        wh[k] = th;
+        wm[k] = tm;
+        th += a;
+        tm += b;
+      }
+      bh = th ? atomicAdd(&P.counters[6], th) : 0u;
+      bm = tm ? atomicAdd(&P.counters[7], tm) : 0u;
+    }
+    __syncthreads();
+    unsigned below = (1u << lane) - 1u;
+    if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
+    else if (live) P.order[n - 1u - (bm + wm[w] + __popc(ml & ~mh & below))] = i;
+    __syncthreads();  // wh, wm, bh, bm are rewritten for the next range
+  }
+}
+
 // One bounce of every live path, each shaded with its own job's scene view
 // (materials, lights, infinite-light bounds, depth and Russian-roulette
 // settings) over the pooled geometry.
@@ -126,6 +166,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     o.cont = o.shadow = false;
     bool live = i < n;
     if (live) {
+      if (P.order) i = P.order[i];
       const DevItem& it = items[Q.ids[i].w];
       DevScene v = pool;
       v.materials = pool.materials + it.mat_off;
@@ -781,6 +822,9 @@ int grid_for(gprt_server* sv, int block) { return std::max(1, sv->ctx->sm_count 
 // Kernels of a step of depth D: raygen, D x (extend, shade, shadow), accumulate.
 int kernels_per_step(int D) { return 2 + 3 * D; }
 
+// The slot-order kernel runs before each shading launch (timed with it).
+bool has_slot_order(const gprt_server* sv) { return sv->P.order != nullptr; }
+
 // Kernel class of launch k of a step (0 extend, 1 shade, 2 shadow, 3 other).
 int kernel_class(int k, int D) { return (k == 0 || k == kernels_per_step(D) - 1) ? 3 : (k - 1) % 3; }
 
@@ -827,6 +871,9 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     launch_pt_extend(pool, P, cur, block, grid, st);
     close();
     open();
+    if (P.order)
+      k_hit_order<<<std::max(1, std::min((int)((sv->step_paths + 1023) / 1024), sv->ctx->sm_count * 2)), 1024, 0, st>>>(
+          P, cur);
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
       k_srv_shade<128, 6><<<std::max(1, grid * block / 128), 128, 0, st>>>(pool, P, items, cur, b);
     else
@@ -884,7 +931,7 @@ void drop_graphs(gprt_server* sv) {
 
 int run_step(gprt_server* sv, int D) {
   gprt_ctx* ctx = sv->ctx;
-  sv->st.kernels += (uint64_t)kernels_per_step(D);
+  sv->st.kernels += (uint64_t)kernels_per_step(D) + (has_slot_order(sv) ? (uint64_t)D : 0u);  // + slot orders
   if (sv->flags & GPRT_SERVER_NO_GRAPHS) {
     launch_step(sv, D, sv->stream, false);
     return GPRT_OK;
