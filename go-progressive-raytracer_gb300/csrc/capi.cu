@@ -152,7 +152,8 @@ void run_chunk(gprt_job* j, const ChunkDesc& ch) {
     TimedLaunch t(j, 3);
     launch_accumulate(j->film, j->paths, ch, 256, j->stream);
   }
-  j->launches += 2 + 3 * (uint64_t)sc.max_depth;
+  // raygen, accumulate; extend, (slot order,) shade, shadow per bounce
+  j->launches += 2 + (uint64_t)(sc.has_infinite ? 4 : 3) * sc.max_depth;
 }
 
 // Adds `spp` samples to each of `npix` pixels (all pixels, or the list).

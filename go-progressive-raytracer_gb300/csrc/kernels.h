@@ -57,7 +57,7 @@ struct DevPaths {
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
   float4* sh_c;    // contribution rgb, target: slot of the next queue, or origin index | kShadowToOrigin
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
-  uint32_t* order; // multi-scene wavefronts: queue slots with hits first, misses last (null: queue order)
+  uint32_t* order; // slots of the queue with hits first, misses last (null: queue order)
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch, [6],[7] order
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
@@ -79,10 +79,11 @@ constexpr uint32_t kShadowToOrigin = 0x80000000u;
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Device bytes of the path state of `cap` paths (one region: counters, two
-// queues, hits, origin radiance, shadow rays; sh_root and order when multi-scene).
+// queues, hits, origin radiance, shadow rays, slot order; sh_root when multi-scene).
 constexpr size_t path_region_bytes(uint32_t cap, bool multi) {
   return 256 + 2 * (5 * align256((size_t)cap * sizeof(float4)) + align256((size_t)cap * sizeof(uint4))) +
-         5 * align256((size_t)cap * sizeof(float4)) + (multi ? 2 * align256((size_t)cap * sizeof(int)) : 0);
+         5 * align256((size_t)cap * sizeof(float4)) + align256((size_t)cap * sizeof(uint32_t)) +
+         (multi ? align256((size_t)cap * sizeof(int)) : 0);
 }
 
 // Points the arrays of P at consecutive 256-byte-aligned ranges of `base`
@@ -107,6 +108,8 @@ void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool
 void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
                       cudaStream_t st);
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
+// Builds P.order for queue `cur` (hits first, misses last) before shading.
+void launch_hit_order(const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st);
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st);
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);

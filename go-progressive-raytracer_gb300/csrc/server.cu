@@ -108,46 +108,6 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
   }
 }
 
-// The slots of queue `cur` reordered: paths whose ray hit a surface first,
-// missed rays (a background lookup) last, each group in blocks of 1,024
-// slots (one atomic per block and group).  The shading kernel then runs warps
-// of hits and warps of misses instead of mixing both lane by lane; every
-// path is shaded exactly as in queue order.
-__global__ void __launch_bounds__(1024) k_hit_order(DevPaths P, int cur) {
-  __shared__ uint32_t wh[32], wm[32];
-  __shared__ uint32_t bh, bm;
-  const uint32_t n = P.counters[cur];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
-    uint32_t i = base + threadIdx.x;
-    bool live = i < n;
-    bool hit = live && __float_as_uint(P.hit[i].y) != kNoHit;
-    unsigned mh = __ballot_sync(0xffffffffu, hit), ml = __ballot_sync(0xffffffffu, live);
-    if (lane == 0) {
-      wh[w] = __popc(mh);
-      wm[w] = __popc(ml & ~mh);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t th = 0, tm = 0;
-      for (int k = 0; k < 32; k++) {
-        uint32_t a = wh[k], b = wm[k];
-        wh[k] = th;
-        wm[k] = tm;
-        th += a;
-        tm += b;
-      }
-      bh = th ? atomicAdd(&P.counters[6], th) : 0u;
-      bm = tm ? atomicAdd(&P.counters[7], tm) : 0u;
-    }
-    __syncthreads();
-    unsigned below = (1u << lane) - 1u;
-    if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
-    else if (live) P.order[n - 1u - (bm + wm[w] + __popc(ml & ~mh & below))] = i;
-    __syncthreads();  // wh, wm, bh, bm are rewritten for the next range
-  }
-}
-
 // One bounce of every live path, each shaded with its own job's scene view
 // (materials, lights, infinite-light bounds, depth and Russian-roulette
 // settings) over the pooled geometry.
@@ -871,9 +831,7 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     launch_pt_extend(pool, P, cur, block, grid, st);
     close();
     open();
-    if (P.order)
-      k_hit_order<<<std::max(1, std::min((int)((sv->step_paths + 1023) / 1024), sv->ctx->sm_count * 2)), 1024, 0, st>>>(
-          P, cur);
+    launch_hit_order(P, cur, sv->step_paths, sv->ctx->sm_count, st);
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
       k_srv_shade<128, 6><<<std::max(1, grid * block / 128), 128, 0, st>>>(pool, P, items, cur, b);
     else
