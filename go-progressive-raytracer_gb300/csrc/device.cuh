@@ -581,8 +581,10 @@ __device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, fl
 
 // Persistent traversal of a batch of rays: every warp loops until its work
 // is exhausted, one node visit per iteration, and lanes whose ray finished
-// take new rays once at least 8 lanes are idle, so warps stay full instead
-// of waiting for their slowest ray.  A warp draws rays from a chunk: with
+// take new rays once at least 16 lanes are idle (half the warp: fewer,
+// larger refills; on the sphere-scene batch extend + shadow ran 665 ms per
+// batch at 8, 632 at 16, 640 at 24), so warps stay full instead of waiting
+// for their slowest ray.  A warp draws rays from a chunk: with
 // `work` != null, chunks of 64 rays come from that counter (zeroed by the
 // previous kernel on the same stream); otherwise each warp owns a static
 // contiguous range of the batch.  Source provides count(),
@@ -611,7 +613,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
   for (;;) {
     bool idle = ray < 0;
     unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
-    if (more && idle_mask && (__popc(idle_mask) >= 8 || idle_mask == 0xffffffffu)) {
+    if (more && idle_mask && (__popc(idle_mask) >= 16 || idle_mask == 0xffffffffu)) {
       if (cur == end && work) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(work, kFetchChunk);
