@@ -204,8 +204,7 @@ int check_device_errors(gprt_job* j) {
   uint32_t err = j->h_words[0];
   if (err) {
     return fail(ctx, GPRT_E_BOUND,
-                std::string("device bound exceeded:") + ((err & kErrStackOverflow) ? " traversal stack" : "") +
-                    ((err & kErrQueueOverflow) ? " queue" : ""));
+                std::string("device bound exceeded:") + ((err & kErrStackOverflow) ? " traversal stack" : ""));
   }
   return GPRT_OK;
 }
@@ -246,13 +245,21 @@ int upload_rest(gprt_ctx* ctx, gprt_scene* s) {
     return GPRT_E_OOM;
   }
   cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
+  if (h.nodes.size() / 8 >= (size_t)kMaxNodes) {
+    free_all(s->buffers);
+    return fail(ctx, GPRT_E_INVALID, "the scene's BVH has more than 2^30 nodes");
+  }
   d.n_nodes = (int)(h.nodes.size() / 8);
-  d.root = d.n_nodes > 0 ? 0 : -1;
+  d.root = d.n_nodes > 0 ? (h.test_stack_cap ? kRootStackCap : 0) : -1;
   d.n_lights = (int)h.lights.size();
   d.quad_base = h.n_tris;
   d.sphere_base = h.n_tris + h.n_quads;
   d.quadric_base = h.n_tris + h.n_quads + h.n_spheres;
   d.n_prims = h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics;
+  if ((uint64_t)h.n_tris + h.n_quads + h.n_spheres + h.n_quadrics >= kOverflowHit) {
+    free_all(s->buffers);
+    return fail(ctx, GPRT_E_INVALID, "the scene has too many primitives for 32-bit primitive ids");
+  }
   d.has_infinite = h.has_infinite;
   d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
   d.world_radius = (float)h.world_radius;
@@ -334,6 +341,7 @@ int gprt_scene_create(gprt_ctx* ctx, const gprt_scene_desc* desc, gprt_scene** o
   if (!build_scene(desc, s->host, err, (desc->build_flags & GPRT_BUILD_DEVICE) != 0))
     return fail(ctx, GPRT_E_INVALID, err);
   HostScene& h = s->host;
+  h.test_stack_cap = (desc->build_flags & GPRT_BUILD_TEST_STACK_CAP) != 0;
   DevScene& d = s->dev;
   int rc = 0;
   if (h.device_bvh) {
@@ -468,7 +476,9 @@ int gprt_intersect_host(gprt_scene* s, const gprt_ray* rays, uint32_t n, uint32_
     free_all(tmp);
     return GPRT_E_OOM;
   }
-  cudaError_t e = cudaMemcpyAsync(dr, rays, (size_t)n * sizeof(gprt_ray), cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e = cudaMemsetAsync(s->d_err, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dr, rays, (size_t)n * sizeof(gprt_ray), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) {
     launch_intersect(s->dev, dr, n, flags == GPRT_ANY, dh, s->d_err, ctx->stream);
     e = cudaGetLastError();
@@ -793,18 +803,18 @@ int gprt_job_stream(gprt_job* j, void** stream) {
 // ============================================================================
 // Allocation-free rendering (gprt_render_noalloc).
 //
-// For callers that cannot allocate device memory while rendering: code that
-// records a CUDA graph (allocation is not capturable), render loops that fix
-// their device-memory budget at start-up, and hosts that share the GPU with an
-// allocator they do not control.  The wavefront path state of one call lives
-// in the file-scope device array below, sized for GPRT_NOALLOC_MAX_PATHS
-// pixel samples; every GPU that loads the library holds it until exit.
-// In host code the name `g_noalloc_scratch` is a host-side stand-in, not a
-// device address: the address is looked up once per device with
-// cudaGetSymbolAddress (with that device current) and passed to the kernels.
-// Calls share the array and keep the previous call's contents, so every
-// counter is cleared at the start of a call; calls that overlap on the GPU
-// race.
+// For callers that cannot allocate device memory while rendering: a plugin
+// inside a host application whose own allocator owns the GPU's memory, and
+// render loops whose device-memory budget is fixed at start-up.  The
+// wavefront path state of one call lives in the file-scope device array
+// below, sized for GPRT_NOALLOC_MAX_PATHS pixel samples; every GPU that loads
+// the library holds it until exit.  In host code the name
+// `g_noalloc_scratch` is a host-side stand-in, not a device address: the
+// address is looked up with cudaGetSymbolAddress (with the context's device
+// current) on the first call through a context, kept in the context, and
+// passed to the kernels.  Calls share the array and keep the previous
+// call's contents, so every counter and the error word are cleared at the
+// start of a call; calls that overlap on the GPU race.
 // ============================================================================
 namespace {
 
@@ -815,30 +825,32 @@ constexpr size_t kNoAllocBytes = path_region_bytes((uint32_t)kNoAllocPaths, fals
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (set-up on the
-// first call per device).
+// Device address of the scratch array for this context's device (set-up on
+// the first call through the context; the caller holds ctx->mu).
 int noalloc_scratch(gprt_ctx* ctx, unsigned char** out) {
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
-    return fail(ctx, GPRT_E_INVALID, "device ordinal out of range for the allocation-free entry point");
-  if (!g_noalloc_addr[ctx->device]) {
+  if (!ctx->noalloc_scratch) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_addr[ctx->device] = static_cast<unsigned char*>(p);
+    ctx->noalloc_scratch = static_cast<unsigned char*>(p);
   }
-  *out = g_noalloc_addr[ctx->device];
+  *out = ctx->noalloc_scratch;
   return GPRT_OK;
 }
 
 // Mean of the `layers` samples of every pixel: the sums of PixelStats.AddSample
-// in sample order, then GetColor (pkg/renderer/stats.go:41-55).
-__global__ void k_noalloc_mean(DevPaths P, uint32_t npix, uint32_t layers, float* out) {
+// in sample order, then GetColor (pkg/renderer/stats.go:41-55).  When a
+// device bound was exceeded the image is NaN and the error bits go to
+// `status` (when given).
+__global__ void k_noalloc_mean(DevPaths P, uint32_t npix, uint32_t layers, float* out, uint32_t* status) {
+  const uint32_t err = *(volatile uint32_t*)(P.counters + 3);
+  if (status && blockIdx.x == 0 && threadIdx.x == 0) *status = err;
+  const float nan = __int_as_float(0x7fc00000);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+    if (err) {
+      out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = nan;
+      continue;
+    }
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint32_t l = 0; l < layers; l++) {
       float4 c = P.Lout[l * npix + i];
@@ -861,7 +873,8 @@ __global__ void k_noalloc_zero(uint32_t* p, uint32_t n) {
 
 }  // namespace
 
-extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, float* rgb_out, void* stream) {
+extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, float* rgb_out, uint32_t* status_out,
+                                   void* stream) {
   if (!s || !rgb_out || spp == 0) return GPRT_E_INVALID;
   gprt_ctx* ctx = s->ctx;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
@@ -907,7 +920,7 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
     launch_pt_shadow(sc, P, cur, block, grid, st);
     cur ^= 1;
   }
-  k_noalloc_mean<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(P, (uint32_t)npix, spp, rgb_out);
+  k_noalloc_mean<<<launch_grid((uint32_t)npix, 256, 0), 256, 0, st>>>(P, (uint32_t)npix, spp, rgb_out, status_out);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "allocation-free render launch");
   return GPRT_OK;

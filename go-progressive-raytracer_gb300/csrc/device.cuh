@@ -68,25 +68,45 @@ __device__ __forceinline__ uint4 pcg4d(uint4 v) {
 }
 __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
+// 32-bit finalizer of MurmurHash3 (fmix32, Austin Appleby): every input bit
+// affects every output bit.
+__host__ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+
+// The fourth pcg4d coordinate of a 64-bit job seed.  The seed is a
+// coordinate of its own, hashed first: keying it into the pixel (pixel ^
+// seed) would give seed s the streams seed 0 gives pixel ^ s, so renders with
+// nearby seeds would reuse each other's random numbers on shuffled pixels.
+__host__ __device__ __forceinline__ uint32_t seed_word(uint64_t seed) {
+  return fmix32((uint32_t)seed ^ fmix32((uint32_t)(seed >> 32) ^ 0x9e3779b9u));
+}
+
 // The uniform numbers of one pixel sample, consumed sequentially in the
 // reference's draw order (RandomSampler, pkg/core/sampling.go:17-39): draw k
-// is word k % 4 of pcg4d(pixel ^ seed_lo, sample ^ seed_hi, k / 4, const).
-// `pos` (draws consumed) is all the state a wavefront path carries between
+// is word k % 4 of pcg4d(pixel, sample, k / 4, seed_word(seed)).  `pos`
+// (draws consumed) is all the state a wavefront path carries between
 // kernels.
 struct Rng {
-  uint32_t k0, k1, pos;
+  uint32_t k0, k1, k3, pos;
   bool valid;
   uint4 buf;
   __device__ __forceinline__ void init(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t start = 0) {
-    k0 = pixel ^ (uint32_t)seed;
-    k1 = sample ^ (uint32_t)(seed >> 32);
+    k0 = pixel;
+    k1 = sample;
+    k3 = seed_word(seed);
     pos = start;
     valid = false;
   }
   __device__ __forceinline__ float next() {
     uint32_t lane = pos & 3u;
     if (lane == 0 || !valid) {
-      buf = pcg4d(make_uint4(k0, k1, pos >> 2, 0x9e3779b9u));
+      buf = pcg4d(make_uint4(k0, k1, pos >> 2, k3));
       valid = true;
     }
     uint32_t r = lane == 0 ? buf.x : lane == 1 ? buf.y : lane == 2 ? buf.z : buf.w;
@@ -430,9 +450,13 @@ struct Trav {
   Hit hit;
 };
 
-// `root` is the BVH node the ray starts at (-1: nothing to intersect).
+// `root` is the BVH node the ray starts at (-1: nothing to intersect).  A
+// root carrying kRootStackCap starts the ray with only kTestStackCap free
+// stack entries (the stack is entered near its top, below a -1 sentinel that
+// ends the traversal when popped), so that tests can drive the stack-overflow
+// path of one job on an ordinary scene.
 __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmin, float tmax, uint32_t skip,
-                                          int root) {
+                                          int root, int* stack) {
   s.o = o;
   s.d = d;
   s.inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
@@ -444,6 +468,11 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmi
   s.skip = skip;
   s.node = root;
   s.sp = 0;
+  if (root >= 0 && (root & kRootStackCap)) {
+    s.node = root & ~kRootStackCap;
+    s.sp = kTraceStack - kTestStackCap;
+    stack[s.sp - 1] = -1;
+  }
   s.hit.prim = kNoHit;
   s.hit.t = -1.f;
   s.hit.u = s.hit.v = 0.f;
@@ -452,9 +481,12 @@ __device__ __forceinline__ void trav_init(Trav& s, float3 o, float3 d, float tmi
 // Visits node s.node: tests its children near-first, intersects the leaves
 // it hits, pushes the farther internal children and moves s.node to the
 // nearest one or to the top of the stack (-1 when the ray is finished).
-// Returns true when an any-hit query found a hit.
+// Returns true when an any-hit query found a hit.  When the farther children
+// do not fit on the stack the ray ends at once with the marker hit
+// (prim = kOverflowHit): its result is not the closest hit, and the caller
+// reports the bound against the ray's job.
 template <bool kAnyHit, bool kCount>
-__device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* stack, int* err, TraceStats* st) {
+__device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* stack, TraceStats* st) {
   const float4* N = sc.nodes + (size_t)s.node * 8;
   if (kCount) st->nodes++;
   int nint = 0;
@@ -547,10 +579,12 @@ __device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* sta
       keep++;
     }
   if (keep > 0) {
-    for (int k = keep - 1; k >= 1; k--) {
-      if (s.sp < kTraceStack) stack[s.sp++] = ich[k];
-      else atomicOr(err, kErrStackOverflow);
+    if (s.sp + keep - 1 > kTraceStack) {
+      s.node = -1;
+      s.hit.prim = kOverflowHit;
+      return false;
     }
+    for (int k = keep - 1; k >= 1; k--) stack[s.sp++] = ich[k];
     s.node = ich[0];
   } else {
     s.node = s.sp > 0 ? stack[--s.sp] : -1;
@@ -558,15 +592,21 @@ __device__ __forceinline__ bool trav_visit(const DevScene& sc, Trav& s, int* sta
   return false;
 }
 
-// Whole traversal of one ray from BVH node `root`.
+// Whole traversal of one ray from BVH node `root`.  A stack overflow returns
+// no hit and, when `err` is given, sets kErrStackOverflow there.
 template <bool kAnyHit, bool kCount>
 __device__ __forceinline__ bool trace_from(const DevScene& sc, int root, float3 o, float3 d, float tmin, float tmax,
                                            uint32_t skip, Hit& hit, int* err, TraceStats* st = nullptr) {
   Trav s;
-  trav_init(s, o, d, tmin, tmax, skip, root);
   int stack[kTraceStack];
+  trav_init(s, o, d, tmin, tmax, skip, root, stack);
   while (s.node >= 0) {
-    if (trav_visit<kAnyHit, kCount>(sc, s, stack, err, st)) break;
+    if (trav_visit<kAnyHit, kCount>(sc, s, stack, st)) break;
+  }
+  if (s.hit.prim == kOverflowHit) {
+    if (err) atomicOr(err, kErrStackOverflow);
+    s.hit.prim = kNoHit;
+    s.hit.t = -1.f;
   }
   hit = s.hit;
   return s.hit.prim != kNoHit;
@@ -588,12 +628,13 @@ __device__ __forceinline__ bool trace(const DevScene& sc, float3 o, float3 d, fl
 // `work` != null, chunks of 64 rays come from that counter (zeroed by the
 // previous kernel on the same stream); otherwise each warp owns a static
 // contiguous range of the batch.  Source provides count(),
-// load(i, o, d, tmin, tmax, skip, root) and store(i, hit).
+// load(i, o, d, tmin, tmax, skip, root) and store(i, hit); store() sees the
+// marker hit of a ray that overflowed its stack and reports it.
 constexpr uint32_t kFetchChunk = 64;
 
 template <bool kAnyHit, bool kCount, class Source>
-__device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src, uint32_t* work, int* err,
-                                                 TraceStats* st, uint32_t* traced) {
+__device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src, uint32_t* work, TraceStats* st,
+                                                 uint32_t* traced) {
   const uint32_t n = src.count();
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -633,7 +674,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
           int root;
           uint32_t mine = cur + rank;
           src.load(mine, o, d, tmin, tmax, skip, root);
-          trav_init(s, o, d, tmin, tmax, skip, root);
+          trav_init(s, o, d, tmin, tmax, skip, root, stack);
           ray = (int)mine;
           if (kCount) (*traced)++;
         }
@@ -642,7 +683,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
     }
     if (__ballot_sync(0xffffffffu, ray >= 0) == 0 && !more) break;
     if (ray >= 0) {
-      if (s.node >= 0) trav_visit<kAnyHit, kCount>(sc, s, stack, err, st);
+      if (s.node >= 0) trav_visit<kAnyHit, kCount>(sc, s, stack, st);
       if (s.node < 0) {
         src.store((uint32_t)ray, s.hit);
         ray = -1;
@@ -650,6 +691,32 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
     }
   }
 }
+
+// Largest k < n with start[k] <= x (start[0] = 0, start ascending).
+__device__ __forceinline__ uint32_t find_range(const uint32_t* start, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(start + mid) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Where a wavefront reports a device bound of one path: the job's error
+// word, or, in a multi-job wavefront, the error word of the work item whose
+// path range [start[k], start[k+1]) holds the path's origin index, so that
+// only that job fails.
+struct ErrSink {
+  uint32_t* word;           // single job: its error word
+  uint32_t* items;          // multi-job: one error word per item (else null)
+  const uint32_t* start;    // multi-job: first origin index of each item
+  const uint32_t* n_items;  // multi-job: items of the step
+  __device__ void report(uint32_t origin, uint32_t bits) const {
+    if (items) atomicOr(items + find_range(start, *n_items, origin), bits);
+    else atomicOr(word, bits);
+  }
+};
 
 // ----------------------------------------------------------------- surface data
 // Resolves a hit into the SurfaceInteraction of the reference: point,

@@ -30,6 +30,9 @@ struct gprt_ctx {
   std::string err;
   std::set<gprt_scene*> scenes;
   std::set<gprt_server*> servers;
+  // device address of the allocation-free entry point's static array,
+  // looked up on its first call through this context
+  unsigned char* noalloc_scratch = nullptr;
 };
 
 struct gprt_scene {

@@ -59,6 +59,11 @@ struct DevPaths {
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
   uint32_t* order; // slots of the queue with hits first, misses last (null: queue order)
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch, [6],[7] order
+  // multi-job wavefronts: one error word per work item and the items' first
+  // origin indices (null for a single job: its error word is counters[3])
+  uint32_t* item_err;
+  const uint32_t* item_start;
+  const uint32_t* n_items;
   unsigned long long* stats;  // traversal counters (extend rays/nodes/boxes/prims, shadow ...) or null
   uint32_t capacity;
   uint32_t variant;  // GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY

@@ -33,6 +33,7 @@ struct BatchSource {
   uint32_t n;
   __device__ uint32_t count() const { return n; }
   int root;
+  int* err;
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
     rt = root;
     const float4* r = reinterpret_cast<const float4*>(rays + i);
@@ -44,16 +45,19 @@ struct BatchSource {
     skip = kNoHit;
   }
   __device__ void store(uint32_t i, const Hit& h) const {
-    bool any = h.prim != kNoHit;
+    bool over = h.prim == kOverflowHit;
+    if (over) atomicOr(err, kErrStackOverflow);
+    bool any = h.prim != kNoHit && !over;
     reinterpret_cast<float4*>(hits)[i] =
-        make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), any ? h.u : 0.f, any ? h.v : 0.f);
+        make_float4(any ? h.t : -1.f, __uint_as_float(any || over ? h.prim : kNoHit), any ? h.u : 0.f,
+                    any ? h.v : 0.f);
   }
 };
 
 // Batches use static per-warp ranges: calls on different streams share no counter.
 template <bool kAny>
-__global__ void __launch_bounds__(128, 8) k_intersect(DevScene sc, BatchSource src, int* err) {
-  trace_persistent<kAny, false>(sc, src, nullptr, err, nullptr, nullptr);
+__global__ void __launch_bounds__(128, 8) k_intersect(DevScene sc, BatchSource src) {
+  trace_persistent<kAny, false>(sc, src, nullptr, nullptr, nullptr);
 }
 
 int persistent_grid(int sm_count, int block) { return std::max(1, sm_count * (1024 / block)); }
@@ -65,9 +69,9 @@ void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = launch_grid((n + 31) / 32 * 32, 128, persistent_grid(sms, 128));
-  BatchSource src{rays, hits, n, sc.root};
-  if (any_hit) k_intersect<true><<<grid, 128, 0, st>>>(sc, src, err);
-  else k_intersect<false><<<grid, 128, 0, st>>>(sc, src, err);
+  BatchSource src{rays, hits, n, sc.root, err};
+  if (any_hit) k_intersect<true><<<grid, 128, 0, st>>>(sc, src);
+  else k_intersect<false><<<grid, 128, 0, st>>>(sc, src);
 }
 
 // ----------------------------------------------------------------- raygen
@@ -130,6 +134,8 @@ struct ExtendSource {
   const float4* ray_d;
   float4* hit;
   const uint32_t* n;
+  const float4* weight;  // origin index of each path (.w), read when reporting a bound
+  ErrSink err;
   __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
     float4 a = ray_o[i], b = ray_d[i];
@@ -140,11 +146,20 @@ struct ExtendSource {
     tmax = kInfF;
     skip = __float_as_uint(a.w);
   }
+  // the marker hit of a stack overflow is stored as a miss and fails the
+  // path's job
   __device__ void store(uint32_t i, const Hit& h) const {
     bool any = h.prim != kNoHit;
-    hit[i] = make_float4(any ? h.t : -1.f, __uint_as_float(h.prim), h.u, h.v);
+    if (h.prim == kOverflowHit) {
+      err.report(__float_as_uint(weight[i].w), kErrStackOverflow);
+      any = false;
+    }
+    hit[i] = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), h.u, h.v);
   }
 };
+
+// The error sink of a wavefront's paths (per job, or per item of a multi-job step).
+static ErrSink err_sink(const DevPaths& P) { return ErrSink{P.counters + 3, P.item_err, P.item_start, P.n_items}; }
 
 template <bool kCount>
 __global__ void __launch_bounds__(128, 8)
@@ -157,7 +172,7 @@ __global__ void __launch_bounds__(128, 8)
   }
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
-  trace_persistent<false, kCount>(sc, src, counters + 4, reinterpret_cast<int*>(counters + 3), &ts, &rays);
+  trace_persistent<false, kCount>(sc, src, counters + 4, &ts, &rays);
   if (kCount) add_counts(stats, rays, ts);
 }
 
@@ -183,7 +198,7 @@ __global__ void __launch_bounds__(256)
       int root;
       src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace_from<false, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(counters + 3), &ts);
+      trace_from<false, kCount>(sc, root, o, d, tmin, tmax, skip, h, nullptr, &ts);
       src.store(i, h);
       rays++;
     }
@@ -199,7 +214,7 @@ static int sm_count_current() {
 }
 
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
-  ExtendSource src{P.q[cur].ray_o, P.q[cur].ray_d, P.hit, P.counters + cur};
+  ExtendSource src{P.q[cur].ray_o, P.q[cur].ray_d, P.hit, P.counters + cur, P.q[cur].weight, err_sink(P)};
   if (P.variant & GPRT_JOB_SIMPLE_EXTEND) {
     int b = std::min(block, 256);
     if (P.stats) k_pt_extend_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, cur, P.stats);
@@ -307,6 +322,8 @@ struct ShadowSource {
   float4* Lout;        // radiance of finished paths, by origin index
   const uint32_t* n;
   int root;
+  const float4* Wnext;  // weights of the next queue (origin index in .w), read when reporting a bound
+  ErrSink err;
   __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
     rt = sh_root ? sh_root[i] : root;
@@ -318,6 +335,11 @@ struct ShadowSource {
     skip = __float_as_uint(b.w);
   }
   __device__ void store(uint32_t i, const Hit& h) const {
+    if (h.prim == kOverflowHit) {  // the visibility is unknown: fail the path's job
+      uint32_t t = __float_as_uint(sh_c[i].w);
+      err.report((t & kShadowToOrigin) ? (t & ~kShadowToOrigin) : __float_as_uint(Wnext[t].w), kErrStackOverflow);
+      return;
+    }
     if (h.prim != kNoHit) return;  // occluded
     float4 c = sh_c[i];
     uint32_t t = __float_as_uint(c.w);
@@ -332,7 +354,7 @@ __global__ void __launch_bounds__(128, 8)
     k_pt_shadow(DevScene sc, ShadowSource src, uint32_t* counters, unsigned long long* stats) {
   TraceStats ts{0, 0, 0};
   uint32_t rays = 0;
-  trace_persistent<true, kCount>(sc, src, counters + 5, reinterpret_cast<int*>(counters + 3), &ts, &rays);
+  trace_persistent<true, kCount>(sc, src, counters + 5, &ts, &rays);
   if (kCount) add_counts(stats + 4, rays, ts);
 }
 
@@ -352,7 +374,7 @@ __global__ void __launch_bounds__(256)
       int root;
       src.load(i, o, d, tmin, tmax, skip, root);
       Hit h;
-      trace_from<true, kCount>(sc, root, o, d, tmin, tmax, skip, h, reinterpret_cast<int*>(counters + 3), &ts);
+      trace_from<true, kCount>(sc, root, o, d, tmin, tmax, skip, h, nullptr, &ts);
       src.store(i, h);
       rays++;
     }
@@ -361,7 +383,8 @@ __global__ void __launch_bounds__(256)
 }
 
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
-  ShadowSource src{P.sh_o, P.sh_d, P.sh_c, P.sh_root, P.q[cur ^ 1].L, P.Lout, P.counters + 2, sc.root};
+  ShadowSource src{P.sh_o,    P.sh_d,          P.sh_c,      P.sh_root, P.q[cur ^ 1].L, P.Lout, P.counters + 2,
+                   sc.root, P.q[cur ^ 1].weight, err_sink(P)};
   if (P.variant & GPRT_JOB_SIMPLE_SHADOW) {
     int b = std::min(block, 256);
     if (P.stats) k_pt_shadow_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, P.stats);

@@ -40,10 +40,20 @@ constexpr int kLeafTypeShift = 8;
 constexpr int kPrimTriangle = 0, kPrimQuad = 1, kPrimSphere = 2, kPrimQuadric = 3;
 constexpr int kQuadricDisc = 0, kQuadricCylinder = 1, kQuadricCone = 2;
 constexpr int kTraceStack = 64;
+// A BVH root with this bit set (test-only, GPRT_JOB_TEST_STACK_CAP) gives the
+// rays of its job kTestStackCap traversal stack entries instead of
+// kTraceStack.  Node indices stay below 2^30 (128 GB of nodes).
+constexpr int kRootStackCap = 1 << 30;
+constexpr int kTestStackCap = 1;
+constexpr int kMaxNodes = 1 << 30;
+// Primitive id of the marker hit a ray returns when its traversal stack
+// overflowed (never a primitive: quadric ids stay below it).
+constexpr uint32_t kOverflowHit = 0xFFFFFFFEu;
 
-// device error bits (status word read by the host after each pass)
+// device error bits (status word read by the host after each pass).  The
+// path queues cannot overflow: a shading step appends at most one path and
+// one shadow ray per slot of a queue of the same capacity.
 constexpr int kErrStackOverflow = 1;
-constexpr int kErrQueueOverflow = 2;
 
 // kMatSpotEmissive: the disc spot light's directional emitter; albedo holds
 // the unit spot direction

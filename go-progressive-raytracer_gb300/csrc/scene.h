@@ -40,6 +40,7 @@ struct HostScene {
   int bvh_depth = 0;
   double build_ms = 0, flatten_ms = 0, bvh_ms = 0, check_ms = 0;
   bool device_bvh = false;  // the BVH and primitive arrays are built on the GPU from `pending`
+  bool test_stack_cap = false;  // GPRT_BUILD_TEST_STACK_CAP: rays get kTestStackCap stack entries
   BuildPrims pending;
 };
 

@@ -64,21 +64,12 @@ struct DevItem {
   DevCamera cam;
 };
 
-// Largest k < n with start[k] <= x (start[0] = 0, start ascending).
-__device__ __forceinline__ uint32_t find_range(const uint32_t* start, uint32_t n, uint32_t x) {
-  uint32_t lo = 0, hi = n;
-  while (hi - lo > 1) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(start + mid) <= x) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
 // Camera rays of every item: path p is sample `layer` of pixel i of its item,
 // drawn exactly as k_pt_raygen draws them for a single job.
 __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* path0, const DevItem* items) {
   uint32_t n = hdr->total_paths, ni = hdr->n_items;
+  // the items' error words start clear (read back after the step)
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ni; k += gridDim.x * blockDim.x) P.item_err[k] = 0;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     uint32_t k = find_range(path0, ni, p);
     const DevItem& it = items[k];
@@ -332,10 +323,11 @@ struct gprt_server {
   uint32_t flags = 0;
   // item table: [hdr | path0[max+1] | pix0[max+1]] then items[max]
   unsigned char* d_table = nullptr;
-  unsigned char* h_table = nullptr;  // pinned (table_bytes, then the step's error word)
+  // then one error word per item at err_off (cleared by the step's raygen)
+  unsigned char* h_table = nullptr;  // pinned staging of the table; its error words receive the read-back
   uint32_t* h_err = nullptr;         // pinned: a pageable read-back would block inside the runtime
                                      // until the step ends, stalling other threads' CUDA calls
-  size_t table_bytes = 0, prefix_bytes = 0;
+  size_t table_bytes = 0, prefix_bytes = 0, err_off = 0;
   std::map<int, cudaGraphExec_t> graphs;  // by depth
   uint64_t graph_gen = ~0ull;
   // instrumentation (GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL in flags):
@@ -537,6 +529,9 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
   size_t cnt[kPoolArrays], off[kPoolArrays];
   scene_counts(s, cnt);
   if (!place(sv, cnt, off)) return nullptr;
+  // node ids stay below the root flag bits, quadric ids below kOverflowHit
+  if (off[kNodes] + cnt[kNodes] >= (size_t)kMaxNodes) return nullptr;
+  if (kPoolQuadricBase + off[kQuadrics] + cnt[kQuadrics] >= (size_t)kOverflowHit) return nullptr;
   auto ps = std::make_unique<PoolScene>();
   ps->serial = s->serial;
   for (int k = 0; k < kPoolArrays; k++) {
@@ -575,7 +570,7 @@ PoolScene* make_resident(gprt_server* sv, gprt_scene* s) {
     k_rebase_lights<<<1, 128, 0, st>>>(L, (uint32_t)cnt[kLights], (int)off[kQuads], (int)off[kSpheres],
                                        (int)off[kQuadrics]);
   }
-  ps->root = cnt[kNodes] ? (int)off[kNodes] : -1;
+  ps->root = cnt[kNodes] ? ((int)off[kNodes] | (s->host.test_stack_cap ? kRootStackCap : 0)) : -1;
   ps->has_infinite = d.has_infinite;
   ps->has_tri_uvs = d.tri_uvs ? 1 : 0;
   ps->max_depth = d.max_depth;
@@ -808,6 +803,11 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
   P.stats = (sv->flags & GPRT_JOB_COUNT_TRAVERSAL) ? sv->d_stats : nullptr;
   const StepHdr* hdr = reinterpret_cast<const StepHdr*>(sv->d_table);
   const uint32_t* path0 = reinterpret_cast<const uint32_t*>(sv->d_table + 16);
+  // device bounds are reported per item: a path's origin index is its index
+  // in the step, so path0 maps it to its item
+  P.item_err = reinterpret_cast<uint32_t*>(sv->d_table + sv->err_off);
+  P.item_start = path0;
+  P.n_items = reinterpret_cast<const uint32_t*>(sv->d_table);  // StepHdr::n_items
   const uint32_t* pix0 = path0 + (sv->desc.max_jobs + 1);
   const DevItem* items = reinterpret_cast<const DevItem*>(sv->d_table + sv->prefix_bytes);
   int block = (int)sv->block;
@@ -1029,10 +1029,10 @@ int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
   int rc = run_step(sv, D);
   if (rc) return rc;
   CK(ctx, cudaEventRecord(sv->ev1, sv->stream));
-  CK(ctx, cudaMemcpyAsync(sv->h_err, sv->P.counters + 3, 4, cudaMemcpyDeviceToHost, sv->stream));
+  CK(ctx, cudaMemcpyAsync(sv->h_err, sv->d_table + sv->err_off, items.size() * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, sv->stream));
   overlap();
   CK(ctx, cudaStreamSynchronize(sv->stream));
-  uint32_t err = *sv->h_err;
   float ms = 0;
   cudaEventElapsedTime(&ms, sv->ev0, sv->ev1);
   if (ms_out) *ms_out = ms;
@@ -1042,16 +1042,20 @@ int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
   sv->st.busy_ms += ms;
   sv->st.last_step_ms = ms;
   sv->st.paths += paths;
-  if (err) {
-    cudaMemsetAsync(sv->P.counters + 3, 0, 4, sv->stream);
-    for (const Item& it : items) {
-      emit(sv, it.j->ticket, GPRT_EV_FAILED, it.j->passes, it.j->spp_done, GPRT_E_BOUND, it.j->submit_ms);
-      release_job(sv, it.j);
-    }
-    return fail(ctx, GPRT_E_BOUND, "device bound exceeded in a batched step");
+  // a device bound fails only the jobs whose paths exceeded it (the
+  // reference scopes errors to the render they occur in); the others keep
+  // this step's samples
+  for (size_t k = 0; k < items.size(); k++) {
+    SrvJob* j = items[k].j;
+    if (!sv->h_err[k]) continue;
+    fail(ctx, GPRT_E_BOUND, "device bound exceeded (traversal stack) in job " + std::to_string(j->ticket));
+    emit(sv, j->ticket, GPRT_EV_FAILED, j->passes, j->spp_done, GPRT_E_BOUND, j->submit_ms);
+    release_job(sv, j);
+    items[k].j = nullptr;
   }
   for (const Item& it : items) {
     SrvJob* j = it.j;
+    if (!j) continue;
     j->spp_done += it.layers;
     j->last_served = sv->st.steps;
     sv->st.samples += (uint64_t)it.layers * j->npix;
@@ -1290,7 +1294,8 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   P.stats = nullptr;
   sv->path_bytes = bytes;
   sv->prefix_bytes = (16 + 2 * (size_t)(d.max_jobs + 1) * 4 + 255) & ~(size_t)255;
-  sv->table_bytes = sv->prefix_bytes + (size_t)d.max_jobs * sizeof(DevItem);
+  sv->err_off = (sv->prefix_bytes + (size_t)d.max_jobs * sizeof(DevItem) + 255) & ~(size_t)255;
+  sv->table_bytes = sv->err_off + (size_t)d.max_jobs * sizeof(uint32_t);
   if (sv->path_bytes + sv->table_bytes > d.hbm_budget_bytes) {
     free_all(b);
     return fail(ctx, GPRT_E_ADMISSION, "the budget does not cover the path state of one step");
@@ -1301,7 +1306,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
     free_all(b);
     return fail(ctx, GPRT_E_OOM, "item table allocation failed");
   }
-  sv->h_err = reinterpret_cast<uint32_t*>(sv->h_table + sv->table_bytes);
+  sv->h_err = reinterpret_cast<uint32_t*>(sv->h_table + sv->err_off);
   if (cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_all(b);
     cudaFreeHost(sv->h_table);

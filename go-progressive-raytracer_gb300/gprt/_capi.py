@@ -27,7 +27,9 @@ NO_SHAPE = 0xFFFFFFFF
 INTEGRATOR_PATH_TRACING, INTEGRATOR_BDPT = 0, 1
 CLOSEST, ANY = 0, 1
 NO_HIT = 0xFFFFFFFF
+BOUND_HIT = 0xFFFFFFFE  # GPRT_BOUND_HIT: the ray's traversal stack overflowed
 BUILD_DEVICE = 1
+BUILD_TEST_STACK_CAP = 2  # tests only: 1-entry traversal stack, so the scene's rays overflow it
 NOALLOC_MAX_PATHS = 131072  # GPRT_NOALLOC_MAX_PATHS
 
 
@@ -197,7 +199,7 @@ SIGNATURES = {
     "gprt_job_get_counters": (C.c_int, [P, C.POINTER(JobCounters)]),
     "gprt_job_reset_counters": (C.c_int, [P]),
     "gprt_job_stream": (C.c_int, [P, PP]),
-    "gprt_render_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint64, P, P]),
+    "gprt_render_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint64, P, P, P]),
     "gprt_autotune": (C.c_int, [P, C.POINTER(JobDesc), C.c_uint32, C.POINTER(TuneResult)]),
     "gprt_server_create": (C.c_int, [P, C.POINTER(ServerDesc), PP]),
     "gprt_server_destroy": (C.c_int, [P]),

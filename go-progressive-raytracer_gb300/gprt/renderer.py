@@ -44,12 +44,15 @@ class Context:
 class GpuScene:
     """scene.Scene after Preprocess, resident on the device."""
 
-    def __init__(self, ctx: Context, scene, device_bvh: bool = False):
+    def __init__(self, ctx: Context, scene, device_bvh: bool = False, test_stack_cap: bool = False):
         """device_bvh: build the BVH on the GPU (GPRT_BUILD_DEVICE) instead of
-        the host SAH builder."""
+        the host SAH builder.  test_stack_cap (tests only): a 1-entry
+        traversal stack, so that rays overflow it and the scene's renders
+        fail with GPRT_E_BOUND."""
         self.ctx = ctx
         self.flat = scene.to_desc() if hasattr(scene, "to_desc") else scene
-        self.flat.desc.build_flags = capi.BUILD_DEVICE if device_bvh else 0
+        self.flat.desc.build_flags = ((capi.BUILD_DEVICE if device_bvh else 0) |
+                                      (capi.BUILD_TEST_STACK_CAP if test_stack_cap else 0))
         h = C.c_void_p()
         ctx.check(ctx.lib.gprt_scene_create(ctx.h, self.flat.ptr(), C.byref(h)))
         self.h = h

@@ -203,6 +203,11 @@ typedef struct gprt_scene_desc {
  * that arrive while a server is running); its tree traverses somewhat
  * slower.  Scenes of fewer than 8 primitives always build on the host. */
 #define GPRT_BUILD_DEVICE 1u
+/* Tests only: every ray of this scene gets a 1-entry traversal stack instead
+ * of 64, so that rays overflow it and the scene's jobs fail with GPRT_E_BOUND
+ * (the device-bound path: the kernels set the error bits and carry on, and
+ * only the jobs whose rays overflowed fail). */
+#define GPRT_BUILD_TEST_STACK_CAP 2u
 
 typedef struct gprt_ray {
   float ox, oy, oz, tmin;
@@ -210,7 +215,9 @@ typedef struct gprt_ray {
 } gprt_ray;
 
 /* Hit record: t, primitive id (GPRT_NO_HIT when missed), barycentric /
- * parametric (u, v) as in SurfaceInteraction.UV for triangles and quads. */
+ * parametric (u, v) as in SurfaceInteraction.UV for triangles and quads.
+ * A ray whose traversal stack overflowed (a device bound: the closest hit is
+ * unknown) gets prim = GPRT_BOUND_HIT and t = -1. */
 typedef struct gprt_hit {
   float t;
   uint32_t prim;
@@ -218,6 +225,7 @@ typedef struct gprt_hit {
 } gprt_hit;
 
 #define GPRT_NO_HIT 0xFFFFFFFFu
+#define GPRT_BOUND_HIT 0xFFFFFFFEu
 #define GPRT_CLOSEST 0u /* closest hit (BVH.Hit with the hit record used) */
 #define GPRT_ANY 1u     /* any hit in (tmin, tmax): the shadow-ray use of BVH.Hit */
 
@@ -335,7 +343,9 @@ int gprt_scene_validate(const gprt_scene_desc* desc, gprt_scene_info* info, char
  * (NULL = the context stream).  Asynchronous. */
 int gprt_intersect(gprt_scene* scene, const gprt_ray* rays, uint32_t n, uint32_t flags,
                    gprt_hit* hits, void* stream);
-/* Same with HOST pointers; copies in, traces and copies out, synchronously. */
+/* Same with HOST pointers; copies in, traces and copies out, synchronously.
+ * Returns GPRT_E_BOUND when a ray's traversal stack overflowed (its hit
+ * record holds GPRT_BOUND_HIT). */
 int gprt_intersect_host(gprt_scene* scene, const gprt_ray* rays, uint32_t n, uint32_t flags,
                         gprt_hit* hits);
 /* Algorithmic work of a host ray batch on this scene's BVH, counted by a CPU
@@ -399,25 +409,37 @@ typedef struct gprt_tune_result {
 int gprt_autotune(gprt_scene* scene, const gprt_job_desc* base, uint32_t spp, gprt_tune_result* out);
 
 /* ---- allocation-free rendering ---------------------------------------------
- * No counterpart in the reference: an entry point for callers that cannot
- * allocate device memory at render time -- code recording a CUDA graph
- * (stream capture), render loops whose device-memory budget is fixed at
- * start-up, and hosts that share the GPU with an allocator they do not own.
- * It path-traces `spp` samples per pixel of `scene` (samples 0..spp-1 of the
- * counter-based sampler keyed by `seed`, the same samples a fresh job with
- * that seed takes) and writes the per-pixel mean radiance, 3 floats per pixel
+ * No counterpart in the reference.  Some callers cannot allocate device
+ * memory when they render: a plugin inside a host application that owns the
+ * GPU's memory through its own allocator (a cudaMalloc behind that
+ * allocator's back can fail or fragment what it manages), and render loops
+ * whose device-memory budget is fixed when they start, which must not grow
+ * or fail later.  This entry point allocates nothing.  It path-traces `spp`
+ * samples per pixel of `scene` (samples 0..spp-1 of the counter-based
+ * sampler keyed by `seed`, the same samples a fresh job with that seed
+ * takes) and writes the per-pixel mean radiance, 3 floats per pixel
  * (PixelStats.GetColor), into the caller's DEVICE buffer `rgb_out`.  The
  * path state lives in one statically sized device array inside the library
  * (GPRT_NOALLOC_MAX_PATHS paths, about 34 MB, held by every GPU that loads
  * the library until the process exits); requests with
  * width * height * spp > GPRT_NOALLOC_MAX_PATHS return GPRT_E_INVALID.  It
- * calls no cudaMalloc or cudaFree.  The first call on a device looks up the
- * array's device address, so make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller.  Asynchronous on
- * `stream` (NULL = the context stream). */
+ * calls no cudaMalloc or cudaFree.  The first call through a context looks
+ * up the array's device address (cudaGetSymbolAddress, with the context's
+ * device current) and keeps it in the context, so make that first call
+ * before any stream capture; a device reset invalidates the address together
+ * with the context, so contexts made before a reset must not be used after
+ * it.  All calls share the array and a call starts by clearing the counters
+ * it keeps there: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Asynchronous on
+ * `stream` (NULL = the context stream).
+ * Device bounds: when a path overflowed its traversal stack the image is not
+ * valid.  The call then fills `rgb_out` with NaN and, when `status_out` (a
+ * DEVICE pointer to one uint32, may be NULL) is given, writes the device
+ * error bits there (0: the image is valid; bit 0: traversal stack).  Read it
+ * after synchronising `stream`; the return code only covers the launches. */
 #define GPRT_NOALLOC_MAX_PATHS 131072u
-int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* rgb_out, void* stream);
+int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* rgb_out, uint32_t* status_out,
+                        void* stream);
 
 /* ---- serving ---------------------------------------------------------------
  * The reference serves concurrent progressive renders from its web server:

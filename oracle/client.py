@@ -34,6 +34,7 @@ def load():
                                                 C.c_int]
         _lib.oracle_renderer_destroy.argtypes = [P]
         _lib.oracle_render_pass.argtypes = [P, C.c_int, C.c_int, P, P]
+        _lib.oracle_render_tiles.argtypes = [P, C.c_int, P, C.c_int, P, P]
         _lib.oracle_renderer_read.argtypes = [P, P, P, P, P, P]
         _lib.oracle_renderer_rgba8.argtypes = [P, P]
         _lib.oracle_samples_for_pass.argtypes = [P, C.c_int]
@@ -103,6 +104,16 @@ class OracleRenderer:
         secs = C.c_double()
         st = (C.c_longlong * 4)()
         rc = load().oracle_render_pass(self.h, p, only_tiles, C.addressof(secs), C.addressof(st))
+        if rc != 0:
+            raise RuntimeError(load().oracle_last_error().decode())
+        return secs.value, tuple(st)
+
+    def render_tiles(self, p, tile_ids):
+        """RenderPass `p` over the listed tile ids only (row-major 64x64 grid)."""
+        ids = np.ascontiguousarray(tile_ids, dtype=np.int32)
+        secs = C.c_double()
+        st = (C.c_longlong * 4)()
+        rc = load().oracle_render_tiles(self.h, p, ids.ctypes.data, len(ids), C.addressof(secs), C.addressof(st))
         if rc != 0:
             raise RuntimeError(load().oracle_last_error().decode())
         return secs.value, tuple(st)

@@ -316,15 +316,26 @@ struct Renderer {
   // RenderPass (progressive.go:126-223) with processSplats (:371-391) and
   // assembleCurrentImage statistics (:395-431)
   RenderStatsR renderPass(int pass, int onlyTiles = -1) {
-    int target = samplesForPass(pass);
     int nt = onlyTiles >= 0 ? std::min(onlyTiles, (int)tiles.size()) : (int)tiles.size();
+    std::vector<int> ids(nt);
+    for (int k = 0; k < nt; k++) ids[k] = k;
+    return renderTiles(pass, ids);
+  }
+  // The same pass over the listed tiles only (fixed windows of a frame:
+  // path tracing has no cross-tile terms, so a window's pixels equal the
+  // whole frame's; BDPT splats from the other tiles are left out).
+  RenderStatsR renderTiles(int pass, const std::vector<int>& ids) {
+    int target = samplesForPass(pass);
+    int nt = (int)ids.size();
+    for (int k : ids)
+      if (k < 0 || k >= (int)tiles.size()) throw std::runtime_error("tile id out of range");
     std::vector<std::vector<std::pair<int, Vec3>>> tileSplats(nt);
     std::atomic<int> next{0};
     auto worker = [&]() {
       for (;;) {
         int k = next.fetch_add(1);
         if (k >= nt) break;
-        renderTile(tiles[k], target, tileSplats[k]);
+        renderTile(tiles[ids[k]], target, tileSplats[k]);
       }
     };
     int th = std::max(1, threads);
@@ -453,6 +464,28 @@ int oracle_render_pass(void* rp, int pass, int only_tiles, double* seconds, long
   try {
     auto t0 = std::chrono::steady_clock::now();
     RenderStatsR st = r->renderPass(pass, only_tiles);
+    auto t1 = std::chrono::steady_clock::now();
+    if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+    if (stats_out) {
+      stats_out[0] = st.totalPixels;
+      stats_out[1] = st.totalSamples;
+      stats_out[2] = st.minSamples;
+      stats_out[3] = st.maxSamplesUsed;
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    setErr(e.what());
+    return -1;
+  }
+}
+
+// RenderPass over the `n` listed tile ids only (row-major 64x64 tile grid of
+// NewTileGrid, progressive.go:455-479).
+int oracle_render_tiles(void* rp, int pass, const int32_t* ids, int n, double* seconds, long long* stats_out) {
+  Renderer* r = static_cast<Renderer*>(rp);
+  try {
+    auto t0 = std::chrono::steady_clock::now();
+    RenderStatsR st = r->renderTiles(pass, std::vector<int>(ids, ids + n));
     auto t1 = std::chrono::steady_clock::now();
     if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
     if (stats_out) {

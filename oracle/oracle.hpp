@@ -159,15 +159,24 @@ struct PcgSampler : Sampler {
 };
 
 // The GPU library's counter-based stream for one pixel sample: draw k is
-// word k % 4 of pcg4d(pixel ^ seed_lo, sample ^ seed_hi, k / 4, 0x9e3779b9)
-// (Jarzynski & Olano, "Hash Functions for GPU Rendering", JCGT 9(3), 2020),
+// word k % 4 of pcg4d(pixel, sample, k / 4, seed word) (Jarzynski & Olano,
+// "Hash Functions for GPU Rendering", JCGT 9(3), 2020), the seed word being
+// fmix32(seed_lo ^ fmix32(seed_hi ^ 0x9e3779b9)) (MurmurHash3's finalizer),
 // mapped to [0,1) as (word >> 8) * 2^-24.  Consumed in the reference's order,
 // it gives the oracle the same inputs as the GPU for per-sample comparisons.
 struct CounterSampler : Sampler {
-  uint32_t k0, k1, pos = 0;
+  uint32_t k0, k1, k3, pos = 0;
   uint32_t buf[4] = {0, 0, 0, 0};
+  static uint32_t fmix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+  }
   CounterSampler(uint64_t seed, uint32_t pixel, uint32_t sample)
-      : k0(pixel ^ (uint32_t)seed), k1(sample ^ (uint32_t)(seed >> 32)) {}
+      : k0(pixel), k1(sample), k3(fmix32((uint32_t)seed ^ fmix32((uint32_t)(seed >> 32) ^ 0x9e3779b9u))) {}
   static void pcg4d(uint32_t v[4]) {
     for (int i = 0; i < 4; i++) v[i] = v[i] * 1664525u + 1013904223u;
     v[0] += v[1] * v[3];
@@ -186,7 +195,7 @@ struct CounterSampler : Sampler {
       buf[0] = k0;
       buf[1] = k1;
       buf[2] = pos >> 2;
-      buf[3] = 0x9e3779b9u;
+      buf[3] = k3;
       pcg4d(buf);
     }
     pos++;

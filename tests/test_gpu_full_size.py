@@ -55,6 +55,11 @@ def test_raw_batch_2_24_rays(ctx, oracle, ico8):
     d = sub[both, 4:7].astype(np.float64)
     cosg = np.abs(np.sum(d * nrm_o[both], axis=1)) / np.linalg.norm(d, axis=1)
     rel_c = rel * np.minimum(1.0, np.maximum(cosg, 1e-6))
+    rel_plain = np.abs(h["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), 1e-30)
+    print("2^24 raw batch, 8,192 sampled rays: %d hits; conditioned rule: %d distance / %d primitive failures; "
+          "plain |dt|/t <= 1e-5 rule: %d distance / %d primitive failures"
+          % (both.sum(), (rel_c[same] > REL).sum(), (~same & (rel_c > REL)).sum(), (rel_plain[same] > REL).sum(),
+             (~same & (rel_plain > REL)).sum()))
     assert (~same & (rel_c > REL)).sum() <= 2
     assert (rel_c[same] > REL).sum() <= 2
     g.close()

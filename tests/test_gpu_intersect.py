@@ -65,9 +65,14 @@ def _compare(ctx, oracle, scene, rays, any_hit=False):
     rel_c = rel * np.minimum(1.0, np.maximum(cosg, 1e-6))
     near_tie = rel_c <= REL
     bad_prim = ~same & ~near_tie
+    # the plain rule (|dt| / t <= 1e-5, no conditioning), reported beside the
+    # conditioned one that is asserted
+    rel_plain = np.abs(hits["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), 1e-30)
+    plain_bad_prim = ~same & ~(rel_plain <= REL)
     return dict(n=len(rays), hit_disagree=int((g_hit != o_hit).sum()), bad_prim=int(bad_prim.sum()),
                 rel_bad=int((rel_c[same] > REL).sum()), rel_median=float(np.median(rel)) if rel.size else 0.0,
-                rel_max_conditioned=float(rel_c[same].max()) if same.any() else 0.0, hits=int(both.sum()))
+                rel_max_conditioned=float(rel_c[same].max()) if same.any() else 0.0, hits=int(both.sum()),
+                plain_rel_bad=int((rel_plain[same] > REL).sum()), plain_bad_prim=int(plain_bad_prim.sum()))
 
 
 SCENES = {

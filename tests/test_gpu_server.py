@@ -81,6 +81,55 @@ def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
     sv.close()
 
 
+def test_device_bound_fails_only_its_job(ctx, scenes):
+    """A device bound -- a traversal-stack overflow, forced by a scene built
+    with a 1-entry stack (GPRT_BUILD_TEST_STACK_CAP) -- fails the render it
+    occurs in and nothing else, as the reference scopes errors to the render
+    (progressive.go:165-167, worker_pool.go:21-26).  The kernels set the error
+    bits and carry on (no trap): the job API returns GPRT_E_BOUND for path
+    tracing and BDPT, raw batches mark the overflowed rays, and in the server
+    only the capped job gets a `failed` event while the jobs batched in the
+    same steps finish with their solo films, bit for bit."""
+    import gprt
+    from gprt import capi
+    from gprt import scenes as S
+    capped = gprt.GpuScene(ctx, S.icosphere_scene(level=4, width=40).to_desc(), test_stack_cap=True)
+    for integ in (None, gprt.BDPTIntegrator()):
+        conf = gprt.ProgressiveConfig(max_samples_per_pixel=2, max_passes=1, seed=1)
+        r = gprt.ProgressiveRaytracer(capped, conf, integ) if integ else gprt.ProgressiveRaytracer(capped, conf)
+        with pytest.raises(capi.GprtError) as e:
+            r.render_pass(1)
+        assert e.value.code == capi.GPRT_E_BOUND
+        assert b"traversal stack" in ctx.lib.gprt_last_error(ctx.h)
+        r.close()
+    # raw batch: camera rays through the sphere overflow, the others do not
+    v, f = S.icosphere(4)
+    rays = S.ray_batch(v, f, 4096, seed=3)
+    with pytest.raises(capi.GprtError) as e:
+        capped.intersect(rays)
+    assert e.value.code == capi.GPRT_E_BOUND
+    normal = gprt.GpuScene(ctx, S.icosphere_scene(level=4, width=40).to_desc())
+    assert (normal.intersect(rays)["prim"] != capi.BOUND_HIT).all()
+    normal.close()
+    # the server: the capped job shares its steps with normal jobs
+    jobs = [("cornell", 3, 8, 4), ("spheres_a", 7, 8, 4), ("ico", 5, 4, 2)]
+    plain = [_plain_film(scenes[n], seed, spp) for n, seed, spp, _ in jobs]
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    bad = sv.submit(capped, _cfg(4, 2, 9))
+    tickets = [sv.submit(scenes[n], _cfg(spp, per, seed)) for n, seed, spp, per in jobs]
+    ev = sv.run_until_idle()
+    mine = [e for e in ev if e.ticket == bad]
+    assert [e.kind for e in mine] == ["admitted", "failed"], mine
+    assert mine[-1].status == capi.GPRT_E_BOUND
+    done = {e.ticket for e in ev if e.kind == "done"}
+    assert done == set(tickets)
+    assert not [e for e in ev if e.kind == "failed" and e.ticket != bad]
+    for t, p in zip(tickets, plain):
+        _same(sv.film(t), p)
+    sv.close()
+    capped.close()
+
+
 def test_graphs_and_direct_launches_agree(ctx, scenes):
     import gprt
     from gprt import capi
