@@ -169,6 +169,42 @@ WorldEnd''')
         loaders.parse_pbrt('WorldBegin\n"float radius" 1\nWorldEnd')
 
 
+def test_block_and_parameter_edge_cases(loaders):
+    from gprt import capi
+    # processAttributeEnd with no open block does nothing; a block still open
+    # at the end of the file never reaches the scene (pbrt.go:201-221)
+    s = loaders.parse_pbrt('WorldBegin\nMaterial "diffuse"\nShape "sphere" "float radius" 2\nAttributeEnd\n'
+                           'AttributeBegin\nShape "sphere" "float radius" 3\nWorldEnd')
+    assert [sh.p[3] for sh in shapes(s.desc)] == [2.0]
+    # a declaration that is not "type name" is skipped, and so is the bare
+    # value after it; a later declaration of the same name wins
+    s = loaders.parse_pbrt('WorldBegin\nMaterial "diffuse"\nShape "sphere" "radius" 5 "float radius" 4 '
+                           '"point3 center" [1 2 3] "point3 center" [4 5 6]\nWorldEnd')
+    sh = shapes(s.desc)[0]
+    assert sh.p[3] == 4.0 and list(sh.p[:3]) == [4, 5, 6]
+    # tabs separate tokens and list items, but a statement line must start
+    # with the directive name and a space (isStatementStart, pbrt.go:707-722)
+    s = loaders.parse_pbrt('WorldBegin\nMaterial "diffuse"\t"rgb reflectance"\t[0.1\t0.2 0.3]\n'
+                           'Shape "sphere"\nWorldEnd')
+    assert albedo(s.desc, shapes(s.desc)[0]) == (0.1, 0.2, 0.3)
+    with pytest.raises(Exception, match="unexpected continuation line"):
+        loaders.parse_pbrt('WorldBegin\nMaterial\t"diffuse"\nWorldEnd')
+    # statements before WorldBegin other than Camera / Film / Sampler /
+    # Integrator are read and dropped
+    s = loaders.parse_pbrt('Material "diffuse"\nShape "sphere"\nWorldBegin\nWorldEnd')
+    assert s.desc.n_shapes == 0 and s.desc.n_materials == 0
+    # a directive with nothing after it is not a statement
+    with pytest.raises(Exception, match="invalid statement format"):
+        loaders.parse_pbrt('WorldBegin\nReverseOrientation\nWorldEnd')
+    # the area light of an outer block applies to the shapes of blocks opened inside it
+    s = loaders.parse_pbrt('WorldBegin\nMaterial "diffuse"\nAttributeBegin\n'
+                           '  AreaLightSource "diffuse" "rgb L" [2 2 2]\n  AttributeBegin\n'
+                           '    Shape "sphere" "float radius" 0.5\n  AttributeEnd\nAttributeEnd\nWorldEnd')
+    assert mat(s.desc, shapes(s.desc)[0]).kind == capi.MAT_EMISSIVE
+    assert [(s.desc.lights[k].kind, s.desc.lights[k].shape) for k in range(s.desc.n_lights)] == \
+        [(capi.LIGHT_SPHERE, 0)]
+
+
 def test_camera_defaults_lookat_and_override(loaders):
     # convertCamera (pbrt_scene.go:93-158) and parseLookAt (pbrt.go:435-490)
     from gprt.scene import CameraConfig
@@ -320,6 +356,21 @@ def test_ply_errors(loaders, tmp_path):
         loaders.load_ply(p)
     write_ply(p, [(0, 0, 0)] * 3, [(0, 1, 7)])
     with pytest.raises(Exception, match="index out of range"):
+        loaders.load_ply(p)
+
+
+def test_ply_extra_elements_and_truncation(loaders, tmp_path):
+    # elements other than vertex and face are skipped; a file that ends early
+    # is an error, not a short mesh
+    p = str(tmp_path / "c.ply")
+    write_ply(p, [(0, 0, 0), (1, 0, 0), (0, 1, 0)], [(0, 1, 2)])
+    head, body = open(p, "rb").read().split(b"end_header\n")
+    head += b"element edge 1\nproperty int vertex1\nproperty int vertex2\n"
+    open(p, "wb").write(head + b"end_header\n" + body + struct.pack("<2i", 0, 1))
+    d = loaders.load_ply(p)
+    assert np.array_equal(d.faces, np.array([(0, 1, 2)]))
+    open(p, "wb").write(head + b"end_header\n" + body[:-5])
+    with pytest.raises(Exception, match="unexpected EOF"):
         loaders.load_ply(p)
 
 
