@@ -14,7 +14,11 @@ aggregate Msamples/s.  Beside it, on the same GPU:
              default-style scenes, target spp 16-256 in passes of 4 spp:
              p50/p99 time-to-first-pass and per-pass latency, aggregate
              Msamples/s, batched server vs plain one-job-at-a-time;
-  bvh_stress the 1024^2 icosphere at 16 spp through the per-job path.
+  per_config every configuration of the reference's path through the
+             autotuned per-job path: Cornell 400^2 64 spp, the reference
+             Cornell spheres 400^2 64 spp, the icosphere 1024^2 16 spp (with
+             its traversal roofline), Cornell boxes 512^2 64 spp under BDPT,
+             and the raw 2^24-ray intersection batch (closest and any hit).
 Every job's film is the same alone and in the batch (bit for bit), so the
 comparison is at equal image RMSE.
 
@@ -61,7 +65,7 @@ def parse():
     ap.add_argument("--stream-requests", type=int, default=48)
     ap.add_argument("--rates", default="20,50,100,200")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-bvh-stress", action="store_true")
+    ap.add_argument("--no-per-config", action="store_true")
     ap.add_argument("--no-stream", action="store_true")
     return ap.parse_args()
 
@@ -317,16 +321,12 @@ def cpu_per_config(seconds=5.0):
     """The oracle on each of the other workloads, about `seconds` of whole
     64x64 tiles each (scene builds excluded): the CPU figure beside each
     per-config GPU number."""
-    from gprt import scenes
     from oracle import client
     threads = os.cpu_count()
     out = {}
-    for name, scene, spp, integ in (("cornell_400_64spp_pt", scenes.cornell_baseline(400), 64, 0),
-                                    ("cornell_spheres_400_64spp_pt", scenes.cornell_scene(), 64, 0),
-                                    ("icosphere_1024_16spp_pt", scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH),
-                                     16, 0),
-                                    ("cornell_boxes_512_64spp_bdpt", scenes.cornell_boxes_bdpt(512), 64, 1)):
-        sc = client.OracleScene(scene.to_desc())
+    for name, spp, bdpt in PER_CONFIG:
+        integ = 1 if bdpt else 0
+        sc = client.OracleScene(config_scene(name).to_desc())
         r = client.OracleRenderer(sc, integ, max_spp=spp, max_passes=1, seed=11, threads=threads)
         secs, st = r.render_pass(1, only_tiles=threads)
         r.close()
@@ -493,58 +493,101 @@ def serving_section(ctx, args, server_kw, tune, flats):
     return out
 
 
-def bvh_stress(ctx, flat, torch):
-    """The icosphere at 1024^2, 16 spp through the autotuned per-job path."""
+def _event_frames(torch, stream, flush, frames, render):
+    """Mean device time of `frames` calls of render() on `stream`: CUDA
+    events around each call, an L2 flush (512 MB write) before each, outside
+    the events."""
+    evs = []
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        render()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / frames
+
+
+def _tuned_job(g, integ, spp, extra_flags=0):
+    import gprt
+    tuned, _ = gprt.renderer.autotune(g, integ, spp=spp, config=gprt.ProgressiveConfig(max_samples_per_pixel=spp))
+    conf = gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1, flags=tuned.flags | extra_flags,
+                                  block_size=tuned.block_size, chunk_paths=tuned.chunk_paths)
+    job = gprt.ProgressiveRaytracer(g, conf, integ) if integ else gprt.ProgressiveRaytracer(g, conf)
+    return job, tuned
+
+
+def render_config(ctx, torch, flush, flat, spp, bdpt=False, frames=8):
+    """One benchmark configuration through the autotuned per-job path: mean
+    device time per frame (`spp` samples per pixel, CUDA events on the job
+    stream, L2 flushed before every frame), the kernel split of a frame, and
+    the first progressive pass (1 spp) of a fresh job on the host clock."""
     import gprt
     from gprt import capi
     g = gprt.GpuScene(ctx, flat)
+    integ = gprt.BDPTIntegrator() if bdpt else None
+    job, tuned = _tuned_job(g, integ, spp, capi.JOB_TIME_KERNELS)
+    stream = torch.cuda.ExternalStream(job.stream())
+    for _ in range(2):
+        job.add_samples(spp)
+    job.sync()
+    job.counters(reset=True)
+    ms = _event_frames(torch, stream, flush, frames, lambda: job.add_samples(spp))
+    kc = job.counters()
+    job.close()
+    conf = gprt.ProgressiveConfig(initial_samples=1, max_samples_per_pixel=spp, max_passes=max(2, spp // 4), seed=2)
+    first = gprt.ProgressiveRaytracer(g, conf, integ) if integ else gprt.ProgressiveRaytracer(g, conf)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    first.render_pass(1)
+    ttfp = (time.perf_counter() - t0) * 1e3
+    first.close()
+    n = g.width * g.height * spp
+    out = {"width": g.width, "height": g.height, "spp": spp, "integrator": "bdpt" if bdpt else "path tracing",
+           "ms_per_frame": ms, "msamples_per_s": n / ms / 1e3, "first_pass_ms": ttfp,
+           "kernel_ms_per_frame": {k: kc[k + "_ms"] / frames for k in ("extend", "shade", "shadow", "other")},
+           "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
+    return out, g, tuned
+
+
+def icosphere_extras(ctx, torch, flush, g, flat, tuned, frame_ms):
+    """The icosphere's closest-hit roofline (algorithmic bytes per ray = 32 B
+    ray in + 16 B hit out + 24 B per child-box test + 36 B per triangle test,
+    counted on the same frame by the counting kernels) and the same scene
+    built on the GPU (GPRT_BUILD_DEVICE)."""
+    import gprt
+    from gprt import capi
     cj = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=ICO_SPP, max_passes=1, seed=1,
-                                                             flags=capi.JOB_COUNT_TRAVERSAL | capi.JOB_TIME_KERNELS))
+                                                             flags=capi.JOB_COUNT_TRAVERSAL))
     cj.add_samples(ICO_SPP)
     cnt = cj.counters()
     cj.close()
-    tuned, tune = gprt.renderer.autotune(g, spp=ICO_SPP, config=gprt.ProgressiveConfig(max_samples_per_pixel=ICO_SPP))
     job = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=1 << 30, max_passes=1, seed=1,
                                                               flags=capi.JOB_TIME_KERNELS | tuned.flags,
                                                               block_size=tuned.block_size,
                                                               chunk_paths=tuned.chunk_paths))
     stream = torch.cuda.ExternalStream(job.stream())
-    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
-    for _ in range(3):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        job.add_samples(ICO_SPP)
+    job.add_samples(ICO_SPP)
     job.sync()
     job.counters(reset=True)
-    steps = 10
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        job.add_samples(ICO_SPP)
-    ev1.record(stream)
-    job.sync()
-    ms = ev0.elapsed_time(ev1)
+    steps = 6
+    _event_frames(torch, stream, flush, steps, lambda: job.add_samples(ICO_SPP))
     kc = job.counters()
-    peak, _ = measured_peaks()
+    job.close()
+    peak, peak_kind = measured_peaks()
     alg = cnt["extend_rays"] * 48 + 24 * cnt["extend_boxes"] + 36 * cnt["extend_prims"]
-    launches_timed = max(1.0, kc["extend_launches"] / steps)  # per frame, as timed (tuned chunk size)
-    per_launch = alg / launches_timed
+    launches = max(1.0, kc["extend_launches"] / steps)
+    per_launch = alg / launches
     avg_ms = kc["extend_ms"] / max(1, kc["extend_launches"])
     achieved = per_launch / (avg_ms / 1e3) / 1e9
-    traffic, _ = committed_traffic("extend_traffic.json", cnt["extend_rays"] / launches_timed)
-    npix = g.width * g.height
-    out = {"workload": "icosphere-L8 displaced (1,310,720 tris), ground quad, uniform sky; 1024x1024, 16 spp, depth 8",
-           "msamples_per_s": npix * ICO_SPP * steps / (ms / 1e3) / 1e6, "ms_per_frame": ms / steps,
-           "mrays_per_s": (cnt["extend_rays"] + cnt["shadow_rays"]) * steps / (ms / 1e3) / 1e6,
-           "extend_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                               "traffic": traffic, "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
-                               **l2_absorption(traffic, per_launch, avg_ms, peak), **l2_fraction(achieved, torch)},
-           "host_bvh_build_ms": g.info.build_ms,
-           "autotuned": {"chunk_paths": tuned.chunk_paths, "block_size": tuned.block_size, "flags": tuned.flags}}
-    job.close()
-    # the same scene built on the GPU (GPRT_BUILD_DEVICE): creation time and frame time
+    traffic, _ = committed_traffic("extend_traffic.json", cnt["extend_rays"] / launches)
+    out = {"mrays_per_s": (cnt["extend_rays"] + cnt["shadow_rays"]) / (frame_ms / 1e3) / 1e6,
+           "extend_roofline": {"kernel": "k_pt_extend", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                               "alg_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
+                               **l2_absorption(traffic, per_launch, avg_ms, peak), **l2_fraction(achieved, torch)}}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     gd = gprt.GpuScene(ctx, flat, device_bvh=True)
@@ -555,21 +598,190 @@ def bvh_stress(ctx, flat, torch):
     sd = torch.cuda.ExternalStream(jd.stream())
     jd.add_samples(ICO_SPP)
     jd.sync()
-    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2.record(sd)
-    for _ in range(3):
-        jd.add_samples(ICO_SPP)
-    e3.record(sd)
-    jd.sync()
     out["scene_build"] = {"host_sah_ms": g.info.build_ms, "host_sah_flatten_ms": g.info.flatten_ms,
                           "device_lbvh_create_ms": create_dev, "device_lbvh_build_ms": gd.info.build_ms,
                           "device_lbvh_nodes": int(gd.info.n_nodes), "host_sah_nodes": int(g.info.n_nodes),
-                          "device_lbvh_ms_per_frame": e2.elapsed_time(e3) / 3}
+                          "device_lbvh_ms_per_frame": _event_frames(torch, sd, flush, 3,
+                                                                    lambda: jd.add_samples(ICO_SPP))}
     jd.close()
     gd.close()
+    return out
+
+
+def raw_batch(ctx, torch, flush, flat, mesh, frames=6):
+    """The raw intersection batch: 2^24 rays on the level-8 icosphere (half
+    camera rays at 1024^2, half surface-point rays in uniform directions,
+    seed 13), closest and any hit, through gprt_intersect on device
+    buffers.  Roofline bytes per ray as for the render's extend kernel,
+    counted on a 1/64 sample of the batch."""
+    import gprt
+    from gprt import capi, scenes
+    n = 1 << 24
+    rays = scenes.ray_batch(mesh.vertices, mesh.faces, n, seed=13, width=ICO_WIDTH)
+    g = gprt.GpuScene(ctx, flat)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()  # a real stream handle (NULL would mean the library's own stream)
+    st.wait_stream(torch.cuda.current_stream())
+    peak, _ = measured_peaks()
+    sample = rays[::64]
+    out = {"rays": n}
+    for name, flag in (("closest", capi.CLOSEST), ("any", capi.ANY)):
+        call = lambda: ctx.check(ctx.lib.gprt_intersect(g.h, d_rays.data_ptr(), n, flag, d_hits.data_ptr(),
+                                                        st.cuda_stream))
+        for _ in range(2):
+            call()
+        ms = _event_frames(torch, st, flush, frames, call)
+        nodes, boxes, prims = g.traversal_counts(sample, any_hit=(flag == capi.ANY))
+        scale = n / len(sample)
+        alg = n * 48 + scale * (24 * boxes + 36 * prims)
+        achieved = alg / (ms / 1e3) / 1e9
+        out[name] = {"ms_per_batch": ms, "mrays_per_s": n / ms / 1e3,
+                     "roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                  "box_tests_per_ray": boxes / len(sample), "tri_tests_per_ray": prims / len(sample),
+                                  **l2_fraction(achieved, torch)}}
+    out["hit_fraction"] = float((d_hits[:, 0] >= 0).float().mean().item())
     g.close()
+    return out
+
+
+PER_CONFIG = (("c0a_cornell_400_64spp_pt", 64, False), ("c0b_cornell_spheres_400_64spp_pt", 64, False),
+              ("c1_icosphere_1024_16spp_pt", ICO_SPP, False), ("c2_cornell_boxes_512_64spp_bdpt", 64, True))
+
+
+def config_scene(name):
+    from gprt import scenes
+    from gprt.scene import CameraConfig
+    if name.startswith("c0a"):
+        return scenes.cornell_baseline(400)
+    if name.startswith("c0b"):  # the reference Cornell scene, every pixel taking every sample
+        s = scenes.cornell_scene(scenes.CORNELL_SPHERES, camera=CameraConfig(width=400))
+        s.sampling.adaptive_min_samples, s.sampling.adaptive_threshold = 1.0, 0.0
+        return s
+    if name.startswith("c1"):
+        return scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH)
+    return scenes.cornell_boxes_bdpt(512)
+
+
+def per_config_section(ctx, torch):
+    """Every benchmark configuration of the reference's path on the GPU:
+    Cornell 400^2 64 spp, reference Cornell spheres 400^2 64 spp, the
+    icosphere 1024^2 16 spp (with its extend roofline and the device-built
+    BVH), Cornell boxes 512^2 64 spp under BDPT, and the raw 2^24-ray batch.
+    The ALU-side figures of the L1-resident scenes come from committed ncu
+    summaries (profiles/*_alu.json) when present."""
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    out = {}
+    ico = None
+    for name, spp, bdpt in PER_CONFIG:
+        scene = config_scene(name)
+        flat = scene.to_desc()
+        r, g, tuned = render_config(ctx, torch, flush, flat, spp, bdpt)
+        if name.startswith("c1"):
+            r.update(icosphere_extras(ctx, torch, flush, g, flat, tuned, r["ms_per_frame"]))
+            ico = (flat, scene.shapes[0].mesh)
+        g.close()
+        alu = os.path.join(ROOT, "profiles", name.split("_")[0] + "_alu.json")
+        if os.path.exists(alu):
+            r["alu"] = json.load(open(alu))
+        out[name] = r
+    out["raw_batch_2_24"] = raw_batch(ctx, torch, flush, *ico)
     del flush
     return out
+
+
+def plain_section(ctx, torch, gscenes, spps, film0, batched_value, tune, world):
+    """The plain per-job path on the same batch, analysed: the host-clock
+    rate of one job at a time (job creation included, as a caller sees
+    it), the device time of each job's pass (CUDA events on the job's
+    stream) and the share of the wall clock the GPU sits idle between jobs,
+    the same jobs with the launch configuration autotuned once per
+    resolution class, and per resolution class the batched server on that
+    class alone against the plain path on it."""
+    import gprt
+    run_plain_batch(gscenes[:16], spps[:16])  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev_ms, per_job = 0.0, []
+    evs = []
+    for g, s in zip(gscenes, spps):
+        r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=s, max_passes=1, seed=1))
+        st = torch.cuda.ExternalStream(r.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        r.add_samples(s)
+        e1.record(st)
+        r.sync()
+        r.close()
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - t0
+    per_job = [a.elapsed_time(b) for a, b in evs]
+    dev_ms = sum(per_job)
+    n = sum(g.width * g.height * s for g, s in zip(gscenes, spps))
+    r = gprt.ProgressiveRaytracer(gscenes[0], gprt.ProgressiveConfig(max_samples_per_pixel=spps[0], max_passes=1,
+                                                                     seed=1))
+    r.add_samples(spps[0])
+    same = all(np.array_equal(a, b) for a, b in zip(r.film(), film0))
+    r.close()
+    classes = {}
+    for k, g in enumerate(gscenes):
+        classes.setdefault("%dx%d" % (g.width, g.height), []).append(k)
+    # plain, launch configuration autotuned on the first job of each class
+    tuned_ms = 0.0
+    by_class = {}
+    for cls, idx in classes.items():
+        g0 = gscenes[idx[0]]
+        tuned, _ = gprt.renderer.autotune(g0, spp=spps[idx[0]],
+                                          config=gprt.ProgressiveConfig(max_samples_per_pixel=spps[idx[0]]))
+        cms, tevs = 0.0, []
+        for k in idx:
+            job = gprt.ProgressiveRaytracer(gscenes[k], gprt.ProgressiveConfig(
+                max_samples_per_pixel=spps[k], max_passes=1, seed=1, flags=tuned.flags, block_size=tuned.block_size,
+                chunk_paths=tuned.chunk_paths))
+            st = torch.cuda.ExternalStream(job.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            job.add_samples(spps[k])
+            e1.record(st)
+            job.sync()
+            job.close()
+            tevs.append((e0, e1))
+        torch.cuda.synchronize()
+        cms = sum(a.elapsed_time(b) for a, b in tevs)
+        tuned_ms += cms
+        samples = sum(gscenes[k].width * gscenes[k].height * spps[k] for k in idx)
+        # the batched server on this class alone (one warm-up batch, one timed)
+        sv = gprt.RenderServer(ctx, step_paths=tune["chunk_paths"], block_size=tune["block_size"],
+                               flags=tune["flags"])
+        sv.configure(tune["chunk_paths"], tune["block_size"], tune["flags"])
+        sub_g, sub_s = [gscenes[k] for k in idx], [spps[k] for k in idx]
+        run_batch(sv, sub_g, sub_s)
+        stream = torch.cuda.ExternalStream(sv.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run_batch(sv, sub_g, sub_s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1)
+        sv.close()
+        plain_dev = sum(per_job[k] for k in idx)
+        by_class[cls] = {"jobs": len(idx), "msamples": samples / 1e6,
+                         "plain_device_msamples_per_s": samples / plain_dev / 1e3,
+                         "plain_tuned_device_msamples_per_s": samples / cms / 1e3,
+                         "batched_class_alone_msamples_per_s": samples / bms / 1e3,
+                         "batched_over_plain_device": plain_dev / bms, "batched_over_plain_tuned": cms / bms,
+                         "plain_mean_job_ms": plain_dev / len(idx)}
+    return {"msamples_per_s": n / tp / 1e6, "s_per_batch": tp, "timing": "host clock, device-synchronised, "
+            "job creation included",
+            "batched_over_plain": batched_value / world / (n / tp / 1e6),
+            "device_msamples_per_s": n / dev_ms / 1e3, "device_ms_per_batch": dev_ms,
+            "gpu_idle_fraction": max(0.0, 1.0 - dev_ms / (tp * 1e3)),
+            "batched_over_plain_device": batched_value / world / (n / dev_ms / 1e3),
+            "tuned_per_class_msamples_per_s": n / tuned_ms / 1e3,
+            "batched_over_plain_tuned": batched_value / world / (n / tuned_ms / 1e3),
+            "by_resolution": by_class, "film_of_job0_identical": bool(same)}
 
 
 def run_gprt(args):
@@ -682,22 +894,8 @@ def run_gprt(args):
     if kc["shade_ms"] > kc["extend_ms"]:
         roof = roof_shade
 
-    # the plain per-job path on the same batch (host clock around device-synchronised jobs)
-    plain = None
-    if rank == 0:
-        run_plain_batch(gscenes[:16], spps[:16])  # warm-up
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        n = run_plain_batch(gscenes, spps)
-        torch.cuda.synchronize()
-        tp = time.perf_counter() - t0
-        r = gprt.ProgressiveRaytracer(gscenes[0], gprt.ProgressiveConfig(max_samples_per_pixel=spps[0], max_passes=1,
-                                                                         seed=1))
-        r.add_samples(spps[0])
-        same = all(np.array_equal(a, b) for a, b in zip(r.film(), film0))
-        r.close()
-        plain = {"msamples_per_s": n / tp / 1e6, "s_per_batch": tp, "timing": "host clock, device-synchronised",
-                 "batched_over_plain": value / world / (n / tp / 1e6), "film_of_job0_identical": bool(same)}
+    # the plain per-job path on the same batch
+    plain = plain_section(ctx, torch, gscenes, spps, film0, value, tune, world) if rank == 0 else None
 
     # end to end through the public API with host buffers: scene descriptions
     # in (host BVH build + upload), every job's RGBA8 image out.  As a serving
@@ -766,18 +964,20 @@ def run_gprt(args):
         flats = [scenes.cornell_baseline(400).to_desc(), ico_flat, scenes.cornell_boxes_bdpt(512).to_desc(), c3]
         serving = serving_section(ctx, args, server_kw, tune, flats)
 
-    stress = None
-    if rank == 0 and not args.no_bvh_stress:
-        from gprt import scenes
-        if ico_flat is None:
-            ico_flat = scenes.icosphere_scene(level=ICO_LEVEL, width=ICO_WIDTH).to_desc()
-        stress = bvh_stress(ctx, ico_flat, torch)
+    per_config = None
+    if rank == 0 and not args.no_per_config:
+        per_config = per_config_section(ctx, torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(jobs)
             cpu["per_config"] = cpu_per_config()
+            if per_config:
+                for k, v in cpu["per_config"]["configs"].items():
+                    if k in per_config:
+                        per_config[k]["cpu_msamples_per_s"] = v["msamples_per_s"]
+                        per_config[k]["gpu_over_cpu"] = per_config[k]["msamples_per_s"] / v["msamples_per_s"]
         except Exception as e:  # the baseline never blocks the GPU line
             cpu = {"value": None, "error": str(e)}
 
@@ -793,7 +993,7 @@ def run_gprt(args):
                                          "simple_shadow": bool(tune["flags"] & capi.JOB_SIMPLE_SHADOW),
                                          "candidates": tune["candidates"]},
                            "server_steps_per_batch": (st1["steps"] - st0["steps"]) / args.steps},
-                "plain": plain, "serving": serving, "bvh_stress": stress,
+                "plain": plain, "serving": serving, "per_config": per_config,
                 "roofline": roof, "rooflines": rooflines, "kernel_ms_per_step": kernel_ms, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(timed_kernels), "clocks": clk}
         print(json.dumps(line))

@@ -1,8 +1,8 @@
 """Small, self-contained render cases for kernel profiling (ncu).
 
-    python -m gprt.profile_cases batch [--jobs 24] [--spp N] [--step-paths P] [--count]
-    python -m gprt.profile_cases icosphere [--width 512] [--spp 4] [--count]
-    python -m gprt.profile_cases bdpt [--width 512] [--spp 4]
+    python profile_cases.py batch [--jobs 24] [--spp N] [--step-paths P] [--count]
+    python profile_cases.py icosphere [--width 512] [--spp 4] [--count]
+    python profile_cases.py bdpt [--width 512] [--spp 4]
 
 `batch` renders the first jobs of the heterogeneous default-style batch
 (seed 17; each job at its own spp, or at --spp N) through the batched render
@@ -13,8 +13,9 @@ most and run each kernel a bounded number of times, so a capture of a few
 launches of one kernel ends by itself.  With --count the same case runs with
 the traversal counters on (and direct launches) and prints the rays, node
 visits, box tests and primitive tests of the extend and shadow kernels, the
-units that scale a capture's DRAM bytes to other launch sizes.  Run from the
-package directory.
+units that scale a capture's DRAM bytes to other launch sizes.  A
+measurement helper beside bench.py (the profiles/ summaries cite its
+command lines); run it from the repository root.
 """
 import argparse
 import json
@@ -23,9 +24,9 @@ import sys
 
 
 def _setup():
-    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    if here not in sys.path:
-        sys.path.insert(0, here)
+    pkg = os.path.join(os.path.dirname(os.path.abspath(__file__)), "go-progressive-raytracer_gb300")
+    if pkg not in sys.path:
+        sys.path.insert(0, pkg)
 
 
 def batch(jobs, step_paths, spp=None, count=False, seed=17):
