@@ -3,6 +3,7 @@
     python profile_cases.py batch [--jobs 24] [--spp N] [--step-paths P] [--count]
     python profile_cases.py icosphere [--width 512] [--spp 4] [--count]
     python profile_cases.py bdpt [--width 512] [--spp 4]
+    python profile_cases.py cornell [--width 400] [--spp 64]
 
 `batch` renders the first jobs of the heterogeneous default-style batch
 (seed 17; each job at its own spp, or at --spp N) through the batched render
@@ -71,6 +72,22 @@ def icosphere(width, spp, count=False):
     print(json.dumps({"case": "icosphere", "width": width, "spp": spp, "counters": c}))
 
 
+def cornell(width, spp):
+    """The Cornell box of the path-tracing workload (cornell_baseline) through
+    the per-job path: one frame of `spp` samples per pixel."""
+    import gprt
+    from gprt import scenes
+    ctx = gprt.Context(0)
+    g = gprt.GpuScene(ctx, scenes.cornell_baseline(width).to_desc())
+    r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=spp, max_passes=1, seed=1))
+    r.add_samples(spp)
+    r.sync()
+    r.close()
+    g.close()
+    ctx.close()
+    print(json.dumps({"case": "cornell", "width": width, "spp": spp}))
+
+
 def bdpt(width, spp):
     import gprt
     from gprt import scenes
@@ -89,7 +106,7 @@ def bdpt(width, spp):
 def main(argv=None):
     _setup()
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["batch", "icosphere", "bdpt"])
+    ap.add_argument("case", choices=["batch", "icosphere", "bdpt", "cornell"])
     ap.add_argument("--jobs", type=int, default=24)
     ap.add_argument("--step-paths", type=int, default=1 << 22)
     ap.add_argument("--width", type=int, default=512)
@@ -100,6 +117,8 @@ def main(argv=None):
         batch(a.jobs, a.step_paths, a.spp or None, a.count)
     elif a.case == "bdpt":
         bdpt(a.width, a.spp or 4)
+    elif a.case == "cornell":
+        cornell(a.width, a.spp or 64)
     else:
         icosphere(a.width, a.spp or 4, a.count)
     return 0
