@@ -23,6 +23,7 @@ int ensure_bdpt(gprt_job* j) {
   rc |= dev_alloc(ctx, b, &P.counters, 64);
   rc |= dev_alloc(ctx, b, &P.Lout, ns);
   for (int k = 0; k < 5; k++) rc |= dev_alloc(ctx, b, &B.v[k], (size_t)ns * 2 * B.maxv);
+  rc |= dev_alloc(ctx, b, &B.pdf, (size_t)ns * 2 * B.maxv);
   rc |= dev_alloc(ctx, b, &B.meta, ns);
   rc |= dev_alloc(ctx, b, &B.masks, ns);
   rc |= dev_alloc(ctx, b, &B.contrib, (size_t)ns * (B.maxv + 1) * B.maxv);

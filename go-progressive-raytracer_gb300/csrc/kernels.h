@@ -39,6 +39,7 @@ struct PathBuf {
 // and one contribution slot per (strategy, sample).
 struct DevBdpt {
   float4* v[5];
+  float4* pdf;    // per vertex: fwd, rev, flags | (light + 1) << 8 (int bits), the subpath's MIS prefix
   uint4* meta;    // nc | nl << 8, sampler position after the subpaths, pixel, sample index
   uint2* masks;   // strategies that draw samples: light-tracing (bit s), direct-lighting (bit t)
   float4* contrib;
@@ -74,7 +75,7 @@ struct DevPaths {
 // of the BDPT working set of `ns` samples.
 inline int bdpt_maxv(int max_depth) { return max_depth <= 9 ? 10 : 18; }
 inline size_t bdpt_bytes(uint32_t ns, int maxv) {
-  return (size_t)ns * (5 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16) + 8 * 256;
+  return (size_t)ns * (6 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16) + 8 * 256;
 }
 
 constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;

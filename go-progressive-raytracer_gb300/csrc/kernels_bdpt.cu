@@ -322,8 +322,6 @@ __device__ __forceinline__ float light_origin_pdf(const DevScene& sc, const BVer
   return pos * sc.lights[lv.light].prob;
 }
 
-__device__ __forceinline__ float remap0(float f) { return f != 0.f ? f : 1.f; }
-
 // Any-hit test of a connection / shadow ray (one call site for all strategies).
 __device__ __forceinline__ bool occluded(const DevScene& sc, float3 o, float3 d, float tmax, uint32_t skip, int* err) {
   Hit hh;
@@ -334,7 +332,7 @@ __device__ __forceinline__ bool occluded(const DevScene& sc, float3 o, float3 d,
 // Subpath vertices live in global memory as 5 float4 fields indexed
 // [vertex * ns + sample], so the 32 lanes of a warp (32 consecutive samples)
 // read one field of one vertex in a single coalesced access.
-__device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, const BVert& x) {
+__device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, const BVert& x, float pre = 0.f) {
   size_t k = (size_t)v * B.ns + i;
   B.v[0][k] = make_float4(x.p.x, x.p.y, x.p.z, x.fwd);
   B.v[1][k] = make_float4(x.n.x, x.n.y, x.n.z, x.rev);
@@ -342,6 +340,7 @@ __device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, co
   B.v[3][k] = make_float4(x.Le.x, x.Le.y, x.Le.z, x.wi.y);
   B.v[4][k] = make_float4(x.wi.z, __int_as_float((x.mat + 1) | (x.flags << 24)), __int_as_float(x.light),
                           __uint_as_float(x.prim));
+  B.pdf[k] = make_float4(x.fwd, x.rev, __int_as_float(x.flags | ((x.light + 1) << 8)), pre);
   if (B.uv) B.uv[k] = x.mat >= 0 ? x.uv : make_float2(0.f, 0.f);
 }
 
@@ -365,24 +364,61 @@ __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
   return x;
 }
 
-// The pdfs and flags of a stored vertex (3 of its 5 fields), all the MIS
-// walk reads away from the connection.
+// The pdfs and flags of a stored vertex and its subpath's MIS prefix (one
+// 16-byte record): all the MIS weight reads away from the connection.
 struct VPdf {
   float fwd, rev;
   int flags, light;
+  float pre;
 };
 __device__ __forceinline__ VPdf get_vpdf(const DevBdpt& B, int v, uint32_t i) {
-  size_t k = (size_t)v * B.ns + i;
+  float4 a = B.pdf[(size_t)v * B.ns + i];
   VPdf r;
-  r.fwd = B.v[0][k].w;
-  r.rev = B.v[1][k].w;
-  r.flags = (__float_as_int(B.v[4][k].y) >> 24) & 0xFF;
-  r.light = r.flags & kFlagLight ? __float_as_int(B.v[4][k].z) : -1;
+  r.fwd = a.x;
+  r.rev = a.y;
+  int m = __float_as_int(a.z);
+  r.flags = m & 0xFF;
+  r.light = (m >> 8) - 1;
+  r.pre = a.w;
   return r;
 }
 // a vertex on a point light (LightTypePoint, bdpt_mis.go:130-137)
 __device__ __forceinline__ bool is_delta_light(const DevScene& sc, const VPdf& v) {
   return (v.flags & kFlagLight) && v.light >= 0 && sc.lights[v.light].kind == kLightPointSpot;
+}
+
+__device__ __forceinline__ float remap0(float f) { return f != 0.f ? f : 1.f; }
+
+// The MIS prefix of a finished subpath, written into each vertex's pdf
+// record.  calculateMISWeight (bdpt_mis.go:13-181) walks each subpath from
+// the connection outwards, multiplying ratios r_i = remap0(rev_i) /
+// remap0(fwd_i) and adding the running product at every connectible vertex;
+// away from the two vertices next to the connection those ratios and flags
+// do not depend on the strategy, so the sum over vertices 0..k is kept as
+//   A_k = r_k * (A_{k-1} + c_k)
+// (camera subpath: from vertex 1, c_k = neither vertex k nor k-1 specular;
+// light subpath: from vertex 0, c_k also excludes delta lights), and each
+// strategy evaluates only its two connection-side steps on top of it.
+__device__ __forceinline__ void subpath_prefix(const DevScene& sc, const DevBdpt& B, int base, int len, uint32_t i,
+                                               bool camera) {
+  float acc = 0.f;
+  bool prev_ok = true;  // the previous vertex is neither specular nor a delta light
+  for (int k = 0; k < len; k++) {
+    size_t at = (size_t)(base + k) * B.ns + i;
+    float4 a = B.pdf[at];
+    int m = __float_as_int(a.z);
+    int flags = m & 0xFF, light = (m >> 8) - 1;
+    bool ok = !(flags & kFlagSpecular);
+    if (!camera) ok = ok && !((flags & kFlagLight) && light >= 0 && sc.lights[light].kind == kLightPointSpot);
+    if (camera && k == 0) {
+      acc = 0.f;  // the camera vertex takes no part in the walk
+    } else {
+      bool conn = ok && (k == 0 || prev_ok);
+      acc = (remap0(a.y) / remap0(a.x)) * (acc + (conn ? 1.f : 0.f));
+    }
+    B.pdf[at].w = acc;
+    prev_ok = ok;
+  }
 }
 
 // The vertices of one sample's subpath (camera: base 0, light: base maxv).
@@ -401,10 +437,29 @@ struct SubState {
   BVert prev;  // the last vertex, written once its reverse pdf is final
   float3 o, d, beta;
   float pdf_fwd;
+  float pre;     // the MIS prefix over the vertices written so far (subpath_prefix)
+  bool prev_ok;  // the last written vertex is neither specular nor a delta light
   int len, b, max_bounces, base;
   uint32_t skip;
   bool camera;
 };
+
+// Writes the subpath's last vertex (index len - 1, its reverse pdf final)
+// with the running MIS prefix of subpath_prefix updated by it.
+__device__ __forceinline__ void emit_vert(const DevScene& sc, const DevBdpt& B, uint32_t i, SubState& st) {
+  const BVert& x = st.prev;
+  const int k = st.len - 1;
+  bool ok = !x.is(kFlagSpecular);
+  if (!st.camera) ok = ok && !(x.is(kFlagLight) && x.light >= 0 && sc.lights[x.light].kind == kLightPointSpot);
+  if (st.camera && k == 0) {
+    st.pre = 0.f;
+  } else {
+    bool conn = ok && (k == 0 || st.prev_ok);
+    st.pre = (remap0(x.rev) / remap0(x.fwd)) * (st.pre + (conn ? 1.f : 0.f));
+  }
+  st.prev_ok = ok;
+  put_vert(B, st.base + k, i, x, st.pre);
+}
 
 // One bounce of extendPath (bdpt.go:206-291): returns true when the subpath
 // has ended (vertex len - 1, `prev`, is then still to be written).
@@ -429,7 +484,7 @@ __device__ __forceinline__ bool subpath_step(const DevScene& sc, const DevBdpt& 
       v.light = -1;
       v.prim = kNoHit;
       v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
-      put_vert(B, st.base + st.len - 1, i, st.prev);
+      emit_vert(sc, B, i, st);
       st.prev = v;
       st.len++;
     }
@@ -454,7 +509,7 @@ __device__ __forceinline__ bool subpath_step(const DevScene& sc, const DevBdpt& 
   v.fwd = to_area(sc, st.prev, v, st.pdf_fwd);
   Scatter scn;
   if (!scatter(sc, m, d, s, rng, scn)) {
-    put_vert(B, st.base + st.len - 1, i, st.prev);
+    emit_vert(sc, B, i, st);
     st.prev = v;
     st.len++;
     return true;
@@ -472,7 +527,7 @@ __device__ __forceinline__ bool subpath_step(const DevScene& sc, const DevBdpt& 
     st.pdf_fwd = 0.f;
   }
   st.prev.rev = to_area(sc, v, st.prev, pdf_rev);
-  put_vert(B, st.base + st.len - 1, i, st.prev);
+  emit_vert(sc, B, i, st);
   st.prev = v;
   st.len++;
   st.o = s.p;
@@ -540,40 +595,45 @@ __device__ __forceinline__ float mis_weight(const DevScene& sc, const SubpathRef
       rv[q] = vertex_pdf(sc, cur, hp ? &prev : nullptr, next);
     }
   }
-  float sum = 0.f, ri = 1.f;
-  VPdf v = t >= 1 ? C.pdfs(t - 1) : VPdf{};
-  for (int i = t - 1; i > 0; i--) {
-    VPdf pv = C.pdfs(i - 1);  // the predecessor: its flags here, the walk's next vertex
-    float fwd = v.fwd, rev = v.rev;
-    bool conn = !(v.flags & kFlagSpecular);
-    if (i == t - 1 && cam1 >= 0) {
-      rev = rv[cam1];
-      conn = true;
-    } else if (i == t - 2 && cam2 >= 0) {
-      rev = rv[cam2];
+  // the walk of bdpt_mis.go:61-178 in prefix form: the two steps next to
+  // the connection on each side (with the recomputed reverse pdfs and the
+  // connection's own connectibility), then the subpath's stored prefix
+  float sum = 0.f;
+  if (t >= 2) {  // camera vertices t-1 .. 1
+    VPdf v1 = C.pdfs(t - 1), v2 = C.pdfs(t - 2);
+    float r1 = remap0(cam1 >= 0 ? rv[cam1] : v1.rev) / remap0(v1.fwd);
+    bool c1 = (cam1 >= 0 || !(v1.flags & kFlagSpecular)) && !(v2.flags & kFlagSpecular);
+    float inner = 0.f;
+    if (t >= 3) {
+      VPdf v3 = C.pdfs(t - 3);
+      float r2 = remap0(cam2 >= 0 ? rv[cam2] : v2.rev) / remap0(v2.fwd);
+      bool c2 = !(v2.flags & kFlagSpecular) && !(v3.flags & kFlagSpecular);
+      inner = r2 * (v3.pre + (c2 ? 1.f : 0.f));
     }
-    conn = conn && !(pv.flags & kFlagSpecular);
-    ri *= remap0(rev) / remap0(fwd);
-    if (conn) sum += ri;
-    v = pv;
+    sum += r1 * (inner + (c1 ? 1.f : 0.f));
   }
-  ri = 1.f;
-  v = s >= 1 ? Lp.pdfs(s - 1) : VPdf{};
-  for (int i = s - 1; i >= 0; i--) {
-    VPdf pv = i > 0 ? Lp.pdfs(i - 1) : VPdf{};
-    float fwd = v.fwd, rev = v.rev;
-    bool conn = !(v.flags & kFlagSpecular) && !is_delta_light(sc, v);
-    if (i > 0) conn = conn && !(pv.flags & kFlagSpecular) && !is_delta_light(sc, pv);
-    if (i == s - 1 && lit1 >= 0) {
-      if (CLS == 2) fwd = sampled->fwd;
-      rev = rv[lit1];
-      conn = true;
-    } else if (i == s - 2 && lit2 >= 0) {
-      rev = rv[lit2];
+  if (s >= 1) {  // light vertices s-1 .. 0
+    VPdf u1 = Lp.pdfs(s - 1);
+    float fw1 = (CLS == 2 && lit1 >= 0) ? sampled->fwd : u1.fwd;
+    float q1 = remap0(lit1 >= 0 ? rv[lit1] : u1.rev) / remap0(fw1);
+    bool d1 = !(u1.flags & kFlagSpecular) && !is_delta_light(sc, u1);
+    float inner = 0.f;
+    if (s >= 2) {
+      VPdf u2 = Lp.pdfs(s - 2);
+      bool ok2 = !(u2.flags & kFlagSpecular) && !is_delta_light(sc, u2);
+      d1 = d1 && ok2;
+      float q2 = remap0(lit2 >= 0 ? rv[lit2] : u2.rev) / remap0(u2.fwd);
+      bool d2 = ok2;
+      float b3 = 0.f;
+      if (s >= 3) {
+        VPdf u3 = Lp.pdfs(s - 3);
+        d2 = d2 && !(u3.flags & kFlagSpecular) && !is_delta_light(sc, u3);
+        b3 = u3.pre;
+      }
+      inner = q2 * (b3 + (d2 ? 1.f : 0.f));
     }
-    ri *= remap0(rev) / remap0(fwd);
-    if (conn) sum += ri;
-    v = pv;
+    if (lit1 >= 0) d1 = true;
+    sum += q1 * (inner + (d1 ? 1.f : 0.f));
   }
   return 1.f / (1.f + sum);
 }
@@ -791,11 +851,13 @@ __global__ void __launch_bounds__(128, 4) k_bdpt_subpaths(DevScene sc, DevFilm f
       st.base = 0;
       st.skip = kNoHit;
       st.camera = true;
+      st.pre = 0.f;
+      st.prev_ok = true;
       inf = false;
       phase = 0;
     }
     if (!subpath_step<MAXV>(sc, B, p, st, rng, err)) continue;
-    put_vert(B, st.base + st.len - 1, p, st.prev);
+    emit_vert(sc, B, p, st);
     int nl = 0;
     if (phase == 0) {
       nc = st.len;
@@ -837,6 +899,8 @@ __global__ void __launch_bounds__(128, 4) k_bdpt_subpaths(DevScene sc, DevFilm f
         st.base = MAXV;
         st.skip = lv.prim;
         st.camera = false;
+        st.pre = 0.f;
+        st.prev_ok = true;
         phase = 1;
         continue;
       }
@@ -852,6 +916,7 @@ __global__ void __launch_bounds__(128, 4) k_bdpt_subpaths(DevScene sc, DevFilm f
         BVert l0 = get_vert(B, MAXV, p);
         l0.fwd = infinite_density(sc, ep, en, ed);
         put_vert(B, MAXV, p, l0);
+        subpath_prefix(sc, B, MAXV, nl, p, false);  // the corrected pdfs change every prefix
       }
     }
     // which strategies draw uniform numbers (draws_before)
@@ -877,34 +942,45 @@ __device__ __forceinline__ bool has_strategy(int s, int t, int nc, int nl) {
 }
 
 // Lists, per strategy, the samples that have it, so that the strategy kernel
-// gives each warp 32 real (s, t, sample) items: one warp-aggregated atomic per
-// strategy and warp.  The order within a list does not matter: every item
-// writes its own contribution slot.
+// gives each warp 32 real (s, t, sample) items.  A block of 1,024 samples
+// counts each strategy's items in shared memory (one shared atomic per warp
+// and strategy), reserves its range of every list with one global atomic per
+// strategy, then writes the items: per-warp global atomics on the
+// (MAXV + 1) x MAXV list counters serialised in L2 (16.7 ms of a 200 ms
+// Cornell-boxes frame).  The order within a list does not matter: every
+// item writes its own contribution slot.
 template <int MAXV>
-__global__ void k_bdpt_list(DevPaths PS, ChunkDesc ch) {
+__global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
+  constexpr int K = (MAXV + 1) * MAXV;
+  __shared__ uint32_t cnt[K], base[K];
+  __shared__ uint16_t wofs[32][K];  // each warp's offset within the block's range (< 1,024)
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
-  const int lane = threadIdx.x & 31;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    uint32_t i = base + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  for (uint32_t start = blockIdx.x * 1024u; start < n; start += gridDim.x * 1024u) {
+    for (int k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    uint32_t i = start + threadIdx.x;
     int nc = 0, nl = -1;
     if (i < n) {
       uint32_t m = B.meta[i].x;
       nc = (int)(m & 0xFF);
       nl = (int)(m >> 8);
     }
-    for (int k = 0; k < (MAXV + 1) * MAXV; k++) {
-      int s = k / MAXV, t = k % MAXV + 1;
-      bool has = has_strategy(s, t, nc, nl);
-      unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
-      if (!mask) continue;
-      int leader = __ffs(mask) - 1;
-      uint32_t at = 0;
-      if (lane == leader) at = atomicAdd(B.scount + k, (uint32_t)__popc(mask));
-      at = __shfl_sync(0xFFFFFFFFu, at, leader);
-      if (has) B.slist[(size_t)k * B.ns + at + __popc(mask & ((1u << lane) - 1u))] = i;
+    for (int k = 0; k < K; k++) {
+      unsigned mask = __ballot_sync(0xFFFFFFFFu, has_strategy(k / MAXV, k % MAXV + 1, nc, nl));
+      if (mask && lane == 0) wofs[w][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) base[k] = cnt[k] ? atomicAdd(B.scount + k, cnt[k]) : 0u;
+    __syncthreads();
+    for (int k = 0; k < K; k++) {
+      bool has = has_strategy(k / MAXV, k % MAXV + 1, nc, nl);
+      unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
+      if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[w][k] + __popc(mask & below)] = i;
+    }
+    __syncthreads();  // cnt, base and wofs are rewritten for the next range
   }
 }
 
@@ -987,10 +1063,11 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
   int g1 = std::min(launch_grid(n, 128, 0), std::max(1, sms * 8));  // persistent subpath kernel
   int g2 = std::max(1, sms * 16);
   int g3 = launch_grid(n, 256, 0);
+  int gl = std::min(launch_grid(n, 1024, 0), std::max(1, sms * 2));
   cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * ((P.bd.maxv + 1) * P.bd.maxv + 1), st);
   if (P.bd.maxv == 10) {
     k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_list<10><<<g3, 256, 0, st>>>(P, ch);
+    k_bdpt_list<10><<<gl, 1024, 0, st>>>(P, ch);
     k_bdpt_strategies<10, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_strategies<10, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_strategies<10, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
@@ -998,7 +1075,7 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
     k_bdpt_sum<10><<<g3, 256, 0, st>>>(P, ch);
   } else {
     k_bdpt_subpaths<18><<<g1, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_list<18><<<g3, 256, 0, st>>>(P, ch);
+    k_bdpt_list<18><<<gl, 1024, 0, st>>>(P, ch);
     k_bdpt_strategies<18, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_strategies<18, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
     k_bdpt_strategies<18, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
