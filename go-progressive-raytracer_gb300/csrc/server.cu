@@ -295,6 +295,10 @@ struct gprt_server {
   gprt_server_desc desc{};
   std::chrono::steady_clock::time_point t0;
   cudaStream_t stream = nullptr;
+  // the BDPT job rendering its first pass runs on this stream, created with
+  // the device's greatest priority: its blocks are scheduled ahead of the
+  // batched path-tracing wavefront's whenever both wait for an SM
+  cudaStream_t bd_first = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // state (smu)
   std::mutex smu;
@@ -306,6 +310,7 @@ struct gprt_server {
   std::vector<void*> path_bufs;
   size_t path_bytes = 0;
   uint64_t bd_rounds = 0;  // BDPT passes run (their least-recently-served order)
+  uint32_t firsts_run = 0; // consecutive steps that carried first passes only
   // read-back staging (resolved image before the copy to the host), grown
   // on demand under smu and kept: a cudaFree per read would synchronise the
   // device while steps run
@@ -923,10 +928,11 @@ struct Item {
 
 // Packs the next samples of the running jobs (least recently served first)
 // into one wavefront of at most step_paths paths.
-std::vector<Item> pack(gprt_server* sv) {
+std::vector<Item> pack(gprt_server* sv, bool firsts_only) {
   std::vector<SrvJob*> order;
   for (auto& kv : sv->jobs)
-    if (kv.second->running && !kv.second->bd) order.push_back(kv.second.get());
+    if (kv.second->running && !kv.second->bd && (!firsts_only || kv.second->passes == 0))
+      order.push_back(kv.second.get());
   // jobs before their first pass first, the smallest first pass first (a
   // burst of arrivals then shows small images at once and does not wait
   // behind the first pass of a 1024^2 job), then the least recently served
@@ -1011,18 +1017,14 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
   return D;
 }
 
-// One batched path-tracing wavefront over the running path-tracing jobs, and
-// its events; `overlap` runs once the wavefront is queued, before waiting for
-// it (work on other streams then shares the GPU with it).  Returns the number
-// of items run (0: none) or a negative status.
-template <class F>
-int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
+// One batched path-tracing wavefront over the running path-tracing jobs
+// (only those before their first pass with `firsts_only`), and its events
+// (work queued on other streams before it shares the GPU with it).  Returns
+// the number of items run (0: none) or a negative status.
+int pt_step(gprt_server* sv, bool dry, double* ms_out, bool firsts_only) {
   gprt_ctx* ctx = sv->ctx;
-  std::vector<Item> items = pack(sv);
-  if (items.empty()) {
-    overlap();
-    return 0;
-  }
+  std::vector<Item> items = pack(sv, firsts_only);
+  if (items.empty()) return 0;
   uint64_t paths = 0;
   int D = upload_items(sv, items, dry, &paths);
   CK(ctx, cudaEventRecord(sv->ev0, sv->stream));
@@ -1031,7 +1033,6 @@ int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
   CK(ctx, cudaEventRecord(sv->ev1, sv->stream));
   CK(ctx, cudaMemcpyAsync(sv->h_err, sv->d_table + sv->err_off, items.size() * sizeof(uint32_t),
                           cudaMemcpyDeviceToHost, sv->stream));
-  overlap();
   CK(ctx, cudaStreamSynchronize(sv->stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, sv->ev0, sv->ev1);
@@ -1066,10 +1067,13 @@ int pt_step(gprt_server* sv, bool dry, double* ms_out, F&& overlap) {
 }
 
 // BDPT samples rendered per step at most (whole samples per pixel, at least
-// one): about 5 ms of Cornell-boxes BDPT, so a step that carries BDPT work
-// stays short and every job's next pass (time to first pass above all)
-// waits for little.
+// one) after a job's first pass: about 3 ms of Cornell-boxes BDPT, so a
+// step that carries BDPT work stays short.  A first pass is rendered whole
+// in one step (up to kBdptFirstPassSamples; about 11 ms for a 512^2 job at
+// 4 spp) on the high-priority stream, instead of one slice per step behind
+// the path-tracing wavefront.
 constexpr uint64_t kBdptStepSamples = 1u << 18;
+constexpr uint64_t kBdptFirstPassSamples = 1u << 22;
 
 // The BDPT job served next: jobs still before their first pass first, the
 // oldest request of those first (a burst then finishes its first passes one
@@ -1092,8 +1096,12 @@ SrvJob* next_bdpt(gprt_server* sv) {
 
 // Completes the pass of `n` samples queued for BDPT job j (status rc of the
 // launch): waits for it and emits its events.
-void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc) {
+void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc, cudaStream_t own) {
   if (rc == GPRT_OK) rc = gprt_job_sync(j->bd);
+  if (own) {  // back to the job's own stream (the pass ran on bd_first)
+    cudaStreamSynchronize(j->bd->stream);
+    j->bd->stream = own;
+  }
   if (rc != GPRT_OK) {
     emit(sv, j->ticket, GPRT_EV_FAILED, j->passes, j->spp_done, rc, j->submit_ms);
     release_job(sv, j);
@@ -1105,28 +1113,51 @@ void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc) {
   if (j->spp_done >= j->pass_target) advance(sv, j, true);
 }
 
-// One step: admission, one batched path-tracing wavefront and, on the BDPT
-// job's own stream at the same time, the next samples of one BDPT job's pass
-// (RenderPass of one job, progressive.go:126-223: all pixels take the pass's
-// new samples, here in slices of at most kBdptStepSamples; splats are applied
-// after each slice); then the events of both.  Returns the number of items
-// run (0: nothing to do) or a negative status.
+// Consecutive steps that may carry first passes only, before one step serves
+// the running jobs' later passes again (so that a sustained stream of
+// arrivals cannot starve them).
+constexpr uint32_t kMaxFirstsSteps = 3;
+
+// One step: admission, the next samples of one BDPT job's pass (RenderPass
+// of one job, progressive.go:126-223: all pixels take the pass's new
+// samples; splats are applied after each slice) and one batched
+// path-tracing wavefront beside it; then the events of both.  A BDPT job's
+// first pass is rendered whole, on the high-priority stream, and is queued
+// before the wavefront so that its blocks are first in line; later passes
+// go in slices of kBdptStepSamples on the job's own stream.  While any job
+// waits for its first pass, the step carries first passes only (time to
+// first pass before throughput), at most kMaxFirstsSteps steps in a row.
+// Returns the number of items run (0: nothing to do) or a negative status.
 int step_impl(gprt_server* sv, bool dry, double* ms_out) {
   if (!dry) admit(sv);
   SrvJob* bj = dry ? nullptr : next_bdpt(sv);
+  bool firsts = false;
+  if (!dry) {
+    bool waiting = bj && bj->passes == 0;
+    for (auto& kv : sv->jobs)
+      if (!waiting && kv.second->running && !kv.second->bd && kv.second->passes == 0) waiting = true;
+    firsts = waiting && sv->firsts_run < kMaxFirstsSteps;
+    sv->firsts_run = firsts ? sv->firsts_run + 1 : 0;
+    if (firsts && bj && bj->passes != 0) bj = nullptr;  // its later pass waits too
+  }
   uint32_t bn = 0;
   int brc = GPRT_OK;
-  bool launched = false;
-  int n = pt_step(sv, dry, ms_out, [&]() {
-    if (!bj) return;
-    uint64_t per = std::max<uint64_t>(1, kBdptStepSamples / std::max<uint32_t>(1, bj->npix));
+  cudaStream_t own = nullptr;
+  if (bj) {
+    bool first = bj->passes == 0;
+    uint64_t cap = first ? kBdptFirstPassSamples : kBdptStepSamples;
+    uint64_t per = std::max<uint64_t>(1, cap / std::max<uint32_t>(1, bj->npix));
     bn = (uint32_t)std::min<uint64_t>(bj->pass_target - bj->spp_done, per);
-    brc = gprt_job_add_samples(bj->bd, bn);  // queued on the job's stream
-    launched = true;
-  });
-  if (launched) finish_bdpt(sv, bj, bn, brc);
+    if (first && sv->bd_first) {
+      own = bj->bd->stream;
+      bj->bd->stream = sv->bd_first;
+    }
+    brc = gprt_job_add_samples(bj->bd, bn);  // queued on the first-pass (or the job's) stream
+  }
+  int n = pt_step(sv, dry, ms_out, firsts);
+  if (bj) finish_bdpt(sv, bj, bn, brc, own);
   if (n < 0) return n;
-  return n + (launched ? 1 : 0);
+  return n + (bj ? 1 : 0);
 }
 
 SrvJob* find_job(gprt_server* sv, uint64_t ticket) {
@@ -1179,18 +1210,26 @@ int stop_loop(gprt_server* sv) {
   return GPRT_OK;
 }
 
-int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out) {
+// Read-back of an admitted job's image: kind 0 RGBA8 (vec3ToColor), 1 the
+// mean radiance, 2 the RGBA8 of the tile rect = {x0, y0, x1, y1} (only the
+// tile's bytes are resolved and copied: extractTileImage,
+// progressive.go:225-255).
+int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out, const uint32_t* rect = nullptr) {
   std::lock_guard<std::mutex> g(sv->smu);
   gprt_ctx* ctx = sv->ctx;
   cudaSetDevice(ctx->device);
   SrvJob* j = find_job(sv, ticket);
   if (!j) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
   if (j->bd)  // BDPT: the per-job film (splats included)
-    return kind == 0 ? gprt_job_read_rgba8(j->bd, static_cast<uint8_t*>(out))
-                     : gprt_job_read_image(j->bd, static_cast<float*>(out));
+    return kind == 0   ? gprt_job_read_rgba8(j->bd, static_cast<uint8_t*>(out))
+           : kind == 1 ? gprt_job_read_image(j->bd, static_cast<float*>(out))
+                       : gprt_job_read_tile(j->bd, rect[0], rect[1], rect[2], rect[3], static_cast<uint8_t*>(out));
   if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
-  size_t npix = j->npix;
-  size_t bytes = kind == 0 ? npix * 4 : npix * 3 * sizeof(float);
+  if (kind == 2 && (rect[2] <= rect[0] || rect[3] <= rect[1] || rect[2] > (uint32_t)j->film.width ||
+                    rect[3] > (uint32_t)j->film.height))
+    return fail(ctx, GPRT_E_INVALID, "tile outside the image");
+  size_t npix = kind == 2 ? (size_t)(rect[2] - rect[0]) * (rect[3] - rect[1]) : (size_t)j->npix;
+  size_t bytes = kind == 1 ? npix * 3 * sizeof(float) : npix * 4;
   if (bytes > sv->rb_bytes) {
     cudaStreamSynchronize(sv->stream);  // the old staging buffer may still be read
     free_all(sv->rb_bufs);
@@ -1213,7 +1252,8 @@ int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out) {
   }
   uint8_t* d = sv->rb;
   if (kind == 0) launch_resolve_rgba8(j->film, d, sv->stream);
-  else launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->stream);
+  else if (kind == 1) launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->stream);
+  else launch_resolve_tile(j->film, rect[0], rect[1], rect[2], rect[3], d, sv->stream);
   cudaError_t e = cudaMemcpyAsync(sv->rb_host, d, bytes, cudaMemcpyDeviceToHost, sv->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server read-back");
@@ -1314,12 +1354,19 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   }
   cudaEventCreate(&sv->ev0);
   cudaEventCreate(&sv->ev1);
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&sv->bd_first, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+    cudaGetLastError();
+    sv->bd_first = nullptr;  // first passes then run on the job's own stream
+  }
   cudaMemsetAsync(P.counters, 0, 8 * sizeof(uint32_t), sv->stream);
   if (sv->d_stats) cudaMemsetAsync(sv->d_stats, 0, 8 * sizeof(unsigned long long), sv->stream);
   cudaError_t e = cudaStreamSynchronize(sv->stream);
   if (e != cudaSuccess) {
     free_all(b);
     cudaFreeHost(sv->h_table);
+    if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
     return cuda_fail(ctx, e, "server init");
   }
   ctx->servers.insert(sv.get());
@@ -1354,6 +1401,7 @@ int gprt_server_destroy(gprt_server* sv) {
     cudaEventDestroy(sv->ev0);
     cudaEventDestroy(sv->ev1);
     cudaStreamDestroy(sv->stream);
+    if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
   }
   {
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
@@ -1507,6 +1555,13 @@ int gprt_server_read_rgba8(gprt_server* sv, uint64_t ticket, uint8_t* rgba) {
   return read_job(sv, ticket, 0, rgba);
 }
 
+int gprt_server_read_tile(gprt_server* sv, uint64_t ticket, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                          uint8_t* rgba) {
+  if (!sv || !rgba) return GPRT_E_INVALID;
+  const uint32_t rect[4] = {x0, y0, x1, y1};
+  return read_job(sv, ticket, 2, rgba, rect);
+}
+
 int gprt_server_release(gprt_server* sv, uint64_t ticket) { return gprt_server_cancel(sv, ticket); }
 
 int gprt_server_get_stats(gprt_server* sv, gprt_server_stats* out) {
@@ -1572,7 +1627,7 @@ int gprt_server_autotune(gprt_server* sv, double max_step_ms, gprt_tune_result* 
   gprt_ctx* ctx = sv->ctx;
   cudaSetDevice(ctx->device);
   admit(sv);
-  if (pack(sv).empty()) return fail(ctx, GPRT_E_INVALID, "autotune needs admitted, unfinished jobs");
+  if (pack(sv, false).empty()) return fail(ctx, GPRT_E_INVALID, "autotune needs admitted, unfinished jobs");
   uint32_t keep_paths = sv->step_paths, keep_block = sv->block, keep_flags = sv->flags;
   // samples per ms of dry steps (no film is changed) of the current jobs
   auto rate = [&](uint32_t paths, uint32_t block, uint32_t flags, double* step_ms) -> double {
@@ -1582,7 +1637,7 @@ int gprt_server_autotune(gprt_server* sv, double max_step_ms, gprt_tune_result* 
       sv->flags = flags;
       drop_graphs(sv);
     }
-    std::vector<Item> items = pack(sv);
+    std::vector<Item> items = pack(sv, false);
     uint64_t n = 0;
     for (auto& it : items) n += (uint64_t)it.layers * it.j->npix;
     double ms = 0;

@@ -212,6 +212,7 @@ SIGNATURES = {
     "gprt_server_read_film": (C.c_int, [P, C.c_uint64, F32P, F32P, F32P, U32P]),
     "gprt_server_read_image": (C.c_int, [P, C.c_uint64, F32P]),
     "gprt_server_read_rgba8": (C.c_int, [P, C.c_uint64, U8P]),
+    "gprt_server_read_tile": (C.c_int, [P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, U8P]),
     "gprt_server_release": (C.c_int, [P, C.c_uint64]),
     "gprt_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "gprt_server_get_counters": (C.c_int, [P, C.POINTER(JobCounters), C.c_int]),

@@ -117,6 +117,25 @@ class RenderServer:
         self.ctx.check(self.ctx.lib.gprt_server_read_rgba8(self.h, ticket, out.ctypes.data_as(capi.U8P)))
         return out
 
+    def tile(self, ticket: int, x0: int, y0: int, x1: int, y1: int):
+        """RGBA8 of tile [x0, x1) x [y0, y1) (only its bytes leave the device)."""
+        out = np.zeros((y1 - y0, x1 - x0, 4), dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.gprt_server_read_tile(self.h, ticket, x0, y0, x1, y1,
+                                                          out.ctypes.data_as(capi.U8P)))
+        return out
+
+    def tiles(self, ticket: int, pass_number: int, total_passes: int, tile_size: int = 64):
+        """The TileCompletionResult events of a finished pass (progressive.go:
+        266-276), in the reference's row-major tile order: every tile of a
+        pass is complete when the job's `pass` event arrives."""
+        from .renderer import TileCompletionResult
+        h, w = self.sizes[ticket]
+        rects = [(x0, y0) for y0 in range(0, h, tile_size) for x0 in range(0, w, tile_size)]
+        for k, (x0, y0) in enumerate(rects):
+            img = self.tile(ticket, x0, y0, min(x0 + tile_size, w), min(y0 + tile_size, h))
+            yield TileCompletionResult(x0 // tile_size, y0 // tile_size, img, pass_number, k + 1, len(rects),
+                                       total_passes)
+
     def stats(self) -> dict:
         s = capi.ServerStats()
         self.ctx.check(self.ctx.lib.gprt_server_get_stats(self.h, C.byref(s)))

@@ -535,6 +535,14 @@ int gprt_server_read_film(gprt_server* server, uint64_t ticket, float* rgb_sum, 
                           uint32_t* count);
 int gprt_server_read_image(gprt_server* server, uint64_t ticket, float* rgb_mean);
 int gprt_server_read_rgba8(gprt_server* server, uint64_t ticket, uint8_t* rgba);
+/* The RGBA8 bytes of tile [x0, x1) x [y0, y1) of a job's current image
+ * (extractTileImage, pkg/renderer/progressive.go:225-255): resolved on the
+ * device, only the tile's bytes cross to the host, row-major, 4 bytes per
+ * pixel.  Every tile of a pass is complete when the job's GPRT_EV_PASS event
+ * is emitted, so a front door streams TileCompletionResult events
+ * (progressive.go:266-276) by reading the tiles after each pass event. */
+int gprt_server_read_tile(gprt_server* server, uint64_t ticket, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                          uint8_t* rgba);
 /* Frees the film of a finished (or cancels and frees a running) job. */
 int gprt_server_release(gprt_server* server, uint64_t ticket);
 int gprt_server_get_stats(gprt_server* server, gprt_server_stats* stats);

@@ -166,6 +166,31 @@ def test_pass_events_follow_the_progressive_schedule(ctx, scenes):
     sv.close()
 
 
+def test_server_tiles_are_windows_of_the_image(ctx, scenes):
+    """gprt_server_read_tile: each tile equals the same window of the whole
+    RGBA8 image (path tracing and BDPT, ragged edge tiles included), and the
+    tile events of a pass cover the image in row-major order."""
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    pt = sv.submit(scenes["spheres_a"], _cfg(4, 2, 3))
+    bd = sv.submit(scenes["cornell"], _cfg(2, 2, 5), integrator=gprt.BDPTIntegrator())
+    sv.run_until_idle()
+    for t in (pt, bd):
+        full = sv.rgba8(t)
+        h, w = full.shape[:2]
+        assert np.array_equal(sv.tile(t, 5, 3, w, h), full[3:h, 5:w])
+        tiles = list(sv.tiles(t, 2, 2, tile_size=20))
+        assert [(r.tile_x, r.tile_y) for r in tiles] == [(x, y) for y in range((h + 19) // 20)
+                                                         for x in range((w + 19) // 20)]
+        for r in tiles:
+            x0, y0 = 20 * r.tile_x, 20 * r.tile_y
+            assert np.array_equal(r.tile_image, full[y0:y0 + 20, x0:x0 + 20])
+        assert tiles[-1].tile_number == tiles[-1].total_tiles == len(tiles)
+    with pytest.raises(gprt.capi.GprtError):
+        sv.tile(pt, 0, 0, 0, 1)  # empty tile
+    sv.close()
+
+
 def test_admission_by_budget(ctx, scenes):
     import gprt
     g = scenes["spheres_a"]
