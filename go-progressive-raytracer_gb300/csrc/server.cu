@@ -1116,7 +1116,7 @@ void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc, cudaStream_t ow
 // Consecutive steps that may carry first passes only, before one step serves
 // the running jobs' later passes again (so that a sustained stream of
 // arrivals cannot starve them).
-constexpr uint32_t kMaxFirstsSteps = 3;
+constexpr uint32_t kMaxFirstsSteps = 8;
 
 // One step: admission, the next samples of one BDPT job's pass (RenderPass
 // of one job, progressive.go:126-223: all pixels take the pass's new
