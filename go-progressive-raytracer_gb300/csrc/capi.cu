@@ -24,6 +24,17 @@ int ensure_bdpt(gprt_job* j) {
   rc |= dev_alloc(ctx, b, &P.Lout, ns);
   for (int k = 0; k < 5; k++) rc |= dev_alloc(ctx, b, &B.v[k], (size_t)ns * 2 * B.maxv);
   rc |= dev_alloc(ctx, b, &B.pdf, (size_t)ns * 2 * B.maxv);
+  for (int k = 0; k < 2; k++) {
+    BdQueue& q = B.q[k];
+    rc |= dev_alloc(ctx, b, &q.o, ns);
+    rc |= dev_alloc(ctx, b, &q.d, ns);
+    rc |= dev_alloc(ctx, b, &q.beta, ns);
+    rc |= dev_alloc(ctx, b, &q.last, ns);
+    rc |= dev_alloc(ctx, b, &q.ids, ns);
+    rc |= dev_alloc(ctx, b, &q.st, ns);
+  }
+  rc |= dev_alloc(ctx, b, &B.hit, ns);
+  rc |= dev_alloc(ctx, b, &B.lorig, (size_t)ns * 3);
   rc |= dev_alloc(ctx, b, &B.meta, ns);
   rc |= dev_alloc(ctx, b, &B.masks, ns);
   rc |= dev_alloc(ctx, b, &B.contrib, (size_t)ns * (B.maxv + 1) * B.maxv);

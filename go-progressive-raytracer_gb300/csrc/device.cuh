@@ -692,6 +692,18 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, Source& src
   }
 }
 
+// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+  unsigned mask = __ballot_sync(__activemask(), want);
+  if (!want) return 0;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
 // Largest k < n with start[k] <= x (start[0] = 0, start ascending).
 __device__ __forceinline__ uint32_t find_range(const uint32_t* start, uint32_t n, uint32_t x) {
   uint32_t lo = 0, hi = n;

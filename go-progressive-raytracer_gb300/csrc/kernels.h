@@ -37,9 +37,30 @@ struct PathBuf {
 // vertices as 5 float4 fields, each indexed [vertex * ns + sample] (camera
 // vertices 0..maxv-1, light vertices maxv..2 maxv-1), per-sample metadata,
 // and one contribution slot per (strategy, sample).
+// The subpaths in flight between bounces of the BDPT subpath wavefront, one
+// slot per subpath (structure of arrays): the ray (origin = the last vertex,
+// the primitive it leaves; direction, the forward pdf of the next vertex),
+// the throughput and the MIS prefix through the vertex before the last, the
+// last vertex's normal and forward pdf, the sample (index in the chunk,
+// sampler position, pixel, sample number) and the state bits (length,
+// bounces, camera / light, connectibility of the last two vertices, whether
+// the last vertex is on a surface or at infinity; the camera subpath's
+// length for a light subpath).
+struct BdQueue {
+  float4* o;
+  float4* d;
+  float4* beta;
+  float4* last;
+  uint4* ids;
+  uint2* st;
+};
+
 struct DevBdpt {
   float4* v[5];
-  float4* pdf;    // per vertex: fwd, rev, flags | (light + 1) << 8 (int bits), the subpath's MIS prefix
+  float4* pdf;    // per vertex: fwd, flags | (light + 1) << 8 (int bits), rev, the subpath's MIS prefix
+  BdQueue q[2];   // the subpath wavefront's two queues
+  float4* hit;    // closest hit of each slot of the current queue
+  float4* lorig;  // per sample, 3 float4: the light subpath's origin (infinite lights: pdf fix-ups)
   uint4* meta;    // nc | nl << 8, sampler position after the subpaths, pixel, sample index
   uint2* masks;   // strategies that draw samples: light-tracing (bit s), direct-lighting (bit t)
   float4* contrib;
@@ -75,7 +96,8 @@ struct DevPaths {
 // of the BDPT working set of `ns` samples.
 inline int bdpt_maxv(int max_depth) { return max_depth <= 9 ? 10 : 18; }
 inline size_t bdpt_bytes(uint32_t ns, int maxv) {
-  return (size_t)ns * (6 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16) + 8 * 256;
+  return (size_t)ns * (6 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16 + 2 * 88 + 16 + 48) +
+         24 * 256;
 }
 
 constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;

@@ -13,9 +13,13 @@
 // (3 KB per thread for the strategy kernel, 245 MB at full occupancy, more
 // than L2), and that stack traffic went to DRAM.
 //
-// Four kernels per chunk of samples:
-//   k_bdpt_subpaths    one thread per sample builds both subpaths into a
-//                      global vertex store (fields indexed [vertex][sample]);
+// Per chunk of samples:
+//   k_bdpt_camgen      the camera vertex and ray of every sample;
+//   k_bdpt_trace       (per bounce) closest hits of the subpath queue;
+//   k_bdpt_extend      (per bounce) each subpath's next vertex into a global
+//                      vertex store (fields indexed [vertex][sample]) and the
+//                      continuing subpaths compacted into the other queue; a
+//                      camera subpath that ends starts its light subpath;
 //   k_bdpt_list        lists, per strategy (s,t), the samples that have it;
 //   k_bdpt_strategies  one thread per listed (strategy, sample) item, the
 //                      items of a strategy in consecutive threads: each warp
@@ -340,7 +344,7 @@ __device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, co
   B.v[3][k] = make_float4(x.Le.x, x.Le.y, x.Le.z, x.wi.y);
   B.v[4][k] = make_float4(x.wi.z, __int_as_float((x.mat + 1) | (x.flags << 24)), __int_as_float(x.light),
                           __uint_as_float(x.prim));
-  B.pdf[k] = make_float4(x.fwd, x.rev, __int_as_float(x.flags | ((x.light + 1) << 8)), pre);
+  B.pdf[k] = make_float4(x.fwd, __int_as_float(x.flags | ((x.light + 1) << 8)), x.rev, pre);
   if (B.uv) B.uv[k] = x.mat >= 0 ? x.uv : make_float2(0.f, 0.f);
 }
 
@@ -351,7 +355,7 @@ __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
   x.p = f3(a);
   x.fwd = a.w;
   x.n = f3(b);
-  x.rev = b.w;
+  x.rev = B.pdf[k].z;  // the reverse pdf lives in the pdf record (patched after the next bounce)
   x.beta = f3(c);
   x.Le = f3(d);
   x.wi = make_float3(c.w, d.w, e.x);
@@ -375,8 +379,8 @@ __device__ __forceinline__ VPdf get_vpdf(const DevBdpt& B, int v, uint32_t i) {
   float4 a = B.pdf[(size_t)v * B.ns + i];
   VPdf r;
   r.fwd = a.x;
-  r.rev = a.y;
-  int m = __float_as_int(a.z);
+  r.rev = a.z;
+  int m = __float_as_int(a.y);
   r.flags = m & 0xFF;
   r.light = (m >> 8) - 1;
   r.pre = a.w;
@@ -406,7 +410,7 @@ __device__ __forceinline__ void subpath_prefix(const DevScene& sc, const DevBdpt
   for (int k = 0; k < len; k++) {
     size_t at = (size_t)(base + k) * B.ns + i;
     float4 a = B.pdf[at];
-    int m = __float_as_int(a.z);
+    int m = __float_as_int(a.y);
     int flags = m & 0xFF, light = (m >> 8) - 1;
     bool ok = !(flags & kFlagSpecular);
     if (!camera) ok = ok && !((flags & kFlagLight) && light >= 0 && sc.lights[light].kind == kLightPointSpot);
@@ -414,7 +418,7 @@ __device__ __forceinline__ void subpath_prefix(const DevScene& sc, const DevBdpt
       acc = 0.f;  // the camera vertex takes no part in the walk
     } else {
       bool conn = ok && (k == 0 || prev_ok);
-      acc = (remap0(a.y) / remap0(a.x)) * (acc + (conn ? 1.f : 0.f));
+      acc = (remap0(a.z) / remap0(a.x)) * (acc + (conn ? 1.f : 0.f));
     }
     B.pdf[at].w = acc;
     prev_ok = ok;
@@ -430,111 +434,71 @@ struct SubpathRef {
   __device__ VPdf pdfs(int k) const { return get_vpdf(*B, base + k, i); }
 };
 
-// extendPath (bdpt.go:206-291), writing vertex `len-1` once its reverse pdf
-// is final; `prev` enters as the subpath's first vertex.  Returns the length.
-// The state of one subpath between bounces of extendPath.
-struct SubState {
-  BVert prev;  // the last vertex, written once its reverse pdf is final
-  float3 o, d, beta;
-  float pdf_fwd;
-  float pre;     // the MIS prefix over the vertices written so far (subpath_prefix)
-  bool prev_ok;  // the last written vertex is neither specular nor a delta light
-  int len, b, max_bounces, base;
-  uint32_t skip;
-  bool camera;
-};
+// ---------------------------------------------------------------- subpath wavefront
+// generateCameraPath / generateLightPath / extendPath (bdpt.go:106-291) one
+// bounce per launch over a compacted queue of subpaths: a persistent
+// closest-hit traversal of the queue, then one thread per slot extends its
+// subpath by the vertex hit, compacting the continuing subpaths into the
+// other queue.  A sample's light subpath starts, in the same sampler stream,
+// in the step that ends its camera subpath, so both kinds share the queue.
+// Each vertex is stored when it is created; its reverse pdf (set by the
+// scatter at the next vertex, bdpt.go:273-285) and its MIS prefix
+// (subpath_prefix) are patched one bounce later with one 8-byte store.
 
-// Writes the subpath's last vertex (index len - 1, its reverse pdf final)
-// with the running MIS prefix of subpath_prefix updated by it.
-__device__ __forceinline__ void emit_vert(const DevScene& sc, const DevBdpt& B, uint32_t i, SubState& st) {
-  const BVert& x = st.prev;
-  const int k = st.len - 1;
-  bool ok = !x.is(kFlagSpecular);
-  if (!st.camera) ok = ok && !(x.is(kFlagLight) && x.light >= 0 && sc.lights[x.light].kind == kLightPointSpot);
-  if (st.camera && k == 0) {
-    st.pre = 0.f;
-  } else {
-    bool conn = ok && (k == 0 || st.prev_ok);
-    st.pre = (remap0(x.rev) / remap0(x.fwd)) * (st.pre + (conn ? 1.f : 0.f));
-  }
-  st.prev_ok = ok;
-  put_vert(B, st.base + k, i, x, st.pre);
+// State bits of a queue slot (BdQueue::st.x): length, bounces, kind, and
+// properties of the last two vertices; st.y holds the camera subpath length.
+constexpr uint32_t kStCamera = 1u << 16, kStOkBefore = 1u << 17, kStOkLast = 1u << 18, kStSurfLast = 1u << 19,
+                   kStInfLast = 1u << 20;
+
+// The subpath vertex is neither specular nor (light subpaths) a delta light:
+// it can take part in a connection (bdpt_mis.go:61-178).
+__device__ __forceinline__ bool vertex_ok(const DevScene& sc, const BVert& v, bool camera) {
+  bool ok = !v.is(kFlagSpecular);
+  if (!camera) ok = ok && !(v.is(kFlagLight) && v.light >= 0 && sc.lights[v.light].kind == kLightPointSpot);
+  return ok;
 }
 
-// One bounce of extendPath (bdpt.go:206-291): returns true when the subpath
-// has ended (vertex len - 1, `prev`, is then still to be written).
+// convertSolidAngleToAreaPdf (bdpt_mis.go:341-363) towards a vertex known by
+// its position, normal and kind.
+__device__ __forceinline__ float to_area_at(float3 from, float3 p, float3 n, bool surface, bool infinite, float pdf) {
+  if (infinite) return pdf;
+  float3 d = p - from;
+  float d2 = dot(d, d);
+  if (d2 == 0.f) return 0.f;
+  float inv = 1.0f / d2;
+  if (surface) pdf *= fabsf(dot(d * sqrtf(inv), n));
+  return pdf * inv;
+}
+
+// The MIS prefix of vertex k of a subpath from the prefix `acc` through
+// vertex k - 1 (subpath_prefix's recurrence; the camera vertex has none).
+__device__ __forceinline__ float next_prefix(bool camera, int k, float rev, float fwd, bool ok, bool ok_before,
+                                             float acc) {
+  if (camera && k == 0) return 0.f;
+  bool conn = ok && (k == 0 || ok_before);
+  return (remap0(rev) / remap0(fwd)) * (acc + (conn ? 1.f : 0.f));
+}
+
+// The reverse pdf and MIS prefix of a stored vertex, once final.
+__device__ __forceinline__ void patch_vert(const DevBdpt& B, int v, uint32_t i, float rev, float pre) {
+  *reinterpret_cast<float2*>(&B.pdf[(size_t)v * B.ns + i].z) = make_float2(rev, pre);
+}
+
+// The strategies that draw uniform numbers (draws_before) and the sample's
+// record for the strategy kernels, once both subpaths are stored.
 template <int MAXV>
-__device__ __forceinline__ bool subpath_step(const DevScene& sc, const DevBdpt& B, uint32_t i, SubState& st, Rng& rng,
-                                             int* err) {
-  if (!(st.b < st.max_bounces && st.len < MAXV)) return true;
-  Hit h;
-  if (!trace<false, false>(sc, st.o, st.d, 0.001f, kInfF, st.skip, h, err)) {
-    if (st.camera) {
-      // createBackgroundVertex (bdpt.go:585-601)
-      float3 bg = background(sc, st.d);
-      BVert v;
-      v.p = st.o + st.d * 1000.f;
-      v.n = -st.d;
-      v.wi = -st.d;
-      v.fwd = st.pdf_fwd;
-      v.rev = 0.f;
-      v.beta = st.beta;
-      v.Le = bg;
-      v.mat = -1;
-      v.light = -1;
-      v.prim = kNoHit;
-      v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
-      emit_vert(sc, B, i, st);
-      st.prev = v;
-      st.len++;
+__device__ __forceinline__ void finish_sample(const DevScene& sc, const DevBdpt& B, uint32_t p, int nc, int nl,
+                                              uint32_t pos, uint32_t pix, uint32_t sample) {
+  uint32_t lm = 0, cm = 0;
+  for (int s = 2; s <= nl; s++)
+    if (!(get_vpdf(B, MAXV + s - 1, p).flags & kFlagSpecular)) lm |= 1u << s;
+  if (sc.n_lights > 0)
+    for (int t = 2; t <= nc; t++) {
+      BVert v = get_vert(B, t - 1, p);
+      if (!v.is(kFlagSpecular) && v.mat >= 0) cm |= 1u << t;
     }
-    return true;
-  }
-  Surface s;
-  const float3 d = st.d;
-  surface_at(sc, st.o, d, h, s);
-  DevMaterial m = load_material(sc, s.mat);
-  BVert v;
-  v.p = s.p;
-  v.n = s.n;
-  v.wi = -d;
-  v.beta = st.beta;
-  v.Le = emitted(m, s.front, d);
-  v.mat = s.mat;
-  v.uv = s.uv;
-  v.light = -1;
-  v.prim = h.prim;
-  v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
-  v.rev = 0.f;
-  v.fwd = to_area(sc, st.prev, v, st.pdf_fwd);
-  Scatter scn;
-  if (!scatter(sc, m, d, s, rng, scn)) {
-    emit_vert(sc, B, i, st);
-    st.prev = v;
-    st.len++;
-    return true;
-  }
-  st.pdf_fwd = scn.pdf;
-  if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
-  float ct = fabsf(dot(scn.dir, s.n));
-  if (scn.pdf <= 0.f) st.beta = st.beta * scn.att;
-  else st.beta = st.beta * scn.att * (ct / scn.pdf);
-  bool rdelta;
-  float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
-  if (rdelta) {
-    v.flags |= kFlagSpecular;
-    pdf_rev = 0.f;
-    st.pdf_fwd = 0.f;
-  }
-  st.prev.rev = to_area(sc, v, st.prev, pdf_rev);
-  emit_vert(sc, B, i, st);
-  st.prev = v;
-  st.len++;
-  st.o = s.p;
-  st.d = scn.dir;
-  st.skip = h.prim;
-  st.b++;
-  return false;
+  B.meta[p] = make_uint4((uint32_t)nc | ((uint32_t)nl << 8), pos, pix, sample);
+  B.masks[p] = make_uint2(lm, cm);
 }
 
 // calculateMISWeight (bdpt_mis.go:13-181) over the stored subpaths
@@ -789,148 +753,298 @@ __device__ __forceinline__ float3 eval_strategy(const DevScene& sc, const DevFil
   return Lc * w;
 }
 
-// generateCameraPath + generateLightPath (bdpt.go:106-202) for every sample
-// of the chunk, in the reference's draw order; records the subpath lengths,
-// the sampler position the strategies start from and the strategy draw masks.
-// Persistent: each lane advances its own sample one bounce at a time and,
-// when that sample's subpaths are done, takes the next sample from a
-// warp-aggregated counter, so a warp is not held by its longest path.
+// generateCameraPath (bdpt.go:106-135): the camera vertex and ray of every
+// sample of the chunk, queue 0 slot p = sample p.
 template <int MAXV>
-__global__ void __launch_bounds__(128, 4) k_bdpt_subpaths(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
+__global__ void k_bdpt_camgen(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
-  uint32_t* next = B.scount + (MAXV + 1) * MAXV;  // the work counter, zeroed with the lists
-  int* err = reinterpret_cast<int*>(PS.counters + 3);
-  int phase = -1;  // -1: needs a sample, 0: camera subpath, 1: light subpath
-  uint32_t p = 0, pix = 0, sample = 0;
-  int nc = 0;
-  Rng rng;
-  SubState st;
-  // the light subpath's start, for the infinite-light corrections after it
-  float3 ep = f3(0.f, 0.f, 0.f), en = f3(0.f, 0.f, 0.f), ed = f3(0.f, 0.f, 0.f);
-  float apdf = 0.f, lprob = 1.f;
-  bool inf = false;
-  for (;;) {
-    if (phase < 0) {
-      unsigned act = __activemask();
-      int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
-      uint32_t at = 0;
-      if (lane == leader) at = atomicAdd(next, (uint32_t)__popc(act));
-      at = __shfl_sync(act, at, leader);
-      p = at + (uint32_t)__popc(act & ((1u << lane) - 1u));
-      if (p >= n) break;
-      uint32_t layer = p / ch.npix, i = p - layer * ch.npix;
-      pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
-      sample = film.count[pix] + layer;
-      int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
-      rng.init(ch.seed, pix, sample);
-      float2 lens = rng.next2();
-      float2 jit = rng.next2();
-      float3 o, d;
-      camera_ray(sc.cam, x, y, lens, jit, o, d);
-      // generateCameraPath (bdpt.go:106-135)
-      BVert& c = st.prev;
-      c.p = o;
-      c.n = -d;
-      c.wi = f3(0.f, 0.f, 0.f);
-      c.beta = f3(1.f, 1.f, 1.f);
-      c.Le = f3(0.f, 0.f, 0.f);
-      c.fwd = 0.f;
-      c.rev = 0.f;
-      c.mat = -1;
-      c.light = -1;
-      c.prim = kNoHit;
-      c.flags = kFlagCamera;
-      st.o = o;
-      st.d = d;
-      st.beta = f3(1.f, 1.f, 1.f);
-      st.pdf_fwd = camera_dir_pdf(sc.cam, o, d);
-      st.len = 1;
-      st.b = 0;
-      st.max_bounces = sc.max_depth;
-      st.base = 0;
-      st.skip = kNoHit;
-      st.camera = true;
-      st.pre = 0.f;
-      st.prev_ok = true;
-      inf = false;
-      phase = 0;
+  const BdQueue& Q = B.q[0];
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    uint32_t layer = p / ch.npix, i = p - layer * ch.npix;
+    uint32_t pix = ch.pix_list ? ch.pix_list[ch.pix0 + i] : ch.pix0 + i;
+    uint32_t sample = film.count[pix] + layer;
+    int x = (int)(pix % (uint32_t)film.width), y = (int)(pix / (uint32_t)film.width);
+    Rng rng;
+    rng.init(ch.seed, pix, sample);
+    float2 lens = rng.next2();
+    float2 jit = rng.next2();
+    float3 o, d;
+    camera_ray(sc.cam, x, y, lens, jit, o, d);
+    BVert c;
+    c.p = o;
+    c.n = -d;
+    c.wi = f3(0.f, 0.f, 0.f);
+    c.beta = f3(1.f, 1.f, 1.f);
+    c.Le = f3(0.f, 0.f, 0.f);
+    c.uv = make_float2(0.f, 0.f);
+    c.fwd = 0.f;
+    c.rev = 0.f;
+    c.mat = -1;
+    c.light = -1;
+    c.prim = kNoHit;
+    c.flags = kFlagCamera;
+    put_vert(B, 0, p, c, 0.f);
+    Q.o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
+    Q.d[p] = make_float4(d.x, d.y, d.z, camera_dir_pdf(sc.cam, o, d));
+    Q.beta[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    Q.last[p] = make_float4(c.n.x, c.n.y, c.n.z, 0.f);
+    Q.ids[p] = make_uint4(p, rng.pos, pix, sample);
+    Q.st[p] = make_uint2(1u | kStCamera | kStOkBefore | kStOkLast, 0u);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    PS.counters[0] = n;
+    PS.counters[1] = 0;
+    PS.counters[4] = 0;
+  }
+}
+
+// The rays of the subpath queue; the marker hit of a stack overflow sets the
+// job's error bits and is stored as a miss.
+struct BdptSource {
+  const float4* o;
+  const float4* d;
+  float4* hit;
+  const uint32_t* n;
+  int root;
+  int* err;
+  __device__ uint32_t count() const { return *n; }
+  __device__ void load(uint32_t i, float3& ro, float3& rd, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
+    float4 a = o[i], b = d[i];
+    ro = f3(a);
+    rd = f3(b);
+    tmin = 0.001f;
+    tmax = kInfF;
+    skip = __float_as_uint(a.w);
+    rt = root;
+  }
+  __device__ void store(uint32_t i, const Hit& h) const {
+    bool any = h.prim != kNoHit;
+    if (h.prim == kOverflowHit) {
+      atomicOr(err, kErrStackOverflow);
+      any = false;
     }
-    if (!subpath_step<MAXV>(sc, B, p, st, rng, err)) continue;
-    emit_vert(sc, B, p, st);
-    int nl = 0;
-    if (phase == 0) {
-      nc = st.len;
-      if (sc.n_lights > 0) {
-        // generateLightPath (bdpt.go:139-202), in the same sampler stream
-        float ul = rng.next();
-        int li = pick_light(sc, ul);
-        DevLight L = sc.lights[li];
-        float2 sp = rng.next2();
-        float2 sd = rng.next2();
-        float3 Le;
-        float dpdf;
-        sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
-        float ct = fabsf(dot(ed, en));
-        BVert& lv = st.prev;
-        lv.p = ep;
-        lv.n = en;
-        lv.wi = f3(0.f, 0.f, 0.f);
-        lv.light = li;
-        lv.mat = -1;
-        lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
-                  : L.kind == kLightSphere ? (L.prim >= 0 ? sc.sphere_base + (uint32_t)L.prim : kNoHit)
-                  : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
-                                                                       : kNoHit;
-        lv.fwd = apdf * L.prob;
-        lv.rev = 0.f;
-        inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
-        lv.flags = kFlagLight | (inf ? kFlagInfinite : 0);
-        lv.beta = Le;
-        lv.Le = Le;
-        lprob = L.prob;
-        st.o = ep;
-        st.d = ed;
-        st.beta = Le * (ct / (L.prob * apdf * dpdf));
-        st.pdf_fwd = dpdf;
-        st.len = 1;
-        st.b = 0;
-        st.max_bounces = sc.max_depth - 1;
-        st.base = MAXV;
-        st.skip = lv.prim;
-        st.camera = false;
-        st.pre = 0.f;
-        st.prev_ok = true;
-        phase = 1;
-        continue;
-      }
-    } else {
-      nl = st.len;
-      if (inf) {
-        if (nl > 1) {
-          BVert fb = get_vert(B, MAXV + 1, p);
-          fb.fwd = apdf * lprob;
-          if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
-          put_vert(B, MAXV + 1, p, fb);
+    hit[i] = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), h.u, h.v);
+  }
+};
+
+__global__ void __launch_bounds__(128, 8) k_bdpt_trace(DevScene sc, BdptSource src, uint32_t* counters, int cur) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) counters[cur ^ 1] = 0;  // the next queue starts empty
+  trace_persistent<false, false>(sc, src, counters + 4, nullptr, nullptr);
+}
+
+// One bounce of extendPath (bdpt.go:206-291) for every subpath of queue
+// `cur`: the vertex hit (or the camera subpath's background vertex,
+// createBackgroundVertex bdpt.go:585-601), its scatter, the reverse pdf of
+// the vertex before it; continuing subpaths move to queue cur ^ 1.  A camera
+// subpath that ends starts the sample's light subpath (generateLightPath,
+// bdpt.go:139-202); a light subpath that ends gets the infinite-light pdf
+// fix-ups and completes its sample.
+template <int MAXV>
+__global__ void __launch_bounds__(128, 4) k_bdpt_extend(DevScene sc, DevPaths PS, ChunkDesc ch, int cur) {
+  const DevBdpt& B = PS.bd;
+  const BdQueue& Q = B.q[cur];
+  const BdQueue& N = B.q[cur ^ 1];
+  const uint32_t n = PS.counters[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) PS.counters[4] = 0;  // the next traversal's ray fetch counter
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    bool live = i < n;
+    bool cont = false;
+    float4 no = make_float4(0.f, 0.f, 0.f, 0.f), nd = no, nb = no, nl4 = no;
+    uint4 nids = make_uint4(0, 0, 0, 0);
+    uint2 nst = make_uint2(0, 0);
+    if (live) {
+      float4 o4 = Q.o[i], d4 = Q.d[i], b4 = Q.beta[i], l4 = Q.last[i], h4 = B.hit[i];
+      uint4 ids = Q.ids[i];
+      uint2 st2 = Q.st[i];
+      const uint32_t p = ids.x;
+      Rng rng;
+      rng.init(ch.seed, ids.z, ids.w, ids.y);
+      const uint32_t bits = st2.x;
+      bool camera = bits & kStCamera;
+      int len = (int)(bits & 0xFF), b = (int)((bits >> 8) & 0xFF);
+      int nc = (int)st2.y;
+      const int vb = camera ? 0 : MAXV;  // vertex base of the subpath
+      const int max_bounces = camera ? sc.max_depth : sc.max_depth - 1;
+      float3 o = f3(o4), d = f3(d4), beta = f3(b4);
+      float pdf_fwd = d4.w, acc = b4.w;
+      bool ok_before = bits & kStOkBefore, ok_last = bits & kStOkLast;
+      bool surf_last = bits & kStSurfLast, inf_last = bits & kStInfLast;
+      float3 last_n = f3(l4);
+      float last_fwd = l4.w;
+      bool ended = true;
+      uint32_t prim = __float_as_uint(h4.y);
+      float rev_last = 0.f;  // the reverse pdf of the last vertex (0 unless the new vertex scatters)
+      BVert v;
+      bool has_v = false, v_ok = false;
+      if (prim == kNoHit) {
+        if (camera) {  // createBackgroundVertex (bdpt.go:585-601)
+          float3 bg = background(sc, d);
+          v.p = o + d * 1000.f;
+          v.n = -d;
+          v.wi = -d;
+          v.fwd = pdf_fwd;
+          v.rev = 0.f;
+          v.beta = beta;
+          v.Le = bg;
+          v.uv = make_float2(0.f, 0.f);
+          v.mat = -1;
+          v.light = -1;
+          v.prim = kNoHit;
+          v.flags = kFlagInfinite | (is_zero(bg) ? 0 : kFlagLight);
+          has_v = true;
         }
-        BVert l0 = get_vert(B, MAXV, p);
-        l0.fwd = infinite_density(sc, ep, en, ed);
-        put_vert(B, MAXV, p, l0);
-        subpath_prefix(sc, B, MAXV, nl, p, false);  // the corrected pdfs change every prefix
+      } else {
+        Hit h{h4.x, prim, h4.z, h4.w};
+        Surface s;
+        surface_at(sc, o, d, h, s);
+        DevMaterial m = load_material(sc, s.mat);
+        v.p = s.p;
+        v.n = s.n;
+        v.wi = -d;
+        v.beta = beta;
+        v.Le = emitted(m, s.front, d);
+        v.mat = s.mat;
+        v.uv = s.uv;
+        v.light = -1;
+        v.prim = prim;
+        v.flags = (s.front ? kFlagFront : 0) | (is_zero(v.Le) ? 0 : kFlagLight);
+        v.rev = 0.f;
+        v.fwd = to_area_at(o, v.p, v.n, v.mat >= 0, false, pdf_fwd);
+        has_v = true;
+        Scatter scn;
+        if (scatter(sc, m, d, s, rng, scn)) {
+          float npdf = scn.pdf;
+          if (scn.pdf <= 0.f) v.flags |= kFlagSpecular;
+          float ct = fabsf(dot(scn.dir, s.n));
+          float3 nbeta = scn.pdf <= 0.f ? beta * scn.att : beta * scn.att * (ct / scn.pdf);
+          bool rdelta;
+          float pdf_rev = mat_pdf(sc, m, scn.dir, -d, s.n, rdelta);
+          if (rdelta) {
+            v.flags |= kFlagSpecular;
+            pdf_rev = 0.f;
+            npdf = 0.f;
+          }
+          rev_last = to_area_at(v.p, o, last_n, surf_last, inf_last, pdf_rev);
+          if (b + 1 < max_bounces && len + 1 < MAXV) {
+            ended = false;
+            no = make_float4(s.p.x, s.p.y, s.p.z, __uint_as_float(prim));
+            nd = make_float4(scn.dir.x, scn.dir.y, scn.dir.z, npdf);
+            beta = nbeta;
+          }
+        }
+      }
+      // the last vertex is final now: its reverse pdf and MIS prefix
+      float pre_last = next_prefix(camera, len - 1, rev_last, last_fwd, ok_last, ok_before, acc);
+      patch_vert(B, vb + len - 1, p, rev_last, pre_last);
+      if (has_v) {
+        v_ok = vertex_ok(sc, v, camera);
+        // a vertex that ends its subpath is stored with its final prefix
+        float pre_v = ended ? next_prefix(camera, len, 0.f, v.fwd, v_ok, ok_last, pre_last) : 0.f;
+        put_vert(B, vb + len, p, v, pre_v);
+        len++;
+      }
+      if (!ended) {
+        nb = make_float4(beta.x, beta.y, beta.z, pre_last);
+        nl4 = make_float4(v.n.x, v.n.y, v.n.z, v.fwd);
+        nids = make_uint4(p, rng.pos, ids.z, ids.w);
+        nst = make_uint2((uint32_t)len | ((uint32_t)(b + 1) << 8) | (camera ? kStCamera : 0u) |
+                             (ok_last ? kStOkBefore : 0u) | (v_ok ? kStOkLast : 0u) | (v.mat >= 0 ? kStSurfLast : 0u),
+                         (uint32_t)nc);
+        cont = true;
+      } else if (camera) {
+        nc = len;
+        if (sc.n_lights > 0) {
+          // generateLightPath (bdpt.go:139-202), in the same sampler stream
+          int li = pick_light(sc, rng.next());
+          DevLight L = sc.lights[li];
+          float2 sp = rng.next2();
+          float2 sd = rng.next2();
+          float3 ep, en, ed, Le;
+          float apdf, dpdf;
+          sample_emission(sc, L, sp, sd, ep, en, ed, Le, apdf, dpdf);
+          float ct = fabsf(dot(ed, en));
+          BVert lv;
+          lv.p = ep;
+          lv.n = en;
+          lv.wi = f3(0.f, 0.f, 0.f);
+          lv.uv = make_float2(0.f, 0.f);
+          lv.light = li;
+          lv.mat = -1;
+          lv.prim = L.kind == kLightQuad     ? sc.quad_base + (uint32_t)L.prim
+                    : L.kind == kLightSphere ? (L.prim >= 0 ? sc.sphere_base + (uint32_t)L.prim : kNoHit)
+                    : (L.kind == kLightDisc || L.kind == kLightDiscSpot) ? sc.quadric_base + (uint32_t)L.prim
+                                                                         : kNoHit;
+          lv.fwd = apdf * L.prob;
+          lv.rev = 0.f;
+          bool inf = L.kind == kLightUniformInfinite || L.kind == kLightGradientInfinite;
+          lv.flags = kFlagLight | (inf ? kFlagInfinite : 0);
+          lv.beta = Le;
+          lv.Le = Le;
+          bool lok = vertex_ok(sc, lv, false);
+          bool lsurf = light_is_area(sc, li);
+          if (inf) {
+            B.lorig[3 * (size_t)p] = make_float4(ep.x, ep.y, ep.z, apdf);
+            B.lorig[3 * (size_t)p + 1] = make_float4(en.x, en.y, en.z, L.prob);
+            B.lorig[3 * (size_t)p + 2] = make_float4(ed.x, ed.y, ed.z, 0.f);
+          }
+          if (0 < sc.max_depth - 1 && 1 < MAXV) {
+            put_vert(B, MAXV, p, lv, 0.f);
+            float3 lb = Le * (ct / (L.prob * apdf * dpdf));
+            no = make_float4(ep.x, ep.y, ep.z, __uint_as_float(lv.prim));
+            nd = make_float4(ed.x, ed.y, ed.z, dpdf);
+            nb = make_float4(lb.x, lb.y, lb.z, 0.f);
+            nl4 = make_float4(en.x, en.y, en.z, lv.fwd);
+            nids = make_uint4(p, rng.pos, ids.z, ids.w);
+            nst = make_uint2(1u | kStOkBefore | (lok ? kStOkLast : 0u) | (lsurf ? kStSurfLast : 0u) |
+                                 (inf ? kStInfLast : 0u),
+                             (uint32_t)nc);
+            cont = true;
+          } else {  // a light subpath of the light vertex alone
+            put_vert(B, MAXV, p, lv, next_prefix(false, 0, 0.f, lv.fwd, lok, true, 0.f));
+            if (inf) {  // the fix-up of the light vertex (bdpt.go:188-199)
+              BVert l0 = get_vert(B, MAXV, p);
+              l0.fwd = infinite_density(sc, ep, en, ed);
+              put_vert(B, MAXV, p, l0);
+              subpath_prefix(sc, B, MAXV, 1, p, false);
+            }
+            finish_sample<MAXV>(sc, B, p, nc, 1, rng.pos, ids.z, ids.w);
+          }
+        } else {
+          finish_sample<MAXV>(sc, B, p, nc, 0, rng.pos, ids.z, ids.w);
+        }
+      } else {
+        int nl = len;
+        if (get_vpdf(B, MAXV, p).flags & kFlagInfinite) {
+          // the infinite-light fix-ups of generateLightPath (bdpt.go:188-199)
+          float4 e0 = B.lorig[3 * (size_t)p], e1 = B.lorig[3 * (size_t)p + 1], e2 = B.lorig[3 * (size_t)p + 2];
+          float3 ep = f3(e0), en = f3(e1), ed = f3(e2);
+          float apdf = e0.w, lprob = e1.w;
+          if (nl > 1) {
+            BVert fb = get_vert(B, MAXV + 1, p);
+            fb.fwd = apdf * lprob;
+            if (fb.mat >= 0) fb.fwd *= fabsf(dot(ed, fb.n));
+            put_vert(B, MAXV + 1, p, fb);
+          }
+          BVert l0 = get_vert(B, MAXV, p);
+          l0.fwd = infinite_density(sc, ep, en, ed);
+          put_vert(B, MAXV, p, l0);
+          subpath_prefix(sc, B, MAXV, nl, p, false);  // the corrected pdfs change every prefix
+        }
+        finish_sample<MAXV>(sc, B, p, nc, nl, rng.pos, ids.z, ids.w);
       }
     }
-    // which strategies draw uniform numbers (draws_before)
-    uint32_t lm = 0, cm = 0;
-    for (int s = 2; s <= nl; s++)
-      if (!get_vert(B, MAXV + s - 1, p).is(kFlagSpecular)) lm |= 1u << s;
-    if (sc.n_lights > 0)
-      for (int t = 2; t <= nc; t++) {
-        BVert v = get_vert(B, t - 1, p);
-        if (!v.is(kFlagSpecular) && v.mat >= 0) cm |= 1u << t;
-      }
-    B.meta[p] = make_uint4((uint32_t)nc | ((uint32_t)nl << 8), rng.pos, pix, sample);
-    B.masks[p] = make_uint2(lm, cm);
-    phase = -1;
+    // continuing subpaths to consecutive slots of the next queue (one atomic per warp)
+    uint32_t slot = warp_append(&PS.counters[cur ^ 1], live && cont);
+    if (live && cont) {
+      N.o[slot] = no;
+      N.d[slot] = nd;
+      N.beta[slot] = nb;
+      N.last[slot] = nl4;
+      N.ids[slot] = nids;
+      N.st[slot] = nst;
+    }
   }
 }
 
@@ -1051,37 +1165,47 @@ __global__ void k_bdpt_sum(DevPaths PS, ChunkDesc ch) {
   }
 }
 
+template <int MAXV>
+void launch_bdpt_maxv(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int sms,
+                      cudaStream_t st) {
+  const uint32_t n = ch.npix * ch.layers;
+  const int gs = launch_grid(n, 128, std::max(1, sms * 8));  // grid-stride kernels over the queue
+  const int gt = std::max(1, sms * 8);                       // persistent traversal
+  const int g2 = std::max(1, sms * 16);
+  const int g3 = launch_grid(n, 256, 0);
+  const int gl = std::min(launch_grid(n, 1024, 0), std::max(1, sms * 2));
+  k_bdpt_camgen<MAXV><<<g3, 256, 0, st>>>(sc, film, P, ch);
+  int cur = 0;
+  // at most max_depth camera bounces, then max_depth - 1 light bounces
+  for (int it = 0; it < 2 * sc.max_depth; it++) {
+    BdptSource src{P.bd.q[cur].o, P.bd.q[cur].d, P.bd.hit, P.counters + cur, sc.root,
+                   reinterpret_cast<int*>(P.counters + 3)};
+    k_bdpt_trace<<<gt, 128, 0, st>>>(sc, src, P.counters, cur);
+    k_bdpt_extend<MAXV><<<gs, 128, 0, st>>>(sc, P, ch, cur);
+    cur ^= 1;
+  }
+  k_bdpt_list<MAXV><<<gl, 1024, 0, st>>>(P, ch);
+  k_bdpt_strategies<MAXV, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
+  k_bdpt_strategies<MAXV, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
+  k_bdpt_strategies<MAXV, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
+  k_bdpt_strategies<MAXV, 3><<<g2, 128, 0, st>>>(sc, film, P, ch);
+  k_bdpt_sum<MAXV><<<g3, 256, 0, st>>>(P, ch);
+}
+
 }  // namespace
 
+// Subpaths as a wavefront (camera rays, then per bounce: traversal and
+// extension over the compacted queue), per-strategy lists, one launch per
+// strategy class, the per-sample sums.
 void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
                  cudaStream_t st) {
-  uint32_t n = ch.npix * ch.layers;
   (void)block;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int g1 = std::min(launch_grid(n, 128, 0), std::max(1, sms * 8));  // persistent subpath kernel
-  int g2 = std::max(1, sms * 16);
-  int g3 = launch_grid(n, 256, 0);
-  int gl = std::min(launch_grid(n, 1024, 0), std::max(1, sms * 2));
   cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * ((P.bd.maxv + 1) * P.bd.maxv + 1), st);
-  if (P.bd.maxv == 10) {
-    k_bdpt_subpaths<10><<<g1, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_list<10><<<gl, 1024, 0, st>>>(P, ch);
-    k_bdpt_strategies<10, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<10, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<10, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<10, 3><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_sum<10><<<g3, 256, 0, st>>>(P, ch);
-  } else {
-    k_bdpt_subpaths<18><<<g1, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_list<18><<<gl, 1024, 0, st>>>(P, ch);
-    k_bdpt_strategies<18, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<18, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<18, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_strategies<18, 3><<<g2, 128, 0, st>>>(sc, film, P, ch);
-    k_bdpt_sum<18><<<g3, 256, 0, st>>>(P, ch);
-  }
+  if (P.bd.maxv == 10) launch_bdpt_maxv<10>(sc, film, P, ch, sms, st);
+  else launch_bdpt_maxv<18>(sc, film, P, ch, sms, st);
 }
 
 }  // namespace gprt

@@ -116,18 +116,6 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q,
   out.ids = make_uint4(ids.x, ids.y, rng.pos, ids.w);
 }
 
-// Warp-aggregated append: one atomic per warp, lanes get consecutive slots.
-__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
-  unsigned mask = __ballot_sync(__activemask(), want);
-  if (!want) return 0;
-  int lane = threadIdx.x & 31;
-  int leader = __ffs(mask) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-  base = __shfl_sync(mask, base, leader);
-  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
-}
-
 // Moves a continuing path to the next queue (a finished path leaves its
 // radiance at its origin index) and queues its shadow ray.  Called by every
 // lane of the warp; `live` is false for lanes without a path.
