@@ -77,7 +77,7 @@ struct DevPaths {
   float4* Lout;    // radiance of every finished path, by origin index
   float4* sh_o;    // shadow ray origin.xyz, tmax
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
-  float4* sh_c;    // contribution rgb, target: slot of the next queue, or origin index | kShadowToOrigin
+  float4* sh_c;    // contribution rgb, origin index of its path (uint bits)
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
   uint32_t* order; // slots of the queue with hits first, misses last (null: queue order)
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch, [6],[7] order
@@ -102,7 +102,6 @@ inline size_t bdpt_bytes(uint32_t ns, int maxv) {
 
 constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;
 
-constexpr uint32_t kShadowToOrigin = 0x80000000u;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 

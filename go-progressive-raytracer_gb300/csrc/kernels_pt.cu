@@ -288,9 +288,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     uint32_t i = base + threadIdx.x;
     ShadeOut o;
-    o.cont = o.shadow = false;
+    o.cont = false;
     bool live = i < n;
-    if (live) shade_path(sc, P.q[cur], P.hit, P.order ? P.order[i] : i, ch.seed, bounce, o);
+    if (live) shade_path(sc, P, P.q[cur], P.hit, P.order ? P.order[i] : i, ch.seed, bounce, o);
     push_shade_out(P, cur, live, o);
   }
 }
@@ -303,8 +303,8 @@ void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch,
   if (sc.has_infinite) launch_hit_order(P, cur, P.capacity, sm_count_current(), st);
   else Po.order = nullptr;
   if (P.variant & GPRT_JOB_SHADE_OCCUPANCY) {
-    int g = std::max(1, (int)((int64_t)grid * block / 128));
-    k_pt_shade<128, 6><<<g, 128, 0, st>>>(sc, Po, ch, cur, bounce);
+    int g = std::max(1, (int)((int64_t)grid * block / 192));
+    k_pt_shade<192, 3><<<g, 192, 0, st>>>(sc, Po, ch, cur, bounce);
   } else {
     k_pt_shade<256, 2><<<grid, std::min(block, 256), 0, st>>>(sc, Po, ch, cur, bounce);
   }
@@ -318,11 +318,9 @@ struct ShadowSource {
   const float4* sh_d;
   const float4* sh_c;
   const int* sh_root;  // null: every ray starts at `root`
-  float4* Lnext;       // radiance of the continuing paths (the next queue)
-  float4* Lout;        // radiance of finished paths, by origin index
+  float4* Lout;        // radiance of the paths, by origin index
   const uint32_t* n;
   int root;
-  const float4* Wnext;  // weights of the next queue (origin index in .w), read when reporting a bound
   ErrSink err;
   __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
@@ -334,16 +332,16 @@ struct ShadowSource {
     tmax = a.w;
     skip = __float_as_uint(b.w);
   }
+  // one shadow ray per path and bounce: the read-modify-write of its origin
+  // slot meets no other ray of the launch
   __device__ void store(uint32_t i, const Hit& h) const {
     if (h.prim == kOverflowHit) {  // the visibility is unknown: fail the path's job
-      uint32_t t = __float_as_uint(sh_c[i].w);
-      err.report((t & kShadowToOrigin) ? (t & ~kShadowToOrigin) : __float_as_uint(Wnext[t].w), kErrStackOverflow);
+      err.report(__float_as_uint(sh_c[i].w), kErrStackOverflow);
       return;
     }
     if (h.prim != kNoHit) return;  // occluded
     float4 c = sh_c[i];
-    uint32_t t = __float_as_uint(c.w);
-    float4* dst = (t & kShadowToOrigin) ? Lout + (t & ~kShadowToOrigin) : Lnext + t;
+    float4* dst = Lout + __float_as_uint(c.w);
     float4 L = *dst;
     *dst = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.f);
   }
@@ -383,8 +381,7 @@ __global__ void __launch_bounds__(256)
 }
 
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
-  ShadowSource src{P.sh_o,    P.sh_d,          P.sh_c,      P.sh_root, P.q[cur ^ 1].L, P.Lout, P.counters + 2,
-                   sc.root, P.q[cur ^ 1].weight, err_sink(P)};
+  ShadowSource src{P.sh_o, P.sh_d, P.sh_c, P.sh_root, P.Lout, P.counters + 2, sc.root, err_sink(P)};
   if (P.variant & GPRT_JOB_SIMPLE_SHADOW) {
     int b = std::min(block, 256);
     if (P.stats) k_pt_shadow_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, P.stats);

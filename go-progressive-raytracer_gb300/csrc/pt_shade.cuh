@@ -8,29 +8,26 @@
 
 namespace gprt {
 
-// The state a shading step leaves: the continuing path (when `cont`) and the
-// shadow ray whose contribution is added when it is unoccluded.
+// The state a shading step leaves: the continuing path (when `cont`).  Its
+// shadow ray is queued as soon as next-event estimation produces it.
 struct ShadeOut {
-  bool cont, shadow;
+  bool cont;
   float4 o, d, w;  // next ray origin (+ skip prim), direction (+ BVH root), weight (+ origin index)
   float3 thr, L;
   uint4 ids;
-  float3 sh_o, sh_d, sh_c;
-  float sh_t;
-  uint32_t sh_skip;
 };
 
 // One level of rayColorRecursive (pkg/integrator/path_tracing.go:35-104) with
 // CalculateDirectLighting (:116-157), CalculateIndirectLighting (:160-189)
 // and ApplyRussianRoulette (:193-220), for slot i of queue Q at depth index
 // `bounce` (= MaxDepth - depth).  The Russian-roulette draw happens first at
-// every level, as in the reference.
-__device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q, const float4* hits, uint32_t i,
-                                           uint64_t seed, int bounce, ShadeOut& out) {
+// every level, as in the reference.  The shadow ray of next-event estimation
+// goes to P's shadow queue at once (its contribution, when unoccluded, is
+// added to the path's radiance at its origin index), so its state is not
+// held to the end of the step.
+__device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P, const PathBuf& Q,
+                                           const float4* hits, uint32_t i, uint64_t seed, int bounce, ShadeOut& out) {
   out.cont = false;
-  out.shadow = false;
-  out.sh_skip = kNoHit;
-  out.sh_t = 0.f;
   float4 o4 = Q.ray_o[i], d4 = Q.ray_d[i], h4 = hits[i], w4 = Q.weight[i];
   uint4 ids = Q.ids[i];
   float3 d = f3(d4);
@@ -80,13 +77,12 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q,
                 float w = power_heuristic(ls.pdf, mp);
                 float3 f = brdf(sc, m, d, ls.dir, s, true);
                 float3 c = W * (f * ls.emission) * (cosine * w / ls.pdf);
-                if (!is_zero(c)) {
-                  out.shadow = true;
-                  out.sh_o = s.p;
-                  out.sh_d = ls.dir;
-                  out.sh_t = ls.dist - 0.001f;
-                  out.sh_c = c;
-                  out.sh_skip = prim;
+                if (!is_zero(c)) {  // one warp-aggregated append among the lanes here
+                  uint32_t ss = warp_append(&P.counters[2], true);
+                  P.sh_o[ss] = make_float4(s.p.x, s.p.y, s.p.z, ls.dist - 0.001f);
+                  P.sh_d[ss] = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(prim));
+                  P.sh_c[ss] = make_float4(c.x, c.y, c.z, w4.w);  // w4.w: the origin index
+                  if (P.sh_root) P.sh_root[ss] = __float_as_int(d4.w);
                 }
               }
             }
@@ -116,13 +112,13 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const PathBuf& Q,
   out.ids = make_uint4(ids.x, ids.y, rng.pos, ids.w);
 }
 
-// Moves a continuing path to the next queue (a finished path leaves its
-// radiance at its origin index) and queues its shadow ray.  Called by every
-// lane of the warp; `live` is false for lanes without a path.
+// Moves a continuing path to the next queue; a finished path adds its
+// radiance at its origin index (where its unoccluded shadow rays add
+// theirs; raygen clears it).  Called by every lane of the warp; `live` is
+// false for lanes without a path.
 __device__ __forceinline__ void push_shade_out(const DevPaths& P, int cur, bool live, const ShadeOut& o) {
   bool cont = live && o.cont;
   uint32_t slot = warp_append(&P.counters[cur ^ 1], cont);
-  uint32_t origin = __float_as_uint(o.w.w);
   if (cont) {
     const PathBuf& N = P.q[cur ^ 1];
     N.ray_o[slot] = o.o;
@@ -132,16 +128,9 @@ __device__ __forceinline__ void push_shade_out(const DevPaths& P, int cur, bool 
     N.L[slot] = make_float4(o.L.x, o.L.y, o.L.z, 0.f);
     N.ids[slot] = o.ids;
   } else if (live) {
-    P.Lout[origin] = make_float4(o.L.x, o.L.y, o.L.z, 0.f);
-  }
-  bool sh = live && o.shadow;
-  uint32_t ss = warp_append(&P.counters[2], sh);
-  if (sh) {
-    uint32_t target = cont ? slot : (origin | kShadowToOrigin);
-    P.sh_o[ss] = make_float4(o.sh_o.x, o.sh_o.y, o.sh_o.z, o.sh_t);
-    P.sh_d[ss] = make_float4(o.sh_d.x, o.sh_d.y, o.sh_d.z, __uint_as_float(o.sh_skip));
-    P.sh_c[ss] = make_float4(o.sh_c.x, o.sh_c.y, o.sh_c.z, __uint_as_float(target));
-    if (P.sh_root) P.sh_root[ss] = __float_as_int(o.d.w);
+    float4* dst = P.Lout + __float_as_uint(o.w.w);
+    float4 a = *dst;
+    *dst = make_float4(a.x + o.L.x, a.y + o.L.y, a.z + o.L.z, 0.f);
   }
 }
 

@@ -102,9 +102,8 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
 // One bounce of every live path, each shaded with its own job's scene view
 // (materials, lights, infinite-light bounds, depth and Russian-roulette
 // settings) over the pooled geometry.
-template <int kThreads, int kMinBlocks>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-    k_srv_shade(DevScene pool, DevPaths P, const DevItem* items, int cur, int bounce) {
+__device__ __forceinline__ void srv_shade(const DevScene& pool, const DevPaths& P, const DevItem* items, int cur,
+                                          int bounce) {
   uint32_t n = P.counters[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.counters[4] = 0;
@@ -114,7 +113,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     uint32_t i = base + threadIdx.x;
     ShadeOut o;
-    o.cont = o.shadow = false;
+    o.cont = false;
     bool live = i < n;
     if (live) {
       if (P.order) i = P.order[i];
@@ -133,10 +132,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
       v.max_depth = it.max_depth;
       v.rr_min_bounces = it.rr_min_bounces;
       v.root = it.root;
-      shade_path(v, Q, P.hit, i, it.seed, bounce, o);
+      shade_path(v, P, Q, P.hit, i, it.seed, bounce, o);
     }
     push_shade_out(P, cur, live, o);
   }
+}
+
+// The kernel at 2 blocks of 256 threads per SM (16 warps, 113 registers)
+// or, as GPRT_JOB_SHADE_OCCUPANCY, 3 blocks of 192 threads (18 warps at 96
+// registers, 64 bytes spilled).  More warps did not pay: the 3-block
+// budget measured 8 % slower on the heterogeneous batch (shade 462 vs 428 ms
+// per batch), a 112-register cap without spills 28 % slower.
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    k_srv_shade(DevScene pool, DevPaths P, const DevItem* items, int cur, int bounce) {
+  srv_shade(pool, P, items, cur, bounce);
 }
 
 // PixelStats.AddSample for every pixel of every item, samples in order (the
@@ -838,7 +848,7 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     open();
     launch_hit_order(P, cur, sv->step_paths, sv->ctx->sm_count, st);
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
-      k_srv_shade<128, 6><<<std::max(1, grid * block / 128), 128, 0, st>>>(pool, P, items, cur, b);
+      k_srv_shade<192, 3><<<std::max(1, grid * block / 192), 192, 0, st>>>(pool, P, items, cur, b);
     else
       k_srv_shade<256, 2><<<grid, std::min(block, 256), 0, st>>>(pool, P, items, cur, b);
     close();

@@ -274,8 +274,8 @@ typedef struct gprt_job_desc {
  * new rays) or one ray per thread. */
 #define GPRT_JOB_SIMPLE_EXTEND 4u
 #define GPRT_JOB_SIMPLE_SHADOW 8u
-/* Shading kernel compiled for 6 resident 128-thread blocks per SM (fewer
- * registers, some spilled to L1) instead of unconstrained registers. */
+/* Shading kernel compiled for 3 resident 192-thread blocks per SM (18 warps,
+ * at most 96 registers) instead of 2 blocks of 256 threads (16 warps). */
 #define GPRT_JOB_SHADE_OCCUPANCY 32u
 
 /* Instrumentation of a job (GPRT_JOB_* flags), summed since the last reset.
