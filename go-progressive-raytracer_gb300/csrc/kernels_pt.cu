@@ -285,13 +285,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     P.counters[4] = 0;  // ray-fetch counters of the next shadow and extend launches
     P.counters[5] = 0;
   }
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t slot = first < n ? (P.order ? P.order[first] : first) : 0u;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
     uint32_t i = base + threadIdx.x;
+    // the slot of the next iteration, read now and prefetched into L2 after this one
+    uint32_t inext = i + stride;
+    uint32_t snext = inext < n ? (P.order ? P.order[inext] : inext) : 0u;
     ShadeOut o;
     o.cont = false;
     bool live = i < n;
-    if (live) shade_path(sc, P, P.q[cur], P.hit, P.order ? P.order[i] : i, ch.seed, bounce, o);
+    if (live) shade_path(sc, P, P.q[cur], P.hit, slot, ch.seed, bounce, o);
     push_shade_out(P, cur, live, o);
+    if (inext < n) prefetch_slot(P.q[cur], P.hit, snext);
+    slot = snext;
   }
 }
 

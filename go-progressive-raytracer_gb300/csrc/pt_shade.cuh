@@ -112,6 +112,16 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P
   out.ids = make_uint4(ids.x, ids.y, rng.pos, ids.w);
 }
 
+// Brings the shading inputs of slot i of queue Q (ray, hit, weight, roulette
+// throughput, radiance, ids) into L2 ahead of their use: a grid-stride
+// shading loop issues this for its next slot at the end of the current one,
+// so the next iteration's dependent loads meet L2 instead of DRAM.
+__device__ __forceinline__ void prefetch_slot(const PathBuf& Q, const float4* hits, uint32_t i) {
+  const void* a[7] = {Q.ray_o + i, Q.ray_d + i, hits + i, Q.weight + i, Q.thr + i, Q.L + i, Q.ids + i};
+#pragma unroll
+  for (int k = 0; k < 7; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a[k]));
+}
+
 // Moves a continuing path to the next queue; a finished path adds its
 // radiance at its origin index (where its unoccluded shadow rays add
 // theirs; raygen clears it).  Called by every lane of the warp; `live` is
