@@ -41,7 +41,10 @@ int ensure_bdpt(gprt_job* j) {
   B.uv = nullptr;
   if (j->scene->dev.has_textures) rc |= dev_alloc(ctx, b, &B.uv, (size_t)ns * 2 * B.maxv);
   rc |= dev_alloc(ctx, b, &B.slist, (size_t)ns * (B.maxv + 1) * B.maxv);
-  rc |= dev_alloc(ctx, b, &B.scount, (size_t)(B.maxv + 1) * B.maxv + 1);  // + the subpath work counter
+  B.nw = bdpt_windows(ns);
+  const size_t nk = (size_t)B.nw * (B.maxv + 1) * B.maxv;
+  rc |= dev_alloc(ctx, b, &B.scount, nk);
+  rc |= dev_alloc(ctx, b, &B.sprefix, 4 * (nk + 1));
   if (rc) return GPRT_E_OOM;
   P.stats = nullptr;
   P.variant = 0;

@@ -65,11 +65,24 @@ struct DevBdpt {
   uint2* masks;   // strategies that draw samples: light-tracing (bit s), direct-lighting (bit t)
   float4* contrib;
   float2* uv;     // surface UV per vertex (scenes with textures only, else null)
-  uint32_t* slist;   // per strategy k: the samples that have it, ns slots from k * ns
-  uint32_t* scount;  // per strategy: entries in slist; then the subpath kernel's work counter
+  // Per strategy k, the samples that have it: ns slots from k * ns, one
+  // range of kBdWindow slots per window of kBdWindow consecutive samples
+  // (window w from k * ns + w * kBdWindow), so that the strategy kernels can
+  // take every strategy of one window of samples before the next window.
+  uint32_t* slist;
+  uint32_t* scount;   // entries of list k in window w at [w * K + k] (K = (maxv + 1) * maxv)
+  uint32_t* sprefix;  // per strategy class c, from c * (nw * K + 1): exclusive prefix of its counts over [w * K + k], then the class total
   uint32_t ns;    // samples per chunk
+  uint32_t nw;    // sample windows per chunk
   int maxv;       // vertices per subpath (10 or 18)
 };
+
+// Samples per window of the BDPT strategy lists: the vertices of a window
+// (2 * maxv records of 96 B per sample: 31 MB at maxv = 10) stay in L2 while
+// all of its strategies run.  A multiple of the list kernel's 1,024-sample
+// block.
+constexpr uint32_t kBdWindow = 16384;
+inline uint32_t bdpt_windows(uint32_t ns) { return (ns + kBdWindow - 1) / kBdWindow; }
 
 struct DevPaths {
   PathBuf q[2];
@@ -97,7 +110,7 @@ struct DevPaths {
 inline int bdpt_maxv(int max_depth) { return max_depth <= 9 ? 10 : 18; }
 inline size_t bdpt_bytes(uint32_t ns, int maxv) {
   return (size_t)ns * (6 * 2 * maxv * 16 + 16 + 8 + (size_t)(maxv + 1) * maxv * 16 + 16 + 2 * 88 + 16 + 48) +
-         24 * 256;
+         (size_t)5 * (bdpt_windows(ns) * (maxv + 1) * maxv + 1) * 4 + 26 * 256;
 }
 
 constexpr uint32_t kVariantBits = GPRT_JOB_SIMPLE_EXTEND | GPRT_JOB_SIMPLE_SHADOW | GPRT_JOB_SHADE_OCCUPANCY;

@@ -20,8 +20,13 @@
 //                      vertex store (fields indexed [vertex][sample]) and the
 //                      continuing subpaths compacted into the other queue; a
 //                      camera subpath that ends starts its light subpath;
-//   k_bdpt_list        lists, per strategy (s,t), the samples that have it;
-//   k_bdpt_strategies  one thread per listed (strategy, sample) item, the
+//   k_bdpt_list        lists, per strategy (s,t) and window of 16,384
+//                      samples, the samples that have it;
+//   k_bdpt_prefix      each strategy class's prefix sums of the list counts
+//                      in (window, strategy) order;
+//   k_bdpt_strategies  one thread per listed (strategy, sample) item, in
+//                      (window, strategy) order, so every strategy of a
+//                      window runs while its vertices are in L2; the
 //                      items of a strategy in consecutive threads: each warp
 //                      runs a single (s,t) for 32 samples that have it, so
 //                      control flow is uniform and neighbouring warps share
@@ -1070,9 +1075,10 @@ __global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
   __shared__ uint16_t wofs[32][K];  // each warp's offset within the block's range (< 1,024)
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const unsigned below = (1u << lane) - 1u;
   for (uint32_t start = blockIdx.x * 1024u; start < n; start += gridDim.x * 1024u) {
+    const uint32_t w = start / kBdWindow;  // the block's samples lie in one window
     for (int k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
     uint32_t i = start + threadIdx.x;
@@ -1084,15 +1090,16 @@ __global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
     }
     for (int k = 0; k < K; k++) {
       unsigned mask = __ballot_sync(0xFFFFFFFFu, has_strategy(k / MAXV, k % MAXV + 1, nc, nl));
-      if (mask && lane == 0) wofs[w][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
+      if (mask && lane == 0) wofs[wp][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < K; k += blockDim.x) base[k] = cnt[k] ? atomicAdd(B.scount + k, cnt[k]) : 0u;
+    for (int k = threadIdx.x; k < K; k += blockDim.x)
+      base[k] = cnt[k] ? w * kBdWindow + atomicAdd(B.scount + w * K + k, cnt[k]) : 0u;
     __syncthreads();
     for (int k = 0; k < K; k++) {
       bool has = has_strategy(k / MAXV, k % MAXV + 1, nc, nl);
       unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
-      if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[w][k] + __popc(mask & below)] = i;
+      if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[wp][k] + __popc(mask & below)] = i;
     }
     __syncthreads();  // cnt, base and wofs are rewritten for the next range
   }
@@ -1106,38 +1113,98 @@ __host__ __device__ constexpr int strategy_class(int s, int t) {
   return s == 0 ? 0 : t == 1 ? 1 : s == 1 ? 2 : 3;
 }
 
-// One thread per listed (strategy, sample) item of class CLS, the items of a
-// strategy consecutive: a warp evaluates one (s, t) for 32 samples that have
-// it (uniform control flow, neighbouring warps on the same code).  The work
-// is latency-bound; 8 blocks per SM (at most 64 registers, a few spilled)
+// The per-class prefix sums of the list counts in (window, strategy) order,
+// which map a strategy kernel's class-wide item index g to the entry
+// e = w * K + k with sprefix[e] <= g < sprefix[e + 1].  One block: each
+// thread sums a contiguous run of entries for the four classes, and a
+// block-wide scan of the runs gives their offsets.
+template <int MAXV>
+__global__ void __launch_bounds__(1024) k_bdpt_prefix(DevPaths PS) {
+  constexpr int K = (MAXV + 1) * MAXV;
+  __shared__ uint32_t part[4][1024];
+  const DevBdpt& B = PS.bd;
+  const uint32_t E = B.nw * K;
+  const uint32_t per = (E + 1023u) / 1024u;
+  const uint32_t t = threadIdx.x;
+  const uint32_t lo = min(E, t * per), hi = min(E, lo + per);
+  uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  for (uint32_t e = lo; e < hi; e++) {
+    int k = (int)(e % K), c = strategy_class(k / MAXV, k % MAXV + 1);
+    uint32_t v = B.scount[e];
+    s0 += c == 0 ? v : 0u;
+    s1 += c == 1 ? v : 0u;
+    s2 += c == 2 ? v : 0u;
+    s3 += c == 3 ? v : 0u;
+  }
+  part[0][t] = s0;
+  part[1][t] = s1;
+  part[2][t] = s2;
+  part[3][t] = s3;
+  __syncthreads();
+  for (uint32_t d = 1; d < 1024u; d <<= 1) {  // inclusive scan (Hillis-Steele)
+    uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    if (t >= d) {
+      a0 = part[0][t - d];
+      a1 = part[1][t - d];
+      a2 = part[2][t - d];
+      a3 = part[3][t - d];
+    }
+    __syncthreads();
+    part[0][t] += a0;
+    part[1][t] += a1;
+    part[2][t] += a2;
+    part[3][t] += a3;
+    __syncthreads();
+  }
+  uint32_t r0 = part[0][t] - s0, r1 = part[1][t] - s1, r2 = part[2][t] - s2, r3 = part[3][t] - s3;
+  uint32_t* P = B.sprefix;
+  for (uint32_t e = lo; e < hi; e++) {
+    P[e] = r0;
+    P[(E + 1) + e] = r1;
+    P[2 * (E + 1) + e] = r2;
+    P[3 * (E + 1) + e] = r3;
+    int k = (int)(e % K), c = strategy_class(k / MAXV, k % MAXV + 1);
+    uint32_t v = B.scount[e];
+    r0 += c == 0 ? v : 0u;
+    r1 += c == 1 ? v : 0u;
+    r2 += c == 2 ? v : 0u;
+    r3 += c == 3 ? v : 0u;
+  }
+  if (t == 1023u) {
+    P[E] = part[0][t];
+    P[(E + 1) + E] = part[1][t];
+    P[2 * (E + 1) + E] = part[2][t];
+    P[3 * (E + 1) + E] = part[3][t];
+  }
+}
+
+// One thread per listed (strategy, sample) item of class CLS, in (window,
+// strategy) order: a warp evaluates one (s, t) for 32 samples of one window
+// that have it (uniform control flow, neighbouring warps on the same code),
+// and every strategy of a window of samples runs before the next window, so
+// the vertex reads of the window's later strategies hit L2.  The work is
+// latency-bound; 8 blocks per SM (at most 64 registers, a few spilled)
 // measured fastest on the Cornell-boxes frame (558 ms vs 624 ms at 96
 // registers and 5 blocks).
 template <int MAXV, int CLS>
 __global__ void __launch_bounds__(128, 8) k_bdpt_strategies(DevScene sc, DevFilm film, DevPaths PS, ChunkDesc ch) {
   constexpr int K = (MAXV + 1) * MAXV;
-  __shared__ uint32_t first[K + 1];  // prefix sums of the list lengths of the class
   const DevBdpt& B = PS.bd;
   const uint32_t n = ch.npix * ch.layers;
-  if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (int k = 0; k < K; k++) {
-      first[k] = acc;
-      if (strategy_class(k / MAXV, k % MAXV + 1) == CLS) acc += B.scount[k];
-    }
-    first[K] = acc;
-  }
-  __syncthreads();
-  const uint32_t total = first[K];
+  const uint32_t E = B.nw * K;
+  const uint32_t* P = B.sprefix + (size_t)CLS * (E + 1);
+  const uint32_t total = __ldg(P + E);
   int* err = reinterpret_cast<int*>(PS.counters + 3);
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-    int lo = 0, hi = K;  // the strategy k with first[k] <= g < first[k + 1]
+    uint32_t lo = 0, hi = E;  // P[lo] <= g < P[hi]
     while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (first[mid] <= g) lo = mid;
+      uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(P + mid) <= g) lo = mid;
       else hi = mid;
     }
-    const int k = lo;
-    const uint32_t i = B.slist[(size_t)k * B.ns + (g - first[k])];
+    const uint32_t w = lo / K;
+    const int k = (int)(lo - w * K);
+    const uint32_t i = B.slist[(size_t)k * B.ns + w * kBdWindow + (g - __ldg(P + lo))];
     const int s = k / MAXV, t = k % MAXV + 1;
     uint4 m = B.meta[i];
     Rng rs;
@@ -1185,6 +1252,7 @@ void launch_bdpt_maxv(const DevScene& sc, const DevFilm& film, const DevPaths& P
     cur ^= 1;
   }
   k_bdpt_list<MAXV><<<gl, 1024, 0, st>>>(P, ch);
+  k_bdpt_prefix<MAXV><<<1, 1024, 0, st>>>(P);
   k_bdpt_strategies<MAXV, 0><<<g2, 128, 0, st>>>(sc, film, P, ch);
   k_bdpt_strategies<MAXV, 1><<<g2, 128, 0, st>>>(sc, film, P, ch);
   k_bdpt_strategies<MAXV, 2><<<g2, 128, 0, st>>>(sc, film, P, ch);
@@ -1203,7 +1271,7 @@ void launch_bdpt(const DevScene& sc, const DevFilm& film, const DevPaths& P, con
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * ((P.bd.maxv + 1) * P.bd.maxv + 1), st);
+  cudaMemsetAsync(P.bd.scount, 0, sizeof(uint32_t) * P.bd.nw * (P.bd.maxv + 1) * P.bd.maxv, st);
   if (P.bd.maxv == 10) launch_bdpt_maxv<10>(sc, film, P, ch, sms, st);
   else launch_bdpt_maxv<18>(sc, film, P, ch, sms, st);
 }
