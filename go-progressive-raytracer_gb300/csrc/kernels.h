@@ -149,7 +149,7 @@ void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P
                       cudaStream_t st);
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
 // Builds P.order for queue `cur` (hits first, misses last) before shading.
-void launch_hit_order(const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st);
+void launch_hit_order(const DevScene& sc, const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st);
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st);
 void launch_pt_shadow(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);

@@ -227,50 +227,17 @@ void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block,
 }
 
 // ----------------------------------------------------------------- shade
-// The slots of queue `cur` reordered: paths whose ray hit a surface first,
-// missed rays (a background lookup) last, each group in blocks of 1,024
-// slots (one atomic per block and group).  The shading kernel then runs warps
-// of hits and warps of misses instead of mixing both lane by lane; every
-// path is shaded exactly as in queue order.
-__global__ void __launch_bounds__(1024) k_hit_order(DevPaths P, int cur) {
-  __shared__ uint32_t wh[32], wm[32];
-  __shared__ uint32_t bh, bm;
-  const uint32_t n = P.counters[cur];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
-    uint32_t i = base + threadIdx.x;
-    bool live = i < n;
-    bool hit = live && __float_as_uint(P.hit[i].y) != kNoHit;
-    unsigned mh = __ballot_sync(0xffffffffu, hit), ml = __ballot_sync(0xffffffffu, live);
-    if (lane == 0) {
-      wh[w] = __popc(mh);
-      wm[w] = __popc(ml & ~mh);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t th = 0, tm = 0;
-      for (int k = 0; k < 32; k++) {
-        uint32_t a = wh[k], b = wm[k];
-        wh[k] = th;
-        wm[k] = tm;
-        th += a;
-        tm += b;
-      }
-      bh = th ? atomicAdd(&P.counters[6], th) : 0u;
-      bm = tm ? atomicAdd(&P.counters[7], tm) : 0u;
-    }
-    __syncthreads();
-    unsigned below = (1u << lane) - 1u;
-    if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
-    else if (live) P.order[n - 1u - (bm + wm[w] + __popc(ml & ~mh & below))] = i;
-    __syncthreads();  // wh, wm, bh, bm are rewritten for the next range
-  }
+// The shading order of queue `cur` (order_slots) for one scene.
+__global__ void __launch_bounds__(1024) k_hit_order(DevScene sc, DevPaths P, int cur) {
+  order_slots(P, cur, [&](uint32_t, uint32_t prim) {
+    return kind_samples_lights(sc.materials[prim_material(sc, prim)].kind);
+  });
 }
 
-void launch_hit_order(const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st) {
+void launch_hit_order(const DevScene& sc, const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st) {
   if (!P.order) return;
   int g = std::max(1, std::min((int)((cap + 1023) / 1024), sms * 2));
-  k_hit_order<<<g, 1024, 0, st>>>(P, cur);
+  k_hit_order<<<g, 1024, 0, st>>>(sc, P, cur);
 }
 
 // One level of rayColorRecursive (path_tracing.go:35-104) with
@@ -308,7 +275,7 @@ void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch,
   // the hit-first slot order pays where rays escape to an infinite light
   // (missed rays are then a large share); in closed scenes it is overhead
   DevPaths Po = P;
-  if (sc.has_infinite) launch_hit_order(P, cur, P.capacity, sm_count_current(), st);
+  if (sc.has_infinite) launch_hit_order(sc, P, cur, P.capacity, sm_count_current(), st);
   else Po.order = nullptr;
   if (P.variant & GPRT_JOB_SHADE_OCCUPANCY) {
     int g = std::max(1, (int)((int64_t)grid * block / 192));

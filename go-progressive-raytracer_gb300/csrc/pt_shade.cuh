@@ -122,6 +122,65 @@ __device__ __forceinline__ void prefetch_slot(const PathBuf& Q, const float4* hi
   for (int k = 0; k < 7; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a[k]));
 }
 
+// The material index (in the scene's material table) of primitive p.
+__device__ __forceinline__ int prim_material(const DevScene& sc, uint32_t p) {
+  if (p < sc.quad_base) return __float_as_int(__ldg(sc.tris + (size_t)p * 3).w);
+  if (p < sc.sphere_base) return __float_as_int(__ldg(sc.quads + (size_t)(p - sc.quad_base) * 5 + 1).w);
+  if (p < sc.quadric_base) return __float_as_int(__ldg(sc.spheres + (size_t)(p - sc.sphere_base) * 2 + 1).x);
+  return __float_as_int(__ldg(sc.quadrics + (size_t)(p - sc.quadric_base) * 5 + 4).y);
+}
+
+// Whether a hit on a material of this kind can run next-event estimation:
+// its scatter has a pdf.  Metal and Dielectric scatter specularly (pdf 0,
+// metal.go:60, dielectric.go:57) and the emitters do not scatter.
+__device__ __forceinline__ bool kind_samples_lights(int kind) {
+  return kind != kMatMetal && kind != kMatDielectric && kind != kMatEmissive && kind != kMatSpotEmissive;
+}
+
+// The slot order the shading kernels read for queue `cur`: hits whose
+// material samples lights first (`lights(i, prim)` for slot i's hit on
+// primitive prim), then, from the back, missed rays (a background lookup)
+// and hits on specular materials and emitters, each group in blocks of
+// 1,024 slots (one atomic per block and group).  Warps then run next-event
+// estimation on all their lanes or on none, instead of mixing them lane by
+// lane; every path is shaded exactly as in queue order.
+template <class Lights>
+__device__ __forceinline__ void order_slots(const DevPaths& P, int cur, Lights lights) {
+  __shared__ uint32_t wh[32], wm[32];
+  __shared__ uint32_t bh, bm;
+  const uint32_t n = P.counters[cur];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
+    uint32_t i = base + threadIdx.x;
+    bool live = i < n;
+    uint32_t prim = live ? __float_as_uint(P.hit[i].y) : kNoHit;
+    bool hit = prim != kNoHit && prim != kOverflowHit && lights(i, prim);
+    unsigned mh = __ballot_sync(0xffffffffu, hit), ml = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) {
+      wh[w] = __popc(mh);
+      wm[w] = __popc(ml & ~mh);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t th = 0, tm = 0;
+      for (int k = 0; k < 32; k++) {
+        uint32_t a = wh[k], b = wm[k];
+        wh[k] = th;
+        wm[k] = tm;
+        th += a;
+        tm += b;
+      }
+      bh = th ? atomicAdd(&P.counters[6], th) : 0u;
+      bm = tm ? atomicAdd(&P.counters[7], tm) : 0u;
+    }
+    __syncthreads();
+    unsigned below = (1u << lane) - 1u;
+    if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
+    else if (live) P.order[n - 1u - (bm + wm[w] + __popc(ml & ~mh & below))] = i;
+    __syncthreads();  // wh, wm, bh, bm are rewritten for the next range
+  }
+}
+
 // Moves a continuing path to the next queue; a finished path adds its
 // radiance at its origin index (where its unoccluded shadow rays add
 // theirs; raygen clears it).  Called by every lane of the warp; `live` is

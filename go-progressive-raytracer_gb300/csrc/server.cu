@@ -64,6 +64,16 @@ struct DevItem {
   DevCamera cam;
 };
 
+// The shading order of the step's queue `cur` (order_slots): a slot's
+// material comes from its item's material table.
+__global__ void __launch_bounds__(1024) k_srv_hit_order(DevScene pool, DevPaths P, const DevItem* items, int cur) {
+  const PathBuf Q = P.q[cur];
+  order_slots(P, cur, [&](uint32_t i, uint32_t prim) {
+    const DevItem& it = items[Q.ids[i].w];
+    return kind_samples_lights(pool.materials[it.mat_off + prim_material(pool, prim)].kind);
+  });
+}
+
 // Camera rays of every item: path p is sample `layer` of pixel i of its item,
 // drawn exactly as k_pt_raygen draws them for a single job.
 __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* path0, const DevItem* items) {
@@ -855,7 +865,8 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     launch_pt_extend(pool, P, cur, block, grid, st);
     close();
     open();
-    launch_hit_order(P, cur, sv->step_paths, sv->ctx->sm_count, st);
+    k_srv_hit_order<<<std::max(1, std::min((int)((sv->step_paths + 1023) / 1024), sv->ctx->sm_count * 2)), 1024, 0,
+                      st>>>(pool, P, items, cur);
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
       k_srv_shade<192, 3><<<std::max(1, grid * block / 192), 192, 0, st>>>(pool, P, items, cur, b);
     else
