@@ -139,45 +139,58 @@ __device__ __forceinline__ bool kind_samples_lights(int kind) {
 
 // The slot order the shading kernels read for queue `cur`: hits whose
 // material samples lights first (`lights(i, prim)` for slot i's hit on
-// primitive prim), then, from the back, missed rays (a background lookup)
-// and hits on specular materials and emitters, each group in blocks of
-// 1,024 slots (one atomic per block and group).  Warps then run next-event
-// estimation on all their lanes or on none, instead of mixing them lane by
-// lane; every path is shaded exactly as in queue order.
+// primitive prim), then, from the back, hits on specular materials and
+// emitters and missed rays (a background lookup).  Each block of 1,024 slots
+// takes one range from the front and one from the back (one atomic each);
+// inside its back range the specular hits come before the misses.  Warps
+// then run next-event estimation on all their lanes or on none, and miss
+// warps are not held up by specular lanes; every path is shaded exactly as
+// in queue order.
 template <class Lights>
 __device__ __forceinline__ void order_slots(const DevPaths& P, int cur, Lights lights) {
-  __shared__ uint32_t wh[32], wm[32];
-  __shared__ uint32_t bh, bm;
+  __shared__ uint32_t wh[32], ws[32], wm[32];
+  __shared__ uint32_t bh, bb, btm;
   const uint32_t n = P.counters[cur];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
     uint32_t i = base + threadIdx.x;
     bool live = i < n;
     uint32_t prim = live ? __float_as_uint(P.hit[i].y) : kNoHit;
-    bool hit = prim != kNoHit && prim != kOverflowHit && lights(i, prim);
-    unsigned mh = __ballot_sync(0xffffffffu, hit), ml = __ballot_sync(0xffffffffu, live);
+    bool surf = prim != kNoHit && prim != kOverflowHit;
+    bool hit = surf && lights(i, prim);
+    bool spec = surf && !hit;
+    unsigned mh = __ballot_sync(0xffffffffu, hit), ms = __ballot_sync(0xffffffffu, spec),
+             ml = __ballot_sync(0xffffffffu, live);
+    unsigned mm = ml & ~mh & ~ms;  // misses
     if (lane == 0) {
       wh[w] = __popc(mh);
-      wm[w] = __popc(ml & ~mh);
+      ws[w] = __popc(ms);
+      wm[w] = __popc(mm);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      uint32_t th = 0, tm = 0;
+      uint32_t th = 0, ts = 0, tm = 0;
       for (int k = 0; k < 32; k++) {
-        uint32_t a = wh[k], b = wm[k];
+        uint32_t a = wh[k], b = ws[k], c = wm[k];
         wh[k] = th;
+        ws[k] = ts;
         wm[k] = tm;
         th += a;
-        tm += b;
+        ts += b;
+        tm += c;
       }
       bh = th ? atomicAdd(&P.counters[6], th) : 0u;
-      bm = tm ? atomicAdd(&P.counters[7], tm) : 0u;
+      bb = ts + tm ? atomicAdd(&P.counters[7], ts + tm) : 0u;
+      btm = tm;
     }
     __syncthreads();
     unsigned below = (1u << lane) - 1u;
+    // back-range entry j sits at n - 1 - (bb + j): misses take j < tm (the
+    // highest positions), specular hits the ts entries below them
     if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
-    else if (live) P.order[n - 1u - (bm + wm[w] + __popc(ml & ~mh & below))] = i;
-    __syncthreads();  // wh, wm, bh, bm are rewritten for the next range
+    else if (spec) P.order[n - 1u - (bb + btm + ws[w] + __popc(ms & below))] = i;
+    else if (live) P.order[n - 1u - (bb + wm[w] + __popc(mm & below))] = i;
+    __syncthreads();  // the counts and bases are rewritten for the next range
   }
 }
 
