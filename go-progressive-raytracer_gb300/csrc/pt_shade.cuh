@@ -130,66 +130,73 @@ __device__ __forceinline__ int prim_material(const DevScene& sc, uint32_t p) {
   return __float_as_int(__ldg(sc.quadrics + (size_t)(p - sc.quadric_base) * 5 + 4).y);
 }
 
-// Whether a hit on a material of this kind can run next-event estimation:
-// its scatter has a pdf.  Metal and Dielectric scatter specularly (pdf 0,
-// metal.go:60, dielectric.go:57) and the emitters do not scatter.
-__device__ __forceinline__ bool kind_samples_lights(int kind) {
-  return kind != kMatMetal && kind != kMatDielectric && kind != kMatEmissive && kind != kMatSpotEmissive;
+// The shading group of a hit on a material of this kind: 0 when its
+// scatter has a pdf, so that shading runs next-event estimation; specular
+// scatter (pdf 0, metal.go:60, dielectric.go:57) 1 for Metal and 2 for
+// Dielectric; 3 for the emitters, which do not scatter (as for missed rays).
+constexpr int kShadeGroups = 4;
+__device__ __forceinline__ int shade_group(int kind) {
+  return kind == kMatMetal ? 1 : kind == kMatDielectric ? 2 : kind == kMatEmissive || kind == kMatSpotEmissive ? 3 : 0;
 }
 
-// The slot order the shading kernels read for queue `cur`: hits whose
-// material samples lights first (`lights(i, prim)` for slot i's hit on
-// primitive prim), then, from the back, hits on specular materials and
-// emitters and missed rays (a background lookup).  Each block of 1,024 slots
-// takes one range from the front and one from the back (one atomic each);
-// inside its back range the specular hits come before the misses.  Warps
-// then run next-event estimation on all their lanes or on none, and miss
-// warps are not held up by specular lanes; every path is shaded exactly as
-// in queue order.
-template <class Lights>
-__device__ __forceinline__ void order_slots(const DevPaths& P, int cur, Lights lights) {
-  __shared__ uint32_t wh[32], ws[32], wm[32];
-  __shared__ uint32_t bh, bb, btm;
+// The slot order the shading kernels read for queue `cur`, by shading group
+// (`group(i, prim)` for slot i's hit on primitive prim; missed rays, which
+// only look up the background, are group 3): group 0 from the front, then,
+// from the back, groups 1, 2 and 3.  Each block of 1,024 slots takes one
+// range from the front and one from the back (one atomic each) and lays its
+// back range out group by group, so warps run one kind of shading (next-event
+// estimation on all lanes or on none; metal, glass or finished paths) instead
+// of mixing them lane by lane.  Every path is shaded exactly as in queue
+// order.
+template <class Group>
+__device__ __forceinline__ void order_slots(const DevPaths& P, int cur, Group group) {
+  constexpr int G = kShadeGroups;
+  __shared__ uint32_t wc[G][32];
+  __shared__ uint32_t bfront, bback, boff[G];
   const uint32_t n = P.counters[cur];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
   for (uint32_t base = blockIdx.x * 1024u; base < n; base += gridDim.x * 1024u) {
     uint32_t i = base + threadIdx.x;
     bool live = i < n;
     uint32_t prim = live ? __float_as_uint(P.hit[i].y) : kNoHit;
-    bool surf = prim != kNoHit && prim != kOverflowHit;
-    bool hit = surf && lights(i, prim);
-    bool spec = surf && !hit;
-    unsigned mh = __ballot_sync(0xffffffffu, hit), ms = __ballot_sync(0xffffffffu, spec),
-             ml = __ballot_sync(0xffffffffu, live);
-    unsigned mm = ml & ~mh & ~ms;  // misses
-    if (lane == 0) {
-      wh[w] = __popc(mh);
-      ws[w] = __popc(ms);
-      wm[w] = __popc(mm);
+    int g = prim != kNoHit && prim != kOverflowHit ? group(i, prim) : G - 1;
+    unsigned mine = 0;  // the lanes of this warp in group g
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      unsigned m = __ballot_sync(0xffffffffu, live && g == k);
+      if (g == k) mine = m;
+      if (lane == 0) wc[k][w] = __popc(m);
+    }
+    __syncthreads();
+    if (threadIdx.x < G) {  // exclusive scan of each group's warp counts
+      uint32_t acc = 0;
+      for (int k = 0; k < 32; k++) {
+        uint32_t c = wc[threadIdx.x][k];
+        wc[threadIdx.x][k] = acc;
+        acc += c;
+      }
+      boff[threadIdx.x] = acc;  // the group's total, for now
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      uint32_t th = 0, ts = 0, tm = 0;
-      for (int k = 0; k < 32; k++) {
-        uint32_t a = wh[k], b = ws[k], c = wm[k];
-        wh[k] = th;
-        ws[k] = ts;
-        wm[k] = tm;
-        th += a;
-        ts += b;
-        tm += c;
+      // back-range entry j sits at n - 1 - (bback + j): the last group takes
+      // the smallest j (the highest positions), group 1 the largest
+      uint32_t back = 0;
+      for (int k = G - 1; k >= 1; k--) {
+        uint32_t t = boff[k];
+        boff[k] = back;
+        back += t;
       }
-      bh = th ? atomicAdd(&P.counters[6], th) : 0u;
-      bb = ts + tm ? atomicAdd(&P.counters[7], ts + tm) : 0u;
-      btm = tm;
+      bfront = boff[0] ? atomicAdd(&P.counters[6], boff[0]) : 0u;
+      bback = back ? atomicAdd(&P.counters[7], back) : 0u;
     }
     __syncthreads();
-    unsigned below = (1u << lane) - 1u;
-    // back-range entry j sits at n - 1 - (bb + j): misses take j < tm (the
-    // highest positions), specular hits the ts entries below them
-    if (hit) P.order[bh + wh[w] + __popc(mh & below)] = i;
-    else if (spec) P.order[n - 1u - (bb + btm + ws[w] + __popc(ms & below))] = i;
-    else if (live) P.order[n - 1u - (bb + wm[w] + __popc(mm & below))] = i;
+    if (live) {
+      uint32_t r = wc[g][w] + __popc(mine & below);
+      if (g == 0) P.order[bfront + r] = i;
+      else P.order[n - 1u - (bback + boff[g] + r)] = i;
+    }
     __syncthreads();  // the counts and bases are rewritten for the next range
   }
 }

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(1024) k_srv_hit_order(DevScene pool, DevPaths 
   const PathBuf Q = P.q[cur];
   order_slots(P, cur, [&](uint32_t i, uint32_t prim) {
     const DevItem& it = items[Q.ids[i].w];
-    return kind_samples_lights(pool.materials[it.mat_off + prim_material(pool, prim)].kind);
+    return shade_group(pool.materials[it.mat_off + prim_material(pool, prim)].kind);
   });
 }
 
