@@ -655,18 +655,10 @@ int gprt_job_render_pass(gprt_job* j, uint32_t pass, gprt_render_stats* stats) {
   if (min_s < target || j->uniform_count < 0 || (uint64_t)j->uniform_count < target) {
     // adaptive rounds of one sample per still-active pixel
     for (;;) {
-      CK(ctx, cudaMemsetAsync(j->d_active, 0, sizeof(uint32_t), j->stream));
-      launch_active_pixels(j->film, target, min_s, (float)sd.adaptive_threshold, j->d_pix_list, j->d_active,
-                           j->stream);
-      j->launches++;
-      CK(ctx, cudaMemcpyAsync(j->h_words + 1, j->d_active, 4, cudaMemcpyDeviceToHost, j->stream));
-      CK(ctx, cudaStreamSynchronize(j->stream));
-      uint32_t active = j->h_words[1];
-      if (active == 0) break;
-      if (active != npix) j->uniform_count = -1;
-      rc = add_samples(j, 1, active, j->d_pix_list);
+      uint32_t active = 0;
+      rc = gprt::job_adaptive_round(j, target, min_s, (float)sd.adaptive_threshold, &active);
       if (rc) return rc;
-      if (j->uniform_count >= 0) j->uniform_count++;
+      if (active == 0) break;
     }
   }
   cudaEventRecord(j->ev1, j->stream);
@@ -1064,6 +1056,28 @@ size_t bdpt_job_bytes(const gprt_scene* s, const gprt_job_desc& d) {
                 (size_t)ns * (maxv + 1) * maxv * sizeof(uint32_t) + 64 * sizeof(uint32_t);  // strategy lists
   if (!h.tex_info.empty()) work += (size_t)ns * 2 * maxv * sizeof(float2);
   return film + work;
+}
+
+
+// One round of an adaptive pass: lists the pixels still active for pass
+// target `target` and minimum `min_s` (k_active_pixels; waits for j's
+// stream), queues one sample for each, and returns their number in *active
+// (0: the pass is complete and nothing is queued).
+int job_adaptive_round(gprt_job* j, uint32_t target, uint32_t min_s, float threshold, uint32_t* active) {
+  gprt_ctx* ctx = j->scene->ctx;
+  const uint32_t npix = (uint32_t)j->film.width * j->film.height;
+  CK(ctx, cudaMemsetAsync(j->d_active, 0, sizeof(uint32_t), j->stream));
+  launch_active_pixels(j->film, target, min_s, threshold, j->d_pix_list, j->d_active, j->stream);
+  j->launches++;
+  CK(ctx, cudaMemcpyAsync(j->h_words + 1, j->d_active, 4, cudaMemcpyDeviceToHost, j->stream));
+  CK(ctx, cudaStreamSynchronize(j->stream));
+  *active = j->h_words[1];
+  if (*active == 0) return GPRT_OK;
+  if (*active != npix) j->uniform_count = -1;
+  int rc = add_samples(j, 1, *active, j->d_pix_list);
+  if (rc) return rc;
+  if (j->uniform_count >= 0) j->uniform_count++;
+  return GPRT_OK;
 }
 
 }  // namespace gprt

@@ -133,6 +133,10 @@ void server_forget_scene(gprt_server* sv, gprt_scene* s);
 // arrays), not listed among the context's scenes; gprt_scene_destroy
 // releases it with the jobs on it.  The server renders BDPT requests on one.
 int clone_scene(gprt_scene* src, gprt_scene** out);
+// One round of an adaptive pass of job j (gprt_job_render_pass's loop body,
+// capi.cu): one sample for every pixel still active for pass target
+// `target` and minimum `min_s`; *active = their number (0: pass complete).
+int job_adaptive_round(gprt_job* j, uint32_t target, uint32_t min_s, float threshold, uint32_t* active);
 // Device bytes of a BDPT job on scene `s`: film, and the subpath vertices and
 // strategy buffers of one chunk as gprt_job_create and its first pass allocate them.
 size_t bdpt_job_bytes(const gprt_scene* s, const gprt_job_desc& d);

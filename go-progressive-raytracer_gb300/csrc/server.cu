@@ -61,6 +61,7 @@ struct DevItem {
   float4* rgbl;
   float* lum2;
   uint32_t* count;
+  const uint32_t* list;  // the item's pixels (a round of an adaptive pass); null: item pixel i is film pixel i
   DevCamera cam;
 };
 
@@ -85,6 +86,7 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
     const DevItem& it = items[k];
     uint32_t rel = p - it.path0;
     uint32_t layer = rel / it.npix, pix = rel - layer * it.npix;
+    if (it.list) pix = it.list[pix];
     uint32_t sample = it.count[pix] + layer;
     int x = (int)(pix % (uint32_t)it.width), y = (int)(pix / (uint32_t)it.width);
     Rng rng;
@@ -177,8 +179,9 @@ __global__ void k_srv_accumulate(DevPaths P, const StepHdr* hdr, const uint32_t*
     uint32_t k = find_range(pix0, ni, t);
     const DevItem& it = items[k];
     uint32_t i = t - it.pix0;
-    float4 acc = it.rgbl[i];
-    float l2 = it.lum2[i];
+    uint32_t f = it.list ? it.list[i] : i;  // the film pixel
+    float4 acc = it.rgbl[f];
+    float l2 = it.lum2[f];
     for (uint32_t layer = 0; layer < it.layers; layer++) {
       float4 c = P.Lout[it.path0 + layer * it.npix + i];
       float lum = luminance(f3(c));
@@ -188,9 +191,9 @@ __global__ void k_srv_accumulate(DevPaths P, const StepHdr* hdr, const uint32_t*
       acc.w += lum;
       l2 += lum * lum;
     }
-    it.rgbl[i] = acc;
-    it.lum2[i] = l2;
-    it.count[i] += it.layers;
+    it.rgbl[f] = acc;
+    it.lum2[f] = l2;
+    it.count[f] += it.layers;
   }
 }
 
@@ -310,6 +313,20 @@ struct SrvJob {
   std::vector<void*> bufs;
   size_t film_bytes = 0;
   uint32_t passes = 0, spp_done = 0, pass_target = 0;
+  // adaptive sampling (the scene's AdaptiveMinSamples < 1), as
+  // gprt_job_render_pass runs it: per pass the minimum samples of every
+  // pixel in bulk, then rounds of one sample for each pixel still active
+  // (k_active_pixels: below the pass target and not converged), each round's
+  // pixel list built on the device after the step before it; the pass ends
+  // when no pixel is active.  spp_done is then the average sample count.
+  bool adaptive = false;
+  double min_frac = 1.0;       // AdaptiveMinSamples
+  float threshold = 0.f;       // AdaptiveThreshold
+  uint32_t min_s = 0;          // the pass's minimum samples per pixel
+  int64_t uniform = 0;         // the sample count of every pixel while all are equal, else -1
+  uint64_t total = 0;          // samples taken over all pixels
+  uint32_t* d_list = nullptr;  // npix entries: the pixels of the next round, then their count
+  uint32_t active = 0;         // pixels listed for the next round (0: none listed)
   bool running = true;
   double submit_ms = 0, admit_ms = 0;
   uint64_t last_served = 0;
@@ -360,8 +377,9 @@ struct gprt_server {
   // then one error word per item at err_off (cleared by the step's raygen)
   unsigned char* h_table = nullptr;  // pinned staging of the table; its error words receive the read-back
   uint32_t* h_err = nullptr;         // pinned: a pageable read-back would block inside the runtime
+  uint32_t* h_act = nullptr;         // pinned: active-pixel counts of the adaptive rounds being listed
                                      // until the step ends, stalling other threads' CUDA calls
-  size_t table_bytes = 0, prefix_bytes = 0, err_off = 0;
+  size_t table_bytes = 0, prefix_bytes = 0, err_off = 0, act_off = 0;
   std::map<int, cudaGraphExec_t> graphs;  // by depth
   uint64_t graph_gen = ~0ull;
   // instrumentation (GPRT_JOB_TIME_KERNELS / GPRT_JOB_COUNT_TRAVERSAL in flags):
@@ -407,7 +425,12 @@ void emit(gprt_server* sv, uint64_t ticket, uint32_t kind, uint32_t passes, uint
   sv->cv_ev.notify_all();
 }
 
-size_t film_bytes_for(uint32_t npix) { return (size_t)npix * (sizeof(float4) + sizeof(float) + sizeof(uint32_t)); }
+// A path-tracing job's film (+ its active-pixel list and count when the
+// scene samples adaptively).
+size_t film_bytes_for(uint32_t npix, bool adaptive) {
+  return (size_t)npix * (sizeof(float4) + sizeof(float) + sizeof(uint32_t)) +
+         (adaptive ? ((size_t)npix + 1) * sizeof(uint32_t) : 0);
+}
 
 size_t bytes_in_use(gprt_server* sv) {
   size_t b = sv->path_bytes + sv->table_bytes + sv->reserve;
@@ -660,6 +683,13 @@ void advance(gprt_server* sv, SrvJob* j, bool emit_pass) {
       return;
     }
     j->pass_target = samples_for_pass(j->desc, j->passes + 1);
+    if (j->adaptive) {
+      // shouldStopSampling's minimum (tile_renderer.go:79); the pass ends
+      // when a round lists no active pixel
+      j->min_s = std::max(1u, (uint32_t)((double)j->pass_target * j->min_frac));
+      j->active = 0;
+      return;
+    }
     if (j->pass_target > j->spp_done) return;
     j->passes++;
     emit(sv, j->ticket, GPRT_EV_PASS, j->passes, j->spp_done, GPRT_OK, j->submit_ms);
@@ -680,12 +710,13 @@ void admit(gprt_server* sv) {
     if (sv->jobs.size() >= sv->desc.max_jobs) return;
     gprt_scene* s = r.scene;
     uint32_t npix = s->host.sampling.width * s->host.sampling.height;
+    const bool adapt = s->host.sampling.adaptive_min_samples < 1.0;
     size_t cnt[kPoolArrays];
     scene_counts(s, cnt);
     bool resident = false;
     for (auto& ps : sv->scenes) resident |= ps->serial == r.serial;
     size_t fixed = sv->path_bytes + sv->table_bytes;
-    size_t need = film_bytes_for(npix) + (resident ? 0 : scene_bytes(sv, cnt));
+    size_t need = film_bytes_for(npix, adapt) + (resident ? 0 : scene_bytes(sv, cnt));
     auto pop = [&]() {
       std::lock_guard<std::mutex> q(sv->qmu);
       sv->pending.pop_front();
@@ -733,6 +764,9 @@ void admit(gprt_server* sv) {
       j->bd_scene = copy;
       j->bd = bj;
       j->film_bytes = need_b;
+      j->adaptive = adapt;
+      j->min_frac = s->host.sampling.adaptive_min_samples;
+      j->threshold = (float)s->host.sampling.adaptive_threshold;
       j->admit_ms = now_ms(sv->t0);
       pop();
       sv->st.admitted++;
@@ -750,7 +784,7 @@ void admit(gprt_server* sv) {
       continue;
     }
     // films must fit beside everything held now (scene bytes are checked as the pool grows)
-    if (bytes_in_use(sv) + film_bytes_for(npix) > sv->desc.hbm_budget_bytes) {
+    if (bytes_in_use(sv) + film_bytes_for(npix, adapt) > sv->desc.hbm_budget_bytes) {
       // unreferenced cached scenes go first
       bool freed = false;
       for (auto& ps : sv->scenes)
@@ -777,11 +811,12 @@ void admit(gprt_server* sv) {
     rc |= dev_alloc(ctx, j->bufs, &f.rgbl, npix);
     rc |= dev_alloc(ctx, j->bufs, &f.lum2, npix);
     rc |= dev_alloc(ctx, j->bufs, &f.count, npix);
+    if (adapt) rc |= dev_alloc(ctx, j->bufs, &j->d_list, (size_t)npix + 1);
     if (rc) {
       free_all(j->bufs);
       return;  // device full: retry next step
     }
-    sv->reserve = film_bytes_for(npix);  // the scene may not take the film's room
+    sv->reserve = film_bytes_for(npix, adapt);  // the scene may not take the film's room
     PoolScene* ps = make_resident(sv, s);
     sv->reserve = 0;
     if (!ps) {
@@ -791,7 +826,10 @@ void admit(gprt_server* sv) {
     cudaMemsetAsync(f.rgbl, 0, (size_t)npix * sizeof(float4), sv->stream);
     cudaMemsetAsync(f.lum2, 0, (size_t)npix * sizeof(float), sv->stream);
     cudaMemsetAsync(f.count, 0, (size_t)npix * sizeof(uint32_t), sv->stream);
-    j->film_bytes = film_bytes_for(npix);
+    j->film_bytes = film_bytes_for(npix, adapt);
+    j->adaptive = adapt;
+    j->min_frac = s->host.sampling.adaptive_min_samples;
+    j->threshold = (float)s->host.sampling.adaptive_threshold;
     ps->refs++;
     ps->last_use = sv->st.steps;
     j->ps = ps;
@@ -954,7 +992,30 @@ int run_step(gprt_server* sv, int D) {
 struct Item {
   SrvJob* j;
   uint32_t layers;
+  uint32_t npix;                   // pixels taking `layers` samples each
+  const uint32_t* list = nullptr;  // those pixels (an adaptive round), null: every pixel
 };
+
+// The next work of a running path-tracing job: `layers` samples for `npix`
+// pixels (a pixel list for an adaptive round).  Returns false when the job
+// has none until its next round is listed.
+bool next_work(const SrvJob* j, uint32_t& layers, uint32_t& npix, const uint32_t*& list) {
+  npix = j->npix;
+  list = nullptr;
+  if (!j->adaptive) {
+    layers = j->pass_target - j->spp_done;
+    return layers > 0;
+  }
+  if (j->uniform >= 0 && (uint64_t)j->uniform < j->min_s) {  // nobody stops before the minimum: bulk
+    layers = (uint32_t)(j->min_s - (uint64_t)j->uniform);
+    return true;
+  }
+  if (!j->active) return false;
+  layers = 1;
+  npix = j->active;
+  list = j->d_list;
+  return true;
+}
 
 // Packs the next samples of the running jobs (least recently served first)
 // into one wavefront of at most step_paths paths.
@@ -970,8 +1031,10 @@ std::vector<Item> pack(gprt_server* sv, bool firsts_only) {
     bool fa = a->passes == 0, fb = b->passes == 0;
     if (fa != fb) return fa;
     if (fa) {
-      uint64_t wa = (uint64_t)(a->pass_target - a->spp_done) * a->npix;
-      uint64_t wb = (uint64_t)(b->pass_target - b->spp_done) * b->npix;
+      uint32_t la = 0, na = 0, lb = 0, nb = 0;
+      const uint32_t *xa, *xb;
+      uint64_t wa = next_work(a, la, na, xa) ? (uint64_t)la * na : 0;
+      uint64_t wb = next_work(b, lb, nb, xb) ? (uint64_t)lb * nb : 0;
       if (wa != wb) return wa < wb;
     }
     return a->last_served < b->last_served;
@@ -980,12 +1043,14 @@ std::vector<Item> pack(gprt_server* sv, bool firsts_only) {
   uint64_t used = 0;
   for (SrvJob* j : order) {
     if (items.size() >= sv->desc.max_jobs) break;
-    uint32_t want = j->pass_target - j->spp_done;
-    uint64_t fit = (sv->step_paths - used) / j->npix;
+    uint32_t want = 0, np = 0;
+    const uint32_t* list = nullptr;
+    if (!next_work(j, want, np, list)) continue;
+    uint64_t fit = (sv->step_paths - used) / np;
     uint32_t layers = (uint32_t)std::min<uint64_t>(want, fit);
     if (layers == 0) continue;
-    items.push_back({j, layers});
-    used += (uint64_t)layers * j->npix;
+    items.push_back({j, layers, np, list});
+    used += (uint64_t)layers * np;
   }
   return items;
 }
@@ -1008,7 +1073,8 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
     pix0[k] = px;
     d.path0 = pp;
     d.pix0 = px;
-    d.npix = j->npix;
+    d.npix = items[k].npix;
+    d.list = items[k].list;
     d.layers = items[k].layers;
     d.root = ps->root;
     d.mat_off = (int)ps->off[kMats];
@@ -1029,8 +1095,8 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
     d.lum2 = j->film.lum2;
     d.count = j->film.count;
     d.cam = ps->cam;
-    pp += items[k].layers * j->npix;
-    px += j->npix;
+    pp += items[k].layers * items[k].npix;
+    px += items[k].npix;
     D = std::max(D, ps->max_depth);
   }
   uint32_t n = (uint32_t)items.size();
@@ -1047,12 +1113,57 @@ int upload_items(gprt_server* sv, const std::vector<Item>& items, bool dry, uint
   return D;
 }
 
+// Lists the next round of every adaptive job whose bulk samples are taken
+// and whose round is not listed yet: one k_active_pixels launch per job on
+// the server stream (after the step that took its last samples) and one
+// read-back of the counts.  A job with no active pixel has finished its pass
+// (then its next pass is listed at once, as gprt_job_render_pass ends a
+// pass that needs no sample).
+int list_rounds(gprt_server* sv) {
+  gprt_ctx* ctx = sv->ctx;
+  for (int again = 0; again < 64; again++) {
+    std::vector<SrvJob*> js;
+    for (auto& kv : sv->jobs) {
+      SrvJob* j = kv.second.get();
+      if (!j->running || j->bd || !j->adaptive || j->active) continue;
+      if (j->uniform >= 0 && (uint64_t)j->uniform < j->min_s) continue;  // its bulk samples come first
+      if (js.size() >= sv->desc.max_jobs) break;
+      js.push_back(j);
+    }
+    if (js.empty()) return GPRT_OK;
+    for (size_t k = 0; k < js.size(); k++) {
+      SrvJob* j = js[k];
+      CK(ctx, cudaMemsetAsync(j->d_list + j->npix, 0, sizeof(uint32_t), sv->stream));
+      launch_active_pixels(j->film, j->pass_target, j->min_s, j->threshold, j->d_list, j->d_list + j->npix,
+                           sv->stream);
+      CK(ctx, cudaMemcpyAsync(sv->h_act + k, j->d_list + j->npix, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              sv->stream));
+    }
+    CK(ctx, cudaStreamSynchronize(sv->stream));
+    bool passed = false;
+    for (size_t k = 0; k < js.size(); k++) {
+      SrvJob* j = js[k];
+      j->active = sv->h_act[k];
+      if (j->active == 0) {
+        advance(sv, j, true);
+        passed = true;
+      }
+    }
+    if (!passed) return GPRT_OK;
+  }
+  return GPRT_OK;
+}
+
 // One batched path-tracing wavefront over the running path-tracing jobs
 // (only those before their first pass with `firsts_only`), and its events
 // (work queued on other streams before it shares the GPU with it).  Returns
 // the number of items run (0: none) or a negative status.
 int pt_step(gprt_server* sv, bool dry, double* ms_out, bool firsts_only) {
   gprt_ctx* ctx = sv->ctx;
+  if (!dry) {
+    int rc = list_rounds(sv);
+    if (rc) return rc;
+  }
   std::vector<Item> items = pack(sv, firsts_only);
   if (items.empty()) return 0;
   uint64_t paths = 0;
@@ -1087,10 +1198,17 @@ int pt_step(gprt_server* sv, bool dry, double* ms_out, bool firsts_only) {
   for (const Item& it : items) {
     SrvJob* j = it.j;
     if (!j) continue;
-    j->spp_done += it.layers;
     j->last_served = sv->st.steps;
-    sv->st.samples += (uint64_t)it.layers * j->npix;
+    sv->st.samples += (uint64_t)it.layers * it.npix;
     if (j->ps) j->ps->last_use = sv->st.steps;
+    if (j->adaptive) {
+      j->total += (uint64_t)it.layers * it.npix;
+      if (j->uniform >= 0) j->uniform = it.npix == j->npix ? j->uniform + it.layers : -1;
+      j->spp_done = (uint32_t)(j->total / j->npix);
+      j->active = 0;  // the round is taken; list_rounds lists the next one
+      continue;
+    }
+    j->spp_done += it.layers;
     if (j->spp_done >= j->pass_target) advance(sv, j, true);
   }
   return (int)items.size();
@@ -1124,9 +1242,11 @@ SrvJob* next_bdpt(gprt_server* sv) {
   return pick;
 }
 
-// Completes the pass of `n` samples queued for BDPT job j (status rc of the
-// launch): waits for it and emits its events.
-void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc, cudaStream_t own) {
+// Completes the work queued for BDPT job j (status rc of the launch): `n`
+// samples per pixel, or, for an adaptive job, `taken` samples in all (a
+// bulk slice or one round; `done`: the round listed no active pixel, so the
+// pass is complete); waits for it and emits its events.
+void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, uint64_t taken, bool done, int rc, cudaStream_t own) {
   if (rc == GPRT_OK) rc = gprt_job_sync(j->bd);
   if (own) {  // back to the job's own stream (the pass ran on bd_first)
     cudaStreamSynchronize(j->bd->stream);
@@ -1137,9 +1257,15 @@ void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, int rc, cudaStream_t ow
     release_job(sv, j);
     return;
   }
-  j->spp_done += n;
   j->last_served = ++sv->bd_rounds;
-  sv->st.samples += (uint64_t)n * j->npix;
+  sv->st.samples += taken;
+  if (j->adaptive) {
+    j->total += taken;
+    j->spp_done = (uint32_t)(j->total / j->npix);
+    if (done) advance(sv, j, true);
+    return;
+  }
+  j->spp_done += n;
   if (j->spp_done >= j->pass_target) advance(sv, j, true);
 }
 
@@ -1171,21 +1297,35 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
     if (firsts && bj && bj->passes != 0) bj = nullptr;  // its later pass waits too
   }
   uint32_t bn = 0;
+  uint64_t taken = 0;
+  bool round_empty = false;
   int brc = GPRT_OK;
   cudaStream_t own = nullptr;
   if (bj) {
     bool first = bj->passes == 0;
     uint64_t cap = first ? kBdptFirstPassSamples : kBdptStepSamples;
     uint64_t per = std::max<uint64_t>(1, cap / std::max<uint32_t>(1, bj->npix));
-    bn = (uint32_t)std::min<uint64_t>(bj->pass_target - bj->spp_done, per);
     if (first && sv->bd_first) {
       own = bj->bd->stream;
       bj->bd->stream = sv->bd_first;
     }
-    brc = gprt_job_add_samples(bj->bd, bn);  // queued on the first-pass (or the job's) stream
+    const int64_t uni = bj->bd->uniform_count;
+    if (!bj->adaptive || (uni >= 0 && (uint64_t)uni < bj->min_s)) {
+      // whole samples per pixel: the pass (or, adaptive, its minimum) in slices
+      uint32_t want = bj->adaptive ? (uint32_t)(bj->min_s - (uint64_t)uni) : bj->pass_target - bj->spp_done;
+      bn = (uint32_t)std::min<uint64_t>(want, per);
+      taken = (uint64_t)bn * bj->npix;
+      brc = gprt_job_add_samples(bj->bd, bn);  // queued on the first-pass (or the job's) stream
+    } else {
+      // one round: a sample for each pixel still active (listed on the device)
+      uint32_t active = 0;
+      brc = job_adaptive_round(bj->bd, bj->pass_target, bj->min_s, bj->threshold, &active);
+      taken = active;
+      round_empty = active == 0;
+    }
   }
   int n = pt_step(sv, dry, ms_out, firsts);
-  if (bj) finish_bdpt(sv, bj, bn, brc, own);
+  if (bj) finish_bdpt(sv, bj, bn, taken, round_empty, brc, own);
   if (n < 0) return n;
   return n + (bj ? 1 : 0);
 }
@@ -1365,7 +1505,8 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   sv->path_bytes = bytes;
   sv->prefix_bytes = (16 + 2 * (size_t)(d.max_jobs + 1) * 4 + 255) & ~(size_t)255;
   sv->err_off = (sv->prefix_bytes + (size_t)d.max_jobs * sizeof(DevItem) + 255) & ~(size_t)255;
-  sv->table_bytes = sv->err_off + (size_t)d.max_jobs * sizeof(uint32_t);
+  sv->act_off = (sv->err_off + (size_t)d.max_jobs * sizeof(uint32_t) + 255) & ~(size_t)255;
+  sv->table_bytes = sv->act_off + (size_t)d.max_jobs * sizeof(uint32_t);
   if (sv->path_bytes + sv->table_bytes > d.hbm_budget_bytes) {
     free_all(b);
     return fail(ctx, GPRT_E_ADMISSION, "the budget does not cover the path state of one step");
@@ -1377,6 +1518,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
     return fail(ctx, GPRT_E_OOM, "item table allocation failed");
   }
   sv->h_err = reinterpret_cast<uint32_t*>(sv->h_table + sv->err_off);
+  sv->h_act = reinterpret_cast<uint32_t*>(sv->h_table + sv->act_off);
   if (cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_all(b);
     cudaFreeHost(sv->h_table);
@@ -1669,7 +1811,7 @@ int gprt_server_autotune(gprt_server* sv, double max_step_ms, gprt_tune_result* 
     }
     std::vector<Item> items = pack(sv, false);
     uint64_t n = 0;
-    for (auto& it : items) n += (uint64_t)it.layers * it.j->npix;
+    for (auto& it : items) n += (uint64_t)it.layers * it.npix;
     double ms = 0;
     if (step_impl(sv, true, &ms) <= 0) return -1.0;  // warm-up (and graph capture)
     double total = 0;

@@ -463,17 +463,25 @@ int gprt_render_noalloc(gprt_scene* scene, uint32_t spp, uint64_t seed, float* r
  *     pass and per-pass latency), completion, refusal and cancellation.
  * Passes follow getSamplesForPass (progressive.go:98-123) over
  * initial_samples / max_samples_per_pixel / max_passes of the request's
- * gprt_job_desc, every pixel taking every sample (the scene's adaptive
- * stopping is not applied).  A job's film equals, bit for bit, the film of a
- * gprt_job with the same scene, seed and sample count: each sample is keyed
- * by (seed, pixel, sample index) and each pixel accumulates its samples in
- * order, whatever else shares the wavefront.  BDPT requests
+ * gprt_job_desc, with the scene's adaptive stop as gprt_job_render_pass
+ * applies it (tile_renderer.go:51-101): a scene with adaptive_min_samples <
+ * 1 brings every pixel to the pass minimum, then takes rounds of one sample
+ * per pixel still active (below the pass target and not converged), one
+ * round per step, until no pixel is; the pass event then reports the
+ * average sample count, and the job ends when that reaches
+ * max_samples_per_pixel or after max_passes (progressive.go:339-361).  A
+ * job's film equals, bit for bit, the film of a gprt_job with the same
+ * scene and seed given the same samples (gprt_job_add_samples, or
+ * gprt_job_render_pass per pass): each sample is keyed by (seed, pixel,
+ * sample index) and each pixel accumulates its samples in order, whatever
+ * else shares the wavefront.  BDPT requests
  * (integrator = GPRT_INTEGRATOR_BDPT) are admitted with a private copy of
  * the scene and the BDPT working set of one chunk (both counted against the
  * budget, held until release); each step renders, beside the batched
  * path-tracing wavefront and on the job's own stream, up to 2^18 samples
- * (whole samples per pixel) of one BDPT job's pass: jobs before their first
- * pass first, then the least recently served.  Their film equals that of a
+ * (whole samples per pixel) of one BDPT job's pass, or one round of its
+ * adaptive pass: jobs before their first pass first, then the least
+ * recently served.  Their film equals that of a
  * gprt_job on the same scene given the same samples, up to the summation
  * order of the light-tracing splats (float atomics; applied after each
  * slice). */

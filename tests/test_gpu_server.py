@@ -66,7 +66,10 @@ def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
     import gprt
     jobs = [("cornell", 3, 8, 4), ("ico", 5, 6, 2), ("spheres_a", 7, 12, 4), ("spheres_b", 11, 4, 1),
             ("cornell", 13, 4, 4), ("textured", 17, 4, 2), ("spot", 19, 4, 4), ("uvmesh", 23, 4, 2)]
-    plain = [_plain_film(scenes[n], seed, spp) for n, seed, spp, _ in jobs]
+    # the textured scene samples adaptively (AdaptiveMinSamples 0.15): its
+    # reference is the per-job progressive render, the others' fixed spp
+    plain = [_progressive(scenes[n], _cfg(spp, per, seed))[0] if n == "textured" else _plain_film(scenes[n], seed, spp)
+             for n, seed, spp, per in jobs]
     # a small step capacity forces jobs to share steps and to be split across them
     sv = gprt.RenderServer(ctx, step_paths=3 * 64 * 48)
     tickets = [sv.submit(scenes[n], _cfg(spp, per, seed)) for n, seed, spp, per in jobs]
@@ -77,7 +80,7 @@ def test_jobs_in_the_mix_equal_their_plain_films(ctx, scenes):
         _same(sv.film(t), p)
     st = sv.stats()
     assert st["resident_scenes"] == 7  # the two cornell requests share one pooled copy
-    assert st["samples"] == sum(scenes[n].width * scenes[n].height * spp for n, _, spp, _ in jobs)
+    assert st["samples"] == sum(int(p[3].sum()) for p in plain)
     sv.close()
 
 
@@ -113,7 +116,10 @@ def test_device_bound_fails_only_its_job(ctx, scenes):
     normal.close()
     # the server: the capped job shares its steps with normal jobs
     jobs = [("cornell", 3, 8, 4), ("spheres_a", 7, 8, 4), ("ico", 5, 4, 2)]
-    plain = [_plain_film(scenes[n], seed, spp) for n, seed, spp, _ in jobs]
+    # the textured scene samples adaptively (AdaptiveMinSamples 0.15): its
+    # reference is the per-job progressive render, the others' fixed spp
+    plain = [_progressive(scenes[n], _cfg(spp, per, seed))[0] if n == "textured" else _plain_film(scenes[n], seed, spp)
+             for n, seed, spp, per in jobs]
     sv = gprt.RenderServer(ctx, step_paths=1 << 16)
     bad = sv.submit(capped, _cfg(4, 2, 9))
     tickets = [sv.submit(scenes[n], _cfg(spp, per, seed)) for n, seed, spp, per in jobs]
@@ -428,3 +434,57 @@ def test_bdpt_admission_by_budget(ctx, scenes):
     assert any(e.ticket == tp and e.kind == "done" for e in ev)
     _same(sv.film(tp), _plain_film(scenes["spheres_b"], 3, 2))
     sv.close()
+
+
+def _adaptive(scene, min_frac=0.25, threshold=0.3):
+    scene.sampling.adaptive_min_samples = min_frac
+    scene.sampling.adaptive_threshold = threshold
+    return scene
+
+
+def _progressive(g, cfg, integrator=None):
+    # the per-job progressive render (gprt_job_render_pass per pass, with the
+    # scene's adaptive stop): its film and each pass's average sample count
+    import gprt
+    r = gprt.ProgressiveRaytracer(g, cfg, integrator) if integrator else gprt.ProgressiveRaytracer(g, cfg)
+    avgs = [int(res.stats.average_samples) for res in r.render_progressive()]
+    f = r.film()
+    r.close()
+    return f, avgs
+
+
+def test_adaptive_sampling_in_the_server_equals_progressive_render(ctx, scenes):
+    """A scene with AdaptiveMinSamples < 1 renders in the server as through
+    gprt_job_render_pass: per pass every pixel first takes the pass minimum,
+    then rounds of one sample per pixel still active (below the pass target
+    and not converged, tile_renderer.go:51-101) until none is.  Path-tracing
+    films agree bit for bit, BDPT films up to the splat summation order, and
+    the pass events report the per-job render's average sample counts;
+    fixed-spp jobs in the same steps are unchanged."""
+    import gprt
+    from gprt import scenes as S
+    made = [gprt.GpuScene(ctx, _adaptive(S.cornell_baseline(48)).to_desc()),
+            gprt.GpuScene(ctx, _adaptive(S.default_style_scene(5, width=64, height=48)).to_desc()),
+            gprt.GpuScene(ctx, _adaptive(S.cornell_boxes_bdpt(32, max_depth=5)).to_desc())]
+    cfgs = [_cfg(16, 4, 31), _cfg(24, 6, 32), _cfg(8, 4, 34)]
+    integ = [None, None, gprt.BDPTIntegrator()]
+    ref = [_progressive(g, c, i) for g, c, i in zip(made, cfgs, integ)]
+    # the stop took effect: some pixels ended below the target
+    for (film, _), c in zip(ref, cfgs):
+        assert film[3].min() < c.max_samples_per_pixel
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    fixed = sv.submit(scenes["spheres_b"], _cfg(4, 2, 33))
+    ts = [sv.submit(g, c, integrator=i) for g, c, i in zip(made, cfgs, integ)]
+    ev = sv.run_until_idle()
+    for t, (film, avgs), i in zip(ts, ref, integ):
+        kinds = [e.kind for e in ev if e.ticket == t]
+        assert kinds[0] == "admitted" and kinds[-1] == "done"
+        assert [e.samples_per_pixel for e in ev if e.ticket == t and e.kind == "pass"] == avgs
+        if i is None:
+            _same(sv.film(t), film)
+        else:
+            _close_bdpt(sv.film(t), film)
+    _same(sv.film(fixed), _plain_film(scenes["spheres_b"], 33, 4))
+    sv.close()
+    for g in made:
+        g.close()
