@@ -5,8 +5,10 @@ Two comparisons:
   (same seed, pixel, sample index), so both render the same paths; per-pixel
   means agree up to FP32-vs-FP64 rounding, except the few paths where a
   rounding difference flips a discrete decision (an edge hit, a Fresnel
-  draw).  Tolerance: median relative pixel error <= 1e-4, and at most 2 % of
-  pixels off by more than 1e-2 relative (+1e-4 absolute).
+  draw).  Tolerance: median relative pixel error <= 1e-6, and at most 0.5 %
+  of pixels (BDPT 1 %) off by more than 1e-2 relative (+1e-4 absolute).  On
+  GB300 the medians measure 3e-8 - 3.5e-7 and the off-pixel shares at most
+  0.22 % (path tracing, cone_test) and 0.54 % (BDPT, cone_test).
 * statistics: against the committed 4096-spp oracle reference
   (tests/golden), relative RMSE(gpu_N) <= 1.10 x RMSE(oracle_N), both
   averaged over 4 seeds and taken on the displayed range (radiance clamped
@@ -119,8 +121,8 @@ def test_pt_same_inputs_parity(ctx, oracle, name):
     med, frac = same_input_stats(gpu, r.image())
     print(name, "median rel", med, "frac > 1e-2", frac)
     assert stats.min_samples == 16 and stats.total_samples == 16 * stats.total_pixels
-    assert med <= 1e-4, (med, frac)
-    assert frac <= 0.02, (med, frac)
+    assert med <= 1e-6, (med, frac)
+    assert frac <= 0.005, (med, frac)
 
 
 @pytest.mark.parametrize("name", ["cornell_boxes", "cornell_spheres", "default_scene", "quadrics",
@@ -146,8 +148,8 @@ def test_bdpt_same_inputs_parity(ctx, oracle, name):
     r, _ = oracle_render(oracle, scene, 8, seed=5, integrator=1)
     med, frac = same_input_stats(gpu, r.image())
     print(name, "bdpt median rel", med, "frac > 1e-2", frac)
-    assert med <= 1e-4, (med, frac)
-    assert frac <= 0.03, (med, frac)
+    assert med <= 1e-6, (med, frac)
+    assert frac <= 0.01, (med, frac)
 
 
 def _rel_rmse(img, ref):
@@ -210,7 +212,10 @@ def test_progressive_passes_schedule(ctx):
 
 def test_adaptive_sampling_matches_oracle_counts(ctx, oracle):
     """Adaptive stop (tile_renderer.go:77-101) with the reference Cornell
-    sampling config (20 % minimum, 0.5 % threshold)."""
+    sampling config (20 % minimum, 0.5 % threshold).  The stop compares a
+    float32 (GPU) or float64 (oracle) relative error with the threshold, so a
+    pixel right at it may stop one sample apart; on GB300 every count
+    matched."""
     import gprt
     from gprt import scenes
     scene = scenes.cornell_scene(scenes.CORNELL_SPHERES, camera=_cam(32))
@@ -223,7 +228,7 @@ def test_adaptive_sampling_matches_oracle_counts(ctx, oracle):
     _, _, _, ocnt = orr.film()
     assert st.max_samples_used <= 40 and st.min_samples >= 8
     assert (cnt >= 8).all() and (cnt <= 40).all()
-    assert np.mean(cnt == ocnt) > 0.9, np.mean(cnt == ocnt)
+    assert np.mean(cnt == ocnt) >= 0.99, np.mean(cnt == ocnt)
 
 
 def test_rgba8_and_tiles_follow_vec3_to_color(ctx):
