@@ -340,35 +340,37 @@ __device__ __forceinline__ bool occluded(const DevScene& sc, float3 o, float3 d,
 // ---------------------------------------------------------------- vertex store
 // Subpath vertices live in global memory as 5 float4 fields indexed
 // [vertex * ns + sample], so the 32 lanes of a warp (32 consecutive samples)
-// read one field of one vertex in a single coalesced access.
+// read one field of one vertex in a single coalesced access.  The first two
+// fields hold what a pdf request of the MIS weight reads of a vertex
+// (position, normal, material, flags, light), so those requests load two
+// fields; the forward and reverse pdfs live in the pdf record.
 __device__ __forceinline__ void put_vert(const DevBdpt& B, int v, uint32_t i, const BVert& x, float pre = 0.f) {
   size_t k = (size_t)v * B.ns + i;
-  B.v[0][k] = make_float4(x.p.x, x.p.y, x.p.z, x.fwd);
-  B.v[1][k] = make_float4(x.n.x, x.n.y, x.n.z, x.rev);
+  B.v[0][k] = make_float4(x.p.x, x.p.y, x.p.z, __int_as_float((x.mat + 1) | (x.flags << 24)));
+  B.v[1][k] = make_float4(x.n.x, x.n.y, x.n.z, __int_as_float(x.light));
   B.v[2][k] = make_float4(x.beta.x, x.beta.y, x.beta.z, x.wi.x);
   B.v[3][k] = make_float4(x.Le.x, x.Le.y, x.Le.z, x.wi.y);
-  B.v[4][k] = make_float4(x.wi.z, __int_as_float((x.mat + 1) | (x.flags << 24)), __int_as_float(x.light),
-                          __uint_as_float(x.prim));
+  B.v[4][k] = make_float4(x.wi.z, __uint_as_float(x.prim), 0.f, 0.f);
   B.pdf[k] = make_float4(x.fwd, __int_as_float(x.flags | ((x.light + 1) << 8)), x.rev, pre);
   if (B.uv) B.uv[k] = x.mat >= 0 ? x.uv : make_float2(0.f, 0.f);
 }
 
 __device__ __forceinline__ BVert get_vert(const DevBdpt& B, int v, uint32_t i) {
   size_t k = (size_t)v * B.ns + i;
-  float4 a = B.v[0][k], b = B.v[1][k], c = B.v[2][k], d = B.v[3][k], e = B.v[4][k];
+  float4 a = B.v[0][k], b = B.v[1][k], c = B.v[2][k], d = B.v[3][k], e = B.v[4][k], q = B.pdf[k];
   BVert x;
   x.p = f3(a);
-  x.fwd = a.w;
+  int mf = __float_as_int(a.w);
+  x.mat = (mf & 0xFFFFFF) - 1;
+  x.flags = (mf >> 24) & 0xFF;
   x.n = f3(b);
-  x.rev = B.pdf[k].z;  // the reverse pdf lives in the pdf record (patched after the next bounce)
+  x.light = __float_as_int(b.w);
+  x.fwd = q.x;
+  x.rev = q.z;  // patched after the next bounce
   x.beta = f3(c);
   x.Le = f3(d);
   x.wi = make_float3(c.w, d.w, e.x);
-  int mf = __float_as_int(e.y);
-  x.mat = (mf & 0xFFFFFF) - 1;
-  x.flags = (mf >> 24) & 0xFF;
-  x.light = __float_as_int(e.z);
-  x.prim = __float_as_uint(e.w);
+  x.prim = __float_as_uint(e.y);
   x.uv = B.uv ? B.uv[k] : make_float2(0.f, 0.f);
   return x;
 }
