@@ -168,7 +168,7 @@ void run_chunk(gprt_job* j, const ChunkDesc& ch) {
     launch_accumulate(j->film, j->paths, ch, 256, j->stream);
   }
   // raygen, accumulate; extend, (slot order,) shade, shadow per bounce
-  j->launches += 2 + (uint64_t)(sc.has_infinite ? 4 : 3) * sc.max_depth;
+  j->launches += 2 + (uint64_t)(sc.has_infinite || sc.has_specular ? 4 : 3) * sc.max_depth;
 }
 
 // Adds `spp` samples to each of `npix` pixels (all pixels, or the list).
@@ -276,6 +276,8 @@ int upload_rest(gprt_ctx* ctx, gprt_scene* s) {
     return fail(ctx, GPRT_E_INVALID, "the scene has too many primitives for 32-bit primitive ids");
   }
   d.has_infinite = h.has_infinite;
+  d.has_specular = 0;
+  for (const DevMaterial& m : h.materials) d.has_specular |= m.kind == kMatMetal || m.kind == kMatDielectric;
   d.world_center = make_float3((float)h.world_center[0], (float)h.world_center[1], (float)h.world_center[2]);
   d.world_radius = (float)h.world_radius;
   d.cam = h.cam;

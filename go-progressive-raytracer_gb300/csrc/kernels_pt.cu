@@ -270,10 +270,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st) {
-  // the hit-first slot order pays where rays escape to an infinite light
-  // (missed rays are then a large share); in closed scenes it is overhead
+  // the shading-group slot order pays where rays escape to an infinite
+  // light (missed rays are then a large share) or where specular and
+  // diffuse materials mix; in closed all-diffuse scenes it is overhead
   DevPaths Po = P;
-  if (sc.has_infinite) launch_hit_order(sc, P, cur, P.capacity, sm_count_current(), st);
+  if (sc.has_infinite || sc.has_specular) launch_hit_order(sc, P, cur, P.capacity, sm_count_current(), st);
   else Po.order = nullptr;
   if (P.variant & GPRT_JOB_SHADE_OCCUPANCY) {
     int g = std::max(1, (int)((int64_t)grid * block / 192));

@@ -114,6 +114,7 @@ struct DevScene {
   int n_lights;
   uint32_t quad_base, sphere_base, quadric_base, n_prims;
   int has_infinite;
+  int has_specular;  // a Metal or Dielectric material: shading groups pay even without misses
   float3 world_center;
   float world_radius;
   DevCamera cam;
