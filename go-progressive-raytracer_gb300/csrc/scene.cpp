@@ -234,9 +234,16 @@ struct BNode {
   }
 };
 
+// Scenes of at most this many primitives get one leaf per primitive type
+// under the root: every ray then tests the same primitives in the same
+// order, so the lanes of a warp stay converged, where a tree walk would
+// split them over a few nodes each.
+constexpr size_t kFlatScenePrims = 32;
+
 struct Builder {
   std::vector<Ref>& refs;
   const PrimArray& prims;
+  bool flat = false;  // one leaf per type (kFlatScenePrims)
   explicit Builder(std::vector<Ref>& r, const PrimArray& p) : refs(r), prims(p) {}
 
   static int max_leaf(int type) { return type == kPrimQuad || type == kPrimQuadric ? 2 : 4; }
@@ -266,7 +273,7 @@ struct Builder {
       n->count = cnt;
       return std::move(n);
     };
-    if (cnt <= 1) return make_leaf();
+    if (cnt <= 1 || flat) return make_leaf();
     // binned SAH over the three axes (16 bins)
     const int B = 16;
     double best_cost = INFINITY;
@@ -858,6 +865,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
   }
   if (!out.device_bvh) {
     Builder bld(all, prims);
+    bld.flat = all.size() <= kFlatScenePrims;
     std::unique_ptr<BNode> roots[4];
     for (int t = 0; t < 4; t++)
       if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
