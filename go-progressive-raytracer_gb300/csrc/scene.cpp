@@ -234,11 +234,13 @@ struct BNode {
   }
 };
 
-// Scenes of at most this many primitives get one leaf per primitive type
-// under the root: every ray then tests the same primitives in the same
-// order, so the lanes of a warp stay converged, where a tree walk would
-// split them over a few nodes each.
-constexpr size_t kFlatScenePrims = 32;
+// Scenes of at most kFlatScenePrims primitives, of which at most
+// kFlatSceneSpheres spheres, get one leaf per primitive type under the root:
+// every ray then tests the same primitives in the same order, so the lanes
+// of a warp stay converged, where a tree walk would split them over a few
+// nodes each.  Sphere tests are the costlier part of a flat leaf: the
+// batched sphere scenes (14-32 spheres at the small end) measured slower flat.
+constexpr size_t kFlatScenePrims = 32, kFlatSceneSpheres = 8;
 
 struct Builder {
   std::vector<Ref>& refs;
@@ -865,7 +867,7 @@ bool build_scene(const gprt_scene_desc* d, HostScene& out, std::string& err, boo
   }
   if (!out.device_bvh) {
     Builder bld(all, prims);
-    bld.flat = all.size() <= kFlatScenePrims;
+    bld.flat = all.size() <= kFlatScenePrims && refs[kPrimSphere].size() <= kFlatSceneSpheres;
     std::unique_ptr<BNode> roots[4];
     for (int t = 0; t < 4; t++)
       if (!refs[t].empty()) roots[t] = bld.build(off[t], off[t] + (uint32_t)refs[t].size(), 0);
