@@ -92,7 +92,7 @@ struct DevPaths {
   float4* sh_d;    // shadow ray direction.xyz, skip primitive
   float4* sh_c;    // contribution rgb, origin index of its path (uint bits)
   int* sh_root;    // BVH root of each shadow ray (multi-scene wavefronts; null: the scene's root)
-  uint32_t* order; // slots of the queue with hits first, misses last (null: queue order)
+  uint32_t* order; // slots of the queue by shading group (order_slots; null: queue order)
   uint32_t* counters;  // [0],[1] path queues, [2] shadow queue, [3] error bits, [4],[5] ray fetch, [6],[7] order
   // multi-job wavefronts: one error word per work item and the items' first
   // origin indices (null for a single job: its error word is counters[3])
@@ -148,7 +148,7 @@ void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool
 void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
                       cudaStream_t st);
 void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
-// Builds P.order for queue `cur` (hits first, misses last) before shading.
+// Builds P.order for queue `cur` (slots by shading group) before shading.
 void launch_hit_order(const DevScene& sc, const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st);
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,
                      int grid, cudaStream_t st);
