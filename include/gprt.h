@@ -506,7 +506,7 @@ typedef struct gprt_event {
   uint64_t ticket;
   uint32_t kind;              /* GPRT_EV_* */
   uint32_t pass_number;       /* passes completed */
-  uint32_t samples_per_pixel; /* samples every pixel of the film holds */
+  uint32_t samples_per_pixel; /* samples every pixel of the film holds (adaptive scenes: their average, truncated) */
   int32_t status;
   double t_ms;                /* host time of the event, ms since the server was created */
   double submit_ms;           /* host time the request was submitted */
