@@ -209,11 +209,12 @@ def l2_fraction(achieved, torch):
 
 # Path-state bytes of one shading step (the SoA queues of the wavefront):
 # a shaded path reads ray origin, direction, hit, weight, roulette
-# throughput, radiance and ids (7 x 16 B); a continuing path writes all but
-# the hit to the next queue (6 x 16 B); a finished path writes its radiance
-# (16 B); a shadow ray writes origin, direction, contribution (3 x 16 B) and
-# its BVH root (4 B).
-SHADE_READ_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 96, 16, 52
+# throughput, radiance and ids (7 x 16 B), except at bounce 0 (one shaded
+# path per sample), where throughput and radiance are implied (5 x 16 B); a
+# continuing path writes all but the hit to the next queue (6 x 16 B); a
+# finished path writes its radiance (16 B); a shadow ray writes origin,
+# direction, contribution (3 x 16 B) and its BVH root (4 B).
+SHADE_READ_B, SHADE_BOUNCE0_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 80, 96, 16, 52
 
 
 def shade_roofline(cnt, kc, kc_batches, samples, peak, peak_kind, timing_source):
@@ -222,8 +223,8 @@ def shade_roofline(cnt, kc, kc_batches, samples, peak, peak_kind, timing_source)
     exactly once, so continuing paths = shaded - samples.  Material, light
     and item tables (a few KB per job, L1-resident) are not counted."""
     shaded, shadow = cnt["extend_rays"], cnt["shadow_rays"]
-    alg = (SHADE_READ_B * shaded + SHADE_CONT_B * (shaded - samples) + SHADE_DONE_B * samples +
-           SHADE_SHADOW_B * shadow)
+    alg = (SHADE_READ_B * (shaded - samples) + SHADE_BOUNCE0_B * samples + SHADE_CONT_B * (shaded - samples) +
+           SHADE_DONE_B * samples + SHADE_SHADOW_B * shadow)
     # per launch of the timed configuration: the counting run may split the
     # batch into steps of another size
     launches = max(1.0, kc["shade_launches"] / kc_batches)

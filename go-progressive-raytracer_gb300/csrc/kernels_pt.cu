@@ -95,9 +95,7 @@ __global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch)
     Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
     Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(sc.root));
     Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
-    Q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    Q.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    Q.ids[p] = make_uint4(pix, sample, rng.pos, 0u);
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, 0u);  // roulette throughput 1, radiance 0: implied at bounce 0
     P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -263,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     bool live = i < n;
     if (live) shade_path(sc, P, P.q[cur], P.hit, slot, ch.seed, bounce, o);
     push_shade_out(P, cur, live, o);
-    if (inext < n) prefetch_slot(P.q[cur], P.hit, snext);
+    if (inext < n) prefetch_slot(P.q[cur], P.hit, snext, bounce > 0);
     slot = snext;
   }
 }

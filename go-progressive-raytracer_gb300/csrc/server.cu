@@ -99,9 +99,7 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
     Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
     Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(it.root));
     Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
-    Q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    Q.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    Q.ids[p] = make_uint4(pix, sample, rng.pos, k);
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, k);  // roulette throughput 1, radiance 0: implied at bounce 0
     P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -154,7 +152,7 @@ __device__ __forceinline__ void srv_shade(const DevScene& pool, const DevPaths& 
       shade_path(v, P, Q, P.hit, i, it.seed, bounce, o);
     }
     push_shade_out(P, cur, live, o);
-    if (inext < n) prefetch_slot(Q, P.hit, snext);
+    if (inext < n) prefetch_slot(Q, P.hit, snext, bounce > 0);
     slot = snext;
   }
 }
