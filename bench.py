@@ -210,11 +210,12 @@ def l2_fraction(achieved, torch):
 # Path-state bytes of one shading step (the SoA queues of the wavefront):
 # a shaded path reads ray origin, direction, hit, weight, roulette
 # throughput, radiance and ids (7 x 16 B), except at bounce 0 (one shaded
-# path per sample), where throughput and radiance are implied (5 x 16 B); a
+# path per sample), where weight, throughput and radiance are implied
+# (4 x 16 B); a
 # continuing path writes all but the hit to the next queue (6 x 16 B); a
 # finished path writes its radiance (16 B); a shadow ray writes origin,
 # direction, contribution (3 x 16 B) and its BVH root (4 B).
-SHADE_READ_B, SHADE_BOUNCE0_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 80, 96, 16, 52
+SHADE_READ_B, SHADE_BOUNCE0_B, SHADE_CONT_B, SHADE_DONE_B, SHADE_SHADOW_B = 112, 64, 96, 16, 52
 
 
 def shade_roofline(cnt, kc, kc_batches, samples, peak, peak_kind, timing_source):

@@ -151,7 +151,7 @@ void run_chunk(gprt_job* j, const ChunkDesc& ch) {
   for (int b = 0; b < sc.max_depth; b++) {
     {
       TimedLaunch t(j, 0);
-      launch_pt_extend(sc, j->paths, cur, block, g, j->stream);
+      launch_pt_extend(sc, j->paths, cur, b, block, g, j->stream);
     }
     {
       TimedLaunch t(j, 1);
@@ -924,7 +924,7 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
   launch_pt_raygen(sc, film, P, ch, block, st);
   int cur = 0;
   for (int b = 0; b < sc.max_depth; b++) {
-    launch_pt_extend(sc, P, cur, block, grid, st);
+    launch_pt_extend(sc, P, cur, b, block, grid, st);
     launch_pt_shade(sc, P, ch, cur, b, block, grid, st);
     launch_pt_shadow(sc, P, cur, block, grid, st);
     cur ^= 1;

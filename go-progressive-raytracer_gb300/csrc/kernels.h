@@ -147,7 +147,7 @@ void launch_intersect(const DevScene& sc, const gprt_ray* rays, uint32_t n, bool
 // path tracing (pkg/integrator/path_tracing.go) in wavefront form
 void launch_pt_raygen(const DevScene& sc, const DevFilm& film, const DevPaths& P, const ChunkDesc& ch, int block,
                       cudaStream_t st);
-void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st);
+void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int bounce, int block, int grid, cudaStream_t st);
 // Builds P.order for queue `cur` (slots by shading group) before shading.
 void launch_hit_order(const DevScene& sc, const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st);
 void launch_pt_shade(const DevScene& sc, const DevPaths& P, const ChunkDesc& ch, int cur, int bounce, int block,

@@ -94,8 +94,9 @@ __global__ void k_pt_raygen(DevScene sc, DevFilm film, DevPaths P, ChunkDesc ch)
     const PathBuf& Q = P.q[0];
     Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
     Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(sc.root));
-    Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
-    Q.ids[p] = make_uint4(pix, sample, rng.pos, 0u);  // roulette throughput 1, radiance 0: implied at bounce 0
+    // weight 1 with origin index p, roulette throughput 1 and radiance 0 are
+    // implied at bounce 0 (not stored)
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, 0u);
     P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -132,7 +133,7 @@ struct ExtendSource {
   const float4* ray_d;
   float4* hit;
   const uint32_t* n;
-  const float4* weight;  // origin index of each path (.w), read when reporting a bound
+  const float4* weight;  // origin index of each path (.w), read when reporting a bound; null at bounce 0 (slot = origin)
   ErrSink err;
   __device__ uint32_t count() const { return *n; }
   __device__ void load(uint32_t i, float3& o, float3& d, float& tmin, float& tmax, uint32_t& skip, int& rt) const {
@@ -149,7 +150,7 @@ struct ExtendSource {
   __device__ void store(uint32_t i, const Hit& h) const {
     bool any = h.prim != kNoHit;
     if (h.prim == kOverflowHit) {
-      err.report(__float_as_uint(weight[i].w), kErrStackOverflow);
+      err.report(weight ? __float_as_uint(weight[i].w) : i, kErrStackOverflow);
       any = false;
     }
     hit[i] = make_float4(any ? h.t : -1.f, __uint_as_float(any ? h.prim : kNoHit), h.u, h.v);
@@ -211,8 +212,9 @@ static int sm_count_current() {
   return sms;
 }
 
-void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int block, int grid, cudaStream_t st) {
-  ExtendSource src{P.q[cur].ray_o, P.q[cur].ray_d, P.hit, P.counters + cur, P.q[cur].weight, err_sink(P)};
+void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int bounce, int block, int grid, cudaStream_t st) {
+  ExtendSource src{P.q[cur].ray_o, P.q[cur].ray_d, P.hit, P.counters + cur, bounce > 0 ? P.q[cur].weight : nullptr,
+                   err_sink(P)};
   if (P.variant & GPRT_JOB_SIMPLE_EXTEND) {
     int b = std::min(block, 256);
     if (P.stats) k_pt_extend_simple<true><<<grid, b, 0, st>>>(sc, src, P.counters, cur, P.stats);

@@ -28,14 +28,19 @@ struct ShadeOut {
 __device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P, const PathBuf& Q,
                                            const float4* hits, uint32_t i, uint64_t seed, int bounce, ShadeOut& out) {
   out.cont = false;
-  float4 o4 = Q.ray_o[i], d4 = Q.ray_d[i], h4 = hits[i], w4 = Q.weight[i];
+  float4 o4 = Q.ray_o[i], d4 = Q.ray_d[i], h4 = hits[i];
   uint4 ids = Q.ids[i];
   float3 d = f3(d4);
-  float3 W = f3(w4), thr = f3(1.f, 1.f, 1.f), L = f3(0.f, 0.f, 0.f);  // at bounce 0 as raygen leaves them (not stored)
+  // at bounce 0 the path state raygen implies (not stored): weight 1, origin
+  // index = the slot, roulette throughput 1, radiance 0
+  float4 w4 = make_float4(1.f, 1.f, 1.f, __uint_as_float(i));
+  float3 thr = f3(1.f, 1.f, 1.f), L = f3(0.f, 0.f, 0.f);
   if (bounce > 0) {
+    w4 = Q.weight[i];
     thr = f3(Q.thr[i]);
     L = f3(Q.L[i]);
   }
+  float3 W = f3(w4);
   out.o = o4;
   out.d = d4;
   Rng rng;
@@ -116,14 +121,14 @@ __device__ __forceinline__ void shade_path(const DevScene& sc, const DevPaths& P
   out.ids = make_uint4(ids.x, ids.y, rng.pos, ids.w);
 }
 
-// Brings the shading inputs of slot i of queue Q (ray, hit, weight, ids and,
-// after bounce 0 (`state`), roulette throughput and radiance) into L2 ahead
-// of their use: a grid-stride shading loop issues this for its next slot at
-// the end of the current one, so the next iteration's dependent loads meet
-// L2 instead of DRAM.
+// Brings the shading inputs of slot i of queue Q (ray, hit, ids and, after
+// bounce 0 (`state`), weight, roulette throughput and radiance) into L2
+// ahead of their use: a grid-stride shading loop issues this for its next
+// slot at the end of the current one, so the next iteration's dependent
+// loads meet L2 instead of DRAM.
 __device__ __forceinline__ void prefetch_slot(const PathBuf& Q, const float4* hits, uint32_t i, bool state) {
-  const void* a[7] = {Q.ray_o + i, Q.ray_d + i, hits + i, Q.weight + i, Q.ids + i, Q.thr + i, Q.L + i};
-  const int m = state ? 7 : 5;
+  const void* a[7] = {Q.ray_o + i, Q.ray_d + i, hits + i, Q.ids + i, Q.weight + i, Q.thr + i, Q.L + i};
+  const int m = state ? 7 : 4;
   for (int k = 0; k < m; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a[k]));
 }
 

@@ -98,8 +98,9 @@ __global__ void k_srv_raygen(DevPaths P, const StepHdr* hdr, const uint32_t* pat
     const PathBuf& Q = P.q[0];
     Q.ray_o[p] = make_float4(o.x, o.y, o.z, __uint_as_float(kNoHit));
     Q.ray_d[p] = make_float4(d.x, d.y, d.z, __int_as_float(it.root));
-    Q.weight[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(p));
-    Q.ids[p] = make_uint4(pix, sample, rng.pos, k);  // roulette throughput 1, radiance 0: implied at bounce 0
+    // weight 1 with origin index p, roulette throughput 1 and radiance 0 are
+    // implied at bounce 0 (not stored)
+    Q.ids[p] = make_uint4(pix, sample, rng.pos, k);
     P.Lout[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -898,7 +899,7 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
   int cur = 0;
   for (int b = 0; b < D; b++) {
     open();
-    launch_pt_extend(pool, P, cur, block, grid, st);
+    launch_pt_extend(pool, P, cur, b, block, grid, st);
     close();
     open();
     k_srv_hit_order<<<std::max(1, std::min((int)((sv->step_paths + 1023) / 1024), sv->ctx->sm_count * 2)), 1024, 0,
