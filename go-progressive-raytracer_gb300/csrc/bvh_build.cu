@@ -227,14 +227,17 @@ __global__ void k_collapse(TreeView T, const uint2* qin, const uint32_t* qin_n, 
 }
 
 // The primitive arrays in sorted (leaf) order, precomputed as the host
-// emitter does (NewQuad, quad.go:109-130; computeNormal, triangle.go:92-99).
+// emitter does (NewQuad, quad.go:109-130; computeNormal, triangle.go:92-99);
+// `group` holds the shading group of each of the n_mat materials.
 __global__ void k_gather(uint32_t n, const float4* box, const double* geo, const uint32_t* idx, uint4 off,
                          float4* tris, float4* tri_normals, float4* quads, float4* spheres, float4* quadrics,
-                         uint32_t* final_index) {
+                         uint32_t* final_index, const int* group, int n_mat) {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     uint32_t k = idx[j];
     uint32_t tw = __float_as_uint(box[2 * k].w), type = tw & 3u;
     float mat = box[2 * k + 1].w;  // material index as int bits
+    int mi = __float_as_int(mat);
+    float grp = __int_as_float(mi >= 0 && mi < n_mat ? group[mi] : 0);
     const double* g = geo + (size_t)9 * k;
     double ax = g[0], ay = g[1], az = g[2], bx = g[3], by = g[4], bz = g[5], cx = g[6], cy = g[7], cz = g[8];
     uint32_t local;
@@ -245,7 +248,7 @@ __global__ void k_gather(uint32_t n, const float4* box, const double* geo, const
       double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
       float4* T = tris + (size_t)local * 3;
       T[0] = make_float4((float)ax, (float)ay, (float)az, mat);
-      T[1] = make_float4((float)e1x, (float)e1y, (float)e1z, 0.f);
+      T[1] = make_float4((float)e1x, (float)e1y, (float)e1z, grp);
       T[2] = make_float4((float)e2x, (float)e2y, (float)e2z, 0.f);
       tri_normals[local] = make_float4((float)(nx * inv), (float)(ny * inv), (float)(nz * inv), 0.f);
     } else if (type == (uint32_t)kPrimQuad) {
@@ -258,13 +261,13 @@ __global__ void k_gather(uint32_t n, const float4* box, const double* geo, const
       float4* Q = quads + (size_t)local * 5;
       Q[0] = make_float4((float)ax, (float)ay, (float)az, (float)dd);
       Q[1] = make_float4((float)bx, (float)by, (float)bz, mat);
-      Q[2] = make_float4((float)cx, (float)cy, (float)cz, 0.f);
+      Q[2] = make_float4((float)cx, (float)cy, (float)cz, grp);
       Q[3] = make_float4((float)nx, (float)ny, (float)nz, 0.f);
       Q[4] = make_float4((float)(nx * w), (float)(ny * w), (float)(nz * w), 0.f);
     } else if (type == (uint32_t)kPrimSphere) {
       local = j - off.z;
       spheres[(size_t)local * 2] = make_float4((float)ax, (float)ay, (float)az, (float)bx);
-      spheres[(size_t)local * 2 + 1] = make_float4(mat, 0.f, 0.f, 0.f);
+      spheres[(size_t)local * 2 + 1] = make_float4(mat, grp, 0.f, 0.f);
     } else {
       // disc / cylinder / cone record (layout.h), as the host's quadric_record
       local = j - off.w;
@@ -272,7 +275,7 @@ __global__ void k_gather(uint32_t n, const float4* box, const double* geo, const
       float4* R = quadrics + (size_t)local * 5;
       float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       R[2] = R[3] = z;
-      R[4] = make_float4(__int_as_float(kind), mat, kind == kQuadricDisc ? 0.f : (float)cz, 0.f);
+      R[4] = make_float4(__int_as_float(kind), mat, kind == kQuadricDisc ? 0.f : (float)cz, grp);
       if (kind == kQuadricDisc) {
         double inv = 1.0 / sqrt(bx * bx + by * by + bz * bz);
         R[0] = make_float4((float)ax, (float)ay, (float)az, (float)cx);
@@ -406,7 +409,13 @@ int device_build_bvh(gprt_ctx* ctx, HostScene& h, DevScene& d, std::vector<void*
   if (rc) return cleanup(GPRT_E_OOM);
   CK(ctx, cudaMemcpyAsync(nodes, nodes_tmp, (size_t)n4 * 128, cudaMemcpyDeviceToDevice, st));
   uint4 off = make_uint4(0, h.n_tris, h.n_tris + h.n_quads, h.n_tris + h.n_quads + h.n_spheres);
-  k_gather<<<grid, 256, 0, st>>>(n, box, geo, idx2, off, tris, normals, quads, spheres, quadrics, final_index);
+  std::vector<int> groups(std::max<size_t>(1, h.materials.size()), 0);
+  for (size_t m = 0; m < h.materials.size(); m++) groups[m] = shade_group(h.materials[m].kind);
+  int* d_groups = nullptr;
+  if (dev_alloc(ctx, tmp, &d_groups, groups.size())) return cleanup(GPRT_E_OOM);
+  CK(ctx, cudaMemcpyAsync(d_groups, groups.data(), groups.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  k_gather<<<grid, 256, 0, st>>>(n, box, geo, idx2, off, tris, normals, quads, spheres, quadrics, final_index,
+                                 d_groups, (int)h.materials.size());
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return cleanup(cuda_fail(ctx, le, "device BVH build launch"));
   // host copies (layout checks, traversal counts) and the primitive maps

@@ -229,7 +229,7 @@ void launch_pt_extend(const DevScene& sc, const DevPaths& P, int cur, int bounce
 // ----------------------------------------------------------------- shade
 // The shading order of queue `cur` (order_slots) for one scene.
 __global__ void __launch_bounds__(1024) k_hit_order(DevScene sc, DevPaths P, int cur) {
-  order_slots(P, cur, [&](uint32_t, uint32_t prim) { return shade_group(sc.materials[prim_material(sc, prim)].kind); });
+  order_slots(P, cur, [&](uint32_t, uint32_t prim) { return prim_group(sc, prim); });
 }
 
 void launch_hit_order(const DevScene& sc, const DevPaths& P, int cur, uint32_t cap, int sms, cudaStream_t st) {

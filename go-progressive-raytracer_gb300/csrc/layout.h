@@ -7,21 +7,23 @@
 //              ref = node index (meta == 0), first primitive of a leaf
 //              (meta = count | type << 8), or kEmptyChild.  Used slots come
 //              first, so a traversal stops at the first empty one.
-//   tris       3 x float4 (48 B): (v0, material) (e1 = v1 - v0, -) (e2 = v2 - v0, -)
+//   tris       3 x float4 (48 B): (v0, material) (e1 = v1 - v0, group) (e2 = v2 - v0, -)
 //   tri_normals 1 x float4 per triangle: normalize(e1 x e2) computed in float64,
 //              or the mesh's custom normal (TriangleMeshOptions.Normals), normalised
 //   tri_uvs    2 x float4 per triangle when a mesh has VertexUVs:
 //              (uv0, uv1) (uv2, has, -), has = 0 for triangles without them
-//   quads      5 x float4 (80 B): (corner, D) (u, material) (v, -) (normal, -) (W, -)
-//   spheres    2 x float4 (32 B): (center, radius) (material, -, -, -)
+//   quads      5 x float4 (80 B): (corner, D) (u, material) (v, group) (normal, -) (W, -)
+//   spheres    2 x float4 (32 B): (center, radius) (material, group, -, -)
 //   quadrics   5 x float4 (80 B): discs, cylinders and cones
-//              (p0, r0) (axis, height) (p1, r1) (apex, tan^2) (kind, material, capped, -)
+//              (p0, r0) (axis, height) (p1, r1) (apex, tan^2) (kind, material, capped, group)
 //              disc: p0 = centre, axis = unit normal, r0 = radius, p1 = right,
 //              apex = up (the in-plane basis of Disc.SampleUniform);
 //              cylinder: p0 = base, p1 = top, r0 = r1 = radius;
 //              cone: p0 = base (radius r0), p1 = top (radius r1), apex of the extended cone
 //   textures   tex_info uint4 per texture (first texel, width, height, -);
 //              texels float4 (r, g, b, -), row-major (ImageTexture.Pixels)
+//   group (int bits): shade_group of the primitive's material kind, read by
+//              the slot-order kernels without a material lookup
 // Primitive ids: triangles [0, quad_base), quads [quad_base, sphere_base),
 // spheres [sphere_base, quadric_base), quadrics [quadric_base, n_prims); each
 // type array is in BVH leaf order.
@@ -62,6 +64,16 @@ enum : int { kMatLambertian = 0, kMatMetal = 1, kMatDielectric = 2, kMatEmissive
              kMatSpotEmissive = 5, kMatMix = 6 };
 enum : int { kLightQuad = 0, kLightSphere = 1, kLightUniformInfinite = 2, kLightGradientInfinite = 3, kLightDisc = 4,
              kLightDiscSpot = 5, kLightPointSpot = 6 };
+
+// The shading group of a hit on a material of this kind (the slot order
+// of the shading kernels): 0 when its scatter has a pdf, so that shading
+// runs next-event estimation; specular scatter (pdf 0, metal.go:60,
+// dielectric.go:57) 1 for Metal and 2 for Dielectric; 3 for the emitters,
+// which do not scatter (as for missed rays).
+constexpr int kShadeGroups = 4;
+__host__ __device__ constexpr int shade_group(int kind) {
+  return kind == kMatMetal ? 1 : kind == kMatDielectric ? 2 : kind == kMatEmissive || kind == kMatSpotEmissive ? 3 : 0;
+}
 
 struct DevMaterial {
   int kind, outer, inner;

@@ -132,21 +132,12 @@ __device__ __forceinline__ void prefetch_slot(const PathBuf& Q, const float4* hi
   for (int k = 0; k < m; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a[k]));
 }
 
-// The material index (in the scene's material table) of primitive p.
-__device__ __forceinline__ int prim_material(const DevScene& sc, uint32_t p) {
-  if (p < sc.quad_base) return __float_as_int(__ldg(sc.tris + (size_t)p * 3).w);
-  if (p < sc.sphere_base) return __float_as_int(__ldg(sc.quads + (size_t)(p - sc.quad_base) * 5 + 1).w);
-  if (p < sc.quadric_base) return __float_as_int(__ldg(sc.spheres + (size_t)(p - sc.sphere_base) * 2 + 1).x);
-  return __float_as_int(__ldg(sc.quadrics + (size_t)(p - sc.quadric_base) * 5 + 4).y);
-}
-
-// The shading group of a hit on a material of this kind: 0 when its
-// scatter has a pdf, so that shading runs next-event estimation; specular
-// scatter (pdf 0, metal.go:60, dielectric.go:57) 1 for Metal and 2 for
-// Dielectric; 3 for the emitters, which do not scatter (as for missed rays).
-constexpr int kShadeGroups = 4;
-__device__ __forceinline__ int shade_group(int kind) {
-  return kind == kMatMetal ? 1 : kind == kMatDielectric ? 2 : kind == kMatEmissive || kind == kMatSpotEmissive ? 3 : 0;
+// The shading group of primitive p, stored in its record by the builders.
+__device__ __forceinline__ int prim_group(const DevScene& sc, uint32_t p) {
+  if (p < sc.quad_base) return __float_as_int(__ldg(sc.tris + (size_t)p * 3 + 1).w);
+  if (p < sc.sphere_base) return __float_as_int(__ldg(sc.quads + (size_t)(p - sc.quad_base) * 5 + 2).w);
+  if (p < sc.quadric_base) return __float_as_int(__ldg(sc.spheres + (size_t)(p - sc.sphere_base) * 2 + 1).y);
+  return __float_as_int(__ldg(sc.quadrics + (size_t)(p - sc.quadric_base) * 5 + 4).w);
 }
 
 // The slot order the shading kernels read for queue `cur`, by shading group

@@ -163,10 +163,11 @@ DBox quadric_box(const Prim& p) {
 }
 
 // The device record of a quadric (layout.h), precomputed in float64.
-void quadric_record(const Prim& p, float4 out[5]) {
+void quadric_record(const Prim& p, int group, float4 out[5]) {
   float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
   out[0] = out[1] = out[2] = out[3] = z;
-  out[4] = make_float4(i2f((uint32_t)p.qkind), i2f(p.material), p.qkind == kQuadricDisc ? 0.f : (float)p.c.z, 0.f);
+  out[4] = make_float4(i2f((uint32_t)p.qkind), i2f(p.material), p.qkind == kQuadricDisc ? 0.f : (float)p.c.z,
+                       i2f((uint32_t)group));
   if (p.qkind == kQuadricDisc) {
     D3 n = p.b.norm(), right, up;
     disc_basis(n, right, up);
@@ -377,6 +378,11 @@ std::unique_ptr<BNode> join(std::unique_ptr<BNode> a, std::unique_ptr<BNode> b) 
 }
 
 // ---------------------------------------------------------------- BVH4 emission
+// The shading group (layout.h) of a primitive with material index `mat`.
+int material_group(const HostScene& h, int64_t mat) {
+  return mat >= 0 && mat < (int64_t)h.materials.size() ? shade_group(h.materials[(size_t)mat].kind) : 0;
+}
+
 struct Emitter {
   HostScene& out;
   const std::vector<Ref>& refs;
@@ -388,13 +394,14 @@ struct Emitter {
     for (uint32_t i = 0; i < leaf->count; i++) {
       uint32_t pid = refs[leaf->begin + i].prim;
       const Prim& p = prims[pid];
+      const float grp = i2f((uint32_t)material_group(out, p.material));
       if (p.type == kPrimTriangle) {
         uint32_t idx = (uint32_t)(out.tris.size() / 3);
         if (i == 0) first = (int)idx;
         final_index[pid] = idx;
         D3 e1 = p.b - p.a, e2 = p.c - p.a;
         out.tris.push_back(mk4(p.a, i2f(p.material)));
-        out.tris.push_back(mk4(e1, 0.f));
+        out.tris.push_back(mk4(e1, grp));
         out.tris.push_back(mk4(e2, 0.f));
         out.tri_normals.push_back(mk4(e1.cross(e2).norm(), 0.f));  // computeNormal (triangle.go:92-99)
       } else if (p.type == kPrimQuad) {
@@ -407,7 +414,7 @@ struct Emitter {
         D3 w = n * (1.0 / n.dot(p.b.cross(p.c)));
         out.quads.push_back(mk4(p.a, (float)d));
         out.quads.push_back(mk4(p.b, i2f(p.material)));
-        out.quads.push_back(mk4(p.c, 0.f));
+        out.quads.push_back(mk4(p.c, grp));
         out.quads.push_back(mk4(n, 0.f));
         out.quads.push_back(mk4(w, 0.f));
       } else if (p.type == kPrimSphere) {
@@ -415,13 +422,13 @@ struct Emitter {
         if (i == 0) first = (int)idx;
         final_index[pid] = idx;
         out.spheres.push_back(mk4(p.a, (float)p.b.x));
-        out.spheres.push_back(make_float4(i2f(p.material), 0.f, 0.f, 0.f));
+        out.spheres.push_back(make_float4(i2f(p.material), grp, 0.f, 0.f));
       } else {
         uint32_t idx = (uint32_t)(out.quadrics.size() / 5);
         if (i == 0) first = (int)idx;
         final_index[pid] = idx;
         float4 rec[5];
-        quadric_record(p, rec);
+        quadric_record(p, material_group(out, p.material), rec);
         out.quadrics.insert(out.quadrics.end(), rec, rec + 5);
       }
     }

@@ -65,14 +65,10 @@ struct DevItem {
   DevCamera cam;
 };
 
-// The shading order of the step's queue `cur` (order_slots): a slot's
-// material comes from its item's material table.
-__global__ void __launch_bounds__(1024) k_srv_hit_order(DevScene pool, DevPaths P, const DevItem* items, int cur) {
-  const PathBuf Q = P.q[cur];
-  order_slots(P, cur, [&](uint32_t i, uint32_t prim) {
-    const DevItem& it = items[Q.ids[i].w];
-    return shade_group(pool.materials[it.mat_off + prim_material(pool, prim)].kind);
-  });
+// The shading order of the step's queue `cur` (order_slots), from the group
+// stored in each pooled primitive's record.
+__global__ void __launch_bounds__(1024) k_srv_hit_order(DevScene pool, DevPaths P, int cur) {
+  order_slots(P, cur, [&](uint32_t, uint32_t prim) { return prim_group(pool, prim); });
 }
 
 // Camera rays of every item: path p is sample `layer` of pixel i of its item,
@@ -903,7 +899,7 @@ void launch_step(gprt_server* sv, int D, cudaStream_t st, bool capturing) {
     close();
     open();
     k_srv_hit_order<<<std::max(1, std::min((int)((sv->step_paths + 1023) / 1024), sv->ctx->sm_count * 2)), 1024, 0,
-                      st>>>(pool, P, items, cur);
+                      st>>>(pool, P, cur);
     if (P.variant & GPRT_JOB_SHADE_OCCUPANCY)
       k_srv_shade<192, 3><<<std::max(1, grid * block / 192), 192, 0, st>>>(pool, P, items, cur, b);
     else
