@@ -353,8 +353,12 @@ struct gprt_server {
   uint64_t bd_rounds = 0;  // BDPT passes run (their least-recently-served order)
   uint32_t firsts_run = 0; // consecutive steps that carried first passes only
   // read-back staging (resolved image before the copy to the host), grown
-  // on demand under smu and kept: a cudaFree per read would synchronise the
-  // device while steps run
+  // on demand under rmu and kept: a cudaFree per read would synchronise the
+  // device while steps run.  Reads run on rb_stream behind rb_ev (recorded
+  // on the step stream), one at a time (rmu, taken before smu).
+  std::mutex rmu;
+  cudaStream_t rb_stream = nullptr;
+  cudaEvent_t rb_ev = nullptr;
   std::vector<void*> rb_bufs;
   size_t rb_bytes = 0;
   unsigned char* rb = nullptr;
@@ -1269,15 +1273,20 @@ void finish_bdpt(gprt_server* sv, SrvJob* j, uint32_t n, uint64_t taken, bool do
 // arrivals cannot starve them).
 constexpr uint32_t kMaxFirstsSteps = 8;
 
+// BDPT first passes started together in one first-passes step at most.
+constexpr size_t kMaxBdptFirsts = 4;
+
 // One step: admission, the next samples of one BDPT job's pass (RenderPass
 // of one job, progressive.go:126-223: all pixels take the pass's new
 // samples; splats are applied after each slice) and one batched
 // path-tracing wavefront beside it; then the events of both.  A BDPT job's
-// first pass is rendered whole, on the high-priority stream, and is queued
-// before the wavefront so that its blocks are first in line; later passes
-// go in slices of kBdptStepSamples on the job's own stream.  While any job
-// waits for its first pass, the step carries first passes only (time to
-// first pass before throughput), at most kMaxFirstsSteps steps in a row.
+// first pass is rendered whole and queued before the wavefront so that its
+// blocks are first in line, the oldest waiting one on the high-priority
+// stream and up to kMaxBdptFirsts - 1 more on their own streams beside it;
+// later passes go in slices of kBdptStepSamples on the job's own stream.
+// While any job waits for its first pass, the step carries first passes
+// only (time to first pass before throughput), at most kMaxFirstsSteps
+// steps in a row.
 // Returns the number of items run (0: nothing to do) or a negative status.
 int step_impl(gprt_server* sv, bool dry, double* ms_out) {
   if (!dry) admit(sv);
@@ -1291,38 +1300,63 @@ int step_impl(gprt_server* sv, bool dry, double* ms_out) {
     sv->firsts_run = firsts ? sv->firsts_run + 1 : 0;
     if (firsts && bj && bj->passes != 0) bj = nullptr;  // its later pass waits too
   }
-  uint32_t bn = 0;
-  uint64_t taken = 0;
-  bool round_empty = false;
-  int brc = GPRT_OK;
-  cudaStream_t own = nullptr;
+  // the BDPT work of this step: one job's next slice or adaptive round; in a
+  // first-passes step, every BDPT job still before its first pass (up to
+  // kMaxBdptFirsts, oldest first), each on its own stream and the oldest on
+  // the priority stream, so a burst's BDPT first passes run side by side
+  // instead of one step after another
+  struct BdWork {
+    SrvJob* j;
+    uint32_t bn = 0;
+    uint64_t taken = 0;
+    bool round_empty = false;
+    int rc = GPRT_OK;
+    cudaStream_t own = nullptr;
+  };
+  std::vector<BdWork> bw;
   if (bj) {
-    bool first = bj->passes == 0;
-    uint64_t cap = first ? kBdptFirstPassSamples : kBdptStepSamples;
-    uint64_t per = std::max<uint64_t>(1, cap / std::max<uint32_t>(1, bj->npix));
-    if (first && sv->bd_first) {
-      own = bj->bd->stream;
-      bj->bd->stream = sv->bd_first;
+    bw.push_back({bj});
+    if (firsts && bj->passes == 0) {
+      std::vector<SrvJob*> more;
+      for (auto& kv : sv->jobs)
+        if (kv.second->bd && kv.second->running && kv.second->passes == 0 && kv.second.get() != bj)
+          more.push_back(kv.second.get());
+      std::sort(more.begin(), more.end(), [](const SrvJob* a, const SrvJob* b) {
+        return a->submit_ms < b->submit_ms || (a->submit_ms == b->submit_ms && a->ticket < b->ticket);
+      });
+      for (SrvJob* m : more)
+        if (bw.size() < kMaxBdptFirsts) bw.push_back({m});
     }
-    const int64_t uni = bj->bd->uniform_count;
-    if (!bj->adaptive || (uni >= 0 && (uint64_t)uni < bj->min_s)) {
+  }
+  for (size_t k = 0; k < bw.size(); k++) {
+    BdWork& w = bw[k];
+    SrvJob* j = w.j;
+    bool first = j->passes == 0;
+    uint64_t cap = first ? kBdptFirstPassSamples : kBdptStepSamples;
+    uint64_t per = std::max<uint64_t>(1, cap / std::max<uint32_t>(1, j->npix));
+    if (first && k == 0 && sv->bd_first) {
+      w.own = j->bd->stream;
+      j->bd->stream = sv->bd_first;
+    }
+    const int64_t uni = j->bd->uniform_count;
+    if (!j->adaptive || (uni >= 0 && (uint64_t)uni < j->min_s)) {
       // whole samples per pixel: the pass (or, adaptive, its minimum) in slices
-      uint32_t want = bj->adaptive ? (uint32_t)(bj->min_s - (uint64_t)uni) : bj->pass_target - bj->spp_done;
-      bn = (uint32_t)std::min<uint64_t>(want, per);
-      taken = (uint64_t)bn * bj->npix;
-      brc = gprt_job_add_samples(bj->bd, bn);  // queued on the first-pass (or the job's) stream
+      uint32_t want = j->adaptive ? (uint32_t)(j->min_s - (uint64_t)uni) : j->pass_target - j->spp_done;
+      w.bn = (uint32_t)std::min<uint64_t>(want, per);
+      w.taken = (uint64_t)w.bn * j->npix;
+      w.rc = gprt_job_add_samples(j->bd, w.bn);  // queued on the first-pass (or the job's) stream
     } else {
       // one round: a sample for each pixel still active (listed on the device)
       uint32_t active = 0;
-      brc = job_adaptive_round(bj->bd, bj->pass_target, bj->min_s, bj->threshold, &active);
-      taken = active;
-      round_empty = active == 0;
+      w.rc = job_adaptive_round(j->bd, j->pass_target, j->min_s, j->threshold, &active);
+      w.taken = active;
+      w.round_empty = active == 0;
     }
   }
   int n = pt_step(sv, dry, ms_out, firsts);
-  if (bj) finish_bdpt(sv, bj, bn, taken, round_empty, brc, own);
+  for (BdWork& w : bw) finish_bdpt(sv, w.j, w.bn, w.taken, w.round_empty, w.rc, w.own);
   if (n < 0) return n;
-  return n + (bj ? 1 : 0);
+  return n + (int)bw.size();
 }
 
 SrvJob* find_job(gprt_server* sv, uint64_t ticket) {
@@ -1378,49 +1412,59 @@ int stop_loop(gprt_server* sv) {
 // Read-back of an admitted job's image: kind 0 RGBA8 (vec3ToColor), 1 the
 // mean radiance, 2 the RGBA8 of the tile rect = {x0, y0, x1, y1} (only the
 // tile's bytes are resolved and copied: extractTileImage,
-// progressive.go:225-255).
+// progressive.go:225-255).  The resolve and the device-to-host copy are
+// queued on the read-back stream behind an event on the step stream (the
+// film as of every step queued so far), and the wait and the host copy
+// happen outside smu, so the loop thread keeps stepping meanwhile; rmu keeps
+// one read at a time on the staging buffers.  A release in between frees the
+// film with cudaFree, which waits for the queued resolve.
 int read_job(gprt_server* sv, uint64_t ticket, int kind, void* out, const uint32_t* rect = nullptr) {
-  std::lock_guard<std::mutex> g(sv->smu);
+  std::lock_guard<std::mutex> r(sv->rmu);
   gprt_ctx* ctx = sv->ctx;
-  cudaSetDevice(ctx->device);
-  SrvJob* j = find_job(sv, ticket);
-  if (!j) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
-  if (j->bd)  // BDPT: the per-job film (splats included)
-    return kind == 0   ? gprt_job_read_rgba8(j->bd, static_cast<uint8_t*>(out))
-           : kind == 1 ? gprt_job_read_image(j->bd, static_cast<float*>(out))
-                       : gprt_job_read_tile(j->bd, rect[0], rect[1], rect[2], rect[3], static_cast<uint8_t*>(out));
-  if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
-  if (kind == 2 && (rect[2] <= rect[0] || rect[3] <= rect[1] || rect[2] > (uint32_t)j->film.width ||
-                    rect[3] > (uint32_t)j->film.height))
-    return fail(ctx, GPRT_E_INVALID, "tile outside the image");
-  size_t npix = kind == 2 ? (size_t)(rect[2] - rect[0]) * (rect[3] - rect[1]) : (size_t)j->npix;
-  size_t bytes = kind == 1 ? npix * 3 * sizeof(float) : npix * 4;
-  if (bytes > sv->rb_bytes) {
-    cudaStreamSynchronize(sv->stream);  // the old staging buffer may still be read
-    free_all(sv->rb_bufs);
-    sv->rb = nullptr;
-    sv->rb_bytes = 0;
-    if (dev_alloc(ctx, sv->rb_bufs, &sv->rb, bytes)) return GPRT_E_OOM;
-    sv->rb_bytes = bytes;
-  }
-  if (bytes > sv->rb_host_bytes) {
-    if (sv->rb_host) cudaFreeHost(sv->rb_host);
-    sv->rb_host = nullptr;
-    sv->rb_host_bytes = 0;
-    void* h = nullptr;
-    if (cudaHostAlloc(&h, bytes, cudaHostAllocDefault) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(ctx, GPRT_E_OOM, "pinned read-back buffer");
+  size_t bytes = 0;
+  {
+    std::lock_guard<std::mutex> g(sv->smu);
+    cudaSetDevice(ctx->device);
+    SrvJob* j = find_job(sv, ticket);
+    if (!j) return fail(ctx, GPRT_E_NOT_FOUND, "unknown or released ticket");
+    if (j->bd)  // BDPT: the per-job film (splats included)
+      return kind == 0   ? gprt_job_read_rgba8(j->bd, static_cast<uint8_t*>(out))
+             : kind == 1 ? gprt_job_read_image(j->bd, static_cast<float*>(out))
+                         : gprt_job_read_tile(j->bd, rect[0], rect[1], rect[2], rect[3], static_cast<uint8_t*>(out));
+    if (j->bufs.empty()) return fail(ctx, GPRT_E_NOT_FOUND, "the job's film was released");
+    if (kind == 2 && (rect[2] <= rect[0] || rect[3] <= rect[1] || rect[2] > (uint32_t)j->film.width ||
+                      rect[3] > (uint32_t)j->film.height))
+      return fail(ctx, GPRT_E_INVALID, "tile outside the image");
+    size_t npix = kind == 2 ? (size_t)(rect[2] - rect[0]) * (rect[3] - rect[1]) : (size_t)j->npix;
+    bytes = kind == 1 ? npix * 3 * sizeof(float) : npix * 4;
+    if (bytes > sv->rb_bytes) {  // no read is in flight (rmu)
+      free_all(sv->rb_bufs);
+      sv->rb = nullptr;
+      sv->rb_bytes = 0;
+      if (dev_alloc(ctx, sv->rb_bufs, &sv->rb, bytes)) return GPRT_E_OOM;
+      sv->rb_bytes = bytes;
     }
-    sv->rb_host = static_cast<unsigned char*>(h);
-    sv->rb_host_bytes = bytes;
+    if (bytes > sv->rb_host_bytes) {
+      if (sv->rb_host) cudaFreeHost(sv->rb_host);
+      sv->rb_host = nullptr;
+      sv->rb_host_bytes = 0;
+      void* h = nullptr;
+      if (cudaHostAlloc(&h, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, GPRT_E_OOM, "pinned read-back buffer");
+      }
+      sv->rb_host = static_cast<unsigned char*>(h);
+      sv->rb_host_bytes = bytes;
+    }
+    uint8_t* d = sv->rb;
+    CK(ctx, cudaEventRecord(sv->rb_ev, sv->stream));
+    CK(ctx, cudaStreamWaitEvent(sv->rb_stream, sv->rb_ev, 0));
+    if (kind == 0) launch_resolve_rgba8(j->film, d, sv->rb_stream);
+    else if (kind == 1) launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->rb_stream);
+    else launch_resolve_tile(j->film, rect[0], rect[1], rect[2], rect[3], d, sv->rb_stream);
+    CK(ctx, cudaMemcpyAsync(sv->rb_host, d, bytes, cudaMemcpyDeviceToHost, sv->rb_stream));
   }
-  uint8_t* d = sv->rb;
-  if (kind == 0) launch_resolve_rgba8(j->film, d, sv->stream);
-  else if (kind == 1) launch_image_mean(j->film, reinterpret_cast<float*>(d), sv->stream);
-  else launch_resolve_tile(j->film, rect[0], rect[1], rect[2], rect[3], d, sv->stream);
-  cudaError_t e = cudaMemcpyAsync(sv->rb_host, d, bytes, cudaMemcpyDeviceToHost, sv->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+  cudaError_t e = cudaStreamSynchronize(sv->rb_stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "server read-back");
   std::memcpy(out, sv->rb_host, bytes);
   return GPRT_OK;
@@ -1521,6 +1565,15 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   }
   cudaEventCreate(&sv->ev0);
   cudaEventCreate(&sv->ev1);
+  if (cudaStreamCreateWithFlags(&sv->rb_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&sv->rb_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    free_all(b);
+    cudaFreeHost(sv->h_table);
+    cudaStreamDestroy(sv->stream);
+    if (sv->rb_stream) cudaStreamDestroy(sv->rb_stream);
+    return fail(ctx, GPRT_E_DEVICE, "read-back stream creation failed");
+  }
   int least = 0, greatest = 0;
   if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
       cudaStreamCreateWithPriority(&sv->bd_first, cudaStreamNonBlocking, greatest) != cudaSuccess) {
@@ -1534,6 +1587,8 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
     free_all(b);
     cudaFreeHost(sv->h_table);
     if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
+    cudaStreamDestroy(sv->rb_stream);
+    cudaEventDestroy(sv->rb_ev);
     return cuda_fail(ctx, e, "server init");
   }
   ctx->servers.insert(sv.get());
@@ -1546,9 +1601,11 @@ int gprt_server_destroy(gprt_server* sv) {
   gprt_ctx* ctx = sv->ctx;
   stop_loop(sv);
   {
+    std::lock_guard<std::mutex> r(sv->rmu);  // no read in flight
     std::lock_guard<std::mutex> g(sv->smu);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(sv->stream);
+    cudaStreamSynchronize(sv->rb_stream);
     for (auto& kv : sv->jobs) {
       kv.second->running = false;  // the server is going: no counters to keep
       release_job(sv, kv.second.get());
@@ -1568,6 +1625,8 @@ int gprt_server_destroy(gprt_server* sv) {
     cudaEventDestroy(sv->ev0);
     cudaEventDestroy(sv->ev1);
     cudaStreamDestroy(sv->stream);
+    cudaStreamDestroy(sv->rb_stream);
+    cudaEventDestroy(sv->rb_ev);
     if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
   }
   {
