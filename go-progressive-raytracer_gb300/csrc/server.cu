@@ -359,6 +359,23 @@ struct gprt_server {
   std::mutex rmu;
   cudaStream_t rb_stream = nullptr;
   cudaEvent_t rb_ev = nullptr;
+  // released path-tracing films kept for the next admissions (a cudaMalloc
+  // per buffer at admission and a cudaFree at release, which waits for the
+  // whole device, cost about 1.5 % of a 256-job batch); counted in
+  // bytes_in_use and freed first when the budget is short.  rb_done is
+  // recorded on the read-back stream as a film enters the cache, and a
+  // reuse waits for it, so a read still queued sees the old image.
+  struct CachedFilm {
+    uint32_t npix = 0;
+    bool adaptive = false;
+    std::vector<void*> bufs;
+    DevFilm film{};
+    uint32_t* d_list = nullptr;
+    size_t bytes = 0;
+  };
+  std::vector<CachedFilm> film_cache;
+  size_t film_cache_bytes = 0;
+  cudaEvent_t rb_done = nullptr;
   std::vector<void*> rb_bufs;
   size_t rb_bytes = 0;
   unsigned char* rb = nullptr;
@@ -424,6 +441,13 @@ void emit(gprt_server* sv, uint64_t ticket, uint32_t kind, uint32_t passes, uint
   sv->cv_ev.notify_all();
 }
 
+// Released films kept for reuse at most.
+constexpr size_t kFilmCacheMax = 1024;
+
+// Frees cached films until `need` more bytes fit the budget (all of them
+// with need = SIZE_MAX).
+void drop_film_cache(gprt_server* sv, size_t need);
+
 // A path-tracing job's film (+ its active-pixel list and count when the
 // scene samples adaptively).
 size_t film_bytes_for(uint32_t npix, bool adaptive) {
@@ -432,10 +456,20 @@ size_t film_bytes_for(uint32_t npix, bool adaptive) {
 }
 
 size_t bytes_in_use(gprt_server* sv) {
-  size_t b = sv->path_bytes + sv->table_bytes + sv->reserve;
+  size_t b = sv->path_bytes + sv->table_bytes + sv->reserve + sv->film_cache_bytes;
   for (auto& a : sv->pool) b += a.bytes();
   for (auto& kv : sv->jobs) b += kv.second->film_bytes;
   return b;
+}
+
+void drop_film_cache(gprt_server* sv, size_t need) {
+  while (!sv->film_cache.empty() &&
+         (need == SIZE_MAX || bytes_in_use(sv) + need > sv->desc.hbm_budget_bytes)) {
+    gprt_server::CachedFilm& c = sv->film_cache.back();
+    free_all(c.bufs);
+    sv->film_cache_bytes -= c.bytes;
+    sv->film_cache.pop_back();
+  }
 }
 
 // Element counts of a gprt_scene in the pool's arrays.
@@ -650,12 +684,26 @@ void release_job(gprt_server* sv, SrvJob* j) {
     j->ps->refs--;
     j->ps = nullptr;
   }
+  if (!j->bd && !j->bufs.empty() && sv->film_cache.size() < kFilmCacheMax) {
+    cudaEventRecord(sv->rb_done, sv->rb_stream);
+    gprt_server::CachedFilm c;
+    c.npix = j->npix;
+    c.adaptive = j->adaptive;
+    c.bufs = std::move(j->bufs);
+    c.film = j->film;
+    c.d_list = j->d_list;
+    c.bytes = j->film_bytes;
+    sv->film_cache_bytes += c.bytes;
+    sv->film_cache.push_back(std::move(c));
+    j->bufs.clear();
+  }
   free_all(j->bufs);
   if (j->bd_scene) {
     gprt_scene_destroy(j->bd_scene);  // and the job on it
     j->bd_scene = nullptr;
     j->bd = nullptr;
   }
+  j->film_bytes = 0;  // freed, or counted in the film cache
 }
 
 // Moves the job past passes that need no new samples; finishes it after its
@@ -729,6 +777,7 @@ void admit(gprt_server* sv) {
         emit(sv, r.ticket, GPRT_EV_REFUSED, 0, 0, GPRT_E_ADMISSION, r.submit_ms);
         continue;
       }
+      drop_film_cache(sv, need_b);
       if (bytes_in_use(sv) + need_b > sv->desc.hbm_budget_bytes) {
         bool freed = false;  // unreferenced cached scenes go first
         for (auto& ps : sv->scenes)
@@ -783,6 +832,7 @@ void admit(gprt_server* sv) {
       continue;
     }
     // films must fit beside everything held now (scene bytes are checked as the pool grows)
+    drop_film_cache(sv, film_bytes_for(npix, adapt));
     if (bytes_in_use(sv) + film_bytes_for(npix, adapt) > sv->desc.hbm_budget_bytes) {
       // unreferenced cached scenes go first
       bool freed = false;
@@ -807,10 +857,27 @@ void admit(gprt_server* sv) {
     f.width = (int)s->host.sampling.width;
     f.height = (int)s->host.sampling.height;
     int rc = 0;
-    rc |= dev_alloc(ctx, j->bufs, &f.rgbl, npix);
-    rc |= dev_alloc(ctx, j->bufs, &f.lum2, npix);
-    rc |= dev_alloc(ctx, j->bufs, &f.count, npix);
-    if (adapt) rc |= dev_alloc(ctx, j->bufs, &j->d_list, (size_t)npix + 1);
+    bool reused = false;
+    for (size_t c = 0; c < sv->film_cache.size(); c++) {
+      gprt_server::CachedFilm& cf = sv->film_cache[c];
+      if (cf.npix != npix || cf.adaptive != adapt) continue;
+      j->bufs = std::move(cf.bufs);
+      f.rgbl = cf.film.rgbl;
+      f.lum2 = cf.film.lum2;
+      f.count = cf.film.count;
+      j->d_list = cf.d_list;
+      sv->film_cache_bytes -= cf.bytes;
+      sv->film_cache.erase(sv->film_cache.begin() + (ptrdiff_t)c);
+      cudaStreamWaitEvent(sv->stream, sv->rb_done, 0);  // reads queued before its release end first
+      reused = true;
+      break;
+    }
+    if (!reused) {
+      rc |= dev_alloc(ctx, j->bufs, &f.rgbl, npix);
+      rc |= dev_alloc(ctx, j->bufs, &f.lum2, npix);
+      rc |= dev_alloc(ctx, j->bufs, &f.count, npix);
+      if (adapt) rc |= dev_alloc(ctx, j->bufs, &j->d_list, (size_t)npix + 1);
+    }
     if (rc) {
       free_all(j->bufs);
       return;  // device full: retry next step
@@ -1566,7 +1633,8 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
   cudaEventCreate(&sv->ev0);
   cudaEventCreate(&sv->ev1);
   if (cudaStreamCreateWithFlags(&sv->rb_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&sv->rb_ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&sv->rb_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&sv->rb_done, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     free_all(b);
     cudaFreeHost(sv->h_table);
@@ -1589,6 +1657,7 @@ int gprt_server_create(gprt_ctx* ctx, const gprt_server_desc* desc, gprt_server*
     if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
     cudaStreamDestroy(sv->rb_stream);
     cudaEventDestroy(sv->rb_ev);
+    cudaEventDestroy(sv->rb_done);
     return cuda_fail(ctx, e, "server init");
   }
   ctx->servers.insert(sv.get());
@@ -1618,6 +1687,7 @@ int gprt_server_destroy(gprt_server* sv) {
     drop_graphs(sv);
     for (auto& kv : sv->step_events)
       for (auto e : kv.second) cudaEventDestroy(e);
+    drop_film_cache(sv, SIZE_MAX);
     free_all(sv->path_bufs);
     free_all(sv->rb_bufs);
     if (sv->rb_host) cudaFreeHost(sv->rb_host);
@@ -1627,6 +1697,7 @@ int gprt_server_destroy(gprt_server* sv) {
     cudaStreamDestroy(sv->stream);
     cudaStreamDestroy(sv->rb_stream);
     cudaEventDestroy(sv->rb_ev);
+    cudaEventDestroy(sv->rb_done);
     if (sv->bd_first) cudaStreamDestroy(sv->bd_first);
   }
   {
