@@ -488,3 +488,74 @@ def test_adaptive_sampling_in_the_server_equals_progressive_render(ctx, scenes):
     sv.close()
     for g in made:
         g.close()
+
+
+def _plain_rgba8(g, seed, spp):
+    import gprt
+    r = gprt.ProgressiveRaytracer(g, gprt.ProgressiveConfig(max_samples_per_pixel=spp, max_passes=1, seed=seed))
+    r.add_samples(spp)
+    img = r.rgba8()
+    r.close()
+    return img
+
+
+def test_reused_films_and_reads_while_the_loop_renders(ctx, scenes):
+    """Released films go to a cache that later admissions of the same size
+    reuse (cleared on reuse), and read-backs run on their own stream while
+    the loop thread keeps stepping: every image read at its job's `done`
+    event (other jobs still rendering) equals the plain job's, including
+    jobs whose film was reused from a released one."""
+    import time
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 14)
+    sv.start()
+    reqs = [("spheres_a", 31, 4), ("cornell", 32, 4), ("spheres_a", 33, 8), ("cornell", 34, 4),
+            ("spheres_b", 35, 4), ("spheres_a", 36, 4)]
+    imgs, seeds, done = {}, {}, set()
+    deadline = time.time() + 120
+    for k, (n, seed, spp) in enumerate(reqs):
+        t = sv.submit(scenes[n], _cfg(spp, 2, seed))
+        seeds[t] = (n, seed, spp)
+        # later requests of a size arrive after an earlier one was read and
+        # released, so their film comes from the cache
+        while k < 2 and time.time() < deadline and t not in done:
+            for e in sv.poll(timeout_ms=50):
+                if e.kind == "done":
+                    imgs[e.ticket] = sv.rgba8(e.ticket)
+                    sv.release(e.ticket)
+                    done.add(e.ticket)
+    while time.time() < deadline and len(done) < len(reqs):
+        for e in sv.poll(timeout_ms=50):
+            assert e.kind not in ("failed", "refused", "cancelled")
+            if e.kind == "done":
+                imgs[e.ticket] = sv.rgba8(e.ticket)
+                sv.release(e.ticket)
+                done.add(e.ticket)
+    sv.stop()
+    assert len(done) == len(reqs)
+    for t, (n, seed, spp) in seeds.items():
+        assert np.array_equal(imgs[t], _plain_rgba8(scenes[n], seed, spp)), (n, seed)
+    sv.close()
+
+
+def test_bdpt_first_passes_of_a_burst_run_together(ctx, scenes):
+    """Several BDPT requests arriving together start their first passes in
+    the same step (each on its own stream): each film equals the per-job
+    render of the same passes, up to the splat summation order."""
+    import gprt
+    sv = gprt.RenderServer(ctx, step_paths=1 << 16)
+    cfgs = [(41, 8, 4), (42, 8, 2), (43, 4, 4)]
+    ts = [sv.submit(scenes["cornell"], _cfg(spp, per, seed), integrator=gprt.BDPTIntegrator())
+          for seed, spp, per in cfgs]
+    tp = sv.submit(scenes["spheres_b"], _cfg(4, 2, 44))
+    ev = sv.run_until_idle()
+    firsts = [next(i for i, e in enumerate(ev) if e.ticket == t and e.kind == "pass") for t in ts]
+    # the three first passes are reported by the first steps, before any later pass
+    later = [i for i, e in enumerate(ev) if e.kind == "pass" and e.ticket in ts and i not in firsts]
+    assert max(firsts) < min(later)
+    for t, (seed, spp, per) in zip(ts, cfgs):
+        passes = _pass_spp(ev, t)
+        assert sum(passes) == spp
+        _close_bdpt(sv.film(t), _bdpt_passes_film(scenes["cornell"], seed, passes))
+    _same(sv.film(tp), _plain_film(scenes["spheres_b"], 44, 4))
+    sv.close()
