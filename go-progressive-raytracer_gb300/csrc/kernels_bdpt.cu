@@ -1062,6 +1062,20 @@ __device__ __forceinline__ bool has_strategy(int s, int t, int nc, int nl) {
   return s <= nl && t <= nc && !(s == 1 && t == 1) && !(s == 0 && t != nc);
 }
 
+// A strategy the sample has whose contribution can be non-zero: listed for
+// the strategy kernels and summed.  The others return zero before drawing
+// any number, so leaving them out changes neither a sampler position
+// (draws_before) nor a sum: light tracing with a specular light vertex
+// (mask bit s clear), direct lighting at a specular or material-less camera
+// vertex or without lights (bit t clear), and a connection with either
+// (bdpt.go:398-561).
+__device__ __forceinline__ bool listed_strategy(int s, int t, int nc, int nl, uint2 m) {
+  if (!has_strategy(s, t, nc, nl)) return false;
+  if (s == 0) return true;
+  bool ls = (m.x >> s) & 1u, ct = (m.y >> t) & 1u;
+  return t == 1 ? ls : s == 1 ? ct : ls && ct;
+}
+
 // Lists, per strategy, the samples that have it, so that the strategy kernel
 // gives each warp 32 real (s, t, sample) items.  A block of 1,024 samples
 // counts each strategy's items in shared memory (one shared atomic per warp
@@ -1085,13 +1099,15 @@ __global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
     __syncthreads();
     uint32_t i = start + threadIdx.x;
     int nc = 0, nl = -1;
+    uint2 mk = make_uint2(0u, 0u);
     if (i < n) {
       uint32_t m = B.meta[i].x;
       nc = (int)(m & 0xFF);
       nl = (int)(m >> 8);
+      mk = B.masks[i];
     }
     for (int k = 0; k < K; k++) {
-      unsigned mask = __ballot_sync(0xFFFFFFFFu, has_strategy(k / MAXV, k % MAXV + 1, nc, nl));
+      unsigned mask = __ballot_sync(0xFFFFFFFFu, listed_strategy(k / MAXV, k % MAXV + 1, nc, nl, mk));
       if (mask && lane == 0) wofs[wp][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
     }
     __syncthreads();
@@ -1099,7 +1115,7 @@ __global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
       base[k] = cnt[k] ? w * kBdWindow + atomicAdd(B.scount + w * K + k, cnt[k]) : 0u;
     __syncthreads();
     for (int k = 0; k < K; k++) {
-      bool has = has_strategy(k / MAXV, k % MAXV + 1, nc, nl);
+      bool has = listed_strategy(k / MAXV, k % MAXV + 1, nc, nl, mk);
       unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
       if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[wp][k] + __popc(mask & below)] = i;
     }
@@ -1222,11 +1238,12 @@ __global__ void k_bdpt_sum(DevPaths PS, ChunkDesc ch) {
   uint32_t n = ch.npix * ch.layers;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint4 m = B.meta[i];
+    const uint2 mk = B.masks[i];
     int nc = (int)(m.x & 0xFF), nl = (int)(m.x >> 8);
     float3 total = f3(0.f, 0.f, 0.f);
     for (int s = 0; s <= nl; s++)
       for (int t = 1; t <= nc; t++) {
-        if (!has_strategy(s, t, nc, nl)) continue;  // (1,1) and (0, t < nc) contribute nothing
+        if (!listed_strategy(s, t, nc, nl, mk)) continue;  // contributes nothing: not evaluated
         float4 c = B.contrib[(size_t)(s * MAXV + t - 1) * n + i];
         total += f3(c);
       }
