@@ -59,7 +59,7 @@ def _compare(ctx, oracle, scene, rays, any_hit=False):
     rel = np.abs(hits["t"][both] - t_o[both]) / np.maximum(np.abs(t_o[both]), np.maximum(o_len, 1e-30))
     # conditioning of the hit distance: a perpendicular position error e moves
     # the hit by e / |cos| along a ray at angle acos|cos| to the surface normal,
-    # so near-tangent hits (on spheres) are judged by rel * |cos|
+    # so near-tangent hits (on spheres) are checked with rel * |cos|
     d = rays[both, 4:7].astype(np.float64)
     cosg = np.abs(np.sum(d * nrm_o[both], axis=1)) / np.linalg.norm(d, axis=1)
     rel_c = rel * np.minimum(1.0, np.maximum(cosg, 1e-6))
