@@ -1106,19 +1106,26 @@ __global__ void __launch_bounds__(1024) k_bdpt_list(DevPaths PS, ChunkDesc ch) {
       nl = (int)(m >> 8);
       mk = B.masks[i];
     }
-    for (int k = 0; k < K; k++) {
-      unsigned mask = __ballot_sync(0xFFFFFFFFu, listed_strategy(k / MAXV, k % MAXV + 1, nc, nl, mk));
-      if (mask && lane == 0) wofs[wp][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
-    }
+    // a warp visits only the strategies its longest subpaths reach (both
+    // loops over the same range: wofs is written and read for those only)
+    const int wnc = __reduce_max_sync(0xFFFFFFFFu, nc), wnl = __reduce_max_sync(0xFFFFFFFFu, nl);
+    for (int s = 0; s <= wnl; s++)
+      for (int t = 1; t <= wnc; t++) {
+        const int k = s * MAXV + t - 1;
+        unsigned mask = __ballot_sync(0xFFFFFFFFu, listed_strategy(s, t, nc, nl, mk));
+        if (mask && lane == 0) wofs[wp][k] = (uint16_t)atomicAdd(&cnt[k], (uint32_t)__popc(mask));
+      }
     __syncthreads();
     for (int k = threadIdx.x; k < K; k += blockDim.x)
       base[k] = cnt[k] ? w * kBdWindow + atomicAdd(B.scount + w * K + k, cnt[k]) : 0u;
     __syncthreads();
-    for (int k = 0; k < K; k++) {
-      bool has = listed_strategy(k / MAXV, k % MAXV + 1, nc, nl, mk);
-      unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
-      if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[wp][k] + __popc(mask & below)] = i;
-    }
+    for (int s = 0; s <= wnl; s++)
+      for (int t = 1; t <= wnc; t++) {
+        const int k = s * MAXV + t - 1;
+        bool has = listed_strategy(s, t, nc, nl, mk);
+        unsigned mask = __ballot_sync(0xFFFFFFFFu, has);
+        if (has) B.slist[(size_t)k * B.ns + base[k] + wofs[wp][k] + __popc(mask & below)] = i;
+      }
     __syncthreads();  // cnt, base and wofs are rewritten for the next range
   }
 }
