@@ -180,7 +180,6 @@ int add_samples(gprt_job* j, uint32_t spp, uint32_t npix, const uint32_t* list) 
   ChunkDesc ch{};
   ch.pix_list = list;
   ch.seed = j->desc.seed;
-  ch.bounce_base = 0;
   if (npix <= cap) {
     uint32_t per = std::max(1u, cap / npix);
     for (uint32_t done = 0; done < spp;) {
@@ -917,7 +916,6 @@ extern "C" int gprt_render_noalloc(gprt_scene* s, uint32_t spp, uint64_t seed, f
   ch.layers = spp;
   ch.pix_list = nullptr;
   ch.seed = seed;
-  ch.bounce_base = 0;
   const DevScene& sc = s->dev;
   const int block = 128;
   int grid = launch_grid((uint32_t)(npix * spp), block, std::max(1, ctx->sm_count * (2048 / block)));

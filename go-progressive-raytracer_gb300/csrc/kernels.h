@@ -136,7 +136,6 @@ struct ChunkDesc {
   uint32_t pix0, npix, layers;
   const uint32_t* pix_list;
   uint64_t seed;
-  int bounce_base;
 };
 
 int launch_grid(uint32_t n, int block, int max_blocks);
