@@ -538,7 +538,11 @@ int gprt_server_start(gprt_server* server);
 int gprt_server_stop(gprt_server* server);
 /* Takes up to `max` events, waiting up to timeout_ms for the first one. */
 int gprt_server_poll(gprt_server* server, gprt_event* events, uint32_t max, uint32_t timeout_ms, uint32_t* n);
-/* Film / image of an admitted job (in flight or done), as gprt_job_read_*. */
+/* Film / image of an admitted job (in flight or done), as gprt_job_read_*.
+ * The image reads (rgb mean, RGBA8, tile) resolve and copy on the server's
+ * own read-back stream after the steps queued so far, and wait without
+ * holding up the server's loop thread: a front door reads each image as its
+ * event arrives while the other jobs keep rendering (one read at a time). */
 int gprt_server_read_film(gprt_server* server, uint64_t ticket, float* rgb_sum, float* lum_sum, float* lum2_sum,
                           uint32_t* count);
 int gprt_server_read_image(gprt_server* server, uint64_t ticket, float* rgb_mean);
