@@ -154,7 +154,7 @@ __device__ __forceinline__ void srv_shade(const DevScene& pool, const DevPaths& 
   }
 }
 
-// The kernel at 2 blocks of 256 threads per SM (16 warps, 113 registers)
+// The kernel at 2 blocks of 256 threads per SM (16 warps, 117 registers)
 // or, as GPRT_JOB_SHADE_OCCUPANCY, 3 blocks of 192 threads (18 warps at 96
 // registers, 64 bytes spilled).  More warps did not pay: the 3-block
 // budget measured 8 % slower on the heterogeneous batch (shade 462 vs 428 ms
