@@ -67,6 +67,26 @@ def test_host_builder_layout_and_world_bounds(gprt_lib, oracle, name):
     assert info.n_nodes >= 1
 
 
+def test_flat_layout_for_tiny_scenes(gprt_lib):
+    """A scene of at most 32 primitives, at most 8 of them spheres, gets one
+    leaf per primitive type under the root (a single BVH node): every ray
+    tests the same primitives, so a warp's lanes stay converged.  Sphere
+    scenes beyond 8 spheres and larger scenes keep a tree."""
+    from gprt import scenes
+    rc, info, err = _validate(scenes.cornell_baseline(32).to_desc())  # 18 quads
+    assert rc == 0, err
+    assert info.n_nodes == 1
+    rc, info, err = _validate(scenes.cornell_scene(scenes.CORNELL_SPHERES).to_desc())  # quads + 2 spheres
+    assert rc == 0, err
+    assert info.n_nodes == 1
+    rc, info, err = _validate(scenes.default_style_scene(80, 32, 32).to_desc())  # 15 spheres
+    assert rc == 0, err
+    assert info.n_nodes > 1
+    rc, info, err = _validate(scenes.icosphere_scene(level=2, width=32).to_desc())  # 320 triangles
+    assert rc == 0, err
+    assert info.n_nodes > 1
+
+
 def test_primitive_counts(gprt_lib):
     from gprt import scenes
     rc, info, err = _validate(scenes.cornell_baseline(64).to_desc())
