@@ -803,7 +803,7 @@ def run_gprt(args):
     gscenes = [gprt.GpuScene(ctx, f) for f, _ in jobs]
     spps = [s for _, s in jobs]
     samples_per_step = sum(g.width * g.height * s for g, s in zip(gscenes, spps))
-    cap = 1 << 24
+    cap = 1 << 25
 
     # work per extend launch, counted once on the same batch (not timed)
     sv = gprt.RenderServer(ctx, step_paths=cap,
